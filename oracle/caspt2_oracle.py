@@ -1,0 +1,983 @@
+"""CPU oracle for the DIRAC-CASPT2 hot path (test infrastructure only).
+
+This module is the CHECKER for the GPU library: a numpy restatement of the reference's
+FP64 Fortran algorithm for CASCI, the CASCI-state Fock build and diagonalisation, the CI
+rotation into the Fock-diagonal spinor basis, the 4-index transformation and the eight
+subspace solvers A-H.  Only ``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline
+leg of ``bench.py`` may import it; the product path never does.
+
+Parity of this oracle is pinned against the reference's own golden outputs
+(``test/dev/*/reference.*.out``) by ``tests/test_oracle_golden.py``.
+
+Every function cites the reference file and lines (paths inside the reference project)
+whose behaviour it restates.  Index convention here: 0-based global CAS-order spinors
+``0..nmo-1`` (inactive, active, secondary); active spinor ``t`` <-> bit ``t`` of a
+determinant bit string.
+
+Two evaluation modes for the ``dimN_density`` elements:
+  * ``literal``: the determinant loop of ``density_matrix.F90:3-247`` element by element
+    (small cases only);
+  * ``rdm``: the same expectation values precomputed as dense tensors through the full
+    N-electron space (identical numbers to rounding; validated against ``literal``).
+"""
+from __future__ import annotations
+
+import dataclasses
+import functools
+import math
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+SMAT_LIN_DEP_THRESHOLD = 1.0e-8     # module_global_variables.F90:181
+BMAT_NO_CUTOFF = 0.0                # module_global_variables.F90:182
+INTRA_CUTOFF = 1.0e-15              # module_intra.F90:85 (write cutoff of transformed classes)
+EFFH_C_SKIP = 1.0e-10               # solve_C_subspace.F90 vCmat: |effh(a,p)| < 1e-10 skipped
+
+SUBSPACES = "ABCDEFGH"
+
+
+# ======================================================================================
+# System description
+# ======================================================================================
+@dataclasses.dataclass
+class System:
+    """Everything the hot path consumes, in CAS order (0-based)."""
+    ninact: int
+    nact: int
+    nsec: int
+    nelec: int
+    nmo: int
+    nsymrpa: int
+    multb: np.ndarray          # (2n,2n) 1-based values, Fortran (i0,j0) at [i0-1, j0-1]
+    irpamo: np.ndarray         # (nmo,) 1-based irreps
+    h: np.ndarray              # (nmo, nmo) complex
+    ecore: float
+    rec_idx: np.ndarray        # (n,4) 1-based MDCINTNEW indices
+    rec_val: np.ndarray        # (n,) complex
+    realonly: bool
+    totsym: int = 1
+    selectroot: int = 1
+    eshift: float = 0.0
+    ras1: Tuple[int, ...] = ()
+    ras2: Tuple[int, ...] = ()
+    ras3: Tuple[int, ...] = ()
+    ras1_max_hole: int = 0
+    ras3_max_elec: int = 0
+    min_hole_ras1: int = 0
+    min_elec_ras3: int = 0
+
+    @property
+    def nmoc(self) -> int:
+        return self.ninact + self.nact
+
+    def space_of(self, g: np.ndarray) -> np.ndarray:
+        """1 inactive, 2 active, 3 secondary, 4 beyond (read_mrconee.F90:311-315)."""
+        g = np.asarray(g)
+        s = np.full(g.shape, 4, dtype=np.int64)
+        s[g < self.ninact + self.nact + self.nsec] = 3
+        s[g < self.ninact + self.nact] = 2
+        s[g < self.ninact] = 1
+        return s
+
+    # multiplication tables (read_mrconee.F90:368-453)
+    @functools.cached_property
+    def multb_s(self):
+        n = self.nsymrpa
+        return self.multb[n:2 * n, n:2 * n] - n
+
+    @functools.cached_property
+    def multb2(self):
+        n2 = 2 * self.nsymrpa
+        m2 = np.zeros((n2, n2), dtype=np.int64)
+        for i0 in range(n2):
+            for j0 in range(n2):
+                m2[i0, self.multb[i0, j0] - 1] = j0 + 1
+        return m2
+
+    @functools.cached_property
+    def multb_d(self):
+        n = self.nsymrpa
+        return self.multb2[0:n, 0:n] - n
+
+    @functools.cached_property
+    def multb_ds(self):
+        n = self.nsymrpa
+        return np.ascontiguousarray(self.multb[n:2 * n, 0:n].T)
+
+
+def system_from_files(directory: str, totsym: Optional[int] = None, selectroot: Optional[int] = None) -> System:
+    """Read active.inp, MRCONEE and MDCINT* of a reference-style case directory."""
+    import os
+    from dirac_caspt2_gb300 import dirac_io
+    inp = dirac_io.read_active_inp(os.path.join(directory, "active.inp"))
+    mrc = dirac_io.read_mrconee(os.path.join(directory, "MRCONEE"), inp)
+    new = dirac_io.read_mdcint_new(directory, mrc, inp)
+    ts, sr = inp.ciroots[0]
+    return System(ninact=inp.ninact, nact=inp.nact, nsec=inp.nsec, nelec=inp.nelec, nmo=mrc.nmo,
+                  nsymrpa=mrc.nsymrpa, multb=mrc.multb, irpamo=mrc.irpamo, h=mrc.h, ecore=mrc.ecore,
+                  rec_idx=new.idx, rec_val=new.val, realonly=new.realonly,
+                  totsym=totsym if totsym is not None else ts,
+                  selectroot=selectroot if selectroot is not None else sr, eshift=inp.eshift,
+                  ras1=tuple(inp.ras1), ras2=tuple(inp.ras2), ras3=tuple(inp.ras3),
+                  ras1_max_hole=inp.ras1_max_hole, ras3_max_elec=inp.ras3_max_elec,
+                  min_hole_ras1=inp.min_hole_ras1, min_elec_ras3=inp.min_elec_ras3)
+
+
+# ======================================================================================
+# Two-electron integrals: 16-partner expansion of MDCINTNEW records into dense regions
+# ======================================================================================
+def expand_partners(idx1: np.ndarray, val: np.ndarray):
+    """All (ij|kl) partners a record stands for (module_2integrals.F90:395-434).
+
+    Returns (P, V): P (16, n, 4) 0-based indices, V (16, n) complex values.  Records with
+    i == j and k > l are dropped as the reference's readers do (module_2integrals.F90:393,
+    divide_2_elec_integral_into_subspaces.F90:117)."""
+    i, j, k, l = (idx1[:, c].astype(np.int64) for c in range(4))
+    keep = ~((i == j) & (k > l))
+    i, j, k, l, v = i[keep], j[keep], k[keep], l[keep], val[keep]
+
+    def tr(x):  # Kramers partner, 1-based: odd -> +1, even -> -1
+        return np.where((x + 1) % 2 == 0, x + 1, x - 1)
+
+    itr, jtr, ktr, ltr = tr(i), tr(j), tr(k), tr(l)
+    sij = np.where((i + j) % 2 == 0, 1.0, -1.0)
+    skl = np.where((k + l) % 2 == 0, 1.0, -1.0)
+    vc = np.conj(v)
+    P = [
+        (i, j, k, l, v), (jtr, itr, k, l, v * sij), (i, j, ltr, ktr, v * skl), (jtr, itr, ltr, ktr, v * sij * skl),
+        (j, i, l, k, vc), (itr, jtr, l, k, vc * sij), (j, i, ktr, ltr, vc * skl), (itr, jtr, ktr, ltr, vc * sij * skl),
+        (k, l, i, j, v), (ltr, ktr, i, j, v * skl), (k, l, jtr, itr, v * sij), (ltr, ktr, jtr, itr, v * sij * skl),
+        (l, k, j, i, vc), (ktr, ltr, j, i, vc * skl), (l, k, itr, jtr, vc * sij), (ktr, ltr, itr, jtr, vc * sij * skl),
+    ]
+    Pidx = np.stack([np.stack([a - 1, b - 1, c - 1, d - 1], axis=1) for (a, b, c, d, _) in P])
+    Pval = np.stack([p[4] for p in P])
+    return Pidx, Pval
+
+
+class Integrals:
+    """Dense two-electron integral blocks (pq|rs) in the ORIGINAL spinor basis, addressed
+    by a space pattern (s1,s2,s3,s4) with s in {1,2,3}."""
+
+    def __init__(self, sysm: System):
+        self.sysm = sysm
+        P, V = expand_partners(sysm.rec_idx, sysm.rec_val)
+        self.P = P.reshape(-1, 4)
+        self.V = V.reshape(-1)
+        sp = sysm.space_of(self.P)
+        self.code = sp[:, 0] * 1000 + sp[:, 1] * 100 + sp[:, 2] * 10 + sp[:, 3]
+        self._cache: Dict[Tuple[int, ...], np.ndarray] = {}
+
+    def rng(self, s: int) -> Tuple[int, int]:
+        ni, na, ns = self.sysm.ninact, self.sysm.nact, self.sysm.nsec
+        return [(0, ni), (ni, ni + na), (ni + na, ni + na + ns)][s - 1]
+
+    def block(self, pattern: Tuple[int, int, int, int]) -> np.ndarray:
+        """Dense block with '=' scatter semantics (later partners overwrite earlier)."""
+        if pattern in self._cache:
+            return self._cache[pattern]
+        r = [self.rng(s) for s in pattern]
+        shape = tuple(b - a for a, b in r)
+        out = np.zeros(shape, dtype=np.complex128)
+        c = pattern[0] * 1000 + pattern[1] * 100 + pattern[2] * 10 + pattern[3]
+        m = self.code == c
+        if np.any(m):
+            p = self.P[m]
+            out[p[:, 0] - r[0][0], p[:, 1] - r[1][0], p[:, 2] - r[2][0], p[:, 3] - r[3][0]] = self.V[m]
+        self._cache[pattern] = out
+        return out
+
+    def occ_block(self) -> np.ndarray:
+        """inttw(nmoc^4): every (pq|rs) with all indices inactive or active."""
+        s = self.sysm
+        nmoc = s.nmoc
+        out = np.zeros((nmoc,) * 4, dtype=np.complex128)
+        m = np.all(self.P < nmoc, axis=1)
+        p = self.P[m]
+        out[p[:, 0], p[:, 1], p[:, 2], p[:, 3]] = self.V[m]
+        return out
+
+
+# ======================================================================================
+# Determinant space and one-electron excitations
+# ======================================================================================
+def popcount(x: int) -> int:
+    return bin(x).count("1")
+
+
+def one_e_exct(I: int, c: int, a: int, nact: int):
+    """E_{ca}|I> = phase * |J> (one_e_exct.F90:3-51); c, a 0-based.  None if zero."""
+    if c == a:
+        return (I, 0) if (I >> a) & 1 else None
+    if not ((I >> a) & 1) or ((I >> c) & 1):
+        return None
+    J = I - (1 << a) + (1 << c)
+    ia = ((1 << nact) - (1 << (a + 1))) if a + 1 < nact else 0
+    ib = ((1 << nact) - (1 << (c + 1))) if c + 1 < nact else 0
+    ph = popcount(I & ia) + popcount((I - (1 << a)) & ib)
+    return J, ph
+
+
+def ras_ok(I: int, s: System) -> bool:
+    """ras_det_check.F90:1-59 applied by search_cas_configuration.F90:91-110."""
+    if s.ras1:
+        n1 = len(s.ras1)
+        ne1 = popcount(I & ((1 << n1) - 1))
+        if not (n1 - s.ras1_max_hole <= ne1 <= n1 - s.min_hole_ras1):
+            return False
+    if s.ras3:
+        sh = len(s.ras1) + len(s.ras2)
+        ne3 = popcount((I >> sh) << sh & I)
+        if not (ne3 <= s.ras3_max_elec and s.min_elec_ras3 <= ne3):
+            return False
+    return True
+
+
+def det_totsym(I: int, s: System) -> int:
+    """cas_configuration_totsym (search_cas_configuration.F90:112-149)."""
+    if s.nsymrpa == 1:
+        return 1
+    mds, md = s.multb_ds, s.multb_d
+    ret = 1
+    ielec = 0
+    for t in range(s.nact):
+        if (I >> t) & 1:
+            ielec += 1
+            jsym = int(s.irpamo[s.ninact + t])
+            if ielec % 2 == 1:
+                ret = int(mds[jsym - 1, ret - 1])
+            else:
+                partner = jsym + 1 if jsym % 2 == 1 else jsym - 1
+                ret = int(md[partner - 1, ret - 1])
+    if ielec % 2 == 0:
+        ret += s.nsymrpa
+    return ret
+
+
+def enumerate_dets(s: System) -> List[int]:
+    """search_cas_configuration.F90:3-110: Gosper order over nelec-of-nact bit strings."""
+    out = []
+    cur = (1 << s.nelec) - 1
+    while cur < (1 << s.nact):
+        if ras_ok(cur, s) and (s.nsymrpa == 1 or det_totsym(cur, s) == s.totsym):
+            out.append(cur)
+        t = (cur | (cur - 1)) + 1
+        cur = t | ((((t & -t) // (cur & -cur)) >> 1) - 1)
+    return out
+
+
+# ======================================================================================
+# CASCI (casmat.F90, diag.F90, casci.F90)
+# ======================================================================================
+def casmat(s: System, dets: List[int], g: np.ndarray) -> np.ndarray:
+    """CASCI Hamiltonian by Slater-Condon rules (casmat.F90:3-222); g = inttw (nmoc^4)."""
+    ni, na = s.ninact, s.nact
+    ndet = len(dets)
+    index = {d: n for n, d in enumerate(dets)}
+    H = np.zeros((ndet, ndet), dtype=np.complex128)
+    h = s.h
+    for n, I in enumerate(dets):
+        occ = [t for t in range(na) if (I >> t) & 1]
+        vir = [t for t in range(na) if not (I >> t) & 1]
+        occg = list(range(ni)) + [ni + t for t in occ]
+        # diagonal (casmat.F90:54-104)
+        d = sum(h[r, r] for r in occg)
+        m0 = 0.0
+        for x in range(len(occg)):
+            r = occg[x]
+            for y in range(x + 1, len(occg)):
+                q = occg[y]
+                m0 += 0.5 * g[r, r, q, q] - 0.5 * g[r, q, q, r]
+        H[n, n] = d + m0 + np.conj(m0)
+        # singles (casmat.F90:106-169)
+        for r_ in occ:
+            ir = ni + r_
+            for a_ in vir:
+                ia = ni + a_
+                res = one_e_exct(I, a_, r_, na)
+                if res is None or res[0] not in index:
+                    continue
+                m = index[res[0]]
+                if m <= n:
+                    continue
+                val = h[ir, ia]
+                for q in occg:
+                    val += g[ir, ia, q, q] - g[ir, q, q, ia]
+                val *= 1 if res[1] % 2 == 0 else -1
+                H[n, m] = val
+                H[m, n] = np.conj(val)
+        # doubles (casmat.F90:170-213)
+        for x in range(len(occ)):
+            for y in range(x + 1, len(occ)):
+                r_, q_ = occ[x], occ[y]
+                for u in range(len(vir)):
+                    for w in range(u + 1, len(vir)):
+                        a_, b_ = vir[u], vir[w]
+                        r1 = one_e_exct(I, a_, r_, na)
+                        if r1 is None:
+                            continue
+                        r2 = one_e_exct(r1[0], b_, q_, na)
+                        if r2 is None or r2[0] not in index:
+                            continue
+                        m = index[r2[0]]
+                        if m <= n:
+                            continue
+                        ir, iq, ia, ib = ni + r_, ni + q_, ni + a_, ni + b_
+                        val = g[ir, ia, iq, ib] - g[ir, ib, iq, ia]
+                        val *= 1 if (r1[1] + r2[1]) % 2 == 0 else -1
+                        H[n, m] = val
+                        H[m, n] = np.conj(val)
+    return H
+
+
+def heev_upper(A: np.ndarray):
+    """ZHEEV/DSYEV(jobz='V', uplo='U') semantics: only the upper triangle is referenced,
+    eigenvalues ascending (diag.F90:43,109)."""
+    return np.linalg.eigh(A, UPLO="U")
+
+
+# ======================================================================================
+# Densities
+# ======================================================================================
+class FullSpace:
+    """The full N-electron active space (every nelec-of-nact bit string, Gosper order) with
+    the CI vector embedded in it.  Intermediate determinants of the reference's
+    ``dimN_density`` loops are unrestricted bit strings, so operator products are exact
+    in this space (density_matrix.F90:3-247)."""
+
+    def __init__(self, s: System, dets: List[int]):
+        na, ne = s.nact, s.nelec
+        full = []
+        cur = (1 << ne) - 1
+        while cur < (1 << na):
+            full.append(cur)
+            t = (cur | (cur - 1)) + 1
+            cur = t | ((((t & -t) // (cur & -cur)) >> 1) - 1)
+        self.full = full
+        self.index = {d: n for n, d in enumerate(full)}
+        self.ci_pos = np.array([self.index[d] for d in dets], dtype=np.int64)
+        self.na = na
+        M = len(full)
+        # E_pq as sparse triplets: for each (p,q) arrays (src, dst, sign)
+        self.ops = {}
+        for p in range(na):
+            for q in range(na):
+                src, dst, sg = [], [], []
+                for n, I in enumerate(full):
+                    r = one_e_exct(I, p, q, na)
+                    if r is None:
+                        continue
+                    src.append(n)
+                    dst.append(self.index[r[0]])
+                    sg.append(1.0 if r[1] % 2 == 0 else -1.0)
+                self.ops[(p, q)] = (np.array(src, dtype=np.int64), np.array(dst, dtype=np.int64),
+                                    np.array(sg))
+        self.M = M
+
+    def embed(self, c: np.ndarray) -> np.ndarray:
+        psi = np.zeros((self.M,) + c.shape[1:], dtype=np.complex128)
+        psi[self.ci_pos] = c
+        return psi
+
+    def apply(self, p: int, q: int, x: np.ndarray) -> np.ndarray:
+        """y = E_pq x (x may carry trailing columns)."""
+        src, dst, sg = self.ops[(p, q)]
+        y = np.zeros_like(x)
+        if len(src):
+            np.add.at(y, dst, x[src] * sg.reshape((-1,) + (1,) * (x.ndim - 1)))
+        return y
+
+    def project(self, x: np.ndarray) -> np.ndarray:
+        """Zero components outside the CI space (final-determinant lookup of the reference)."""
+        y = np.zeros_like(x)
+        y[self.ci_pos] = x[self.ci_pos]
+        return y
+
+
+class RDM:
+    """Dense <0|E..E|0> tensors for one CI vector (rdm mode).
+
+    D1[a,b]      = <E_ab>                       (dim1_density)
+    D2[a,b,c,d]  = <E_ab E_cd>                  (dim2_density)
+    D3[...]      = <E_ab E_cd E_ef>             (dim3_density)
+    T1/T2/T3     = same with sum_w eps_w E_ww rightmost (dim2/3/4_density(...,w,w) weighted)
+    """
+
+    def __init__(self, fs: FullSpace, c: np.ndarray, eps_act: Optional[np.ndarray] = None, order: int = 3):
+        na = fs.na
+        psi = fs.embed(c)
+        bra = fs.project(psi)              # <0| lives in the CI space
+        self.na = na
+        Y = np.stack([fs.apply(p, q, psi) for p in range(na) for q in range(na)], axis=1)  # (M, na^2)
+        # <0|E_ab X> = (E_ba ... ) : bra is the CI vector itself
+        self.D1 = (np.conj(bra) @ Y).reshape(na, na)
+        # D2[ab,cd] = sum_K conj( (E_ba psi)_K restricted ) ... use <0|E_ab = (E_ba |0>)^dagger
+        Yb = np.stack([fs.apply(q, p, bra) for p in range(na) for q in range(na)], axis=1)  # col ab = E_ba bra
+        self.D2 = (np.conj(Yb).T @ Y).reshape(na, na, na, na)
+        if order >= 3:
+            Z = np.stack([fs.apply(p, q, Y) for p in range(na) for q in range(na)], axis=1)  # (M, na^2, na^2)
+            self.D3 = np.einsum("ka,kbc->abc", np.conj(Yb), Z).reshape((na,) * 6)
+        if eps_act is not None:
+            occ_e = np.array([sum(eps_act[t] for t in range(na) if (I >> t) & 1) for I in fs.full])
+            psit = psi * occ_e
+            Yt = np.stack([fs.apply(p, q, psit) for p in range(na) for q in range(na)], axis=1)
+            self.T1 = (np.conj(bra) @ Yt).reshape(na, na)
+            self.T2 = (np.conj(Yb).T @ Yt).reshape(na, na, na, na)
+            if order >= 3:
+                Zt = np.stack([fs.apply(p, q, Yt) for p in range(na) for q in range(na)], axis=1)
+                self.T3 = np.einsum("ka,kbc->abc", np.conj(Yb), Zt).reshape((na,) * 6)
+            self.e0_weights = occ_e
+
+
+def density_literal(ops: List[Tuple[int, int]], dets: List[int], c: np.ndarray, na: int) -> complex:
+    """<0|E_{c1a1} ... E_{cnan}|0> by the reference's determinant loop
+    (density_matrix.F90:3-247); ops given left to right, applied right to left."""
+    index = {d: n for n, d in enumerate(dets)}
+    acc = 0.0 + 0.0j
+    for n, I in enumerate(dets):
+        cur, ph = I, 0
+        ok = True
+        for (cc, aa) in reversed(ops):
+            r = one_e_exct(cur, cc, aa, na)
+            if r is None:
+                ok = False
+                break
+            cur, ph = r[0], ph + r[1]
+        if not ok or cur not in index:
+            continue
+        m = index[cur]
+        v = c[n] * np.conj(c[m])
+        acc += v if ph % 2 == 0 else -v
+    return acc
+
+
+# ======================================================================================
+# Fock matrix, its diagonalisation and the CI rotation
+# ======================================================================================
+def fock_casci(s: System, ints: Integrals, g_occ: np.ndarray, D1: np.ndarray) -> np.ndarray:
+    """CASCI-state Fock matrix on the occ x occ and sec x sec blocks (fockcasci.F90:4-90)."""
+    ni, na, ns, nmo = s.ninact, s.nact, s.nsec, s.nmo
+    nmoc = ni + na
+    f = np.zeros((nmo, nmo), dtype=np.complex128)
+    Dt = np.zeros((nmoc, nmoc), dtype=np.complex128)
+    Dt[np.arange(ni), np.arange(ni)] = 1.0
+    Dt[ni:, ni:] = D1
+    # occ block: h + sum_kl Dt_kl [(ij|kl) - (il|kj)]
+    fo = s.h[:nmoc, :nmoc] + np.einsum("ijkl,kl->ij", g_occ, Dt) - np.einsum("ilkj,kl->ij", g_occ, Dt)
+    iu = np.triu_indices(nmoc)
+    fu = np.zeros_like(fo)
+    fu[iu] = fo[iu]
+    f[:nmoc, :nmoc] = fu + np.conj(np.triu(fu, 1)).T
+    if ns:
+        sl = slice(nmoc, nmoc + ns)
+        fs_ = s.h[sl, sl].copy()
+        # (ab|kl) with k,l occupied: patterns (3,3,1,1),(3,3,2,2) and (3,3,1,2),(3,3,2,1) are
+        # absent from the reference (only diagonal-space pairs are stored); Dt is block diagonal.
+        f1_11 = ints.block((3, 3, 1, 1))
+        f1_22 = ints.block((3, 3, 2, 2))
+        f2_11 = ints.block((3, 1, 1, 3))
+        f2_22 = ints.block((3, 2, 2, 3))
+        fs_ += np.einsum("abkk->ab", f1_11) - np.einsum("akkb->ab", f2_11)
+        fs_ += np.einsum("abkl,kl->ab", f1_22, D1) - np.einsum("alkb,kl->ab", f2_22, D1)
+        iu2 = np.triu_indices(ns)
+        fu2 = np.zeros_like(fs_)
+        fu2[iu2] = fs_[iu2]
+        f[sl, sl] = fu2 + np.conj(np.triu(fu2, 1)).T
+    return f
+
+
+def fock_diag(s: System, f: np.ndarray):
+    """fockdiag.F90:4-78 with cdiag0 (diag.F90:230-375): per space and irrep Hermitian
+    eigendecomposition.  Returns (U, eps) with U block diagonal (column j = new spinor j)."""
+    nmo = s.nmo
+    U = np.zeros((nmo, nmo), dtype=np.complex128)
+    eps = np.zeros(nmo)
+    ranges = [(0, s.ninact), (s.ninact, s.nmoc), (s.nmoc, s.nmoc + s.nsec)]
+    for (n0, n1) in ranges:
+        if n1 <= n0:
+            continue
+        for sym in range(1, s.nsymrpa + 1):
+            ind = [i for i in range(n0, n1) if s.irpamo[i] == sym]
+            if not ind:
+                continue
+            blk = f[np.ix_(ind, ind)]
+            # facsym(i,j) = fock(ind(i),ind(j)) for i >= j, then hermitian fill: lower triangle drives
+            low = np.tril(blk)
+            herm = low + np.conj(np.tril(low, -1)).T
+            w, v = heev_upper(herm)
+            eps[ind] = w
+            U[np.ix_(ind, ind)] = v
+    return U, eps
+
+
+def ci_rotate(s: System, dets: List[int], U_act: np.ndarray, c: np.ndarray) -> np.ndarray:
+    """tracic (trac.F90:76-156) with detsc (sdet.F90:58-110): ds(k,k~) = det(U[occ_k, occ_k~]),
+    then solve ds c' = c (ZGESV)."""
+    occ = [[t for t in range(s.nact) if (I >> t) & 1] for I in dets]
+    nd = len(dets)
+    ds = np.zeros((nd, nd), dtype=np.complex128)
+    for a in range(nd):
+        oa = occ[a]
+        for b in range(nd):
+            ds[a, b] = np.linalg.det(U_act[np.ix_(oa, occ[b])]) if s.nelec else 1.0
+    return np.linalg.solve(ds, c)
+
+
+# ======================================================================================
+# Transformation (module_intra.F90, tramo.F90)
+# ======================================================================================
+def transform_block(blk: np.ndarray, U: np.ndarray, r: List[Tuple[int, int]]) -> np.ndarray:
+    """(i'j'|k'l') = sum conj(U_ii') U_jj' conj(U_kk') U_ll' (ij|kl)  (module_intra.F90:130-277);
+    the |x| <= 1e-15 write cutoff of each pass is applied after the full transformation."""
+    Ui = U[r[0][0]:r[0][1], r[0][0]:r[0][1]]
+    Uj = U[r[1][0]:r[1][1], r[1][0]:r[1][1]]
+    Uk = U[r[2][0]:r[2][1], r[2][0]:r[2][1]]
+    Ul = U[r[3][0]:r[3][1], r[3][0]:r[3][1]]
+    x = np.einsum("ijkl,lL->ijkL", blk, Ul, optimize=True)
+    x = np.einsum("ijkL,kK->ijKL", x, np.conj(Uk), optimize=True)
+    x = np.einsum("ijKL,jJ->iJKL", x, Uj, optimize=True)
+    x = np.einsum("iJKL,iI->IJKL", x, np.conj(Ui), optimize=True)
+    x[np.abs(x) <= INTRA_CUTOFF] = 0.0
+    return x
+
+
+# ======================================================================================
+# Subspace solver core (shared by A-G)
+# ======================================================================================
+def solve_block(S: np.ndarray, B: np.ndarray, Vcols: np.ndarray, alphas: np.ndarray):
+    """S eigendecomposition with the 1e-8 cutoff (cdiag + ccutoff, cutoff.F90:37-70),
+    X = U lambda^-1/2 (ulambda_s_half.F90:14-75), B' = X^H B X, its eigendecomposition,
+    then e2 = -sum |W^H X^H v|^2/(alpha+w), sumc2 = sum |.|^2/(alpha+w)^2
+    (solve_A_subspace.F90:149-261).  Vcols: (dimn, nouter)."""
+    ws, us = heev_upper(S)
+    keep = ws >= SMAT_LIN_DEP_THRESHOLD
+    dimm = int(np.count_nonzero(keep))
+    if dimm == 0:
+        return 0.0, 0.0, 0
+    X = us[:, keep] * (ws[keep] ** -0.5)
+    Bp = np.conj(X).T @ B @ X
+    wb, W = heev_upper(Bp)
+    vc1 = np.conj(W).T @ (np.conj(X).T @ Vcols)          # (dimm, nouter)
+    den = alphas[None, :] + wb[:, None]
+    a2 = np.abs(vc1) ** 2
+    e2 = -float(np.sum(a2 / den))
+    sc2 = float(np.sum(a2 / den ** 2))
+    return e2, sc2, dimm
+
+
+def herm_from_upper(A: np.ndarray) -> np.ndarray:
+    u = np.triu(A)
+    return u + np.conj(np.triu(u, 1)).T
+
+
+# ======================================================================================
+# Driver
+# ======================================================================================
+@dataclasses.dataclass
+class Result:
+    casci_energies: np.ndarray
+    e0: float
+    e2: Dict[str, float]
+    sumc2: Dict[str, float]
+    e2_sym: Dict[str, Dict[int, float]]
+    total_energy: float
+    ndet: int
+    eps: np.ndarray
+
+    @property
+    def e2_total(self) -> float:
+        return float(sum(self.e2.values()))
+
+    @property
+    def sumc2_total(self) -> float:
+        return float(sum(self.sumc2.values()))
+
+
+def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool = False) -> Result:
+    """r4dcasci (r4dcasci.F90:1-134) followed by r4dcaspt2_tra (r4dcaspt2_tra.F90:4-482)."""
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    ints = Integrals(s)
+    g_occ = ints.occ_block()
+    dets = enumerate_dets(s)
+    ndet = len(dets)
+    if ndet == 0:
+        raise ValueError("no CASCI configuration for this totsym")
+    H = casmat(s, dets, g_occ)
+    w, v = heev_upper(H)
+    eigen = w + s.ecore                                           # casci.F90:72
+    iroot = s.selectroot - 1
+    c0 = v[:, iroot].copy()
+    fs = FullSpace(s, dets)
+
+    # ---- Fock matrix of the CASCI state and its diagonalisation
+    rd_c = RDM(fs, c0, order=1)
+    f = fock_casci(s, ints, g_occ, rd_c.D1)
+    U, eps = fock_diag(s, f)
+    c = ci_rotate(s, dets, U[ni:nmoc, ni:nmoc], c0)
+    eps_act = eps[ni:nmoc]
+    rd = RDM(fs, c, eps_act=eps_act, order=3)
+    e0 = float(np.real(np.sum(np.diag(rd.D1) * eps_act)))          # calce0.F90:4-50
+
+    # ---- transformed integral classes (local indices)
+    cls = {}
+    patterns = {"A1": (2, 1, 2, 2), "A2": (2, 1, 1, 1), "B": (2, 1, 2, 1), "C1": (3, 2, 2, 2),
+                "C2": (3, 2, 1, 1), "C3": (3, 1, 1, 2), "D1": (3, 1, 2, 2), "D2": (3, 2, 2, 1),
+                "D3": (3, 1, 1, 1), "E": (3, 1, 2, 1), "F": (3, 2, 3, 2), "G": (3, 1, 3, 2),
+                "H": (3, 1, 3, 1)}
+    for name, pat in patterns.items():
+        cls[name] = transform_block(ints.block(pat), U, [ints.rng(p) for p in pat])
+    hU = np.conj(U).T @ s.h @ U                                       # tramo1 (tramo.F90:4-68)
+
+    res_e2, res_sc2, res_sym = {}, {}, {}
+    kw = dict(s=s, rd=rd, cls=cls, hU=hU, eps=eps, e0=e0)
+    for X in SUBSPACES:
+        skip = (X in "ABDEGH" and ni == 0) or (X in "CDEFGH" and ns == 0)
+        if skip or X not in subspaces:
+            continue
+        e2, sc2, per = SOLVERS[X](**kw)
+        res_e2[X], res_sc2[X], res_sym[X] = e2, sc2, per
+        if verbose:
+            print(f" e2{X.lower()} = {e2: .15e}  sumc2,{X.lower()} = {sc2: .15e}")
+    e2all = sum(res_e2.values())
+    sumc2 = sum(res_sc2.values())
+    total = e2all + float(eigen[iroot]) - s.eshift * sumc2               # r4dcaspt2_tra.F90:437-442
+    return Result(casci_energies=eigen, e0=e0, e2=res_e2, sumc2=res_sc2, e2_sym=res_sym,
+                  total_energy=total, ndet=ndet, eps=eps)
+
+
+# --------------------------------------------------------------------------------------
+# helpers for the solvers
+# --------------------------------------------------------------------------------------
+def _md(s, a, b):
+    return int(s.multb_d[a - 1, b - 1])
+
+
+def _ms(s, a, b):
+    return int(s.multb_s[a - 1, b - 1])
+
+
+def _kp(x):
+    """irrep of the Kramers partner: irpamo - (-1)**mod(irpamo,2)."""
+    return x + 1 if x % 2 == 1 else x - 1
+
+
+# --------------------------------------------------------------------------------------
+# A: E_ti E_uv|0>  (solve_A_subspace.F90:26-678)
+# --------------------------------------------------------------------------------------
+def solve_A(s, rd, cls, hU, eps, e0):
+    ni, na = s.ninact, s.nact
+    gi = lambda t: ni + t
+    A1, A2 = cls["A1"], cls["A2"]
+    # effh(p,i) = tramo1(p,i) + sum_{k != i}[(pi|kk) - (pk|ki)]   (vAmat 546-631)
+    effh = hU[ni:ni + na, :ni].copy()
+    for i in range(ni):
+        for k in range(ni):
+            if k == i:
+                continue
+            effh[:, i] += A2[:, i, k, k] - A2[:, k, k, i]
+    D1, D2, D3 = rd.D1, rd.D2, rd.D3
+    V = (-np.einsum("piqr,vuptqr->ituv", A1, D3, optimize=True)
+         + np.einsum("tipq,vupq->ituv", A1, D2, optimize=True)
+         + np.einsum("ti,vu->ituv", effh, D1, optimize=True)
+         - np.einsum("pi,vupt->ituv", effh, D2, optimize=True))
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    for isym in range(1, s.nsymrpa + 1):
+        ind = []
+        for x in range(na):
+            for y in range(na):
+                for z in range(na):
+                    if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[gi(x)], isym), _md(s, s.irpamo[gi(y)], s.irpamo[gi(z)])) == 1:
+                        ind.append((x, y, z))
+        if not ind:
+            continue
+        ind = np.array(ind)
+        x, y, z = ind[:, 0], ind[:, 1], ind[:, 2]
+        t, u, v = x, y, z
+        Sm = (-D3[z[:, None], y[:, None], t[None, :], x[:, None], u[None, :], v[None, :]]
+              + (t[None, :] == x[:, None]) * D2[z[:, None], y[:, None], u[None, :], v[None, :]])
+        e = eps[gi(u)] + eps[gi(t)] - eps[gi(v)]
+        Bm = (-rd.T3[z[:, None], y[:, None], t[None, :], x[:, None], u[None, :], v[None, :]]
+              + (t[None, :] == x[:, None]) * rd.T2[z[:, None], y[:, None], u[None, :], v[None, :]]
+              + Sm * e[None, :])
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [i for i in range(ni) if s.nsymrpa == 1 or s.irpamo[i] == isym]
+        if not outer:
+            # the reference still diagonalises; no outer index contributes
+            per[isym] = 0.0
+            continue
+        Vc = V[np.array(outer)][:, x, y, z].T
+        alphas = np.array([-eps[i] - e0 + s.eshift for i in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# B: E_ti E_uj|0>, t>u, i>j  (solve_B_subspace.F90:27-591)
+# --------------------------------------------------------------------------------------
+def solve_B(s, rd, cls, hU, eps, e0):
+    ni, na = s.ninact, s.nact
+    gi = lambda t: ni + t
+    Bc = cls["B"]                       # (t i|u j)
+    D1, D2 = rd.D1, rd.D2
+    # V(ij;x,y) for i>j from records R[t,u] = (t i|u j)   (vBmat_complex)
+    R = np.einsum("tiuj->ijtu", Bc)
+    V = (R - np.einsum("ijyx->ijxy", R)
+         + np.einsum("ijyu,ux->ijxy", R, D1) - np.einsum("ijxu,uy->ijxy", R, D1)
+         - np.einsum("ijty,tx->ijxy", R, D1)
+         + np.einsum("ijtu,txuy->ijxy", R, D2, optimize=True))
+    pairs = [(i, j) for i in range(ni) for j in range(i)]
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    for isym in range(1, s.nsymrpa + 1):
+        ind = [(t, u) for t in range(na) for u in range(t)
+               if s.nsymrpa == 1 or _md(s, s.irpamo[gi(t)], _kp(s.irpamo[gi(u)])) == isym]
+        if not ind:
+            continue
+        ind = np.array(ind)
+        x, y = ind[:, 0], ind[:, 1]
+        t, u = x[None, :], y[None, :]
+        X_, Y_ = x[:, None], y[:, None]
+        Sm = (D2[t, X_, u, Y_] - (t == X_) * D1[u, Y_] - (u == Y_) * D1[t, X_] - (t == Y_) * D1[u, X_]
+              + ((t == X_) & (u == Y_)))
+        e = eps[gi(x)] + eps[gi(y)]
+        Bm = (rd.T2[t, X_, u, Y_] - (t == X_) * rd.T1[u, Y_] - (u == Y_) * rd.T1[t, X_] - (t == Y_) * rd.T1[u, X_]
+              + ((t == X_) & (u == Y_)) * e0 + Sm * e[None, :])
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [(i, j) for (i, j) in pairs
+                 if s.nsymrpa == 1 or _ms(s, _md(s, _kp(s.irpamo[i]), s.irpamo[j]), isym) == 1]
+        if not outer:
+            continue
+        Vc = np.stack([V[i, j][x, y] for (i, j) in outer], axis=1)
+        alphas = np.array([-eps[i] - eps[j] - e0 + s.eshift for (i, j) in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# C: E_at E_uv|0>  (solve_C_subspace.F90:26-658)
+# --------------------------------------------------------------------------------------
+def solve_C(s, rd, cls, hU, eps, e0):
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    gi = lambda t: ni + t
+    C1, C2, C3 = cls["C1"], cls["C2"], cls["C3"]
+    effh = hU[nmoc:nmoc + ns, ni:nmoc].copy()                 # tramo1(a,t)
+    effh -= np.einsum("aqqp->ap", C1)
+    effh += np.einsum("apkk->ap", C2)
+    effh -= np.einsum("akkp->ap", C3)
+    effh[np.abs(effh) < EFFH_C_SKIP] = 0.0
+    D2, D3 = rd.D2, rd.D3
+    V = (np.einsum("ajkl,vutjkl->atuv", C1, D3, optimize=True)
+         + np.einsum("ap,vutp->atuv", effh, D2, optimize=True))
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    for isym in range(1, s.nsymrpa + 1):
+        ind = []
+        for x in range(na):
+            for y in range(na):
+                for z in range(na):
+                    if s.nsymrpa == 1 or _ms(s, _md(s, isym, s.irpamo[gi(x)]), _md(s, s.irpamo[gi(y)], s.irpamo[gi(z)])) == 1:
+                        ind.append((x, y, z))
+        if not ind:
+            continue
+        ind = np.array(ind)
+        x, y, z = ind[:, 0], ind[:, 1], ind[:, 2]
+        t, u, v = x[None, :], y[None, :], z[None, :]
+        Sm = D3[z[:, None], y[:, None], x[:, None], t, u, v]
+        e = eps[gi(y)] - eps[gi(z)] - eps[gi(x)]
+        Bm = rd.T3[z[:, None], y[:, None], x[:, None], t, u, v] + Sm * e[None, :]
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [a for a in range(ns) if s.nsymrpa == 1 or s.irpamo[nmoc + a] == isym]
+        if not outer:
+            continue
+        Vc = V[np.array(outer)][:, x, y, z].T
+        alphas = np.array([eps[nmoc + a] - e0 + s.eshift for a in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# D: E_ai E_tu|0>  (solve_D_subspace.F90:25-609)
+# --------------------------------------------------------------------------------------
+def solve_D(s, rd, cls, hU, eps, e0):
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    gi = lambda t: ni + t
+    D1c, D2c, D3c = cls["D1"], cls["D2"], cls["D3"]
+    effh = hU[nmoc:nmoc + ns, :ni].copy()
+    for i in range(ni):
+        for k in range(ni):
+            if k == i:
+                continue
+            effh[:, i] += D3c[:, i, k, k] - D3c[:, k, k, i]
+    D1, D2 = rd.D1, rd.D2
+    V = (np.einsum("aikl,utkl->aitu", D1c, D2, optimize=True)
+         - np.einsum("ajki,utkj->aitu", D2c, D2, optimize=True)
+         + np.einsum("ai,ut->aitu", effh, D1))
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    for isym in range(1, s.nsymrpa + 1):
+        ind = [(t, u) for t in range(na) for u in range(na)
+               if s.nsymrpa == 1 or _md(s, s.irpamo[gi(t)], s.irpamo[gi(u)]) == isym]
+        if not ind:
+            continue
+        ind = np.array(ind)
+        x, y = ind[:, 0], ind[:, 1]
+        t, u = x[None, :], y[None, :]
+        Sm = D2[y[:, None], x[:, None], t, u]
+        e = eps[gi(x)] - eps[gi(y)]
+        Bm = rd.T2[y[:, None], x[:, None], t, u] + Sm * e[None, :]
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [(a, i) for a in range(ns) for i in range(ni)
+                 if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[nmoc + a], s.irpamo[i]), isym) == 1]
+        if not outer:
+            continue
+        Vc = np.stack([V[a, i][x, y] for (a, i) in outer], axis=1)
+        alphas = np.array([eps[nmoc + a] - eps[i] - e0 + s.eshift for (a, i) in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# E: E_ti E_aj|0>, i>j  (solve_E_subspace.F90:26-476)
+# --------------------------------------------------------------------------------------
+def solve_E(s, rd, cls, hU, eps, e0):
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    gi = lambda t: ni + t
+    Ec = cls["E"]                              # (a i|p j)
+    D1 = rd.D1
+    # V(a,i>j;t) = -(ai|tj) + (aj|ti) + sum_p D1[t,p][(ai|pj) - (aj|pi)]
+    W = Ec - np.einsum("ajpi->aipj", Ec)       # (ai|pj) - (aj|pi)
+    V = -np.einsum("aitj->aijt", W) + np.einsum("tp,aipj->aijt", D1, W)
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    trip = [(i, j, a) for i in range(ni) for j in range(i) for a in range(ns)]
+    for isym in range(1, s.nsymrpa + 1):
+        ind = np.array([t for t in range(na) if s.irpamo[gi(t)] == isym], dtype=np.int64)
+        if len(ind) == 0:
+            continue
+        Sm = np.eye(len(ind)) - D1[ind[None, :], ind[:, None]]
+        Bm = -rd.T1[ind[None, :], ind[:, None]] + np.eye(len(ind)) * e0 + Sm * eps[gi(ind)][None, :]
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [(i, j, a) for (i, j, a) in trip
+                 if s.nsymrpa == 1 or _ms(s, _md(s, isym, s.irpamo[i]), _md(s, s.irpamo[nmoc + a], s.irpamo[j])) == 1]
+        if not outer:
+            continue
+        Vc = np.stack([V[a, i, j][ind] for (i, j, a) in outer], axis=1)
+        alphas = np.array([eps[nmoc + a] - eps[i] - eps[j] - e0 + s.eshift for (i, j, a) in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# F: E_at E_bu|0>, a>b, t>u  (solve_F_subspace.F90:26-544)
+# --------------------------------------------------------------------------------------
+def solve_F(s, rd, cls, hU, eps, e0):
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    gi = lambda t: ni + t
+    Fc = cls["F"]                              # (a p|b q)
+    D1, D2 = rd.D1, rd.D2
+    V = (np.einsum("apbq,xpyq->abxy", Fc, D2, optimize=True)
+         - np.einsum("aybq,xq->abxy", Fc, D1, optimize=True))
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    pairs = [(a, b) for a in range(ns) for b in range(a)]
+    for isym in range(1, s.nsymrpa + 1):
+        ind = [(t, u) for t in range(na) for u in range(t)
+               if s.nsymrpa == 1 or _md(s, _kp(s.irpamo[gi(u)]), s.irpamo[gi(t)]) == isym]
+        if not ind:
+            continue
+        ind = np.array(ind)
+        vv, xx = ind[:, 0], ind[:, 1]             # row (v,x), column (t,u)
+        t, u = vv[None, :], xx[None, :]
+        V_, X_ = vv[:, None], xx[:, None]
+        Sm = D2[V_, t, X_, u] - (X_ == t) * D1[V_, u]
+        e = -eps[gi(xx)] - eps[gi(vv)]
+        Bm = rd.T2[V_, t, X_, u] - (X_ == t) * rd.T1[V_, u] + Sm * e[None, :]
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [(a, b) for (a, b) in pairs
+                 if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[nmoc + a], _kp(s.irpamo[nmoc + b])), isym) == 1]
+        if not outer:
+            continue
+        Vc = np.stack([V[a, b][vv, xx] for (a, b) in outer], axis=1)
+        alphas = np.array([eps[nmoc + a] + eps[nmoc + b] - e0 + s.eshift for (a, b) in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# G: E_ai E_bt|0>, a>b  (solve_G_subspace.F90:26-469)
+# --------------------------------------------------------------------------------------
+def solve_G(s, rd, cls, hU, eps, e0):
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    gi = lambda t: ni + t
+    Gc = cls["G"]                              # (a i|b p)
+    D1 = rd.D1
+    W = Gc - np.einsum("biap->aibp", Gc)       # (ai|bp) - (bi|ap)
+    V = np.einsum("tp,aibp->abit", D1, W)
+    e2_tot, sc2_tot, per = 0.0, 0.0, {}
+    trip = [(a, b, i) for a in range(ns) for b in range(a) for i in range(ni)]
+    for isym in range(1, s.nsymrpa + 1):
+        ind = np.array([t for t in range(na) if s.irpamo[gi(t)] == isym], dtype=np.int64)
+        if len(ind) == 0:
+            continue
+        Sm = D1[ind[:, None], ind[None, :]]
+        Bm = rd.T1[ind[:, None], ind[None, :]] - Sm * eps[gi(ind)][:, None]
+        Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
+        outer = [(a, b, i) for (a, b, i) in trip
+                 if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[nmoc + b], isym), _md(s, s.irpamo[nmoc + a], s.irpamo[i])) == 1]
+        if not outer:
+            continue
+        Vc = np.stack([V[a, b, i][ind] for (a, b, i) in outer], axis=1)
+        alphas = np.array([-eps[i] + eps[nmoc + a] + eps[nmoc + b] - e0 + s.eshift for (a, b, i) in outer])
+        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
+        per[isym] = e2
+        e2_tot += e2
+        sc2_tot += sc2
+    return e2_tot, sc2_tot, per
+
+
+# --------------------------------------------------------------------------------------
+# H: E_ai E_bj|0>, a>b, i>j  (solve_H_subspace.F90:23-191)
+# --------------------------------------------------------------------------------------
+def solve_H(s, rd, cls, hU, eps, e0):
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    nmoc = ni + na
+    Hc = cls["H"]                              # (a i|b j)
+    V = Hc - np.einsum("ajbi->aibj", Hc)       # (ai|bj) - (aj|bi)
+    e2, sc2 = 0.0, 0.0
+    ea = eps[nmoc:nmoc + ns]
+    ei = eps[:ni]
+    a_, b_ = np.tril_indices(ns, -1)
+    i_, j_ = np.tril_indices(ni, -1)
+    Vab = V[a_[:, None], i_[None, :], b_[:, None], j_[None, :]]
+    den = ea[a_][:, None] + ea[b_][:, None] - ei[i_][None, :] - ei[j_][None, :] + s.eshift
+    ir = s.irpamo
+    sy = np.array([[_ms(s, _md(s, ir[nmoc + a], ir[i]), _md(s, ir[nmoc + b], ir[j])) for (i, j) in zip(i_, j_)]
+                   for (a, b) in zip(a_, b_)]) if len(a_) and len(i_) else np.zeros((len(a_), len(i_)))
+    mask = sy == 1
+    c = Vab / den
+    sc2 = float(np.sum((np.abs(c) ** 2)[mask]))
+    e2 = -float(np.sum((np.abs(Vab) ** 2 / den)[mask]))
+    return e2, sc2, {}
+
+
+SOLVERS = {"A": solve_A, "B": solve_B, "C": solve_C, "D": solve_D,
+           "E": solve_E, "F": solve_F, "G": solve_G, "H": solve_H}
