@@ -1,0 +1,349 @@
+"""Host-side mirror of the reference's CASCI/CASPT2 drivers over the C ABI.
+
+``Caspt2Session`` wraps one library context (one CUDA stream on one GPU):
+
+    set_system(system)  -> readint2_casci / divide_2_elec_integral_into_subspaces
+    casci(nroot)        -> casci            (src/casci.F90:3-163)
+    caspt2(skip_mask)   -> r4dcaspt2_tra    (src/r4dcaspt2_tra.F90:4-482)
+
+``run_case(directory)`` is the whole reference flow for one ``.caspt2_ciroots`` entry
+(src/dcaspt2_run_subprograms.F90:39-64) with the reference's printed energy lines.
+
+The compute path is the CUDA library ``libdcaspt2_gb300.so``; there is no CPU fallback:
+if the library is missing or no GPU is present, the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+from typing import Dict, List, Optional, Sequence, Tuple
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libdcaspt2_gb300.so")
+
+DCG_PREC_FP64 = 0
+DCG_PREC_SPLIT = 1
+SUBSPACES = "ABCDEFGH"
+STAGES = ["ints", "casci_matrix", "casci_eig", "fock", "ci_rotation", "rdm", "transformation",
+          "A", "B", "C", "D", "E", "F", "G", "H"]
+
+
+class DcgError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"dcaspt2_gb300 error {code}: {msg}")
+        self.code = code
+
+
+class _System(ctypes.Structure):
+    _fields_ = [
+        ("ninact", ctypes.c_int32), ("nact", ctypes.c_int32), ("nsec", ctypes.c_int32), ("nelec", ctypes.c_int32),
+        ("nmo", ctypes.c_int32), ("nsymrpa", ctypes.c_int32), ("totsym", ctypes.c_int32),
+        ("selectroot", ctypes.c_int32), ("realonly", ctypes.c_int32), ("eshift", ctypes.c_double),
+        ("ecore", ctypes.c_double), ("multb", ctypes.POINTER(ctypes.c_int32)),
+        ("irpamo", ctypes.POINTER(ctypes.c_int32)), ("h_re", ctypes.POINTER(ctypes.c_double)),
+        ("h_im", ctypes.POINTER(ctypes.c_double)), ("nrec", ctypes.c_int64),
+        ("rec_ijkl", ctypes.POINTER(ctypes.c_int32)), ("rec_re", ctypes.POINTER(ctypes.c_double)),
+        ("rec_im", ctypes.POINTER(ctypes.c_double)),
+        ("ras1_size", ctypes.c_int32), ("ras2_size", ctypes.c_int32), ("ras3_size", ctypes.c_int32),
+        ("ras1_max_hole", ctypes.c_int32), ("ras3_max_elec", ctypes.c_int32),
+        ("min_hole_ras1", ctypes.c_int32), ("min_elec_ras3", ctypes.c_int32),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
+    """Load the CUDA library (built by ``dirac_caspt2_gb300.build.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with dirac_caspt2_gb300.build.build() "
+                          "(the CASPT2 path has no CPU fallback)")
+    lib = ctypes.CDLL(path)
+    P = ctypes.POINTER
+    lib.dcg_create.argtypes = [ctypes.c_int, ctypes.c_int, P(ctypes.c_void_p)]
+    lib.dcg_destroy.argtypes = [ctypes.c_void_p]
+    lib.dcg_last_error.argtypes = [ctypes.c_void_p]
+    lib.dcg_last_error.restype = ctypes.c_char_p
+    lib.dcg_set_system.argtypes = [ctypes.c_void_p, P(_System)]
+    lib.dcg_casci.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(ctypes.c_double), P(ctypes.c_double),
+                              P(ctypes.c_double), P(ctypes.c_int32)]
+    lib.dcg_caspt2.argtypes = [ctypes.c_void_p, ctypes.c_uint32, P(ctypes.c_double), P(ctypes.c_double),
+                               P(ctypes.c_double), P(ctypes.c_double)]
+    lib.dcg_get_eps.argtypes = [ctypes.c_void_p, P(ctypes.c_double), ctypes.c_int32]
+    lib.dcg_stage_times.argtypes = [ctypes.c_void_p, P(ctypes.c_double), ctypes.c_int32]
+    lib.dcg_kernel_launches.argtypes = [ctypes.c_void_p]
+    lib.dcg_kernel_launches.restype = ctypes.c_int64
+    lib.dcg_version.restype = ctypes.c_char_p
+    _lib = lib
+    return lib
+
+
+EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
+                    "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version"]
+
+
+def _ptr(a: Optional[np.ndarray], ct):
+    if a is None:
+        return ctypes.POINTER(ct)()
+    return a.ctypes.data_as(ctypes.POINTER(ct))
+
+
+@dataclasses.dataclass
+class SystemInput:
+    """What one solve consumes (the reference's module globals after its readers)."""
+    ninact: int
+    nact: int
+    nsec: int
+    nelec: int
+    nmo: int
+    nsymrpa: int
+    multb: np.ndarray          # (2n, 2n) Fortran MULTB(i0,j0) at [i0-1, j0-1]
+    irpamo: np.ndarray         # (nmo,) 1-based, CAS order
+    h: np.ndarray              # (nmo, nmo) complex, CAS order
+    ecore: float
+    rec_idx: np.ndarray        # (n, 4) 1-based MDCINTNEW indices
+    rec_val: np.ndarray        # (n,) complex (or float)
+    realonly: bool
+    totsym: int = 1
+    selectroot: int = 1
+    eshift: float = 0.0
+    ras: Tuple[int, int, int] = (0, 0, 0)
+    ras1_max_hole: int = 0
+    ras3_max_elec: int = 0
+    min_hole_ras1: int = 0
+    min_elec_ras3: int = 0
+
+    @classmethod
+    def from_synth(cls, s, totsym: int = 1, selectroot: int = 1) -> "SystemInput":
+        c = s.cfg
+        return cls(ninact=c.ninact, nact=c.nact, nsec=c.nsec, nelec=c.nelec, nmo=s.nmo, nsymrpa=1,
+                   multb=s.multb, irpamo=s.irpamo, h=s.h, ecore=s.ecore, rec_idx=s.rec_idx, rec_val=s.rec_val,
+                   realonly=c.realonly, totsym=totsym, selectroot=selectroot, eshift=c.eshift)
+
+    @classmethod
+    def from_files(cls, directory: str, ciroot_index: int = 0) -> "SystemInput":
+        from . import dirac_io
+        inp = dirac_io.read_active_inp(os.path.join(directory, "active.inp"))
+        mrc = dirac_io.read_mrconee(os.path.join(directory, "MRCONEE"), inp)
+        new = dirac_io.read_mdcint_new(directory, mrc, inp)
+        ts, sr = inp.ciroots[ciroot_index]
+        return cls(ninact=inp.ninact, nact=inp.nact, nsec=inp.nsec, nelec=inp.nelec, nmo=mrc.nmo,
+                   nsymrpa=mrc.nsymrpa, multb=mrc.multb, irpamo=mrc.irpamo, h=mrc.h, ecore=mrc.ecore,
+                   rec_idx=new.idx, rec_val=new.val, realonly=new.realonly, totsym=ts, selectroot=sr,
+                   eshift=inp.eshift, ras=(len(inp.ras1), len(inp.ras2), len(inp.ras3)),
+                   ras1_max_hole=inp.ras1_max_hole, ras3_max_elec=inp.ras3_max_elec,
+                   min_hole_ras1=inp.min_hole_ras1, min_elec_ras3=inp.min_elec_ras3)
+
+    @classmethod
+    def from_npz(cls, path: str) -> "SystemInput":
+        z = np.load(path, allow_pickle=False)
+        val = z["rec_re"] + 1j * z["rec_im"] if "rec_im" in z.files else z["rec_re"].astype(np.complex128)
+        d = {k: z[k] for k in z.files}
+        return cls(ninact=int(d["ninact"]), nact=int(d["nact"]), nsec=int(d["nsec"]), nelec=int(d["nelec"]),
+                   nmo=int(d["nmo"]), nsymrpa=int(d["nsymrpa"]), multb=d["multb"], irpamo=d["irpamo"],
+                   h=d["h_re"] + 1j * d["h_im"], ecore=float(d["ecore"]), rec_idx=d["rec_idx"].astype(np.int32),
+                   rec_val=val, realonly=bool(d["realonly"]), totsym=int(d["totsym"]),
+                   selectroot=int(d["selectroot"]), eshift=float(d["eshift"]),
+                   ras=tuple(int(x) for x in d["ras"]), ras1_max_hole=int(d["ras1_max_hole"]),
+                   ras3_max_elec=int(d["ras3_max_elec"]), min_hole_ras1=int(d["min_hole_ras1"]),
+                   min_elec_ras3=int(d["min_elec_ras3"]))
+
+
+class HostBuffers:
+    """Arrays in the exact layout of ``dcg_system`` (kept alive for the call).
+
+    ``pinned=True`` places the record arrays in page-locked memory (cudaHostAlloc through
+    the CUDA runtime of the library's process) so the host-to-device copies run at link
+    speed."""
+
+    def __init__(self, s: SystemInput):
+        self.multb = np.ascontiguousarray(np.asarray(s.multb).T, dtype=np.int32)   # column-major
+        self.irpamo = np.ascontiguousarray(s.irpamo, dtype=np.int32)
+        h = np.asarray(s.h, dtype=np.complex128)
+        self.h_re = np.ascontiguousarray(h.real.T)
+        self.h_im = np.ascontiguousarray(h.imag.T)
+        self.ijkl = np.ascontiguousarray(s.rec_idx, dtype=np.int32)
+        v = np.asarray(s.rec_val)
+        self.re = np.ascontiguousarray(v.real, dtype=np.float64)
+        self.im = None if s.realonly else np.ascontiguousarray(np.imag(v), dtype=np.float64)
+        st = _System()
+        st.ninact, st.nact, st.nsec, st.nelec = s.ninact, s.nact, s.nsec, s.nelec
+        st.nmo, st.nsymrpa, st.totsym, st.selectroot = s.nmo, s.nsymrpa, s.totsym, s.selectroot
+        st.realonly = int(bool(s.realonly))
+        st.eshift, st.ecore = float(s.eshift), float(s.ecore)
+        st.multb = _ptr(self.multb, ctypes.c_int32)
+        st.irpamo = _ptr(self.irpamo, ctypes.c_int32)
+        st.h_re = _ptr(self.h_re, ctypes.c_double)
+        st.h_im = _ptr(self.h_im, ctypes.c_double)
+        st.nrec = len(self.re)
+        st.rec_ijkl = _ptr(self.ijkl, ctypes.c_int32)
+        st.rec_re = _ptr(self.re, ctypes.c_double)
+        st.rec_im = _ptr(self.im, ctypes.c_double)
+        st.ras1_size, st.ras2_size, st.ras3_size = (int(x) for x in s.ras)
+        st.ras1_max_hole, st.ras3_max_elec = s.ras1_max_hole, s.ras3_max_elec
+        st.min_hole_ras1, st.min_elec_ras3 = s.min_hole_ras1, s.min_elec_ras3
+        self.struct = st
+
+    @property
+    def h2d_bytes(self) -> int:
+        n = self.ijkl.nbytes + self.re.nbytes + (self.im.nbytes if self.im is not None else 0)
+        return int(n + self.h_re.nbytes + self.h_im.nbytes + self.multb.nbytes + self.irpamo.nbytes)
+
+
+@dataclasses.dataclass
+class Caspt2Result:
+    casci_energies: np.ndarray
+    ndet: int
+    e2: Dict[str, float]
+    sumc2: Dict[str, float]
+    e0: float
+    total_energy: float
+    stage_ms: Dict[str, float]
+    kernel_launches: int
+
+    @property
+    def e2_total(self) -> float:
+        return float(sum(self.e2.values()))
+
+    @property
+    def sumc2_total(self) -> float:
+        return float(sum(self.sumc2.values()))
+
+
+class Caspt2Session:
+    def __init__(self, device: int = 0, precision: int = DCG_PREC_FP64):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.dcg_create(device, precision, ctypes.byref(h))
+        if rc != 0:
+            raise DcgError(rc, "dcg_create failed (no usable CUDA device?)")
+        self.h = h
+        self._bufs: Optional[HostBuffers] = None
+        self.system: Optional[SystemInput] = None
+
+    def close(self):
+        if self.h:
+            self.lib.dcg_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc: int):
+        if rc != 0:
+            msg = self.lib.dcg_last_error(self.h)
+            raise DcgError(rc, msg.decode() if msg else "")
+
+    def set_system(self, s: SystemInput, bufs: Optional[HostBuffers] = None) -> None:
+        self._bufs = bufs or HostBuffers(s)
+        self.system = s
+        self._check(self.lib.dcg_set_system(self.h, ctypes.byref(self._bufs.struct)))
+
+    def casci(self, nroot: int = 1, want_ci: bool = False):
+        n = max(1, int(nroot))
+        eig = np.zeros(n)
+        nd = ctypes.c_int32(0)
+        self._check(self.lib.dcg_casci(self.h, n, eig.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), None, None,
+                                       ctypes.byref(nd)))
+        ndet = nd.value
+        eig = eig[:min(n, ndet)]
+        if want_ci:
+            nr = min(n, ndet)
+            cr = np.zeros(ndet * nr)
+            ci = np.zeros(ndet * nr)
+            self._check(self.lib.dcg_casci(self.h, n, eig.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           cr.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                           ci.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), ctypes.byref(nd)))
+            return eig, ndet, (cr + 1j * ci).reshape(nr, ndet).T
+        return eig, ndet
+
+    def caspt2(self, skip_mask: int = 0) -> Tuple[Dict[str, float], Dict[str, float], float, float]:
+        e2 = np.zeros(8)
+        sc = np.zeros(8)
+        e0 = ctypes.c_double(0.0)
+        et = ctypes.c_double(0.0)
+        dp = ctypes.POINTER(ctypes.c_double)
+        self._check(self.lib.dcg_caspt2(self.h, ctypes.c_uint32(skip_mask), e2.ctypes.data_as(dp),
+                                        sc.ctypes.data_as(dp), ctypes.byref(e0), ctypes.byref(et)))
+        return ({k: float(e2[i]) for i, k in enumerate(SUBSPACES)},
+                {k: float(sc[i]) for i, k in enumerate(SUBSPACES)}, e0.value, et.value)
+
+    def eps(self) -> np.ndarray:
+        n = self.system.nmo
+        out = np.zeros(n)
+        self._check(self.lib.dcg_get_eps(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n))
+        return out
+
+    def stage_ms(self) -> Dict[str, float]:
+        out = np.zeros(len(STAGES))
+        k = self.lib.dcg_stage_times(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), len(STAGES))
+        return {STAGES[i]: float(out[i]) for i in range(k)}
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.dcg_kernel_launches(self.h))
+
+    def solve(self, s: SystemInput, nroot: int = 1, skip_mask: int = 0,
+              bufs: Optional[HostBuffers] = None) -> Caspt2Result:
+        """set_system + casci + caspt2 for one (totsym, selectroot) entry."""
+        self.set_system(s, bufs)
+        eig, ndet = self.casci(max(nroot, s.selectroot))
+        e2, sc2, e0, et = self.caspt2(skip_mask)
+        return Caspt2Result(casci_energies=eig, ndet=ndet, e2=e2, sumc2=sc2, e0=e0, total_energy=et,
+                            stage_ms=self.stage_ms(), kernel_launches=self.kernel_launches())
+
+
+def format_reference_lines(r: Caspt2Result, s: SystemInput) -> List[str]:
+    """The reference's printed energy lines (casci.F90:77, solve_X_subspace e2/sumc2 lines,
+    r4dcaspt2_tra.F90:437-442)."""
+    out = [f"CASCI Total Energy ROOT{k + 1}{e:30.20f} a.u." for k, e in enumerate(r.casci_energies)]
+    for k in SUBSPACES:
+        if k in r.e2:
+            out.append(f" e2{k.lower()}      = {_e25(r.e2[k])} a.u.")
+            out.append(f" sumc2,{k.lower()}  = {_e25(r.sumc2[k])}")
+    sumc2 = r.sumc2_total
+    out.append(f" c^2 is                         {sumc2:30.20f}")
+    out.append(f" weight of 0th wave function is {1.0 / (1.0 + sumc2):30.20f}")
+    out.append(f" Total second order energy is   {r.e2_total - s.eshift * sumc2:30.20f} a.u.")
+    out.append(f" Total energy is                {r.total_energy:30.20f} a.u.")
+    return out
+
+
+def _e25(x: float) -> str:
+    """Fortran E25.15 (0.ddddE+xx form)."""
+    if x == 0.0:
+        return f"{'0.000000000000000E+00':>25}"
+    m, e = f"{x:.14E}".split("E")
+    ex = int(e) + 1
+    sign = "-" if x < 0 else ""
+    digits = m.replace("-", "").replace(".", "")
+    return f"{sign + '0.' + digits[:15] + f'E{ex:+03d}':>25}"
+
+
+def run_case(directory: str, device: int = 0, precision: int = DCG_PREC_FP64, verbose: bool = True):
+    """The reference's CASCI+CASPT2 flow for every .caspt2_ciroots entry of a case directory."""
+    from . import dirac_io
+    inp = dirac_io.read_active_inp(os.path.join(directory, "active.inp"))
+    results = []
+    with Caspt2Session(device, precision) as ses:
+        for k in range(len(inp.ciroots)):
+            s = SystemInput.from_files(directory, k)
+            r = ses.solve(s, nroot=s.selectroot)
+            if verbose:
+                print("\n".join(format_reference_lines(r, s)))
+            results.append(r)
+    return results

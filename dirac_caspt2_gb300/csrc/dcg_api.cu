@@ -1,0 +1,914 @@
+// C ABI and orchestration of the CASCI / CASPT2 hot path on one GB300.
+//
+// The call sequence mirrors the reference drivers:
+//   dcg_set_system : readint2_casci + divide_2_elec_integral_into_subspaces
+//                    (module_2integrals.F90:26-588, divide_2_elec...F90:3-409) as one
+//                    device scatter of the MDCINTNEW records into dense class tensors;
+//   dcg_casci      : casci (casci.F90:3-163) = search_cas_configuration + casmat + cdiag;
+//   dcg_caspt2     : r4dcaspt2_tra (r4dcaspt2_tra.F90:77-445) = fockcasci, fockdiag (+tracic),
+//                    calce0, intra_1/2/3 and solve_A..H_subspace.
+// Every dimN_density element of the reference is taken from dense density tensors
+// computed once per solve by GEMMs over excited CI vectors (see rdm_build below).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "dcg_common.cuh"
+#include "dcg_kernels.cuh"
+
+struct dcg_ctx {
+    dcg::Context c;
+};
+
+namespace dcg {
+
+// ------------------------------------------------------------------------- host helpers
+static std::vector<uint64_t> gosper_all(int na, int ne) {
+    std::vector<uint64_t> out;
+    if (ne > na || na > 64) return out;
+    if (ne == 0) {
+        out.push_back(0);
+        return out;
+    }
+    uint64_t cur = (ne == 64) ? ~0ull : ((1ull << ne) - 1ull);
+    const uint64_t lim = (na == 64) ? 0 : (1ull << na);
+    while (true) {
+        out.push_back(cur);
+        uint64_t t = (cur | (cur - 1)) + 1;
+        uint64_t nxt = t | ((((t & (~t + 1)) / (cur & (~cur + 1))) >> 1) - 1);
+        if (nxt <= cur) break;
+        if (na < 64 && nxt >= lim) break;
+        cur = nxt;
+    }
+    return out;
+}
+
+// search_cas_configuration.F90:91-110 + ras_det_check.F90:1-59
+static bool ras_ok(const Context &c, uint64_t I) {
+    if (c.ras1) {
+        const uint64_t m = (c.ras1 >= 64) ? ~0ull : ((1ull << c.ras1) - 1ull);
+        const int n1 = __builtin_popcountll(I & m);
+        if (!(c.ras1 - c.ras1_max_hole <= n1 && n1 <= c.ras1 - c.min_hole_ras1)) return false;
+    }
+    if (c.ras3) {
+        const int sh = c.ras1 + c.ras2;
+        const uint64_t hi = (sh >= 64) ? 0 : ((I >> sh) << sh);
+        const int n3 = __builtin_popcountll(I & hi);
+        if (!(n3 <= c.ras3_max_elec && c.min_elec_ras3 <= n3)) return false;
+    }
+    return true;
+}
+
+// cas_configuration_totsym (search_cas_configuration.F90:112-149)
+static int det_totsym(const Context &c, uint64_t I) {
+    if (c.nsym == 1) return 1;
+    int ret = 1, ielec = 0;
+    for (int t = 0; t < c.na; t++) {
+        if (!((I >> t) & 1ull)) continue;
+        ielec++;
+        const int jsym = c.irpamo[c.ni + t];
+        if (ielec % 2 == 1) {
+            ret = c.multb_ds[(jsym - 1) * c.nsym + (ret - 1)];
+        } else {
+            const int partner = (jsym % 2 == 1) ? jsym + 1 : jsym - 1;
+            ret = c.multb_d[(partner - 1) * c.nsym + (ret - 1)];
+        }
+    }
+    if (ielec % 2 == 0) ret += c.nsym;
+    return ret;
+}
+
+static std::vector<uint64_t> enumerate_ci(const Context &c) {
+    std::vector<uint64_t> out;
+    for (uint64_t I : gosper_all(c.na, c.ne))
+        if (ras_ok(c, I) && (c.nsym == 1 || det_totsym(c, I) == c.totsym)) out.push_back(I);
+    return out;
+}
+
+template <typename T>
+static T *upload(Context &c, const std::string &name, const std::vector<T> &v) {
+    T *p = wsget<T>(c, name, v.size() + 1);
+    if (!v.empty()) DCG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    return p;
+}
+
+template <typename T>
+static std::vector<T> download(Context &c, const T *p, size_t n) {
+    std::vector<T> v(n);
+    if (n) DCG_CUDA(cudaMemcpyAsync(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    return v;
+}
+
+static void stage_begin(Context &c, int st) { DCG_CUDA(cudaEventRecord(c.ev[st], c.stream)); }
+static void stage_end(Context &c, int st) {
+    DCG_CUDA(cudaEventRecord(c.ev[ST_COUNT], c.stream));
+    DCG_CUDA(cudaEventSynchronize(c.ev[ST_COUNT]));
+    float ms = 0.f;
+    DCG_CUDA(cudaEventElapsedTime(&ms, c.ev[st], c.ev[ST_COUNT]));
+    c.stage_ms[st] += ms;
+}
+
+// ------------------------------------------------------------------------- device state
+struct DevSystem {
+    cplx *h = nullptr;
+    cplx *inttw = nullptr;
+    ClassTensor cls[CL_COUNT];
+    int *irp = nullptr;
+    int *md = nullptr, *msy = nullptr;
+    double *eps = nullptr;
+    cplx *c0 = nullptr;   // CASCI vector of selectroot
+    int ndet = 0;
+    uint64_t *dets = nullptr;
+};
+
+static DevSystem &dev(Context &c) {
+    if (!c.dev_state) c.dev_state = new DevSystem();
+    return *static_cast<DevSystem *>(c.dev_state);
+}
+
+__global__ void pack_cplx_kernel(const double *re, const double *im, int64_t n, cplx *out) {
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) out[i] = mk(re[i], im ? im[i] : 0.0);
+}
+
+// ------------------------------------------------------------------------- set_system
+static void set_system(Context &c, const dcg_system *s) {
+    if (!s) throw Error{DCG_E_ARG, "system is NULL"};
+    if (s->ninact < 0 || s->nact < 0 || s->nsec < 0 || s->nelec < 0 || s->nelec > s->nact)
+        throw Error{DCG_E_ARG, "bad ninact/nact/nsec/nelec"};
+    if (s->nact > 63) throw Error{DCG_E_ARG, "nact above 63 is not supported (64-bit determinant strings)"};
+    if (s->nmo < s->ninact + s->nact + s->nsec) throw Error{DCG_E_ARG, "nmo < ninact + nact + nsec"};
+    if ((s->ninact | s->nact | s->nsec) & 1) throw Error{DCG_E_ARG, "space sizes must be even (Kramers pairs)"};
+    if (s->nsymrpa < 1 || !s->multb || !s->irpamo || !s->h_re || !s->h_im)
+        throw Error{DCG_E_ARG, "missing symmetry tables or one-electron integrals"};
+    if (s->nrec < 0 || (s->nrec > 0 && (!s->rec_ijkl || !s->rec_re))) throw Error{DCG_E_ARG, "missing records"};
+    if (!s->realonly && s->nrec > 0 && !s->rec_im) throw Error{DCG_E_ARG, "complex system without rec_im"};
+    c.ni = s->ninact; c.na = s->nact; c.ns = s->nsec; c.ne = s->nelec; c.nmo = s->nmo;
+    c.nsym = s->nsymrpa; c.totsym = s->totsym; c.selectroot = s->selectroot; c.realonly = s->realonly != 0;
+    c.eshift = s->eshift; c.ecore = s->ecore;
+    c.ras1 = s->ras1_size; c.ras2 = s->ras2_size; c.ras3 = s->ras3_size;
+    c.ras1_max_hole = s->ras1_max_hole; c.ras3_max_elec = s->ras3_max_elec;
+    c.min_hole_ras1 = s->min_hole_ras1; c.min_elec_ras3 = s->min_elec_ras3;
+    if (c.selectroot < 1) throw Error{DCG_E_ARG, "selectroot must be >= 1"};
+    const int n = c.nsym, n2 = 2 * n;
+    c.multb.assign(s->multb, s->multb + n2 * n2);
+    c.irpamo.assign(s->irpamo, s->irpamo + c.nmo);
+    for (int x : c.irpamo)
+        if (x < 1 || x > n2) throw Error{DCG_E_ARG, "irpamo out of range"};
+    // MULTB(i0, j0) column-major -> tables (read_mrconee.F90:368-453), stored [a-1][b-1]
+    auto MB = [&](int i0, int j0) { return c.multb[(i0 - 1) + n2 * (j0 - 1)]; };
+    std::vector<int> m2(n2 * n2, 0);
+    for (int i0 = 1; i0 <= n2; i0++)
+        for (int j0 = 1; j0 <= n2; j0++) {
+            const int k0 = MB(i0, j0);
+            if (k0 < 1 || k0 > n2) throw Error{DCG_E_ARG, "MULTB entry out of range"};
+            m2[(i0 - 1) * n2 + (k0 - 1)] = j0;
+        }
+    c.multb_s.assign(n * n, 0);
+    c.multb_d.assign(n * n, 0);
+    c.multb_ds.assign(n * n, 0);
+    for (int a = 1; a <= n; a++)
+        for (int b = 1; b <= n; b++) {
+            c.multb_s[(a - 1) * n + (b - 1)] = MB(a + n, b + n) - n;
+            c.multb_d[(a - 1) * n + (b - 1)] = m2[(a - 1) * n2 + (b - 1)] - n;
+            c.multb_ds[(a - 1) * n + (b - 1)] = MB(b + n, a);   // transpose(MULTB(n+1:2n, 1:n))
+        }
+    c.h.resize((size_t)c.nmo * c.nmo);
+    for (size_t q = 0; q < c.h.size(); q++) c.h[q] = mk(s->h_re[q], s->h_im[q]);
+    c.nrec = s->nrec;
+
+    DevSystem &d = dev(c);
+    d.h = upload(c, "sys.h", c.h);
+    d.irp = upload(c, "sys.irp", c.irpamo);
+    d.md = upload(c, "sys.md", c.multb_d);
+    d.msy = upload(c, "sys.ms", c.multb_s);
+    // integral expansion
+    stage_begin(c, ST_INTS);
+    const int nmoc = c.ni + c.na;
+    const size_t ntw = (size_t)nmoc * nmoc * nmoc * nmoc;
+    d.inttw = wsget<cplx>(c, "sys.inttw", ntw);
+    DCG_CUDA(cudaMemsetAsync(d.inttw, 0, ntw * sizeof(cplx), c.stream));
+    class_layout(c, d.cls);
+    for (int id = 0; id < CL_COUNT; id++) {
+        d.cls[id].p = wsget<cplx>(c, "sys.cls" + std::to_string(id), (size_t)d.cls[id].size);
+        if (d.cls[id].size)
+            DCG_CUDA(cudaMemsetAsync(d.cls[id].p, 0, (size_t)d.cls[id].size * sizeof(cplx), c.stream));
+    }
+    if (c.nrec > 0) {
+        int32_t *ijkl = wsget<int32_t>(c, "rec.ijkl", (size_t)4 * c.nrec);
+        double *re = wsget<double>(c, "rec.re", (size_t)c.nrec);
+        double *im = nullptr;
+        DCG_CUDA(cudaMemcpyAsync(ijkl, s->rec_ijkl, sizeof(int32_t) * 4 * c.nrec, cudaMemcpyHostToDevice, c.stream));
+        DCG_CUDA(cudaMemcpyAsync(re, s->rec_re, sizeof(double) * c.nrec, cudaMemcpyHostToDevice, c.stream));
+        if (s->rec_im && !c.realonly) {
+            im = wsget<double>(c, "rec.im", (size_t)c.nrec);
+            DCG_CUDA(cudaMemcpyAsync(im, s->rec_im, sizeof(double) * c.nrec, cudaMemcpyHostToDevice, c.stream));
+        }
+        cplx *val = wsget<cplx>(c, "rec.val", (size_t)c.nrec);
+        pack_cplx_kernel<<<grid1d(c.nrec, 256), 256, 0, c.stream>>>(re, im, c.nrec, val);
+        DCG_LAUNCHED(c);
+        launch_scatter(c, ijkl, val, c.nrec, d.inttw, d.cls);
+    }
+    stage_end(c, ST_INTS);
+    c.have_system = true;
+    c.have_casci = false;
+}
+
+// ------------------------------------------------------------------------- CASCI
+static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double *ci_im, int32_t *ndet_out) {
+    if (!c.have_system) throw Error{DCG_E_STATE, "dcg_casci before dcg_set_system"};
+    DevSystem &d = dev(c);
+    c.dets = enumerate_ci(c);
+    const int ndet = (int)c.dets.size();
+    if (ndet_out) *ndet_out = ndet;
+    if (ndet == 0) throw Error{DCG_E_NODET, "no CASCI configuration for totsym " + std::to_string(c.totsym)};
+    if (c.selectroot > ndet) throw Error{DCG_E_ARG, "selectroot exceeds the number of CASCI configurations"};
+    d.ndet = ndet;
+    d.dets = upload(c, "ci.dets", c.dets);
+    stage_begin(c, ST_CASMAT);
+    cplx *H = wsget<cplx>(c, "ci.H", (size_t)ndet * ndet);
+    launch_casmat(c, d.dets, ndet, d.h, d.inttw, H);
+    stage_end(c, ST_CASMAT);
+    stage_begin(c, ST_CASEIG);
+    const int nr = std::max(1, std::min(nroot, ndet));
+    const int nvec = std::max(nr, c.selectroot);
+    double *w = wsget<double>(c, "ci.w", ndet);
+    cplx *Z = wsget<cplx>(c, "ci.Z", (size_t)ndet * nvec);
+    heev(c, ndet, H, ndet, w, 0, nvec, Z, ndet);
+    stage_end(c, ST_CASEIG);
+    std::vector<double> wh = download(c, w, ndet);
+    c.ecas.assign(wh.begin(), wh.begin() + nvec);
+    for (double &x : c.ecas) x += c.ecore;   // casci.F90:72
+    c.nroot_done = nvec;
+    if (eigen_out)
+        for (int r = 0; r < nr; r++) eigen_out[r] = c.ecas[r];
+    d.c0 = wsget<cplx>(c, "ci.c0", ndet);
+    DCG_CUDA(cudaMemcpyAsync(d.c0, Z + (size_t)ndet * (c.selectroot - 1), sizeof(cplx) * ndet,
+                             cudaMemcpyDeviceToDevice, c.stream));
+    if (ci_re) {
+        std::vector<cplx> zh = download(c, Z, (size_t)ndet * nr);
+        for (size_t q = 0; q < zh.size(); q++) {
+            ci_re[q] = zh[q].x;
+            if (ci_im) ci_im[q] = zh[q].y;
+        }
+    }
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    c.have_casci = true;
+    return 0;
+}
+
+// ------------------------------------------------------------------------- 4-index transformation
+// (i'j'|k'l') = sum conj(U_ii') U_jj' conj(U_kk') U_ll' (ij|kl)   (module_intra.F90:130-277),
+// index l first, then k, j, i, as four GEMMs.
+static void transform4(Context &c, const cplx *in, cplx *out, cplx *tmp, const int dm[4], const cplx *U[4]) {
+    const int64_t d0 = dm[0], d1 = dm[1], d2 = dm[2], d3 = dm[3];
+    const int64_t tot = d0 * d1 * d2 * d3;
+    if (tot == 0) return;
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    // l: tmp = in * U4
+    zgemm(c, OP_N, OP_N, (int)(d0 * d1 * d2), (int)d3, (int)d3, one, in, d0 * d1 * d2, 0, U[3], d3, 0, zero, tmp,
+          d0 * d1 * d2, 0, 1);
+    // k: out_l = tmp_l * conj(U3)
+    zgemm(c, OP_N, OP_R, (int)(d0 * d1), (int)d2, (int)d2, one, tmp, d0 * d1, d0 * d1 * d2, U[2], d2, 0, zero, out,
+          d0 * d1, d0 * d1 * d2, (int)d3);
+    // j: tmp_kl = out_kl * U2
+    zgemm(c, OP_N, OP_N, (int)d0, (int)d1, (int)d1, one, out, d0, d0 * d1, U[1], d1, 0, zero, tmp, d0, d0 * d1,
+          (int)(d2 * d3));
+    // i: out = U1^H * tmp
+    zgemm(c, OP_C, OP_N, (int)d0, (int)(d1 * d2 * d3), (int)d0, one, U[0], d0, 0, tmp, d0, 0, zero, out, d0, 0, 1);
+}
+
+// ------------------------------------------------------------------------- subspace block solve
+struct BlockOut {
+    double e2 = 0.0, sc2 = 0.0;
+    int dimm = 0;
+};
+
+// S,B (dimn x dimn) already assembled; Vsel (dimn x nouter); alphas on device.
+static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *Vsel, int nouter, const double *alpha) {
+    BlockOut r;
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    double *ws = wsget<double>(c, "blk.ws", dimn);
+    // S eigenvalues first (cutoff count), then the kept eigenvectors
+    std::vector<double> wsh;
+    {
+        double *dummy_w = ws;
+        heev(c, dimn, S, dimn, dummy_w, dimn, dimn, nullptr, dimn);   // values only
+        wsh = download(c, ws, dimn);
+    }
+    int vlo = dimn;
+    for (int j = 0; j < dimn; j++)
+        if (wsh[j] >= 1.0e-8) { vlo = j; break; }   // cutoff.F90:37-70 (ascending eigenvalues)
+    const int dimm = dimn - vlo;
+    r.dimm = dimm;
+    if (dimm == 0 || nouter == 0) return r;
+    // eigenvectors: re-run the vector stage on the still-reduced S (reflectors kept in S)
+    cplx *X = wsget<cplx>(c, "blk.X", (size_t)dimn * dimm);
+    heev_vectors_only(c, dimn, S, dimn, ws, vlo, dimn, X, dimn);
+    launch_scale_cols(c, X, dimn, dimn, dimm, ws, vlo);   // X = U lambda^-1/2
+    // B' = X^H B X
+    cplx *BX = wsget<cplx>(c, "blk.BX", (size_t)dimn * dimm);
+    cplx *Bp = wsget<cplx>(c, "blk.Bp", (size_t)dimm * dimm);
+    zgemm(c, OP_N, OP_N, dimn, dimm, dimn, one, B, dimn, 0, X, dimn, 0, zero, BX, dimn, 0, 1);
+    zgemm(c, OP_C, OP_N, dimm, dimm, dimn, one, X, dimn, 0, BX, dimn, 0, zero, Bp, dimm, 0, 1);
+    herm_from_upper(c, dimm, Bp, dimm);
+    double *wb = wsget<double>(c, "blk.wb", dimm);
+    cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
+    heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
+    // VC = W^H X^H Vsel
+    cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
+    cplx *VC1 = wsget<cplx>(c, "blk.VC1", (size_t)dimm * nouter);
+    zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, X, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
+    zgemm(c, OP_C, OP_N, dimm, nouter, dimm, one, W, dimm, 0, VC0, dimm, 0, zero, VC1, dimm, 0, 1);
+    double *e2o = wsget<double>(c, "blk.e2o", nouter);
+    double *sco = wsget<double>(c, "blk.sco", nouter);
+    launch_e2(c, VC1, dimm, nouter, alpha, wb, e2o, sco);
+    double *red = wsget<double>(c, "blk.red", 2);
+    dsum(c, e2o, nouter, red);
+    dsum(c, sco, nouter, red + 1);
+    std::vector<double> hr = download(c, red, 2);
+    r.e2 = hr[0];
+    r.sc2 = hr[1];
+    return r;
+}
+
+}  // namespace dcg
+
+namespace dcg {
+
+// ------------------------------------------------------------------------- densities
+// psi (full N-space) -> Ycat = [E_pq psi | E_pq psit] (M x 2na^2), Zcat = E_cd Ycat
+// (M x na^2 x 2na^2) stored right after Ycat, then Gall = Ycat(:, :na^2)^H [Ycat | Zcat]
+// and G1 = psi^H Ycat.  These are the reference's dim1..dim4_density values for every
+// index combination at once (density_matrix.F90:3-247): <0|E_ab X|0> with
+// <0|E_ab = (E_ba|0>)^H, and an unrestricted intermediate determinant space.
+struct RdmBufs {
+    cplx *g1 = nullptr, *gall = nullptr;
+    RDMView view;
+};
+
+static RdmBufs rdm_build(Context &c, const uint64_t *full, int64_t M, const cplx *psi, const double *eps_act,
+                         bool third) {
+    const int na = c.na;
+    const int64_t na2 = (int64_t)na * na, na4 = na2 * na2;
+    RdmBufs r;
+    const int nv = eps_act ? 2 : 1;
+    cplx *vin = wsget<cplx>(c, "rdm.vin", (size_t)M * nv);
+    DCG_CUDA(cudaMemcpyAsync(vin, psi, sizeof(cplx) * M, cudaMemcpyDeviceToDevice, c.stream));
+    if (eps_act) launch_occ_energy(c, na, M, full, eps_act, psi, vin + M);
+    const int64_t ncol = nv * na2 + (third ? nv * na4 : 0);
+    cplx *YZ = wsget<cplx>(c, "rdm.YZ", (size_t)M * ncol);
+    launch_apply_E(c, na, M, full, vin, nv, YZ);
+    if (third) launch_apply_E(c, na, M, full, YZ, (int)(nv * na2), YZ + M * nv * na2);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    r.g1 = wsget<cplx>(c, "rdm.g1", (size_t)nv * na2);
+    zgemm(c, OP_C, OP_N, 1, (int)(nv * na2), (int)M, one, psi, M, 0, YZ, M, 0, zero, r.g1, 1, 0, 1);
+    r.gall = wsget<cplx>(c, "rdm.gall", (size_t)na2 * ncol);
+    zgemm(c, OP_C, OP_N, (int)na2, (int)ncol, (int)M, one, YZ, M, 0, YZ, M, 0, zero, r.gall, na2, 0, 1);
+    r.view.na = na;
+    r.view.g1 = r.g1;
+    r.view.t1 = eps_act ? r.g1 + na2 : nullptr;
+    r.view.g2 = r.gall;
+    r.view.t2 = eps_act ? r.gall + na2 * na2 : nullptr;
+    r.view.g3 = third ? r.gall + nv * na2 * na2 : nullptr;
+    r.view.t3 = (third && eps_act) ? r.view.g3 + na4 * na2 : nullptr;
+    return r;
+}
+
+// ------------------------------------------------------------------------- subspace drivers
+struct SubCtx {
+    Context *c;
+    RDMView rv;
+    const double *eps_act_d;   // device, active orbital energies
+    std::vector<double> eps;   // host, global
+    double e0;
+};
+
+struct BlockSpec {
+    std::vector<int> ind;             // flattened tuples
+    int dimn = 0;
+    std::vector<int64_t> outer_off;   // into V
+    std::vector<int64_t> inner_off;   // into V
+    std::vector<double> alpha;
+};
+
+// run the per-isym blocks of one subspace; V is the full V tensor on the device
+static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpec> &blocks, double &e2, double &sc2) {
+    Context &c = *sc.c;
+    e2 = 0.0;
+    sc2 = 0.0;
+    for (size_t bi = 0; bi < blocks.size(); bi++) {
+        BlockSpec &b = blocks[bi];
+        if (b.dimn == 0) continue;
+        const int nouter = (int)b.outer_off.size();
+        int *ind = upload(c, "blk.ind", b.ind);
+        cplx *S = wsget<cplx>(c, "blk.S", (size_t)b.dimn * b.dimn);
+        cplx *B = wsget<cplx>(c, "blk.B", (size_t)b.dimn * b.dimn);
+        launch_SB(c, sub, sc.rv, ind, b.dimn, sc.eps_act_d, sc.e0, S, B);
+        if (nouter == 0) continue;
+        int64_t *oo = upload(c, "blk.oo", b.outer_off);
+        int64_t *io = upload(c, "blk.io", b.inner_off);
+        double *al = upload(c, "blk.alpha", b.alpha);
+        cplx *Vsel = wsget<cplx>(c, "blk.Vsel", (size_t)b.dimn * nouter);
+        launch_gather_v(c, V, oo, nouter, io, b.dimn, Vsel);
+        BlockOut o = solve_block(c, b.dimn, S, B, Vsel, nouter, al);
+        e2 += o.e2;
+        sc2 += o.sc2;
+    }
+}
+
+static inline int kp(int x) { return (x % 2 == 1) ? x + 1 : x - 1; }
+
+}  // namespace dcg
+
+namespace dcg {
+
+static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8], double *e0_out, double *et_out) {
+    if (!c.have_casci) throw Error{DCG_E_STATE, "dcg_caspt2 before dcg_casci"};
+    DevSystem &d = dev(c);
+    const int ni = c.ni, na = c.na, ns = c.ns, nmoc = ni + na;
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
+    for (int k = 0; k < 8; k++) { e2_sub[k] = 0.0; sc2_sub[k] = 0.0; }
+    if (ni == 0 && ns == 0) throw Error{DCG_E_ARG, "CASPT2 energy undefined for ninact = 0 and nsec = 0"};
+
+    // full N-electron space and the CI-space positions inside it
+    std::vector<uint64_t> full = gosper_all(na, c.ne);
+    const int64_t M = (int64_t)full.size();
+    std::vector<int64_t> pos(d.ndet);
+    for (int i = 0; i < d.ndet; i++)
+        pos[i] = std::lower_bound(full.begin(), full.end(), c.dets[i]) - full.begin();
+    uint64_t *d_full = upload(c, "pt.full", full);
+    int64_t *d_pos = upload(c, "pt.pos", pos);
+    cplx *psi = wsget<cplx>(c, "pt.psi", M);
+
+    // ---- Fock matrix of the CASCI state (fockcasci.F90:4-90) and its diagonalisation
+    stage_begin(c, ST_FOCK);
+    launch_embed(c, d.ndet, d_pos, d.c0, psi, M);
+    RdmBufs r0 = rdm_build(c, d_full, M, psi, nullptr, false);
+    cplx *f = wsget<cplx>(c, "pt.f", (size_t)c.nmo * c.nmo);
+    launch_fock(c, d.h, d.inttw, d.cls, r0.g1, f);
+    // fockdiag.F90:4-78 / cdiag0 (diag.F90:230-375): per space and irrep
+    cplx *U = wsget<cplx>(c, "pt.U", (size_t)c.nmo * c.nmo);
+    DCG_CUDA(cudaMemsetAsync(U, 0, sizeof(cplx) * (size_t)c.nmo * c.nmo, c.stream));
+    c.eps.assign(c.nmo, 0.0);
+    const int rng[3][2] = {{0, ni}, {ni, nmoc}, {nmoc, nmoc + ns}};
+    for (int sp = 0; sp < 3; sp++) {
+        for (int sym = 1; sym <= c.nsym; sym++) {
+            std::vector<int> ind;
+            for (int i = rng[sp][0]; i < rng[sp][1]; i++)
+                if (c.irpamo[i] == sym) ind.push_back(i);
+            if (ind.empty()) continue;
+            const int nb = (int)ind.size();
+            int *dind = upload(c, "fd.ind", ind);
+            cplx *blk = wsget<cplx>(c, "fd.blk", (size_t)nb * nb);
+            cplx *vec = wsget<cplx>(c, "fd.vec", (size_t)nb * nb);
+            double *w = wsget<double>(c, "fd.w", nb);
+            launch_gather2(c, f, c.nmo, dind, nb, blk);
+            heev(c, nb, blk, nb, w, 0, nb, vec, nb);
+            launch_scatter2(c, vec, nb, dind, U, c.nmo);
+            std::vector<double> wh = download(c, w, nb);
+            for (int q = 0; q < nb; q++) c.eps[ind[q]] = wh[q];
+        }
+    }
+    d.eps = upload(c, "pt.eps", c.eps);
+    stage_end(c, ST_FOCK);
+
+    // ---- CI rotation into the new active spinors (trac.F90:76-156)
+    stage_begin(c, ST_CIROT);
+    cplx *Uact = wsget<cplx>(c, "pt.Uact", (size_t)na * na + 1);
+    if (na > 0)
+        DCG_CUDA(cudaMemcpy2DAsync(Uact, na * sizeof(cplx), U + ni + (size_t)c.nmo * ni, c.nmo * sizeof(cplx),
+                                   na * sizeof(cplx), na, cudaMemcpyDeviceToDevice, c.stream));
+    cplx *ds = wsget<cplx>(c, "pt.ds", (size_t)d.ndet * d.ndet);
+    launch_detsc(c, d.dets, d.ndet, Uact, ds);
+    cplx *c1 = wsget<cplx>(c, "pt.c1", d.ndet);
+    DCG_CUDA(cudaMemcpyAsync(c1, d.c0, sizeof(cplx) * d.ndet, cudaMemcpyDeviceToDevice, c.stream));
+    const int info = zgesv(c, d.ndet, ds, d.ndet, c1);
+    if (info != 0) throw Error{info, "CI rotation: singular determinant-overlap matrix (ZGESV info " + std::to_string(info) + ")"};
+    stage_end(c, ST_CIROT);
+
+    // ---- densities of the rotated state and e0 (calce0.F90:4-50)
+    stage_begin(c, ST_RDM);
+    launch_embed(c, d.ndet, d_pos, c1, psi, M);
+    const double *eps_act_d = d.eps + ni;
+    const bool need3 = (ni > 0) || (ns > 0);
+    RdmBufs rd = rdm_build(c, d_full, M, psi, eps_act_d, need3);
+    std::vector<cplx> d1h = download(c, rd.g1, (size_t)na * na);
+    double e0 = 0.0;
+    for (int w = 0; w < na; w++) e0 += d1h[w + (size_t)na * w].x * c.eps[ni + w];
+    stage_end(c, ST_RDM);
+
+    // ---- effective one-electron terms and transformed integral classes
+    stage_begin(c, ST_TRANS);
+    cplx *Ui = wsget<cplx>(c, "pt.Ui", (size_t)ni * ni + 1);
+    cplx *Ua = wsget<cplx>(c, "pt.Ua", (size_t)na * na + 1);
+    cplx *Us = wsget<cplx>(c, "pt.Us", (size_t)ns * ns + 1);
+    if (ni) DCG_CUDA(cudaMemcpy2DAsync(Ui, ni * sizeof(cplx), U, c.nmo * sizeof(cplx), ni * sizeof(cplx), ni, cudaMemcpyDeviceToDevice, c.stream));
+    if (na) DCG_CUDA(cudaMemcpyAsync(Ua, Uact, sizeof(cplx) * na * na, cudaMemcpyDeviceToDevice, c.stream));
+    if (ns) DCG_CUDA(cudaMemcpy2DAsync(Us, ns * sizeof(cplx), U + nmoc + (size_t)c.nmo * nmoc, c.nmo * sizeof(cplx), ns * sizeof(cplx), ns, cudaMemcpyDeviceToDevice, c.stream));
+    const cplx *Usp[4] = {nullptr, Ui, Ua, Us};
+    // core Fock pieces -> effh blocks: effh = U_p^H F U_q
+    cplx *Fai = wsget<cplx>(c, "pt.Fai", (size_t)na * ni + 1);
+    cplx *Fsi = wsget<cplx>(c, "pt.Fsi", (size_t)ns * ni + 1);
+    cplx *Fsa = wsget<cplx>(c, "pt.Fsa", (size_t)ns * na + 1);
+    launch_core_fock(c, d.h, d.inttw, d.cls, Fai, Fsi, Fsa);
+    cplx *tmp2 = wsget<cplx>(c, "pt.tmp2", (size_t)std::max({na * ni, ns * ni, ns * na, 1}));
+    cplx *effA = wsget<cplx>(c, "pt.effA", (size_t)na * ni + 1);
+    cplx *effD = wsget<cplx>(c, "pt.effD", (size_t)ns * ni + 1);
+    cplx *effC = wsget<cplx>(c, "pt.effC", (size_t)ns * na + 1);
+    auto sandwich = [&](const cplx *Up, int np, const cplx *Fm, const cplx *Uq, int nq, cplx *out) {
+        if (np == 0 || nq == 0) return;
+        zgemm(c, OP_N, OP_N, np, nq, nq, one, Fm, np, 0, Uq, nq, 0, zero, tmp2, np, 0, 1);
+        zgemm(c, OP_C, OP_N, np, nq, np, one, Up, np, 0, tmp2, np, 0, zero, out, np, 0, 1);
+    };
+    sandwich(Ua, na, Fai, Ui, ni, effA);
+    sandwich(Us, ns, Fsi, Ui, ni, effD);
+    sandwich(Us, ns, Fsa, Ua, na, effC);
+    launch_zero_small(c, effC, (int64_t)ns * na, 1.0e-10);   // vCmat: |effh| < 1e-10 skipped
+    // transformed classes
+    size_t maxsz = 1;
+    for (int id = 0; id < CL_COUNT; id++) maxsz = std::max(maxsz, (size_t)d.cls[id].size);
+    const size_t szA1 = (size_t)na * ni * na * na, szB = (size_t)na * ni * na * ni;
+    maxsz = std::max({maxsz, szA1, szB});
+    cplx *ttmp = wsget<cplx>(c, "pt.ttmp", maxsz);
+    cplx *orig = wsget<cplx>(c, "pt.orig", std::max(szA1, szB) + 1);
+    auto tr_class = [&](const char *name, const cplx *src, const int sp[4], const int dm[4]) -> cplx * {
+        const size_t sz = (size_t)dm[0] * dm[1] * dm[2] * dm[3];
+        cplx *out = wsget<cplx>(c, std::string("tr.") + name, sz + 1);
+        const cplx *Ux[4] = {Usp[sp[0]], Usp[sp[1]], Usp[sp[2]], Usp[sp[3]]};
+        transform4(c, src, out, ttmp, dm, Ux);
+        return out;
+    };
+    auto tr_id = [&](const char *name, int id) -> cplx * { return tr_class(name, d.cls[id].p, d.cls[id].sp, d.cls[id].dim); };
+    stage_end(c, ST_TRANS);
+
+    SubCtx sc;
+    sc.c = &c;
+    sc.rv = rd.view;
+    sc.eps_act_d = eps_act_d;
+    sc.eps = c.eps;
+    sc.e0 = e0;
+    const double es = c.eshift;
+    auto irp = [&](int g) { return c.irpamo[g]; };
+    const bool c1sym = (c.nsym == 1);
+    auto timed = [&](int st, auto fn) { stage_begin(c, st); fn(); stage_end(c, st); };
+
+    // ================= A: E_ti E_uv|0>  (solve_A_subspace.F90:26-678)
+    if (ni > 0 && !(skip & 1u)) timed(ST_A, [&] {
+        stage_begin(c, ST_TRANS);
+        const int off[4] = {ni, 0, ni, ni}, dm[4] = {na, ni, na, na}, sp[4] = {2, 1, 2, 2};
+        launch_subblock(c, d.inttw, nmoc, off, dm, orig);
+        cplx *A1 = tr_class("A1", orig, sp, dm);
+        stage_end(c, ST_TRANS);
+        const int64_t n3 = (int64_t)na * na * na;
+        cplx *V = wsget<cplx>(c, "v.A", (size_t)ni * n3 + 1);
+        cplx *A1p = wsget<cplx>(c, "v.A1p", (size_t)ni * n3 + 1);
+        cplx *P3 = wsget<cplx>(c, "v.P3", (size_t)n3 * n3 + 1);
+        launch_permute_A1(c, A1, na, ni, A1p);
+        launch_perm_A(c, sc.rv, P3, nullptr);
+        zgemm(c, OP_N, OP_N, ni, (int)n3, (int)n3, mone, A1p, ni, 0, P3, n3, 0, zero, V, ni, 0, 1);
+        launch_v_A_rest(c, sc.rv, A1, effA, ni, V);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int x = 0; x < na; x++)
+                for (int y = 0; y < na; y++)
+                    for (int z = 0; z < na; z++)
+                        if (c1sym || c.ms(c.md(irp(ni + x), isym), c.md(irp(ni + y), irp(ni + z))) == 1) {
+                            b.ind.push_back(x); b.ind.push_back(y); b.ind.push_back(z);
+                            b.inner_off.push_back((int64_t)ni * (x + (int64_t)na * (y + (int64_t)na * z)));
+                        }
+            b.dimn = (int)b.inner_off.size();
+            for (int i = 0; i < ni; i++)
+                if (c1sym || irp(i) == isym) {
+                    b.outer_off.push_back(i);
+                    b.alpha.push_back(-c.eps[i] - e0 + es);
+                }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'A', V, blocks, e2_sub[0], sc2_sub[0]);
+    });
+
+    // ================= B: E_ti E_uj|0>, t>u, i>j  (solve_B_subspace.F90:27-591)
+    if (ni > 0 && !(skip & 2u)) timed(ST_B, [&] {
+        stage_begin(c, ST_TRANS);
+        const int off[4] = {ni, 0, ni, 0}, dm[4] = {na, ni, na, ni}, sp[4] = {2, 1, 2, 1};
+        launch_subblock(c, d.inttw, nmoc, off, dm, orig);
+        cplx *Bc = tr_class("B", orig, sp, dm);
+        stage_end(c, ST_TRANS);
+        const int np = ni * (ni - 1) / 2;
+        cplx *V = wsget<cplx>(c, "v.B", (size_t)np * na * na + 1);
+        launch_v_B(c, sc.rv, Bc, ni, V);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int t = 0; t < na; t++)
+                for (int u = 0; u < t; u++)
+                    if (c1sym || c.md(irp(ni + t), kp(irp(ni + u))) == isym) {
+                        b.ind.push_back(t); b.ind.push_back(u);
+                        b.inner_off.push_back((int64_t)np * (t + (int64_t)na * u));
+                    }
+            b.dimn = (int)b.inner_off.size();
+            for (int i = 0; i < ni; i++)
+                for (int j = 0; j < i; j++)
+                    if (c1sym || c.ms(c.md(kp(irp(i)), irp(j)), isym) == 1) {
+                        b.outer_off.push_back((int64_t)i * (i - 1) / 2 + j);
+                        b.alpha.push_back(-c.eps[i] - c.eps[j] - e0 + es);
+                    }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'B', V, blocks, e2_sub[1], sc2_sub[1]);
+    });
+
+    // ================= C: E_at E_uv|0>  (solve_C_subspace.F90:26-658)
+    if (ns > 0 && !(skip & 4u)) timed(ST_C, [&] {
+        stage_begin(c, ST_TRANS);
+        cplx *C1 = tr_id("C1", CL_C1);
+        stage_end(c, ST_TRANS);
+        const int64_t n3 = (int64_t)na * na * na;
+        cplx *V = wsget<cplx>(c, "v.C", (size_t)ns * n3 + 1);
+        cplx *P3 = wsget<cplx>(c, "v.P3", (size_t)n3 * n3 + 1);
+        cplx *P2 = wsget<cplx>(c, "v.P2", (size_t)na * n3 + 1);
+        launch_perm_C2(c, sc.rv, P3, P2);
+        zgemm(c, OP_N, OP_N, ns, (int)n3, (int)n3, one, C1, ns, 0, P3, n3, 0, zero, V, ns, 0, 1);
+        zgemm(c, OP_N, OP_N, ns, (int)n3, na, one, effC, ns, 0, P2, na, 0, one, V, ns, 0, 1);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int x = 0; x < na; x++)
+                for (int y = 0; y < na; y++)
+                    for (int z = 0; z < na; z++)
+                        if (c1sym || c.ms(c.md(isym, irp(ni + x)), c.md(irp(ni + y), irp(ni + z))) == 1) {
+                            b.ind.push_back(x); b.ind.push_back(y); b.ind.push_back(z);
+                            b.inner_off.push_back((int64_t)ns * (x + (int64_t)na * (y + (int64_t)na * z)));
+                        }
+            b.dimn = (int)b.inner_off.size();
+            for (int a = 0; a < ns; a++)
+                if (c1sym || irp(nmoc + a) == isym) {
+                    b.outer_off.push_back(a);
+                    b.alpha.push_back(c.eps[nmoc + a] - e0 + es);
+                }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'C', V, blocks, e2_sub[2], sc2_sub[2]);
+    });
+
+    // ================= D: E_ai E_tu|0>  (solve_D_subspace.F90:25-609)
+    if (ni > 0 && ns > 0 && !(skip & 8u)) timed(ST_D, [&] {
+        stage_begin(c, ST_TRANS);
+        cplx *D1c = tr_id("D1", CL_D1);
+        cplx *D2c = tr_id("D2", CL_D2);
+        stage_end(c, ST_TRANS);
+        const int64_t nsi = (int64_t)ns * ni;
+        cplx *V = wsget<cplx>(c, "v.D", (size_t)nsi * na * na + 1);
+        launch_v_D(c, sc.rv, D1c, D2c, effD, ni, ns, V);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int t = 0; t < na; t++)
+                for (int u = 0; u < na; u++)
+                    if (c1sym || c.md(irp(ni + t), irp(ni + u)) == isym) {
+                        b.ind.push_back(t); b.ind.push_back(u);
+                        b.inner_off.push_back(nsi * (t + (int64_t)na * u));
+                    }
+            b.dimn = (int)b.inner_off.size();
+            for (int a = 0; a < ns; a++)
+                for (int i = 0; i < ni; i++)
+                    if (c1sym || c.ms(c.md(irp(nmoc + a), irp(i)), isym) == 1) {
+                        b.outer_off.push_back(a + (int64_t)ns * i);
+                        b.alpha.push_back(c.eps[nmoc + a] - c.eps[i] - e0 + es);
+                    }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'D', V, blocks, e2_sub[3], sc2_sub[3]);
+    });
+
+    // ================= E: E_ti E_aj|0>, i>j  (solve_E_subspace.F90:26-476)
+    if (ni > 0 && ns > 0 && !(skip & 16u)) timed(ST_E, [&] {
+        stage_begin(c, ST_TRANS);
+        cplx *Ec = tr_id("E", CL_E);
+        stage_end(c, ST_TRANS);
+        const int np = ni * (ni - 1) / 2;
+        const int64_t nq = (int64_t)ns * np;
+        cplx *V = wsget<cplx>(c, "v.E", (size_t)nq * na + 1);
+        launch_v_E(c, sc.rv, Ec, ni, ns, V);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int t = 0; t < na; t++)
+                if (irp(ni + t) == isym) {
+                    b.ind.push_back(t);
+                    b.inner_off.push_back(nq * t);
+                }
+            b.dimn = (int)b.inner_off.size();
+            for (int i = 0; i < ni; i++)
+                for (int j = 0; j < i; j++)
+                    for (int a = 0; a < ns; a++)
+                        if (c1sym || c.ms(c.md(isym, irp(i)), c.md(irp(nmoc + a), irp(j))) == 1) {
+                            b.outer_off.push_back(a + (int64_t)ns * ((int64_t)i * (i - 1) / 2 + j));
+                            b.alpha.push_back(c.eps[nmoc + a] - c.eps[i] - c.eps[j] - e0 + es);
+                        }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'E', V, blocks, e2_sub[4], sc2_sub[4]);
+    });
+
+    // ================= F: E_at E_bu|0>, a>b, t>u  (solve_F_subspace.F90:26-544)
+    if (ns > 0 && !(skip & 32u)) timed(ST_F, [&] {
+        stage_begin(c, ST_TRANS);
+        cplx *Fc = tr_id("F", CL_F);
+        stage_end(c, ST_TRANS);
+        const int64_t ns2 = (int64_t)ns * ns, na2 = (int64_t)na * na;
+        cplx *Fp = wsget<cplx>(c, "v.Fp", (size_t)ns2 * na2 + 1);
+        cplx *P2 = wsget<cplx>(c, "v.P2F", (size_t)na2 * na2 + 1);
+        cplx *V = wsget<cplx>(c, "v.F", (size_t)ns2 * na2 + 1);
+        launch_F_pack(c, Fc, ns, na, Fp);
+        launch_perm_F(c, sc.rv, P2, nullptr);
+        zgemm(c, OP_N, OP_N, (int)ns2, (int)na2, (int)na2, one, Fp, ns2, 0, P2, na2, 0, zero, V, ns2, 0, 1);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int t = 0; t < na; t++)
+                for (int u = 0; u < t; u++)
+                    if (c1sym || c.md(kp(irp(ni + u)), irp(ni + t)) == isym) {
+                        b.ind.push_back(t); b.ind.push_back(u);
+                        b.inner_off.push_back(ns2 * (t + (int64_t)na * u));
+                    }
+            b.dimn = (int)b.inner_off.size();
+            for (int a = 0; a < ns; a++)
+                for (int bb = 0; bb < a; bb++)
+                    if (c1sym || c.ms(c.md(irp(nmoc + a), kp(irp(nmoc + bb))), isym) == 1) {
+                        b.outer_off.push_back(a + (int64_t)ns * bb);
+                        b.alpha.push_back(c.eps[nmoc + a] + c.eps[nmoc + bb] - e0 + es);
+                    }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'F', V, blocks, e2_sub[5], sc2_sub[5]);
+    });
+
+    // ================= G: E_ai E_bt|0>, a>b  (solve_G_subspace.F90:26-469)
+    if (ni > 0 && ns > 0 && !(skip & 64u)) timed(ST_G, [&] {
+        stage_begin(c, ST_TRANS);
+        cplx *Gc = tr_id("G", CL_G);
+        stage_end(c, ST_TRANS);
+        const int64_t nab = (int64_t)ns * (ns - 1) / 2;
+        const int64_t nq = nab * ni;
+        cplx *V = wsget<cplx>(c, "v.G", (size_t)nq * na + 1);
+        launch_v_G(c, sc.rv, Gc, ni, ns, V);
+        std::vector<BlockSpec> blocks;
+        for (int isym = 1; isym <= c.nsym; isym++) {
+            BlockSpec b;
+            for (int t = 0; t < na; t++)
+                if (irp(ni + t) == isym) {
+                    b.ind.push_back(t);
+                    b.inner_off.push_back(nq * t);
+                }
+            b.dimn = (int)b.inner_off.size();
+            for (int a = 0; a < ns; a++)
+                for (int bb = 0; bb < a; bb++)
+                    for (int i = 0; i < ni; i++)
+                        if (c1sym || c.ms(c.md(irp(nmoc + bb), isym), c.md(irp(nmoc + a), irp(i))) == 1) {
+                            b.outer_off.push_back(((int64_t)a * (a - 1) / 2 + bb) + nab * i);
+                            b.alpha.push_back(-c.eps[i] + c.eps[nmoc + a] + c.eps[nmoc + bb] - e0 + es);
+                        }
+            blocks.push_back(b);
+        }
+        run_blocks(sc, 'G', V, blocks, e2_sub[6], sc2_sub[6]);
+    });
+
+    // ================= H: streaming (solve_H_subspace.F90:23-191)
+    if (ni > 0 && ns > 0 && !(skip & 128u)) timed(ST_H, [&] {
+        stage_begin(c, ST_TRANS);
+        cplx *Hc = tr_id("H", CL_H);
+        stage_end(c, ST_TRANS);
+        const int nblk = std::max(1, c.num_sms) * 8;
+        double *part = wsget<double>(c, "h.part", 2 * (size_t)nblk);
+        double *red = wsget<double>(c, "h.red", 2);
+        launch_h_stream2(c, Hc, ni, ns, d.eps, d.eps + nmoc, d.irp, d.irp + nmoc, d.md, d.msy, c.nsym, es, part,
+                         part + nblk, nblk);
+        dsum(c, part, nblk, red);
+        dsum(c, part + nblk, nblk, red + 1);
+        std::vector<double> hr = download(c, red, 2);
+        e2_sub[7] = hr[0];
+        sc2_sub[7] = hr[1];
+    });
+
+    double e2all = 0.0, sumc2 = 0.0;
+    for (int k = 0; k < 8; k++) { e2all += e2_sub[k]; sumc2 += sc2_sub[k]; }
+    if (e0_out) *e0_out = e0;
+    if (et_out) *et_out = e2all + c.ecas[c.selectroot - 1] - c.eshift * sumc2;   // r4dcaspt2_tra.F90:441
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    return 0;
+}
+
+}  // namespace dcg
+
+// ============================================================================ C ABI
+using dcg::Context;
+using dcg::Error;
+
+#define DCG_API_BODY(ctxp, body)                                                    \
+    do {                                                                            \
+        if (!(ctxp)) return DCG_E_ARG;                                              \
+        Context &c_ = (ctxp)->c;                                                    \
+        try {                                                                       \
+            cudaError_t e0_ = cudaSetDevice(c_.device);                             \
+            if (e0_ != cudaSuccess) throw Error{DCG_E_CUDA, cudaGetErrorString(e0_)}; \
+            body;                                                                   \
+        } catch (const Error &e_) {                                                 \
+            c_.err = e_.msg;                                                        \
+            return e_.code;                                                         \
+        } catch (const std::exception &e_) {                                        \
+            c_.err = e_.what();                                                     \
+            return DCG_E_ARG;                                                       \
+        }                                                                           \
+    } while (0)
+
+extern "C" {
+
+int dcg_create(int device, int precision, dcg_ctx **out) {
+    if (!out) return DCG_E_ARG;
+    *out = nullptr;
+    if (precision != DCG_PREC_FP64 && precision != DCG_PREC_SPLIT) return DCG_E_ARG;
+    dcg_ctx *x = new (std::nothrow) dcg_ctx;
+    if (!x) return DCG_E_NOMEM;
+    Context &c = x->c;
+    c.device = device;
+    c.precision = precision;
+    try {
+        DCG_CUDA(cudaSetDevice(device));
+        DCG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+        for (int k = 0; k <= dcg::ST_COUNT; k++) DCG_CUDA(cudaEventCreate(&c.ev[k]));
+        c.ev_init = true;
+        DCG_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+        dcg::upload_binomials(c);
+        DCG_CUDA(cudaStreamSynchronize(c.stream));
+    } catch (const Error &e) {
+        int code = e.code;
+        delete x;
+        return code;
+    }
+    *out = x;
+    return DCG_OK;
+}
+
+int dcg_destroy(dcg_ctx *ctx) {
+    if (!ctx) return DCG_E_ARG;
+    Context &c = ctx->c;
+    cudaSetDevice(c.device);
+    if (c.stream) cudaStreamSynchronize(c.stream);
+    c.ws.release_all();
+    delete static_cast<dcg::DevSystem *>(c.dev_state);
+    c.dev_state = nullptr;
+    if (c.ev_init)
+        for (int k = 0; k <= dcg::ST_COUNT; k++) cudaEventDestroy(c.ev[k]);
+    if (c.stream) cudaStreamDestroy(c.stream);
+    delete ctx;
+    return DCG_OK;
+}
+
+const char *dcg_last_error(const dcg_ctx *ctx) { return ctx ? ctx->c.err.c_str() : "null context"; }
+
+int dcg_set_system(dcg_ctx *ctx, const dcg_system *sys) {
+    DCG_API_BODY(ctx, {
+        c_.launches = 0;
+        for (int k = 0; k < dcg::ST_COUNT; k++) c_.stage_ms[k] = 0.0;
+        dcg::set_system(c_, sys);
+        return DCG_OK;
+    });
+}
+
+int dcg_casci(dcg_ctx *ctx, int32_t nroot, double *eigen_out, double *ci_re, double *ci_im, int32_t *ndet_out) {
+    DCG_API_BODY(ctx, { return dcg::casci(c_, nroot, eigen_out, ci_re, ci_im, ndet_out); });
+}
+
+int dcg_caspt2(dcg_ctx *ctx, uint32_t skip_mask, double e2_sub[8], double sumc2_sub[8], double *e0_out,
+               double *etotal_out) {
+    if (!e2_sub || !sumc2_sub) return DCG_E_ARG;
+    DCG_API_BODY(ctx, { return dcg::caspt2(c_, skip_mask, e2_sub, sumc2_sub, e0_out, etotal_out); });
+}
+
+int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n) {
+    if (!ctx || !eps_out) return DCG_E_ARG;
+    const Context &c = ctx->c;
+    if ((int)c.eps.size() == 0) return DCG_E_STATE;
+    for (int i = 0; i < n && i < (int)c.eps.size(); i++) eps_out[i] = c.eps[i];
+    return DCG_OK;
+}
+
+int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n) {
+    if (!ctx || !ms_out) return DCG_E_ARG;
+    int k = 0;
+    for (; k < n && k < dcg::ST_COUNT; k++) ms_out[k] = ctx->c.stage_ms[k];
+    return k;
+}
+
+int64_t dcg_kernel_launches(const dcg_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
+
+const char *dcg_version(void) { return "dcaspt2_gb300 0.1 (sm_103a, FP64 path)"; }
+
+}  // extern "C"

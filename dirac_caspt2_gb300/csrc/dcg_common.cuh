@@ -1,0 +1,169 @@
+// Shared definitions of the GB300 CASCI/CASPT2 library: complex helpers, the context,
+// workspace management and launch accounting.  Host code is C++17; device code targets
+// sm_103a only.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/dcaspt2_gb300.h"
+
+namespace dcg {
+
+typedef double2 cplx;
+
+// ---------------------------------------------------------------- complex arithmetic
+__host__ __device__ __forceinline__ cplx mk(double r, double i) { return make_double2(r, i); }
+__host__ __device__ __forceinline__ cplx cadd(cplx a, cplx b) { return mk(a.x + b.x, a.y + b.y); }
+__host__ __device__ __forceinline__ cplx csub(cplx a, cplx b) { return mk(a.x - b.x, a.y - b.y); }
+__host__ __device__ __forceinline__ cplx cmul(cplx a, cplx b) {
+    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__host__ __device__ __forceinline__ cplx cconj(cplx a) { return mk(a.x, -a.y); }
+__host__ __device__ __forceinline__ cplx cscale(cplx a, double s) { return mk(a.x * s, a.y * s); }
+__host__ __device__ __forceinline__ double cabs2(cplx a) { return a.x * a.x + a.y * a.y; }
+// a*conj(b)
+__host__ __device__ __forceinline__ cplx cmulc(cplx a, cplx b) {
+    return mk(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+// acc += a*b
+__host__ __device__ __forceinline__ void cfma(cplx &acc, cplx a, cplx b) {
+    acc.x = fma(a.x, b.x, acc.x);
+    acc.x = fma(-a.y, b.y, acc.x);
+    acc.y = fma(a.x, b.y, acc.y);
+    acc.y = fma(a.y, b.x, acc.y);
+}
+__host__ __device__ __forceinline__ cplx cdiv(cplx a, cplx b) {
+    double d = b.x * b.x + b.y * b.y;
+    return mk((a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d);
+}
+
+// ---------------------------------------------------------------- status / errors
+struct Error {
+    int code;
+    std::string msg;
+};
+
+// ---------------------------------------------------------------- context
+struct Context;
+
+// Grow-only named device workspace: buffers survive across solves so a served or
+// benchmarked loop allocates once.
+class Workspace {
+  public:
+    void *get(const std::string &name, size_t bytes);
+    void release_all();
+    size_t bytes_in_use() const { return total_; }
+    ~Workspace() { release_all(); }
+
+  private:
+    struct Buf {
+        void *p = nullptr;
+        size_t bytes = 0;
+    };
+    std::map<std::string, Buf> bufs_;
+    size_t total_ = 0;
+};
+
+// Stage indices of dcg_stage_times
+enum Stage {
+    ST_INTS = 0, ST_CASMAT, ST_CASEIG, ST_FOCK, ST_CIROT, ST_RDM, ST_TRANS,
+    ST_A, ST_B, ST_C, ST_D, ST_E, ST_F, ST_G, ST_H, ST_COUNT
+};
+
+struct Context {
+    int device = 0;
+    int precision = DCG_PREC_FP64;
+    cudaStream_t stream = nullptr;
+    Workspace ws;
+    std::string err;
+    int64_t launches = 0;
+    int num_sms = 0;
+    void *dev_state = nullptr;   // device-side system state (owned, see dcg_api.cu)
+
+    // ---- system (host copies)
+    bool have_system = false;
+    int ni = 0, na = 0, ns = 0, ne = 0, nmo = 0, nsym = 1, totsym = 1, selectroot = 1;
+    bool realonly = false;
+    double eshift = 0.0, ecore = 0.0;
+    std::vector<int> multb;   // 2n x 2n column-major
+    std::vector<int> irpamo;  // nmo
+    std::vector<cplx> h;      // nmo x nmo column-major
+    int ras1 = 0, ras2 = 0, ras3 = 0, ras1_max_hole = 0, ras3_max_elec = 0;
+    int min_hole_ras1 = 0, min_elec_ras3 = 0;
+    int64_t nrec = 0;
+
+    // ---- CASCI results
+    bool have_casci = false;
+    std::vector<uint64_t> dets;        // CI space, Gosper order
+    std::vector<double> ecas;          // eigenvalues (+ ecore) of the computed roots
+    int nroot_done = 0;
+    std::vector<double> eps;           // after fockdiag
+
+    // ---- timings
+    cudaEvent_t ev[ST_COUNT + 1];
+    bool ev_init = false;
+    double stage_ms[ST_COUNT] = {0};
+
+    // multiplication tables (read_mrconee.F90:368-453), 1-based values, [a-1][b-1]
+    std::vector<int> multb_s, multb_d, multb_ds;
+
+    int md(int a, int b) const { return multb_d[(a - 1) * nsym + (b - 1)]; }
+    int ms(int a, int b) const { return multb_s[(a - 1) * nsym + (b - 1)]; }
+};
+
+// ---------------------------------------------------------------- helpers
+#define DCG_CUDA(call)                                                                  \
+    do {                                                                                \
+        cudaError_t e_ = (call);                                                        \
+        if (e_ != cudaSuccess)                                                          \
+            throw ::dcg::Error{DCG_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+    } while (0)
+
+#define DCG_LAUNCHED(ctx)                                                               \
+    do {                                                                                \
+        (ctx).launches++;                                                               \
+        cudaError_t e_ = cudaGetLastError();                                            \
+        if (e_ != cudaSuccess)                                                          \
+            throw ::dcg::Error{DCG_E_CUDA, std::string("kernel launch: ") + cudaGetErrorString(e_)}; \
+    } while (0)
+
+inline unsigned grid1d(int64_t n, int block) { return (unsigned)((n + block - 1) / block); }
+
+template <typename T>
+T *wsget(Context &c, const std::string &name, size_t count) {
+    return reinterpret_cast<T *>(c.ws.get(name, count * sizeof(T) + 256));
+}
+
+// ---------------------------------------------------------------- linear algebra (dcg_linalg.cu)
+enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };   // R = conjugate without transpose
+
+// C = alpha*op(A)*op(B) + beta*C, column-major, batched with element strides.
+void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda,
+           int64_t sa, const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc,
+           int64_t sc, int batch = 1);
+
+// Hermitian eigendecomposition of A (n x n, lda), ascending eigenvalues in w (device).
+// Eigenvectors for eigenvalue indices [vlo, n) are written to Z (n x (n-vlo), ldz) as
+// columns 0..n-vlo-1.  A is destroyed.  Pass vlo = n for eigenvalues only.
+void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz);
+
+// Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (same A, w).
+void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
+                       int64_t ldz);
+
+// Solve A x = b (n x n, LU with partial pivoting), b overwritten.  Returns info.
+int zgesv(Context &c, int n, cplx *A, int64_t lda, cplx *b);
+
+// Hermitian fill from the upper triangle (ZHEEV uplo='U' semantics): A(j,i) = conj(A(i,j))
+// for i < j, Im A(i,i) = 0.
+void herm_from_upper(Context &c, int n, cplx *A, int64_t lda);
+
+// deterministic sum of n doubles on the device into *out (device)
+void dsum(Context &c, const double *x, int64_t n, double *out);
+
+}  // namespace dcg

@@ -1,0 +1,114 @@
+/*
+ * dcaspt2_gb300.h -- C ABI of the GB300 CASCI/CASPT2 hot path.
+ *
+ * The reference program (DIRAC-CASPT2, Fortran) reaches this path through two
+ * argument-less driver calls that communicate through module globals and scratch
+ * files:
+ *   r4dcasci       (src/r4dcasci.F90:1-134, called from src/dcaspt2_run_subprograms.F90:57)
+ *   r4dcaspt2_tra  (src/r4dcaspt2_tra.F90:4-482, called from src/dcaspt2_run_subprograms.F90:62)
+ * The Fortran side keeps its input parser and MRCONEE/MDCINT readers
+ * (read_input, read_mrconee, check_realonly, create_newmdcint) and hands the results
+ * to this library; everything from readint2_casci onwards runs on the GPU.
+ *
+ * Conventions
+ *   - every entry point returns an int status: 0 = success, negative = library error
+ *     (DCG_E_*), positive = LAPACK-style info of a failed factorisation;
+ *     dcg_last_error() gives a one-line message.  The library never exits the process.
+ *   - arrays are column-major (Fortran order); spinor indices are 1-based CAS order
+ *     (inactive, active, secondary, sorted by orbital energy) as produced by
+ *     read_mrconee; complex values are passed as separate real and imaginary planes,
+ *     the storage of the reference (one_elec_int_r/_i, cir/cii).
+ *   - the caller owns all host arrays; they are read during the call only.
+ *   - one context per host thread; a context owns one CUDA stream on one device.
+ */
+#ifndef DCASPT2_GB300_H
+#define DCASPT2_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DCG_OK 0
+#define DCG_E_ARG (-1)        /* invalid argument / inconsistent dimensions            */
+#define DCG_E_CUDA (-2)       /* CUDA runtime error (message in dcg_last_error)         */
+#define DCG_E_STATE (-3)      /* call order violated (e.g. caspt2 before casci)         */
+#define DCG_E_NODET (-4)      /* no CASCI configuration for totsym (search_cas_configuration.F90:158-172) */
+#define DCG_E_NOMEM (-5)      /* device memory exhausted                                */
+#define DCG_E_NUMERIC (-6)    /* eigensolver or solver did not converge                 */
+
+/* precision of the dense contractions (the transformation and S/B/V builds) */
+#define DCG_PREC_FP64 0       /* native FP64 everywhere                                  */
+#define DCG_PREC_SPLIT 1      /* split-precision tensor-core contractions, FP64 recombine */
+
+typedef struct dcg_ctx dcg_ctx;
+
+/* The system one CASCI/CASPT2 solve consumes: the module globals the reference's
+ * readers fill (src/module_global_variables.F90) plus the MDCINTNEW record stream
+ * (src/create_newmdcint.F90:171-177). */
+typedef struct dcg_system {
+    int32_t ninact, nact, nsec, nelec;   /* .ninact .nact .nsec .nelec                     */
+    int32_t nmo;                         /* NMO of MRCONEE (may exceed ninact+nact+nsec)   */
+    int32_t nsymrpa;                     /* abelian double-group irreps; MULTB is 2n x 2n  */
+    int32_t totsym, selectroot;          /* .caspt2_ciroots entry                          */
+    int32_t realonly;                    /* MDCINT realonly (module_realonly.F90:29-77)    */
+    double eshift;                       /* .eshift                                        */
+    double ecore;                        /* ECORE of MRCONEE                               */
+    const int32_t *multb;                /* MULTB(2n,2n), 1-based values                   */
+    const int32_t *irpamo;               /* irpamo(nmo), CAS order, 1-based                */
+    const double *h_re, *h_im;           /* one_elec_int_r/_i (nmo,nmo), CAS order         */
+    int64_t nrec;                        /* number of MDCINTNEW records                    */
+    const int32_t *rec_ijkl;             /* (4,nrec): i,j,k,l of (ij|kl), 1-based CAS      */
+    const double *rec_re, *rec_im;       /* values; rec_im may be NULL when realonly       */
+    int32_t ras1_size, ras2_size, ras3_size;          /* RAS partition sizes (0 = CAS)      */
+    int32_t ras1_max_hole, ras3_max_elec;             /* .ras1 / .ras3 limits               */
+    int32_t min_hole_ras1, min_elec_ras3;             /* .minholeras1 / .minelecras3        */
+} dcg_system;
+
+/* Create a context on CUDA device `device`.  precision: DCG_PREC_*. */
+int dcg_create(int device, int precision, dcg_ctx **out);
+int dcg_destroy(dcg_ctx *ctx);
+const char *dcg_last_error(const dcg_ctx *ctx);
+
+/* Upload a system and expand its integrals on the device (replaces readint2_casci,
+ * src/module_2integrals.F90:26-588, and divide_2_elec_integral_into_subspaces,
+ * src/divide_2_elec_integral_into_subspaces.F90:3-409). */
+int dcg_set_system(dcg_ctx *ctx, const dcg_system *sys);
+
+/* CASCI (replaces casci, src/casci.F90:3-163: search_cas_configuration, casmat,
+ * cdiag/rdiag).  Writes min(nroot, ndet) total energies eigen(i) = ecas(i) + ecore
+ * and, when ci_re is not NULL, the CI coefficients cir/cii (ndet, nroot) that the
+ * reference stores in CIDATA_sym<n>.  *ndet_out receives ndet. */
+int dcg_casci(dcg_ctx *ctx, int32_t nroot, double *eigen_out, double *ci_re, double *ci_im,
+              int32_t *ndet_out);
+
+/* CASPT2 for ctx->selectroot (replaces r4dcaspt2_tra, src/r4dcaspt2_tra.F90:4-482:
+ * fockcasci, fockdiag/tracic, calce0, intra_1/2/3 and solve_A..H_subspace).
+ * e2_sub[8], sumc2_sub[8]: per-subspace E2 and c^2 in the order A..H (0 for skipped
+ * subspaces); skip_mask bit k (k = 0 for A .. 7 for H) skips subspace k the way a
+ * caspt2_restart file does (src/module_restart_file.F90:15-24).
+ * *e0_out = sum_w eps_w D_ww (calce0.F90), *etotal_out = e2all + eigen(selectroot)
+ * - eshift*sumc2 (r4dcaspt2_tra.F90:437-442). */
+int dcg_caspt2(dcg_ctx *ctx, uint32_t skip_mask, double e2_sub[8], double sumc2_sub[8],
+               double *e0_out, double *etotal_out);
+
+/* Orbital energies after fockdiag (eps, nmo entries, CAS order). */
+int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n);
+
+/* Per-stage device times of the last dcg_casci/dcg_caspt2 (ms), in the order:
+ * 0 integral expansion, 1 CASCI matrix, 2 CASCI eigensolve, 3 Fock build+diag,
+ * 4 CI rotation, 5 RDMs, 6 transformation, 7..14 subspaces A..H.  Returns the count. */
+int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n);
+
+/* Device kernel launches issued by the last dcg_set_system+dcg_casci+dcg_caspt2. */
+int64_t dcg_kernel_launches(const dcg_ctx *ctx);
+
+/* Library self-description: number of CUDA kernels compiled in, build string. */
+const char *dcg_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* DCASPT2_GB300_H */

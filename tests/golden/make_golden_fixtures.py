@@ -1,0 +1,73 @@
+"""Regenerate the golden fixtures from the reference's runnable test cases.
+
+For each case directory of the reference's ``test/dev`` tree that ships its MDCINT files,
+this reads ``active.inp``, ``MRCONEE`` and ``MDCINT*`` with the package's readers
+(restatements of read_mrconee / create_newmdcint) and stores the resulting system in
+``<case>.npz`` together with the energies printed in ``reference.<case>.out``:
+the CASCI total energy of the selected root, the per-subspace ``e2X`` and ``sumc2,X`` and
+the total CASPT2 energy.
+
+Usage:  python tests/golden/make_golden_fixtures.py /path/to/reference/test/dev
+"""
+import os
+import re
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from dirac_caspt2_gb300 import dirac_io  # noqa: E402
+
+CASES = ["c2_h2o_dev", "check_minelecras3_dev", "ninact_0_h2_dev", "mdcint_scheme_6_dirac23_c32h_n2_dev"]
+
+
+def parse_output(path: str, selectroot: int):
+    txt = open(path, errors="replace").read().splitlines()
+    e2, sc2 = {}, {}
+    casci = None
+    total = None
+    for ln in txt:
+        m = re.match(r"^\s*e2([a-h])\s*=\s*([-+0-9.Ee]+)\s*a\.u\.", ln)
+        if m:
+            e2[m.group(1).upper()] = float(m.group(2))
+        m = re.match(r"^\s*sumc2,([a-h])\s*=\s*([-+0-9.Ee]+)", ln)
+        if m:
+            sc2[m.group(1).upper()] = float(m.group(2))
+        m = re.match(r"^CASCI Total Energy ROOT(\d+)\s+([-+0-9.Ee]+)\s+a\.u\.", ln)
+        if m and int(m.group(1)) == selectroot and casci is None:
+            casci = float(m.group(2))
+        m = re.match(r"^\s*Total energy is\s+([-+0-9.Ee]+)\s+a\.u\.", ln)
+        if m:
+            total = float(m.group(1))
+    return casci, e2, sc2, total
+
+
+def main(devdir: str):
+    for case in CASES:
+        d = os.path.join(devdir, case)
+        inp = dirac_io.read_active_inp(os.path.join(d, "active.inp"))
+        mrc = dirac_io.read_mrconee(os.path.join(d, "MRCONEE"), inp)
+        new = dirac_io.read_mdcint_new(d, mrc, inp)
+        ts, sr = inp.ciroots[0]
+        casci, e2, sc2, total = parse_output(os.path.join(d, f"reference.{case}.out"), sr)
+        out = dict(ninact=inp.ninact, nact=inp.nact, nsec=inp.nsec, nelec=inp.nelec, nmo=mrc.nmo,
+                   nsymrpa=mrc.nsymrpa, multb=mrc.multb.astype(np.int32), irpamo=mrc.irpamo.astype(np.int32),
+                   h_re=mrc.h.real, h_im=mrc.h.imag, ecore=mrc.ecore,
+                   rec_idx=new.idx.astype(np.int16), rec_re=new.val.real, realonly=new.realonly,
+                   totsym=ts, selectroot=sr, eshift=inp.eshift,
+                   ras=np.array([len(inp.ras1), len(inp.ras2), len(inp.ras3)], dtype=np.int32),
+                   ras1_max_hole=inp.ras1_max_hole, ras3_max_elec=inp.ras3_max_elec,
+                   min_hole_ras1=inp.min_hole_ras1, min_elec_ras3=inp.min_elec_ras3,
+                   ref_casci=casci, ref_total=total,
+                   ref_e2=np.array([e2.get(k, np.nan) for k in "ABCDEFGH"]),
+                   ref_sumc2=np.array([sc2.get(k, np.nan) for k in "ABCDEFGH"]))
+        if not new.realonly:
+            out["rec_im"] = new.val.imag
+        np.savez_compressed(os.path.join(HERE, f"{case}.npz"), **out)
+        print(case, "records", len(new), "total", total)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test/dev")
