@@ -50,6 +50,7 @@ class _System(ctypes.Structure):
         ("ras1_size", ctypes.c_int32), ("ras2_size", ctypes.c_int32), ("ras3_size", ctypes.c_int32),
         ("ras1_max_hole", ctypes.c_int32), ("ras3_max_elec", ctypes.c_int32),
         ("min_hole_ras1", ctypes.c_int32), ("min_elec_ras3", ctypes.c_int32),
+        ("rec_on_device", ctypes.c_int32),
     ]
 
 
@@ -80,12 +81,19 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.dcg_kernel_launches.restype = ctypes.c_int64
     lib.dcg_version.restype = ctypes.c_char_p
+    lib.dcg_stream.argtypes = [ctypes.c_void_p]
+    lib.dcg_stream.restype = ctypes.c_void_p
+    lib.dcg_time_family.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.dcg_family_stats.argtypes = [ctypes.c_void_p, P(ctypes.c_double), P(ctypes.c_int64), P(ctypes.c_double)]
     _lib = lib
     return lib
 
 
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
-                    "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version"]
+                    "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
+                    "dcg_stream", "dcg_time_family", "dcg_family_stats"]
+FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
+            "eig_val": 7, "eig_vec": 8, "eig_back": 9}
 
 
 def _ptr(a: Optional[np.ndarray], ct):
@@ -189,6 +197,28 @@ class HostBuffers:
         st.ras1_max_hole, st.ras3_max_elec = s.ras1_max_hole, s.ras3_max_elec
         st.min_hole_ras1, st.min_elec_ras3 = s.min_hole_ras1, s.min_elec_ras3
         self.struct = st
+
+    def rebind(self) -> None:
+        """Re-point the struct at the current record arrays (e.g. after swapping them for
+        page-locked copies)."""
+        st = self.struct
+        st.rec_ijkl = _ptr(self.ijkl, ctypes.c_int32)
+        st.rec_re = _ptr(self.re, ctypes.c_double)
+        st.rec_im = _ptr(self.im, ctypes.c_double)
+        st.rec_on_device = 0
+
+    def use_device_records(self, ijkl_ptr: int, re_ptr: int, im_ptr: int) -> None:
+        """Point the record arrays at device memory already holding them (HBM-resident input)."""
+        st = self.struct
+        st.rec_ijkl = ctypes.cast(ctypes.c_void_p(ijkl_ptr), ctypes.POINTER(ctypes.c_int32))
+        st.rec_re = ctypes.cast(ctypes.c_void_p(re_ptr), ctypes.POINTER(ctypes.c_double))
+        st.rec_im = ctypes.cast(ctypes.c_void_p(im_ptr), ctypes.POINTER(ctypes.c_double)) if im_ptr else \
+            ctypes.POINTER(ctypes.c_double)()
+        st.rec_on_device = 1
+
+    @property
+    def record_bytes(self) -> int:
+        return int(self.ijkl.nbytes + self.re.nbytes + (self.im.nbytes if self.im is not None else 0))
 
     @property
     def h2d_bytes(self) -> int:
@@ -296,6 +326,20 @@ class Caspt2Session:
 
     def kernel_launches(self) -> int:
         return int(self.lib.dcg_kernel_launches(self.h))
+
+    @property
+    def stream_ptr(self) -> int:
+        return int(self.lib.dcg_stream(self.h) or 0)
+
+    def time_family(self, family: str) -> None:
+        self._check(self.lib.dcg_time_family(self.h, FAMILIES[family]))
+
+    def family_stats(self) -> Tuple[float, int, float]:
+        ms = ctypes.c_double(0.0)
+        n = ctypes.c_int64(0)
+        w = ctypes.c_double(0.0)
+        self._check(self.lib.dcg_family_stats(self.h, ctypes.byref(ms), ctypes.byref(n), ctypes.byref(w)))
+        return ms.value, n.value, w.value
 
     def solve(self, s: SystemInput, nroot: int = 1, skip_mask: int = 0,
               bufs: Optional[HostBuffers] = None) -> Caspt2Result:

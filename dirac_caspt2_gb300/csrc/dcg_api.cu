@@ -199,21 +199,31 @@ static void set_system(Context &c, const dcg_system *s) {
             DCG_CUDA(cudaMemsetAsync(d.cls[id].p, 0, (size_t)d.cls[id].size * sizeof(cplx), c.stream));
     }
     if (c.nrec > 0) {
-        int32_t *ijkl = wsget<int32_t>(c, "rec.ijkl", (size_t)4 * c.nrec);
-        double *re = wsget<double>(c, "rec.re", (size_t)c.nrec);
-        double *im = nullptr;
-        DCG_CUDA(cudaMemcpyAsync(ijkl, s->rec_ijkl, sizeof(int32_t) * 4 * c.nrec, cudaMemcpyHostToDevice, c.stream));
-        DCG_CUDA(cudaMemcpyAsync(re, s->rec_re, sizeof(double) * c.nrec, cudaMemcpyHostToDevice, c.stream));
-        if (s->rec_im && !c.realonly) {
-            im = wsget<double>(c, "rec.im", (size_t)c.nrec);
-            DCG_CUDA(cudaMemcpyAsync(im, s->rec_im, sizeof(double) * c.nrec, cudaMemcpyHostToDevice, c.stream));
+        const int32_t *ijkl = s->rec_ijkl;
+        const double *re = s->rec_re, *im = c.realonly ? nullptr : s->rec_im;
+        if (!s->rec_on_device) {
+            int32_t *dijkl = wsget<int32_t>(c, "rec.ijkl", (size_t)4 * c.nrec);
+            double *dre = wsget<double>(c, "rec.re", (size_t)c.nrec);
+            DCG_CUDA(cudaMemcpyAsync(dijkl, s->rec_ijkl, sizeof(int32_t) * 4 * c.nrec, cudaMemcpyHostToDevice, c.stream));
+            DCG_CUDA(cudaMemcpyAsync(dre, s->rec_re, sizeof(double) * c.nrec, cudaMemcpyHostToDevice, c.stream));
+            ijkl = dijkl;
+            re = dre;
+            if (im) {
+                double *dim = wsget<double>(c, "rec.im", (size_t)c.nrec);
+                DCG_CUDA(cudaMemcpyAsync(dim, s->rec_im, sizeof(double) * c.nrec, cudaMemcpyHostToDevice, c.stream));
+                im = dim;
+            }
         }
+        size_t cls_bytes = 0;
+        for (int id = 0; id < CL_COUNT; id++) cls_bytes += (size_t)d.cls[id].size * sizeof(cplx);
+        FamScope fs(c, DCG_FAM_SCATTER, (double)c.nrec * (16.0 + (im ? 16.0 : 8.0)) + (double)cls_bytes + (double)ntw * sizeof(cplx));
         cplx *val = wsget<cplx>(c, "rec.val", (size_t)c.nrec);
         pack_cplx_kernel<<<grid1d(c.nrec, 256), 256, 0, c.stream>>>(re, im, c.nrec, val);
         DCG_LAUNCHED(c);
         launch_scatter(c, ijkl, val, c.nrec, d.inttw, d.cls);
     }
     stage_end(c, ST_INTS);
+    fam_collect(c);
     c.have_system = true;
     c.have_casci = false;
 }
@@ -365,6 +375,7 @@ static RdmBufs rdm_build(Context &c, const uint64_t *full, int64_t M, const cplx
     launch_apply_E(c, na, M, full, vin, nv, YZ);
     if (third) launch_apply_E(c, na, M, full, YZ, (int)(nv * na2), YZ + M * nv * na2);
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    FamScope fs(c, DCG_FAM_RDM, 8.0 * (double)M * (double)nv * na2 + 8.0 * (double)na2 * ncol * M);
     r.g1 = wsget<cplx>(c, "rdm.g1", (size_t)nv * na2);
     zgemm(c, OP_C, OP_N, 1, (int)(nv * na2), (int)M, one, psi, M, 0, YZ, M, 0, zero, r.g1, 1, 0, 1);
     r.gall = wsget<cplx>(c, "rdm.gall", (size_t)na2 * ncol);
@@ -540,6 +551,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         const size_t sz = (size_t)dm[0] * dm[1] * dm[2] * dm[3];
         cplx *out = wsget<cplx>(c, std::string("tr.") + name, sz + 1);
         const cplx *Ux[4] = {Usp[sp[0]], Usp[sp[1]], Usp[sp[2]], Usp[sp[3]]};
+        FamScope fs(c, DCG_FAM_TRANSFORM, 8.0 * (double)sz * (dm[0] + dm[1] + dm[2] + dm[3]));
         transform4(c, src, out, ttmp, dm, Ux);
         return out;
     };
@@ -788,8 +800,11 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         const int nblk = std::max(1, c.num_sms) * 8;
         double *part = wsget<double>(c, "h.part", 2 * (size_t)nblk);
         double *red = wsget<double>(c, "h.red", 2);
-        launch_h_stream2(c, Hc, ni, ns, d.eps, d.eps + nmoc, d.irp, d.irp + nmoc, d.md, d.msy, c.nsym, es, part,
-                         part + nblk, nblk);
+        {
+            FamScope fs(c, DCG_FAM_HSTREAM, (double)d.cls[CL_H].size * sizeof(cplx));
+            launch_h_stream2(c, Hc, ni, ns, d.eps, d.eps + nmoc, d.irp, d.irp + nmoc, d.md, d.msy, c.nsym, es, part,
+                             part + nblk, nblk);
+        }
         dsum(c, part, nblk, red);
         dsum(c, part + nblk, nblk, red + 1);
         std::vector<double> hr = download(c, red, 2);
@@ -799,6 +814,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
 
     double e2all = 0.0, sumc2 = 0.0;
     for (int k = 0; k < 8; k++) { e2all += e2_sub[k]; sumc2 += sc2_sub[k]; }
+    fam_collect(c);
     if (e0_out) *e0_out = e0;
     if (et_out) *et_out = e2all + c.ecas[c.selectroot - 1] - c.eshift * sumc2;   // r4dcaspt2_tra.F90:441
     DCG_CUDA(cudaStreamSynchronize(c.stream));
@@ -910,5 +926,27 @@ int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n) {
 int64_t dcg_kernel_launches(const dcg_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
 
 const char *dcg_version(void) { return "dcaspt2_gb300 0.1 (sm_103a, FP64 path)"; }
+
+void *dcg_stream(const dcg_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+int dcg_time_family(dcg_ctx *ctx, int32_t family) {
+    if (!ctx || family < 0 || family > DCG_FAM_EIG_BACK) return DCG_E_ARG;
+    Context &c = ctx->c;
+    dcg::fam_collect(c);
+    c.fam = family;
+    c.fam_ms = 0.0;
+    c.fam_work = 0.0;
+    c.fam_launches = 0;
+    return DCG_OK;
+}
+
+int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work) {
+    if (!ctx) return DCG_E_ARG;
+    const Context &c = ctx->c;
+    if (ms) *ms = c.fam_ms;
+    if (launches) *launches = c.fam_launches;
+    if (work) *work = c.fam_work;
+    return DCG_OK;
+}
 
 }  // extern "C"

@@ -85,6 +85,12 @@ struct Context {
     int num_sms = 0;
     void *dev_state = nullptr;   // device-side system state (owned, see dcg_api.cu)
 
+    // ---- per-family kernel timing (dcg_time_family)
+    int fam = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fam_ev;
+    double fam_ms = 0.0, fam_work = 0.0;
+    int64_t fam_launches = 0;
+
     // ---- system (host copies)
     bool have_system = false;
     int ni = 0, na = 0, ns = 0, ne = 0, nmo = 0, nsym = 1, totsym = 1, selectroot = 1;
@@ -138,6 +144,29 @@ template <typename T>
 T *wsget(Context &c, const std::string &name, size_t count) {
     return reinterpret_cast<T *>(c.ws.get(name, count * sizeof(T) + 256));
 }
+
+// Records CUDA events around the launches of one kernel family when that family is
+// selected; elapsed times are collected by fam_collect() after the stream synchronises.
+struct FamScope {
+    Context &c;
+    bool on;
+    int64_t l0;
+    cudaEvent_t a = nullptr, b = nullptr;
+    FamScope(Context &cc, int family, double work) : c(cc), on(cc.fam == family && family != 0), l0(cc.launches) {
+        if (!on) return;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c.stream);
+        c.fam_work += work;
+    }
+    ~FamScope() {
+        if (!on) return;
+        cudaEventRecord(b, c.stream);
+        c.fam_ev.push_back({a, b});
+        c.fam_launches += c.launches - l0;
+    }
+};
+void fam_collect(Context &c);
 
 // ---------------------------------------------------------------- linear algebra (dcg_linalg.cu)
 enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };   // R = conjugate without transpose

@@ -596,14 +596,33 @@ static void tridiag(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
     DCG_LAUNCHED(c);
 }
 
+void fam_collect(Context &c) {
+    for (auto &pr : c.fam_ev) {
+        cudaEventSynchronize(pr.second);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, pr.first, pr.second);
+        c.fam_ms += ms;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    c.fam_ev.clear();
+}
+
 void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
     if (n <= 0) return;
+    FamScope fs(c, DCG_FAM_EIG, (16.0 / 3.0) * (double)n * n * n);
     HeevWork h = heev_work(c, n);
-    tridiag(c, n, A, lda, h);
-    gersh_kernel<<<1, 1024, 0, c.stream>>>(n, h.d, h.e, h.bounds);
-    DCG_LAUNCHED(c);
-    bisect_kernel<<<grid1d(n, 128), 128, 0, c.stream>>>(n, h.d, h.e, h.bounds, w);
-    DCG_LAUNCHED(c);
+    {
+        FamScope f1(c, DCG_FAM_EIG_TRI, (16.0 / 3.0) * (double)n * n * n);
+        tridiag(c, n, A, lda, h);
+    }
+    {
+        FamScope f2(c, DCG_FAM_EIG_VAL, (double)n * n);
+        gersh_kernel<<<1, 1024, 0, c.stream>>>(n, h.d, h.e, h.bounds);
+        DCG_LAUNCHED(c);
+        bisect_kernel<<<grid1d(n, 128), 128, 0, c.stream>>>(n, h.d, h.e, h.bounds, w);
+        DCG_LAUNCHED(c);
+    }
     heev_vectors_only(c, n, A, lda, w, vlo, vhi, Z, ldz);
 }
 
@@ -616,10 +635,15 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
     HeevWork h = heev_work(c, n);
     double *scr = wsget<double>(c, "heev.scr", (size_t)n * nvec * 5 + 16);
     double *zt = wsget<double>(c, "heev.z", (size_t)n * nvec + 16);
-    invit_kernel<<<grid1d(nvec, 64), 64, 0, c.stream>>>(n, h.d, h.e, w, h.bounds, vlo, nvec, scr, zt);
-    DCG_LAUNCHED(c);
-    cluster_mgs_kernel<<<nvec, 256, 0, c.stream>>>(n, w, h.bounds, vlo, nvec, zt, 1e-7);
-    DCG_LAUNCHED(c);
+    FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nvec);
+    {
+        FamScope f3(c, DCG_FAM_EIG_VEC, 10.0 * (double)n * nvec);
+        invit_kernel<<<grid1d(nvec, 64), 64, 0, c.stream>>>(n, h.d, h.e, w, h.bounds, vlo, nvec, scr, zt);
+        DCG_LAUNCHED(c);
+        cluster_mgs_kernel<<<nvec, 256, 0, c.stream>>>(n, w, h.bounds, vlo, nvec, zt, 1e-7);
+        DCG_LAUNCHED(c);
+    }
+    FamScope f4(c, DCG_FAM_EIG_BACK, 8.0 * (double)n * n * nvec);
     backtransform_kernel<<<grid1d(nvec, BT_COLS), 256, 0, c.stream>>>(n, A, lda, h.tau, zt, nvec, Z, ldz);
     DCG_LAUNCHED(c);
 }

@@ -184,17 +184,18 @@ def make_system(cfg: SynthConfig, keep_factors: Optional[bool] = None) -> SynthS
         Q = np.arange(r[1][0], r[1][1])
         R = np.arange(r[2][0], r[2][1])
         S = np.arange(r[3][0], r[3][1])
-        pp, qq, rr, ss = np.meshgrid(P, Q, R, S, indexing="ij")
-        mask = _canonical_mask(pp, qq, rr, ss)
+        # dense block by one GEMM over the fitting index, then the canonical entries
+        Bpq = B[:, r[0][0]:r[0][1], r[1][0]:r[1][1]].reshape(L, -1)
+        Brs = B[:, r[2][0]:r[2][1], r[3][0]:r[3][1]].reshape(L, -1)
+        blk = (Bpq.T @ Brs).reshape(len(P), len(Q), len(R), len(S))
+        pp, qq, rr, ss = np.meshgrid(P, Q, R, S, indexing="ij", sparse=True)
+        mask = np.broadcast_to(_canonical_mask(pp, qq, rr, ss), blk.shape)
         if not np.any(mask):
             continue
-        pi, qi, ri, si = pp[mask], qq[mask], rr[mask], ss[mask]
-        # g = sum_L B[L,p,q] B[L,r,s] for the selected entries, chunked
-        vals = np.empty(len(pi), dtype=np.complex128)
-        chunk = 1 << 18
-        for c0 in range(0, len(pi), chunk):
-            sl = slice(c0, c0 + chunk)
-            vals[sl] = np.einsum("Ln,Ln->n", B[:, pi[sl], qi[sl]], B[:, ri[sl], si[sl]])
+        sel = np.nonzero(mask)
+        pi, qi, ri, si = P[sel[0]], Q[sel[1]], R[sel[2]], S[sel[3]]
+        vals = blk[sel]
+        del blk
         idx_out.append(np.stack([pi, qi, ri, si], axis=1).astype(np.int32) + 1)
         val_out.append(vals)
     rec_idx = np.concatenate(idx_out) if idx_out else np.zeros((0, 4), np.int32)

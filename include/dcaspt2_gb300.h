@@ -65,6 +65,8 @@ typedef struct dcg_system {
     int32_t ras1_size, ras2_size, ras3_size;          /* RAS partition sizes (0 = CAS)      */
     int32_t ras1_max_hole, ras3_max_elec;             /* .ras1 / .ras3 limits               */
     int32_t min_hole_ras1, min_elec_ras3;             /* .minholeras1 / .minelecras3        */
+    int32_t rec_on_device;               /* 1: rec_ijkl/rec_re/rec_im are device pointers on the
+                                            context's device (already resident in HBM)           */
 } dcg_system;
 
 /* Create a context on CUDA device `device`.  precision: DCG_PREC_*. */
@@ -105,8 +107,29 @@ int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n);
 /* Device kernel launches issued by the last dcg_set_system+dcg_casci+dcg_caspt2. */
 int64_t dcg_kernel_launches(const dcg_ctx *ctx);
 
-/* Library self-description: number of CUDA kernels compiled in, build string. */
+/* Library self-description (build string). */
 const char *dcg_version(void);
+
+/* The context's CUDA stream (a cudaStream_t), so a caller can order or time its own work
+ * against the library's. */
+void *dcg_stream(const dcg_ctx *ctx);
+
+/* Kernel families whose launches can be timed with CUDA events on the context stream. */
+#define DCG_FAM_NONE 0
+#define DCG_FAM_TRANSFORM 1   /* 4-index transformation GEMMs; work = FLOPs (complex MAC = 8)  */
+#define DCG_FAM_HSTREAM 2     /* H-subspace streaming reduction; work = bytes of the H class    */
+#define DCG_FAM_RDM 3         /* density GEMMs; work = FLOPs                                     */
+#define DCG_FAM_SCATTER 4     /* record expansion; work = record bytes read                      */
+#define DCG_FAM_EIG 5         /* Hermitian eigensolver launches; work = nominal FLOPs 16/3 n^3   */
+#define DCG_FAM_EIG_TRI 6     /* eigensolver phases: tridiagonal reduction (FLOPs 16/3 n^3)      */
+#define DCG_FAM_EIG_VAL 7     /*   bisection for the eigenvalues (Sturm steps)                   */
+#define DCG_FAM_EIG_VEC 8     /*   tridiagonal eigenvectors (inverse iteration + cluster MGS)    */
+#define DCG_FAM_EIG_BACK 9    /*   back-transformation (FLOPs 8 n^2 m)                            */
+
+/* Select the family timed during subsequent calls (DCG_FAM_NONE disables; resets stats). */
+int dcg_time_family(dcg_ctx *ctx, int32_t family);
+/* Accumulated device time (ms), launch count and algorithmic work of the timed family. */
+int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work);
 
 #ifdef __cplusplus
 }

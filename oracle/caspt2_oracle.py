@@ -157,45 +157,58 @@ def expand_partners(idx1: np.ndarray, val: np.ndarray):
 
 class Integrals:
     """Dense two-electron integral blocks (pq|rs) in the ORIGINAL spinor basis, addressed
-    by a space pattern (s1,s2,s3,s4) with s in {1,2,3}."""
+    by a space pattern (s1,s2,s3,s4) with s in {1,2,3}; '=' scatter semantics of the
+    reference arrays (later partners overwrite earlier ones).  Records are expanded in
+    chunks straight into the blocks the path reads."""
 
-    def __init__(self, sysm: System):
+    PATTERNS = [(2, 1, 2, 2), (2, 1, 1, 1), (2, 1, 2, 1), (3, 2, 2, 2), (3, 2, 1, 1), (3, 1, 1, 2),
+                (3, 1, 2, 2), (3, 2, 2, 1), (3, 1, 1, 1), (3, 1, 2, 1), (3, 2, 3, 2), (3, 1, 3, 2),
+                (3, 1, 3, 1), (3, 3, 1, 1), (3, 3, 2, 2), (3, 1, 1, 3), (3, 2, 2, 3)]
+
+    def __init__(self, sysm: System, chunk: int = 1 << 20):
         self.sysm = sysm
-        P, V = expand_partners(sysm.rec_idx, sysm.rec_val)
-        self.P = P.reshape(-1, 4)
-        self.V = V.reshape(-1)
-        sp = sysm.space_of(self.P)
-        self.code = sp[:, 0] * 1000 + sp[:, 1] * 100 + sp[:, 2] * 10 + sp[:, 3]
+        nmoc = sysm.nmoc
+        self._occ = np.zeros((nmoc,) * 4, dtype=np.complex128)
         self._cache: Dict[Tuple[int, ...], np.ndarray] = {}
+        codes = {}
+        for pat in self.PATTERNS:
+            r = [self.rng(x) for x in pat]
+            self._cache[pat] = np.zeros(tuple(b - a for a, b in r), dtype=np.complex128)
+            codes[pat[0] * 1000 + pat[1] * 100 + pat[2] * 10 + pat[3]] = pat
+        n = len(sysm.rec_val)
+        for c0 in range(0, max(n, 1), chunk):
+            P, V = expand_partners(sysm.rec_idx[c0:c0 + chunk], sysm.rec_val[c0:c0 + chunk])
+            P = P.reshape(-1, 4)
+            V = V.reshape(-1)
+            m = np.all(P < nmoc, axis=1)
+            if np.any(m):
+                q = P[m]
+                self._occ[q[:, 0], q[:, 1], q[:, 2], q[:, 3]] = V[m]
+            sp = sysm.space_of(P)
+            code = sp[:, 0] * 1000 + sp[:, 1] * 100 + sp[:, 2] * 10 + sp[:, 3]
+            for cd, pat in codes.items():
+                mm = code == cd
+                if not np.any(mm):
+                    continue
+                q = P[mm]
+                r = [self.rng(x) for x in pat]
+                self._cache[pat][q[:, 0] - r[0][0], q[:, 1] - r[1][0], q[:, 2] - r[2][0], q[:, 3] - r[3][0]] = V[mm]
 
     def rng(self, s: int) -> Tuple[int, int]:
         ni, na, ns = self.sysm.ninact, self.sysm.nact, self.sysm.nsec
         return [(0, ni), (ni, ni + na), (ni + na, ni + na + ns)][s - 1]
 
     def block(self, pattern: Tuple[int, int, int, int]) -> np.ndarray:
-        """Dense block with '=' scatter semantics (later partners overwrite earlier)."""
         if pattern in self._cache:
             return self._cache[pattern]
-        r = [self.rng(s) for s in pattern]
-        shape = tuple(b - a for a, b in r)
-        out = np.zeros(shape, dtype=np.complex128)
-        c = pattern[0] * 1000 + pattern[1] * 100 + pattern[2] * 10 + pattern[3]
-        m = self.code == c
-        if np.any(m):
-            p = self.P[m]
-            out[p[:, 0] - r[0][0], p[:, 1] - r[1][0], p[:, 2] - r[2][0], p[:, 3] - r[3][0]] = self.V[m]
-        self._cache[pattern] = out
-        return out
+        r = [self.rng(x) for x in pattern]
+        if all(x <= 2 for x in pattern):
+            return self._occ[r[0][0]:r[0][1], r[1][0]:r[1][1], r[2][0]:r[2][1], r[3][0]:r[3][1]]
+        raise KeyError(f"integral block {pattern} is not read by the hot path")
 
     def occ_block(self) -> np.ndarray:
         """inttw(nmoc^4): every (pq|rs) with all indices inactive or active."""
-        s = self.sysm
-        nmoc = s.nmoc
-        out = np.zeros((nmoc,) * 4, dtype=np.complex128)
-        m = np.all(self.P < nmoc, axis=1)
-        p = self.P[m]
-        out[p[:, 0], p[:, 1], p[:, 2], p[:, 3]] = self.V[m]
-        return out
+        return self._occ
 
 
 # ======================================================================================
@@ -593,8 +606,14 @@ class Result:
         return float(sum(self.sumc2.values()))
 
 
-def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool = False) -> Result:
-    """r4dcasci (r4dcasci.F90:1-134) followed by r4dcaspt2_tra (r4dcaspt2_tra.F90:4-482)."""
+def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool = False,
+        active_pair_rotation: Optional[np.random.Generator] = None) -> Result:
+    """r4dcasci (r4dcasci.F90:1-134) followed by r4dcaspt2_tra (r4dcaspt2_tra.F90:4-482).
+
+    ``active_pair_rotation``: when given, the eigenvectors of every exactly degenerate pair of
+    active Fock eigenvalues are rotated by a random unitary 2x2 matrix.  Such a rotation is
+    an equally valid ZHEEV result; every subspace except E is invariant under it (see
+    ``e_subspace_envelope``)."""
     ni, na, ns = s.ninact, s.nact, s.nsec
     nmoc = ni + na
     ints = Integrals(s)
@@ -614,6 +633,13 @@ def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool 
     rd_c = RDM(fs, c0, order=1)
     f = fock_casci(s, ints, g_occ, rd_c.D1)
     U, eps = fock_diag(s, f)
+    if active_pair_rotation is not None:
+        for p in range(ni, nmoc - 1):
+            if abs(eps[p] - eps[p + 1]) <= 1e-12 * max(1.0, abs(eps[p])):
+                g = active_pair_rotation
+                M2 = g.normal(size=(2, 2)) + (0.0 if s.realonly else 1j * g.normal(size=(2, 2)))
+                Q, _ = np.linalg.qr(M2)   # real systems: DSYEV vectors are real (orthogonal Q)
+                U[:, p:p + 2] = U[:, p:p + 2] @ Q
     c = ci_rotate(s, dets, U[ni:nmoc, ni:nmoc], c0)
     eps_act = eps[ni:nmoc]
     rd = RDM(fs, c, eps_act=eps_act, order=3)
@@ -969,14 +995,32 @@ def solve_H(s, rd, cls, hU, eps, e0):
     i_, j_ = np.tril_indices(ni, -1)
     Vab = V[a_[:, None], i_[None, :], b_[:, None], j_[None, :]]
     den = ea[a_][:, None] + ea[b_][:, None] - ei[i_][None, :] - ei[j_][None, :] + s.eshift
-    ir = s.irpamo
-    sy = np.array([[_ms(s, _md(s, ir[nmoc + a], ir[i]), _md(s, ir[nmoc + b], ir[j])) for (i, j) in zip(i_, j_)]
-                   for (a, b) in zip(a_, b_)]) if len(a_) and len(i_) else np.zeros((len(a_), len(i_)))
-    mask = sy == 1
+    ir = np.asarray(s.irpamo)
+    md, msy = s.multb_d, s.multb_s
+    s1 = md[ir[nmoc + a_][:, None] - 1, ir[i_][None, :] - 1]
+    s2 = md[ir[nmoc + b_][:, None] - 1, ir[j_][None, :] - 1]
+    mask = msy[s1 - 1, s2 - 1] == 1
     c = Vab / den
     sc2 = float(np.sum((np.abs(c) ** 2)[mask]))
     e2 = -float(np.sum((np.abs(Vab) ** 2 / den)[mask]))
     return e2, sc2, {}
+
+
+def e_subspace_envelope(s: System, trials: int = 6, seed: int = 0) -> Tuple[float, float]:
+    """Range of the E-subspace energy over equally valid eigenvector choices inside
+    degenerate active Kramers pairs.
+
+    The reference's complex E-space V build (solve_E_subspace.F90 vEmat_complex) contracts
+    the integrals with dim1_density(it, k) = <E_tp>; covariance under a phase change of the
+    active spinors would need <E_pt>.  For real integrals the two are equal; for complex
+    integrals without point-group symmetry the active Fock block has exactly degenerate
+    Kramers pairs, ZHEEV's choice of vectors inside a pair is decided by rounding, and so
+    the reference's e2E is defined only to within this range."""
+    vals = [run(s, subspaces="E").e2.get("E", 0.0)]
+    g = np.random.default_rng(seed)
+    for _ in range(trials):
+        vals.append(run(s, subspaces="E", active_pair_rotation=g).e2.get("E", 0.0))
+    return float(min(vals)), float(max(vals))
 
 
 SOLVERS = {"A": solve_A, "B": solve_B, "C": solve_C, "D": solve_D,

@@ -1,0 +1,42 @@
+"""C ABI: the library builds for sm_103a, loads, and exports every entry point the public
+header declares (no compute calls: this runs without a GPU)."""
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "dcaspt2_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(dcg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_declared_symbol():
+    from dirac_caspt2_gb300 import build, api
+    lib = build.build()
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True).stdout
+    exported = set(re.findall(r"\bT (dcg_\w+)", out))
+    declared = _declared()
+    assert declared, "no declarations found"
+    missing = [s for s in declared if s not in exported]
+    assert not missing, missing
+    L = api.load_library()
+    for s in declared:
+        assert hasattr(L, s)
+    assert set(api.EXPORTED_SYMBOLS) <= set(declared)
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    from dirac_caspt2_gb300 import api
+    monkeypatch.setattr(api, "_lib", None)
+    with pytest.raises(ImportError):
+        api.load_library(str(tmp_path / "nope.so"))
+
+
+def test_version_string_without_gpu():
+    from dirac_caspt2_gb300 import api
+    assert b"sm_103a" in api.load_library().dcg_version()

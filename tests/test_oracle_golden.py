@@ -1,0 +1,29 @@
+"""The CPU oracle reproduces the reference's own printed energies on every runnable golden
+case (per subspace and total, abs 1e-10 Eh: the reference tests' tolerance)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, GOLDEN_DIR, oracle_system
+
+TOL = 1e-10
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_oracle_matches_reference_golden(case):
+    from dirac_caspt2_gb300 import api
+    from oracle import caspt2_oracle as O
+    path = os.path.join(GOLDEN_DIR, f"{case}.npz")
+    s = api.SystemInput.from_npz(path)
+    z = np.load(path)
+    r = O.run(oracle_system(s))
+    assert abs(r.casci_energies[s.selectroot - 1] - float(z["ref_casci"])) < TOL
+    for i, k in enumerate("ABCDEFGH"):
+        ref = z["ref_e2"][i]
+        if np.isnan(ref):        # subspace skipped by the reference (ninact = 0 or nsec = 0)
+            assert k not in r.e2
+            continue
+        assert abs(r.e2[k] - ref) < TOL, (k, r.e2[k], ref)
+        assert abs(r.sumc2[k] - z["ref_sumc2"][i]) < TOL, (k, r.sumc2[k], z["ref_sumc2"][i])
+    assert abs(r.total_energy - float(z["ref_total"])) < TOL
