@@ -81,6 +81,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.dcg_kernel_launches.restype = ctypes.c_int64
     lib.dcg_version.restype = ctypes.c_char_p
+    lib.dcg_solve_h.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p,
+                                ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                ctypes.c_int32, ctypes.c_double, P(ctypes.c_double)]
     lib.dcg_stream.argtypes = [ctypes.c_void_p]
     lib.dcg_stream.restype = ctypes.c_void_p
     lib.dcg_time_family.argtypes = [ctypes.c_void_p, ctypes.c_int32]
@@ -91,7 +94,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
-                    "dcg_stream", "dcg_time_family", "dcg_family_stats"]
+                    "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9}
 
@@ -326,6 +329,15 @@ class Caspt2Session:
 
     def kernel_launches(self) -> int:
         return int(self.lib.dcg_kernel_launches(self.h))
+
+    def solve_h(self, hclass_ptr: int, ninact: int, nsec: int, eps_i_ptr: int, eps_s_ptr: int, irp_i_ptr: int,
+                irp_s_ptr: int, md_ptr: int, ms_ptr: int, nsymrpa: int, eshift: float) -> Tuple[float, float]:
+        """solve_H_subspace on device-resident inputs (all *_ptr are device addresses)."""
+        out = np.zeros(2)
+        self._check(self.lib.dcg_solve_h(self.h, hclass_ptr, ninact, nsec, eps_i_ptr, eps_s_ptr, irp_i_ptr,
+                                         irp_s_ptr, md_ptr, ms_ptr, nsymrpa, eshift,
+                                         out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))))
+        return float(out[0]), float(out[1])
 
     @property
     def stream_ptr(self) -> int:

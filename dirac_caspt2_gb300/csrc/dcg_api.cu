@@ -929,6 +929,28 @@ const char *dcg_version(void) { return "dcaspt2_gb300 0.1 (sm_103a, FP64 path)";
 
 void *dcg_stream(const dcg_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
 
+int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
+                const double *eps_s, const int32_t *irp_i, const int32_t *irp_s, const int32_t *multb_d,
+                const int32_t *multb_s, int32_t nsymrpa, double eshift, double out[2]) {
+    if (!out || ninact < 0 || nsec < 0 || nsymrpa < 1) return DCG_E_ARG;
+    if ((int64_t)ninact * nsec > 0 && (!hclass || !eps_i || !eps_s || !irp_i || !irp_s || !multb_d || !multb_s))
+        return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        out[0] = out[1] = 0.0;
+        if ((int64_t)ninact * nsec == 0) return DCG_OK;
+        const int nblk = std::max(1, c_.num_sms) * 8;
+        double *part = dcg::wsget<double>(c_, "hsolve.part", 2 * (size_t)nblk);
+        double *red = dcg::wsget<double>(c_, "hsolve.red", 2);
+        dcg::launch_h_stream2(c_, static_cast<const dcg::cplx *>(hclass), ninact, nsec, eps_i, eps_s, irp_i, irp_s,
+                              multb_d, multb_s, nsymrpa, eshift, part, part + nblk, nblk);
+        dcg::dsum(c_, part, nblk, red);
+        dcg::dsum(c_, part + nblk, nblk, red + 1);
+        DCG_CUDA(cudaMemcpyAsync(out, red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        return DCG_OK;
+    });
+}
+
 int dcg_time_family(dcg_ctx *ctx, int32_t family) {
     if (!ctx || family < 0 || family > DCG_FAM_EIG_BACK) return DCG_E_ARG;
     Context &c = ctx->c;

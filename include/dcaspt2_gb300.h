@@ -96,6 +96,19 @@ int dcg_casci(dcg_ctx *ctx, int32_t nroot, double *eigen_out, double *ci_re, dou
 int dcg_caspt2(dcg_ctx *ctx, uint32_t skip_mask, double e2_sub[8], double sumc2_sub[8],
                double *e0_out, double *etotal_out);
 
+/* H subspace on a caller-supplied, device-resident transformed H class (replaces
+ * solve_H_subspace, src/solve_H_subspace.F90:23-191): with V = (ai|bj) - (aj|bi),
+ * e = eps_a + eps_b - eps_i - eps_j + eshift, over a > b, i > j whose symmetry product
+ * MULTB_S(MULTB_D(irp_a, irp_i), MULTB_D(irp_b, irp_j)) is 1:
+ *   out[0] = e2h = -sum |V|^2 / e,  out[1] = sumc2,h = sum |V/e|^2.
+ * Device inputs: hclass (ns, ni, ns, ni) complex column-major ((a i|b j) at
+ * a + ns*(i + ni*(b + ns*j)), local indices), eps_i[ni], eps_s[ns], irp_i[ni], irp_s[ns]
+ * (1-based irreps), multb_d and multb_s (nsymrpa x nsymrpa, [a-1][b-1] row-major,
+ * 1-based values).  out is a host array.  Partial sums live in the context workspace. */
+int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
+                const double *eps_s, const int32_t *irp_i, const int32_t *irp_s, const int32_t *multb_d,
+                const int32_t *multb_s, int32_t nsymrpa, double eshift, double out[2]);
+
 /* Orbital energies after fockdiag (eps, nmo entries, CAS order). */
 int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n);
 

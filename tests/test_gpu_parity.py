@@ -48,7 +48,7 @@ def test_gpu_matches_reference_golden(session, case):
 SYNTH = [
     (4, 4, 8, 2, 1, False),
     (2, 4, 6, 2, 2, False),
-    (6, 6, 10, 3, 3, False),
+    (6, 6, 10, 4, 3, False),
     (4, 6, 12, 2, 4, True),     # real-valued integrals through the complex path
     (8, 6, 40, 4, 0, False),    # the 8/6/40 (4e) benchmark system
 ]
