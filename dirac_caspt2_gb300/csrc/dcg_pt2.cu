@@ -490,3 +490,113 @@ void launch_h_stream2(Context &c, const cplx *Hc, int ni, int ns, const double *
 }
 
 }  // namespace dcg
+
+// ============================================================================ allocation-free H subspace
+// dcg_solve_h for callers that cannot allocate device memory (a host that owns every
+// device allocation through its own pool, a plug-in running under another runtime's
+// allocator): the same H-subspace sum with one partial pair per inactive pair i > j,
+// held in a file-scope device array instead of the context workspace.  The array is
+// sized for at most DCG_H_NOALLOC_MAX_NINACT inactive spinors (8128 pairs, 127 KiB) and
+// stays resident on every device that loads the library until the process exits.
+#include <mutex>
+
+namespace dcg {
+
+constexpr int H_NOALLOC_MAX_NINACT = 128;
+constexpr int H_NOALLOC_MAX_PAIRS = H_NOALLOC_MAX_NINACT * (H_NOALLOC_MAX_NINACT - 1) / 2;
+// [0, P): e2 partial per pair; [P, 2P): sumc2 partial per pair; [2P, 2P+2): results
+static __device__ __align__(256) double g_h_noalloc_scratch[2 * H_NOALLOC_MAX_PAIRS + 2];
+
+// one block per inactive pair (i, j), i > j, ordered (1,0),(2,0),(2,1),...
+__global__ void h_pair_kernel(const cplx *__restrict__ Hc, int ni, int ns, const double *__restrict__ eps_i,
+                              const double *__restrict__ eps_s, const int *__restrict__ irp_i,
+                              const int *__restrict__ irp_s, const int *__restrict__ md, const int *__restrict__ msy,
+                              int nsym, double eshift, double *scratch) {
+    __shared__ double sh[2][32];
+    const int p = blockIdx.x;
+    int i = 1, cnt = p;
+    while (cnt >= i) { cnt -= i; i++; }
+    const int j = cnt;
+    const int64_t S = ns, I = ni;
+    double e2 = 0.0, sc2 = 0.0;
+    for (int64_t q = threadIdx.x; q < S * S; q += blockDim.x) {
+        const int a = (int)(q % S), b = (int)(q / S);
+        if (a <= b) continue;
+        const int s1 = md[(irp_s[a] - 1) * nsym + irp_i[i] - 1];
+        const int s2 = md[(irp_s[b] - 1) * nsym + irp_i[j] - 1];
+        if (msy[(s1 - 1) * nsym + s2 - 1] != 1) continue;
+        const cplx v = csub(Hc[a + S * (i + I * (b + S * (int64_t)j))], Hc[a + S * (j + I * (b + S * (int64_t)i))]);
+        const double e = eps_s[a] + eps_s[b] - eps_i[i] - eps_i[j] + eshift;
+        const double a2 = cabs2(v);
+        e2 -= a2 / e;
+        sc2 += a2 / (e * e);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        e2 += __shfl_down_sync(0xffffffffu, e2, o);
+        sc2 += __shfl_down_sync(0xffffffffu, sc2, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) { sh[0][wid] = e2; sh[1][wid] = sc2; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { x += sh[0][w]; y += sh[1][w]; }
+        scratch[p] = x;
+        scratch[H_NOALLOC_MAX_PAIRS + p] = y;
+    }
+}
+
+// fixed-order sum of the npair partials into the two result slots
+__global__ void h_pair_final_kernel(double *scratch, int npair) {
+    if (threadIdx.x != 0) return;
+    double x = 0.0, y = 0.0;
+    for (int p = 0; p < npair; p++) {
+        x += scratch[p];
+        y += scratch[H_NOALLOC_MAX_PAIRS + p];
+    }
+    scratch[2 * H_NOALLOC_MAX_PAIRS] = x;
+    scratch[2 * H_NOALLOC_MAX_PAIRS + 1] = y;
+}
+
+static std::mutex g_noalloc_mu;
+static double *g_noalloc_ptr[128] = {};
+
+}  // namespace dcg
+
+extern "C" int dcg_solve_h_noalloc(const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
+                                   const double *eps_s, const int32_t *irp_i, const int32_t *irp_s,
+                                   const int32_t *multb_d, const int32_t *multb_s, int32_t nsymrpa, double eshift,
+                                   void *stream, double out[2]) {
+    using namespace dcg;
+    if (!out || ninact < 0 || nsec < 0 || nsymrpa < 1) return DCG_E_ARG;
+    if (ninact > H_NOALLOC_MAX_NINACT) return DCG_E_ARG;   // beyond the static scratch
+    out[0] = out[1] = 0.0;
+    if (ninact < 2 || nsec < 2) return DCG_OK;              // no pair i > j or a > b
+    if (!hclass || !eps_i || !eps_s || !irp_i || !irp_s || !multb_d || !multb_s) return DCG_E_ARG;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return DCG_E_CUDA;
+    double *scratch = nullptr;
+    {
+        // once per device, with that device current: the device address of the array
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            cudaError_t e = cudaGetSymbolAddress((void **)&g_noalloc_ptr[dev], g_h_noalloc_scratch);
+            if (e != cudaSuccess) {
+                g_noalloc_ptr[dev] = nullptr;
+                return DCG_E_CUDA;
+            }
+        }
+        scratch = g_noalloc_ptr[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const int npair = ninact * (ninact - 1) / 2;
+    h_pair_kernel<<<npair, 256, 0, st>>>(static_cast<const cplx *>(hclass), ninact, nsec, eps_i, eps_s, irp_i, irp_s,
+                                         multb_d, multb_s, nsymrpa, eshift, scratch);
+    h_pair_final_kernel<<<1, 32, 0, st>>>(scratch, npair);
+    if (cudaGetLastError() != cudaSuccess) return DCG_E_CUDA;
+    if (cudaMemcpyAsync(out, scratch + 2 * H_NOALLOC_MAX_PAIRS, 2 * sizeof(double), cudaMemcpyDeviceToHost, st) !=
+        cudaSuccess)
+        return DCG_E_CUDA;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return DCG_E_CUDA;
+    return DCG_OK;
+}

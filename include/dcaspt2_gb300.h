@@ -109,6 +109,21 @@ int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, 
                 const double *eps_s, const int32_t *irp_i, const int32_t *irp_s, const int32_t *multb_d,
                 const int32_t *multb_s, int32_t nsymrpa, double eshift, double out[2]);
 
+/* dcg_solve_h without any device allocation, for callers that cannot allocate device
+ * memory themselves (a host program whose device memory all comes from its own pool or
+ * from another runtime's allocator).  This entry point has no counterpart in the
+ * reference.  Same inputs and result as dcg_solve_h, run on `stream` (a cudaStream_t,
+ * NULL = default stream) of the current device, without a context.  Its partial sums live
+ * in a file-scope device array of the library sized for ninact <= 128 (8128 inactive
+ * pairs, 127 KiB), which every device that loads the library keeps until the process
+ * exits; ninact > 128 returns DCG_E_ARG.  The first call on a device looks up that array's
+ * device address (make that first call before any stream capture).  All calls share the
+ * array: calls that overlap on the GPU race on it and must be serialised by the caller. */
+int dcg_solve_h_noalloc(const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
+                        const double *eps_s, const int32_t *irp_i, const int32_t *irp_s,
+                        const int32_t *multb_d, const int32_t *multb_s, int32_t nsymrpa, double eshift,
+                        void *stream, double out[2]);
+
 /* Orbital energies after fockdiag (eps, nmo entries, CAS order). */
 int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n);
 
