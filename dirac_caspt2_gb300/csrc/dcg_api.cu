@@ -434,6 +434,55 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
 
 static inline int kp(int x) { return (x % 2 == 1) ? x + 1 : x - 1; }
 
+// First index whose value is within a relative 1e-8 of the maximum.
+static int first_near_max(const std::vector<double> &x) {
+    double m = x[0];
+    for (double v : x) m = std::max(m, v);
+    for (size_t i = 0; i < x.size(); i++)
+        if (x[i] >= m - 1e-8 * std::fabs(m)) return (int)i;
+    return 0;
+}
+
+// Canonical vectors inside exactly degenerate eigenvalue pairs of the active Fock block.
+// ZHEEV's choice inside a degenerate pair is decided by rounding and the reference's
+// complex E-space V build (solve_E_subspace.F90 vEmat_complex, dim1_density(it,k)) is not
+// invariant under it; this picks one of those equally valid choices deterministically:
+// v1 = P e_k/|P e_k| with k the first index of near-maximal P_kk (P the pair projector),
+// v2 the orthogonal unit vector of the pair with its first near-largest component real
+// positive.  V is n x n column-major.
+static void canonical_pairs(int n, const std::vector<double> &w, std::vector<cplx> &V) {
+    int q = 0;
+    while (q < n - 1) {
+        if (std::fabs(w[q + 1] - w[q]) > 1e-10 * std::max(1.0, std::fabs(w[q]))) {
+            q++;
+            continue;
+        }
+        cplx *c0 = V.data() + (size_t)n * q, *c1 = V.data() + (size_t)n * (q + 1);
+        std::vector<double> pk(n);
+        for (int r = 0; r < n; r++) pk[r] = cabs2(c0[r]) + cabs2(c1[r]);
+        const int k = first_near_max(pk);
+        cplx a0 = cconj(c0[k]), a1 = cconj(c1[k]);
+        const double na = std::sqrt(cabs2(a0) + cabs2(a1));
+        a0 = cscale(a0, 1.0 / na);
+        a1 = cscale(a1, 1.0 / na);
+        const cplx b0 = mk(-a1.x, a1.y), b1 = cconj(a0);   // (-conj(a1), conj(a0))
+        std::vector<cplx> v1(n), v2(n);
+        std::vector<double> m2(n);
+        for (int r = 0; r < n; r++) {
+            v1[r] = cadd(cmul(c0[r], a0), cmul(c1[r], a1));
+            v2[r] = cadd(cmul(c0[r], b0), cmul(c1[r], b1));
+            m2[r] = std::sqrt(cabs2(v2[r]));
+        }
+        const int l = first_near_max(m2);
+        const cplx ph = cscale(cconj(v2[l]), 1.0 / m2[l]);
+        for (int r = 0; r < n; r++) {
+            c0[r] = v1[r];
+            c1[r] = cmul(v2[r], ph);
+        }
+        q += 2;
+    }
+}
+
 }  // namespace dcg
 
 namespace dcg {
@@ -480,8 +529,14 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
             double *w = wsget<double>(c, "fd.w", nb);
             launch_gather2(c, f, c.nmo, dind, nb, blk);
             heev(c, nb, blk, nb, w, 0, nb, vec, nb);
-            launch_scatter2(c, vec, nb, dind, U, c.nmo);
             std::vector<double> wh = download(c, w, nb);
+            if (sp == 1) {   // active space: canonical vectors inside degenerate pairs
+                std::vector<cplx> vh = download(c, vec, (size_t)nb * nb);
+                canonical_pairs(nb, wh, vh);
+                DCG_CUDA(cudaMemcpyAsync(vec, vh.data(), sizeof(cplx) * vh.size(), cudaMemcpyHostToDevice, c.stream));
+                DCG_CUDA(cudaStreamSynchronize(c.stream));
+            }
+            launch_scatter2(c, vec, nb, dind, U, c.nmo);
             for (int q = 0; q < nb; q++) c.eps[ind[q]] = wh[q];
         }
     }

@@ -499,6 +499,46 @@ def fock_casci(s: System, ints: Integrals, g_occ: np.ndarray, D1: np.ndarray) ->
     return f
 
 
+PAIR_DEGENERACY = 1e-10
+TIE = 1e-8
+
+
+def _first_near_max(x: np.ndarray) -> int:
+    """Smallest index whose value is within a relative 1e-8 of the maximum."""
+    m = float(np.max(x))
+    return int(np.flatnonzero(x >= m - TIE * abs(m))[0])
+
+
+def canonical_pairs(w: np.ndarray, V: np.ndarray) -> np.ndarray:
+    """Canonical vectors inside exactly degenerate eigenvalue pairs.
+
+    ZHEEV's choice of vectors inside a degenerate pair is decided by rounding, and the
+    reference's complex E-space formula is not invariant under it.  For each pair (q,q+1)
+    with |w_q+1 - w_q| <= 1e-10 max(1,|w_q|): v1 = P e_k / |P e_k| with k the first basis
+    index of near-maximal P_kk (P the pair projector), v2 the unit vector of the pair
+    orthogonal to v1 with its first near-largest component real positive."""
+    V = V.copy()
+    n = len(w)
+    q = 0
+    while q < n - 1:
+        if abs(w[q + 1] - w[q]) <= PAIR_DEGENERACY * max(1.0, abs(w[q])):
+            W = V[:, q:q + 2]
+            pk = np.sum(np.abs(W) ** 2, axis=1)          # P_kk
+            k = _first_near_max(pk)
+            a = np.conj(W[k, :])
+            a = a / np.linalg.norm(a)
+            b = np.array([-np.conj(a[1]), np.conj(a[0])])
+            v1 = W @ a
+            v2 = W @ b
+            l = _first_near_max(np.abs(v2))
+            v2 = v2 * (np.conj(v2[l]) / abs(v2[l]))
+            V[:, q], V[:, q + 1] = v1, v2
+            q += 2
+        else:
+            q += 1
+    return V
+
+
 def fock_diag(s: System, f: np.ndarray):
     """fockdiag.F90:4-78 with cdiag0 (diag.F90:230-375): per space and irrep Hermitian
     eigendecomposition.  Returns (U, eps) with U block diagonal (column j = new spinor j)."""
@@ -518,6 +558,8 @@ def fock_diag(s: System, f: np.ndarray):
             low = np.tril(blk)
             herm = low + np.conj(np.tril(low, -1)).T
             w, v = heev_upper(herm)
+            if n0 == s.ninact and n1 == s.nmoc:      # active space: canonical degenerate pairs
+                v = canonical_pairs(w, v)
             eps[ind] = w
             U[np.ix_(ind, ind)] = v
     return U, eps

@@ -4,8 +4,8 @@ Tolerances: the reference tests compare total energies at abs 1e-10 Eh; per subs
 target is |dE2_X| <= 1e-9 Eh and |dE2| <= 1e-8 Eh in total.  For complex systems without
 point-group symmetry the reference's E-subspace energy depends on the eigenvector choice
 inside degenerate Kramers pairs of active spinors (its V build is not covariant under
-their phases, see oracle.e_subspace_envelope): there the GPU value must lie inside the
-range the reference algorithm produces over those choices, widened by 1e-9."""
+their phases, see oracle.e_subspace_envelope); the GPU path and the oracle both take the
+same canonical choice inside such pairs, so E is compared as strictly as the rest."""
 import os
 
 import numpy as np
@@ -65,14 +65,13 @@ def test_gpu_matches_oracle_synthetic(session, ni, na, ns, ne, seed, realonly):
     assert abs(r.casci_energies[0] - ref.casci_energies[0]) < 1e-10
     assert abs(r.e0 - ref.e0) < 1e-10
     for k in "ABCDEFGH":
-        if k == "E" and not realonly:
-            lo, hi = O.e_subspace_envelope(oracle_system(s), trials=4)
-            assert lo - TOL_SUB <= r.e2[k] <= hi + TOL_SUB, (r.e2[k], lo, hi)
-            continue
         assert abs(r.e2[k] - ref.e2.get(k, 0.0)) < TOL_SUB, (k, r.e2[k], ref.e2.get(k))
         assert abs(r.sumc2[k] - ref.sumc2.get(k, 0.0)) < TOL_SUB
-    e_slack = 0.0 if realonly else abs(r.e2["E"] - ref.e2.get("E", 0.0))
-    assert abs(r.total_energy - ref.total_energy) < TOL_TOTAL + e_slack
+    assert abs(r.total_energy - ref.total_energy) < TOL_TOTAL
+    if not realonly:
+        # the canonical choice is one of the values the reference algorithm can produce
+        lo, hi = O.e_subspace_envelope(oracle_system(s), trials=3)
+        assert lo - TOL_SUB <= r.e2["E"] <= hi + TOL_SUB
     eps = session.eps()
     assert np.allclose(np.sort(eps[:ni + na + ns]), np.sort(ref.eps[:ni + na + ns]), atol=1e-10)
 
