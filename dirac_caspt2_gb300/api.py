@@ -88,13 +88,18 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_stream.restype = ctypes.c_void_p
     lib.dcg_time_family.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_family_stats.argtypes = [ctypes.c_void_p, P(ctypes.c_double), P(ctypes.c_int64), P(ctypes.c_double)]
+    lib.dcg_stedc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                              ctypes.c_void_p]
+    lib.dcg_heev.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                             ctypes.c_void_p, ctypes.c_void_p]
     _lib = lib
     return lib
 
 
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
-                    "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h"]
+                    "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
+                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_stedc"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9}
 
@@ -329,6 +334,31 @@ class Caspt2Session:
 
     def kernel_launches(self) -> int:
         return int(self.lib.dcg_kernel_launches(self.h))
+
+    def heev(self, a: np.ndarray, vectors: bool = True):
+        """Hermitian eigendecomposition on the device (dcg_heev): ascending eigenvalues and,
+        when ``vectors``, the eigenvectors as columns.  Reads the upper triangle of ``a``."""
+        a = np.asarray(a)
+        n = a.shape[0]
+        are = np.asfortranarray(a.real, dtype=np.float64)
+        aim = np.asfortranarray(a.imag, dtype=np.float64) if np.iscomplexobj(a) else None
+        w = np.zeros(n)
+        zr = np.zeros((n, n), order="F") if vectors else None
+        zi = np.zeros((n, n), order="F") if vectors else None
+        ptr = lambda x: None if x is None else x.ctypes.data
+        self._check(self.lib.dcg_heev(self.h, n, ptr(are), ptr(aim), ptr(w), ptr(zr), ptr(zi)))
+        return (w, zr + 1j * zi) if vectors else w
+
+    def stedc(self, d: np.ndarray, e: np.ndarray, vectors: bool = True):
+        """Symmetric tridiagonal eigendecomposition on the device (dcg_stedc)."""
+        d = np.ascontiguousarray(d, dtype=np.float64)
+        e = np.ascontiguousarray(e, dtype=np.float64)
+        n = d.shape[0]
+        w = np.zeros(n)
+        z = np.zeros((n, n), order="F") if vectors else None
+        self._check(self.lib.dcg_stedc(self.h, n, d.ctypes.data, e.ctypes.data if n > 1 else None, w.ctypes.data,
+                                       z.ctypes.data if vectors else None))
+        return (w, z) if vectors else w
 
     def solve_h(self, hclass_ptr: int, ninact: int, nsec: int, eps_i_ptr: int, eps_s_ptr: int, irp_i_ptr: int,
                 irp_s_ptr: int, md_ptr: int, ms_ptr: int, nsymrpa: int, eshift: float) -> Tuple[float, float]:

@@ -16,6 +16,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "dcg_common.cuh"
 #include "dcg_kernels.cuh"
 
@@ -28,7 +30,7 @@ namespace dcg {
 // ------------------------------------------------------------------------- host helpers
 static std::vector<uint64_t> gosper_all(int na, int ne) {
     std::vector<uint64_t> out;
-    if (ne > na || na > 64) return out;
+    if (ne < 0 || ne > na || na > 64) return out;
     if (ne == 0) {
         out.push_back(0);
         return out;
@@ -103,8 +105,15 @@ static std::vector<T> download(Context &c, const T *p, size_t n) {
     return v;
 }
 
-static void stage_begin(Context &c, int st) { DCG_CUDA(cudaEventRecord(c.ev[st], c.stream)); }
+// Stage names double as NVTX range names, so a profiler can select one stage's launches.
+static const char *const kStageName[ST_COUNT] = {"ints", "casci_matrix", "casci_eig", "fock", "ci_rotation",
+                                                 "rdm", "transformation", "A", "B", "C", "D", "E", "F", "G", "H"};
+static void stage_begin(Context &c, int st) {
+    nvtxRangePushA(kStageName[st]);
+    DCG_CUDA(cudaEventRecord(c.ev[st], c.stream));
+}
 static void stage_end(Context &c, int st) {
+    nvtxRangePop();
     DCG_CUDA(cudaEventRecord(c.ev[ST_COUNT], c.stream));
     DCG_CUDA(cudaEventSynchronize(c.ev[ST_COUNT]));
     float ms = 0.f;
@@ -358,6 +367,8 @@ namespace dcg {
 // <0|E_ab = (E_ba|0>)^H, and an unrestricted intermediate determinant space.
 struct RdmBufs {
     cplx *g1 = nullptr, *gall = nullptr;
+    const cplx *Y = nullptr;   // E_pq psi over the full space (M x na^2, column p + na q)
+    int64_t M = 0;
     RDMView view;
 };
 
@@ -380,6 +391,8 @@ static RdmBufs rdm_build(Context &c, const uint64_t *full, int64_t M, const cplx
     zgemm(c, OP_C, OP_N, 1, (int)(nv * na2), (int)M, one, psi, M, 0, YZ, M, 0, zero, r.g1, 1, 0, 1);
     r.gall = wsget<cplx>(c, "rdm.gall", (size_t)na2 * ncol);
     zgemm(c, OP_C, OP_N, (int)na2, (int)ncol, (int)M, one, YZ, M, 0, YZ, M, 0, zero, r.gall, na2, 0, 1);
+    r.Y = YZ;
+    r.M = M;
     r.view.na = na;
     r.view.g1 = r.g1;
     r.view.t1 = eps_act ? r.g1 + na2 : nullptr;
@@ -397,6 +410,8 @@ struct SubCtx {
     const double *eps_act_d;   // device, active orbital energies
     std::vector<double> eps;   // host, global
     double e0;
+    const cplx *Y = nullptr;   // E_pq psi over the full nelec-electron space (M x na^2)
+    int64_t M = 0;
 };
 
 struct BlockSpec {
@@ -407,15 +422,106 @@ struct BlockSpec {
     std::vector<double> alpha;
 };
 
+// Subspace blocks A and C through the Gram factor of their overlap (S = G^H G, B = G^H D G,
+// G of size Mp x dimn over the (nelec +- 1)-electron determinants).  With G = P Sigma Q^H,
+// the kept eigenvectors of S are U = G^H P Lambda^-1/2 (Lambda = Sigma^2, the eigenvalues of
+// K = G G^H, which are those of S), so that
+//   X = U Lambda^-1/2 = G^H P Lambda^-1,   X^H v = Lambda^-1 P^H (G v),   B' = X^H B X = P^H D P.
+// The reference's 1e-8 cutoff is applied to the eigenvalues of K.  E2 is invariant to the basis
+// chosen inside the kept space, so this reproduces solve_block on (S, B) with an Mp x Mp
+// eigenproblem instead of a dimn x dimn one.
+static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, const double *Dd, const cplx *Vsel,
+                                 int nouter, const double *alpha) {
+    BlockOut r;
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    cplx *K = wsget<cplx>(c, "gram.K", (size_t)Mp * Mp);
+    zgemm(c, OP_N, OP_C, Mp, Mp, dimn, one, G, Mp, 0, G, Mp, 0, zero, K, Mp, 0, 1);
+    herm_from_upper(c, Mp, K, Mp);
+    double *wk = wsget<double>(c, "gram.wk", Mp);
+    heev(c, Mp, K, Mp, wk, Mp, Mp, nullptr, Mp);   // values first (cutoff count)
+    std::vector<double> wh = download(c, wk, Mp);
+    int vlo = Mp;
+    for (int j = 0; j < Mp; j++)
+        if (wh[j] >= 1.0e-8) { vlo = j; break; }   // cutoff.F90:37-70
+    const int dimm = Mp - vlo;
+    r.dimm = dimm;
+    if (dimm == 0 || nouter == 0) return r;
+    cplx *P = wsget<cplx>(c, "gram.P", (size_t)Mp * dimm);
+    heev_vectors_only(c, Mp, K, Mp, wk, vlo, Mp, P, Mp);
+    // VC0 = Lambda^-1 P^H (G v)
+    cplx *GV = wsget<cplx>(c, "gram.GV", (size_t)Mp * nouter);
+    zgemm(c, OP_N, OP_N, Mp, nouter, dimn, one, G, Mp, 0, Vsel, dimn, 0, zero, GV, Mp, 0, 1);
+    cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
+    zgemm(c, OP_C, OP_N, dimm, nouter, Mp, one, P, Mp, 0, GV, Mp, 0, zero, VC0, dimm, 0, 1);
+    launch_scale_rows(c, dimm, nouter, VC0, dimm, wk, vlo, true);
+    // B' = P^H D P
+    cplx *PD = wsget<cplx>(c, "gram.PD", (size_t)Mp * dimm);
+    DCG_CUDA(cudaMemcpyAsync(PD, P, sizeof(cplx) * (size_t)Mp * dimm, cudaMemcpyDeviceToDevice, c.stream));
+    launch_scale_rows(c, Mp, dimm, PD, Mp, Dd, 0, false);
+    cplx *Bp = wsget<cplx>(c, "blk.Bp", (size_t)dimm * dimm);
+    zgemm(c, OP_C, OP_N, dimm, dimm, Mp, one, P, Mp, 0, PD, Mp, 0, zero, Bp, dimm, 0, 1);
+    herm_from_upper(c, dimm, Bp, dimm);
+    double *wb = wsget<double>(c, "blk.wb", dimm);
+    cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
+    heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
+    cplx *VC1 = wsget<cplx>(c, "blk.VC1", (size_t)dimm * nouter);
+    zgemm(c, OP_C, OP_N, dimm, nouter, dimm, one, W, dimm, 0, VC0, dimm, 0, zero, VC1, dimm, 0, 1);
+    double *e2o = wsget<double>(c, "blk.e2o", nouter);
+    double *sco = wsget<double>(c, "blk.sco", nouter);
+    launch_e2(c, VC1, dimm, nouter, alpha, wb, e2o, sco);
+    double *red = wsget<double>(c, "blk.red", 2);
+    dsum(c, e2o, nouter, red);
+    dsum(c, sco, nouter, red + 1);
+    std::vector<double> hr = download(c, red, 2);
+    r.e2 = hr[0];
+    r.sc2 = hr[1];
+    return r;
+}
+
 // run the per-isym blocks of one subspace; V is the full V tensor on the device
 static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpec> &blocks, double &e2, double &sc2) {
     Context &c = *sc.c;
     e2 = 0.0;
     sc2 = 0.0;
+    // Gram route for A (nelec+1 electrons) and C (nelec-1): taken for a block whose dimension
+    // exceeds the number of determinants of that space
+    const bool gram_kind = (sub == 'A' || sub == 'C') && sc.Y != nullptr;
+    const int ne_p = sub == 'A' ? c.ne + 1 : c.ne - 1;
+    std::vector<uint64_t> dets_p;
+    if (gram_kind) dets_p = gosper_all(c.na, ne_p);
+    const int Mp = (int)dets_p.size();
+    uint64_t *d_dets_p = nullptr;
+    double *d_Dp = nullptr;
     for (size_t bi = 0; bi < blocks.size(); bi++) {
         BlockSpec &b = blocks[bi];
         if (b.dimn == 0) continue;
         const int nouter = (int)b.outer_off.size();
+        if (gram_kind && b.dimn > Mp) {
+            if (Mp == 0 || nouter == 0) continue;   // S = 0 (or no outer index): no contribution
+            if (!d_dets_p) {
+                std::vector<double> Dp(Mp);
+                for (int r = 0; r < Mp; r++) {
+                    double e = 0.0;
+                    for (int w = 0; w < c.na; w++)
+                        if ((dets_p[r] >> w) & 1ull) e += sc.eps[c.ni + w];
+                    Dp[r] = e;
+                }
+                d_dets_p = upload(c, "gram.dets", dets_p);
+                d_Dp = upload(c, "gram.D", Dp);
+            }
+            int *ind = upload(c, "blk.ind", b.ind);
+            cplx *G = wsget<cplx>(c, "gram.G", (size_t)Mp * b.dimn);
+            launch_gram(c, c.na, Mp, d_dets_p, sc.M, sc.Y, ind, b.dimn, sub == 'A' ? 1 : 0, G);
+            int64_t *oo = upload(c, "blk.oo", b.outer_off);
+            int64_t *io = upload(c, "blk.io", b.inner_off);
+            double *al = upload(c, "blk.alpha", b.alpha);
+            cplx *Vsel = wsget<cplx>(c, "blk.Vsel", (size_t)b.dimn * nouter);
+            launch_gather_v(c, V, oo, nouter, io, b.dimn, Vsel);
+            BlockOut o = solve_gram_block(c, Mp, b.dimn, G, d_Dp, Vsel, nouter, al);
+            e2 += o.e2;
+            sc2 += o.sc2;
+            continue;
+        }
         int *ind = upload(c, "blk.ind", b.ind);
         cplx *S = wsget<cplx>(c, "blk.S", (size_t)b.dimn * b.dimn);
         cplx *B = wsget<cplx>(c, "blk.B", (size_t)b.dimn * b.dimn);
@@ -607,7 +713,9 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         cplx *out = wsget<cplx>(c, std::string("tr.") + name, sz + 1);
         const cplx *Ux[4] = {Usp[sp[0]], Usp[sp[1]], Usp[sp[2]], Usp[sp[3]]};
         FamScope fs(c, DCG_FAM_TRANSFORM, 8.0 * (double)sz * (dm[0] + dm[1] + dm[2] + dm[3]));
+        nvtxRangePushA((std::string("tr_") + name).c_str());
         transform4(c, src, out, ttmp, dm, Ux);
+        nvtxRangePop();
         return out;
     };
     auto tr_id = [&](const char *name, int id) -> cplx * { return tr_class(name, d.cls[id].p, d.cls[id].sp, d.cls[id].dim); };
@@ -619,6 +727,8 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
     sc.eps_act_d = eps_act_d;
     sc.eps = c.eps;
     sc.e0 = e0;
+    sc.Y = rd.Y;
+    sc.M = rd.M;
     const double es = c.eshift;
     auto irp = [&](int g) { return c.irpamo[g]; };
     const bool c1sym = (c.nsym == 1);
@@ -984,6 +1094,50 @@ const char *dcg_version(void) { return "dcaspt2_gb300 0.1 (sm_103a, FP64 path)";
 
 void *dcg_stream(const dcg_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
 
+int dcg_stedc(dcg_ctx *ctx, int32_t n, const double *d, const double *e, double *w_out, double *z_out) {
+    if (n < 0 || (n > 0 && (!d || !w_out || (n > 1 && !e)))) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        if (n == 0) return DCG_OK;
+        double *dd = dcg::wsget<double>(c_, "abi.stedc.d", n);
+        double *de = dcg::wsget<double>(c_, "abi.stedc.e", n);
+        double *w = dcg::wsget<double>(c_, "abi.stedc.w", n);
+        DCG_CUDA(cudaMemcpyAsync(dd, d, n * sizeof(double), cudaMemcpyHostToDevice, c_.stream));
+        if (n > 1) DCG_CUDA(cudaMemcpyAsync(de, e, (n - 1) * sizeof(double), cudaMemcpyHostToDevice, c_.stream));
+        const double *Q = dcg::stedc(c_, n, dd, de, w);
+        DCG_CUDA(cudaMemcpyAsync(w_out, w, n * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+        if (z_out)
+            DCG_CUDA(cudaMemcpyAsync(z_out, Q, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        return DCG_OK;
+    });
+}
+
+int dcg_heev(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, double *w_out, double *z_re,
+             double *z_im) {
+    if (n < 0 || (n > 0 && (!a_re || !w_out))) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        if (n == 0) return DCG_OK;
+        const size_t nn = (size_t)n * n;
+        std::vector<dcg::cplx> h(nn);
+        for (size_t x = 0; x < nn; x++) h[x] = dcg::mk(a_re[x], a_im ? a_im[x] : 0.0);
+        dcg::cplx *A = dcg::wsget<dcg::cplx>(c_, "abi.heev.A", nn);
+        dcg::cplx *Z = dcg::wsget<dcg::cplx>(c_, "abi.heev.Z", nn);
+        double *w = dcg::wsget<double>(c_, "abi.heev.w", n);
+        DCG_CUDA(cudaMemcpyAsync(A, h.data(), nn * sizeof(dcg::cplx), cudaMemcpyHostToDevice, c_.stream));
+        dcg::herm_from_upper(c_, n, A, n);
+        dcg::heev(c_, n, A, n, w, 0, z_re ? n : 0, z_re ? Z : nullptr, n);
+        DCG_CUDA(cudaMemcpyAsync(w_out, w, n * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+        if (z_re) DCG_CUDA(cudaMemcpyAsync(h.data(), Z, nn * sizeof(dcg::cplx), cudaMemcpyDeviceToHost, c_.stream));
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        if (z_re)
+            for (size_t x = 0; x < nn; x++) {
+                z_re[x] = h[x].x;
+                if (z_im) z_im[x] = h[x].y;
+            }
+        return DCG_OK;
+    });
+}
+
 int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
                 const double *eps_s, const int32_t *irp_i, const int32_t *irp_s, const int32_t *multb_d,
                 const int32_t *multb_s, int32_t nsymrpa, double eshift, double out[2]) {
@@ -1020,6 +1174,9 @@ int dcg_time_family(dcg_ctx *ctx, int32_t family) {
 int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work) {
     if (!ctx) return DCG_E_ARG;
     const Context &c = ctx->c;
+    // fold in events still pending from calls that do not collect them (dcg_heev, dcg_stedc)
+    cudaSetDevice(c.device);
+    dcg::fam_collect(const_cast<Context &>(c));
     if (ms) *ms = c.fam_ms;
     if (launches) *launches = c.fam_launches;
     if (work) *work = c.fam_work;

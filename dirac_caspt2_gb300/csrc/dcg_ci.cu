@@ -214,6 +214,56 @@ void launch_apply_E(Context &c, int na, int64_t M, const uint64_t *full, const c
     DCG_LAUNCHED(c);
 }
 
+// Gram factor of the A and C overlap matrices.  Column j of G holds, over the determinants of
+// the (nelec +- 1)-electron space (colex order, dets_p), the vector
+//   create = 1 (subspace A): a_x^+ E_yz |0>     create = 0 (subspace C): a_x E_yz |0>
+// with (x, y, z) = ind[3j..3j+2] and E_yz|0> taken from Y (column y + na z, M rows, the
+// nelec-electron full space).  Sign convention of the CI code: a creation or annihilation of
+// orbital x carries (-1)^(occupied orbitals above x).  With it, S = G^H G and B = G^H D G
+// where D is the active Fock operator, diagonal over the determinants of dets_p.
+__global__ void gram_kernel(int na, int64_t Mp, const uint64_t *__restrict__ dets_p, int64_t M,
+                            const cplx *__restrict__ Y, const int *__restrict__ ind, int dimn, int create,
+                            cplx *G) {
+    const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (r >= Mp || j >= dimn) return;
+    const int x = ind[3 * j], y = ind[3 * j + 1], z = ind[3 * j + 2];
+    const uint64_t J = dets_p[r];
+    const uint64_t bit = 1ull << x;
+    cplx val = mk(0.0, 0.0);
+    const bool has = (J & bit) != 0;
+    if (create ? has : !has) {
+        const uint64_t I = create ? (J & ~bit) : (J | bit);   // nelec-electron source determinant
+        const uint64_t above = I & ~((bit << 1) - 1);
+        val = Y[colex_rank(I) + M * (int64_t)(y + na * z)];
+        if (__popcll(above) & 1) val = mk(-val.x, -val.y);
+    }
+    G[r + Mp * (int64_t)j] = val;
+}
+
+void launch_gram(Context &c, int na, int64_t Mp, const uint64_t *dets_p, int64_t M, const cplx *Y, const int *ind,
+                 int dimn, int create, cplx *G) {
+    dim3 grid(grid1d(Mp, 128), (unsigned)dimn);
+    gram_kernel<<<grid, 128, 0, c.stream>>>(na, Mp, dets_p, M, Y, ind, dimn, create, G);
+    DCG_LAUNCHED(c);
+}
+
+// A(i, j) *= s[i] (column-major, lda)
+__global__ void scale_rows_kernel(int m, int n, cplx *A, int64_t lda, const double *__restrict__ s, int soff, int inv) {
+    const int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)m * n) return;
+    const int i = (int)(idx % m), j = (int)(idx / m);
+    const double f = inv ? 1.0 / s[soff + i] : s[soff + i];
+    cplx &a = A[i + (int64_t)j * lda];
+    a = mk(a.x * f, a.y * f);
+}
+
+void launch_scale_rows(Context &c, int m, int n, cplx *A, int64_t lda, const double *s, int soff, bool inv) {
+    if ((int64_t)m * n == 0) return;
+    scale_rows_kernel<<<grid1d((int64_t)m * n, 256), 256, 0, c.stream>>>(m, n, A, lda, s, soff, inv ? 1 : 0);
+    DCG_LAUNCHED(c);
+}
+
 // psi_t[K] = psi[K] * sum_{w in K} eps_act[w]  (Fock operator of the active space acting
 // on |0>, the E_ww factor of the reference's dim(n+1)_density(..., w, w) calls)
 __global__ void occ_energy_kernel(int na, int64_t M, const uint64_t *__restrict__ full, const double *__restrict__ eps_act,

@@ -89,6 +89,10 @@ struct Context {
     int fam = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fam_ev;
     double fam_ms = 0.0, fam_work = 0.0;
+    // tridiagonal eigenvectors of the last heev (device, n x n), for heev_vectors_only
+    const double *eig_Q = nullptr;
+    int eig_n = 0;
+    int *eig_status = nullptr;
     int64_t fam_launches = 0;
 
     // ---- system (host copies)
@@ -184,6 +188,10 @@ void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, 
 // Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (same A, w).
 void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
                        int64_t ldz);
+
+// Symmetric tridiagonal eigendecomposition by divide and conquer (d: n, e: n-1, device);
+// ascending eigenvalues into w, eigenvectors returned (n x n, ld n, workspace-owned).
+const double *stedc(Context &c, int n, const double *d, const double *e, double *w);
 
 // Solve A x = b (n x n, LU with partial pivoting), b overwritten.  Returns info.
 int zgesv(Context &c, int n, cplx *A, int64_t lda, cplx *b);

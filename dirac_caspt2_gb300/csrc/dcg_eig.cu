@@ -1,0 +1,1017 @@
+// Hermitian eigensolver on the device (FP64), the replacement of the reference's ZHEEV /
+// DSYEV calls (src/diag.F90:43,109).  Eigenvalues come out ascending, as there.
+//
+// Three phases, each written from the published algorithm:
+//   1. Householder reduction of the Hermitian matrix to a real symmetric tridiagonal
+//      (Golub & Van Loan, Matrix Computations, 4th ed., 8.3.1) with the complex reflector
+//      of LAPACK's documented xLARFG definition (beta real).
+//   2. Cuppen's divide and conquer on the tridiagonal (GVL 8.4.4): the tridiagonal is torn
+//      into 1x1 leaves by rank-one modifications; sibling blocks are merged level by level.
+//      Each merge deflates (small rank-one components, and Givens rotations for pairs of
+//      close poles: Dongarra & Sorensen, SIAM J. Sci. Stat. Comput. 8 (1987) s139), solves
+//      the secular equation one root per warp with a bracketed two-pole rational model
+//      (Bunch, Nielsen & Sorensen, Numer. Math. 31 (1978) 31), recomputes the rank-one
+//      vector from the roots so the eigenvectors stay orthogonal (Gu & Eisenstat, SIAM J.
+//      Matrix Anal. Appl. 16 (1995) 172), and applies the merge's eigenvector matrix with one
+//      batched GEMM per level.
+//   3. Back-transformation of the requested eigenvectors by the stored reflectors.
+//
+// The merge tree is the power-of-two tree: at level l a node covers columns
+// [i 2^l, min((i+1) 2^l, n)) and is split after its first 2^(l-1) columns, so a node's
+// geometry follows from (l, i) and no tree is stored.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+
+#include "dcg_common.cuh"
+
+namespace dcg {
+
+constexpr double kUnitRoundoff = 1.1102230246251565e-16;   // 2^-53
+constexpr int kSecularMaxIter = 100;
+
+__device__ __forceinline__ double eig_warp_sum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);   // lane 0's value in every lane
+}
+__device__ __forceinline__ double eig_warp_prod(double v) {
+    for (int o = 16; o > 0; o >>= 1) v *= __shfl_down_sync(0xffffffffu, v, o);
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+__device__ __forceinline__ double eig_warp_max(double v) {
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return __shfl_sync(0xffffffffu, v, 0);
+}
+
+// Deterministic block sum (fixed tree); every thread gets the result.  sh >= 32 doubles.
+__device__ double eig_block_sum(double v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = eig_warp_sum(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (wid == 0) {
+        t = lane < nw ? sh[lane] : 0.0;
+        t = eig_warp_sum(t);
+        if (lane == 0) sh[0] = t;
+    }
+    __syncthreads();
+    t = sh[0];
+    __syncthreads();
+    return t;
+}
+
+__device__ double eig_block_max(double v, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = eig_warp_max(v);
+    __syncthreads();
+    if (lane == 0) sh[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    if (wid == 0) {
+        t = lane < nw ? sh[lane] : 0.0;
+        t = eig_warp_max(t);
+        if (lane == 0) sh[0] = t;
+    }
+    __syncthreads();
+    t = sh[0];
+    __syncthreads();
+    return t;
+}
+
+// ===================================================================== 1. tridiagonal reduction
+// Step k: reflector for column k (rows k+1..n-1), v stored in A(k+1:n-1, k) with v0 = 1.
+__global__ void hh_gen_kernel(int n, int k, cplx *A, int64_t lda, double *d, double *e, cplx *tau) {
+    __shared__ double sh[32];
+    __shared__ cplx s_scale;
+    __shared__ int s_skip;
+    const int m = n - k - 1;
+    cplx *x = A + (k + 1) + (int64_t)k * lda;
+    double s = 0.0;
+    for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) s += cabs2(x[i]);
+    s = eig_block_sum(s, sh);
+    if (threadIdx.x == 0) {
+        cplx alpha = x[0];
+        double xnorm = sqrt(s);
+        cplx t;
+        double beta;
+        if (xnorm == 0.0 && alpha.y == 0.0) {
+            t = mk(0.0, 0.0);
+            beta = alpha.x;
+            s_skip = 1;
+        } else {
+            double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+            beta = alpha.x >= 0.0 ? -nrm : nrm;
+            t = mk((beta - alpha.x) / beta, -alpha.y / beta);
+            s_scale = cdiv(mk(1.0, 0.0), mk(alpha.x - beta, alpha.y));
+            s_skip = 0;
+        }
+        tau[k] = t;
+        e[k] = beta;
+        d[k] = A[k + (int64_t)k * lda].x;
+    }
+    __syncthreads();
+    if (!s_skip)
+        for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) x[i] = cmul(x[i], s_scale);
+    __syncthreads();
+    if (threadIdx.x == 0) x[0] = mk(1.0, 0.0);
+}
+
+// partial p(i) = sum_{j in chunk} A(k+1+i, k+1+j) v(j)
+constexpr int HH_CHUNK = 256;
+__global__ void hh_matvec_kernel(int n, int k, const cplx *__restrict__ A, int64_t lda, const cplx *__restrict__ tau,
+                                 cplx *ppart) {
+    __shared__ cplx vs[HH_CHUNK];
+    const int m = n - k - 1;
+    const cplx t = tau[k];
+    const int j0 = blockIdx.y * HH_CHUNK;
+    const int j1 = min(m, j0 + HH_CHUNK);
+    const cplx *v = A + (k + 1) + (int64_t)k * lda;
+    for (int j = threadIdx.x; j < j1 - j0; j += blockDim.x) vs[j] = v[j0 + j];
+    __syncthreads();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= m) return;
+    cplx acc = mk(0.0, 0.0);
+    if (t.x != 0.0 || t.y != 0.0) {
+        const cplx *Ai = A + (k + 1 + i) + (int64_t)(k + 1) * lda;
+        for (int j = j0; j < j1; j++) cfma(acc, Ai[(int64_t)j * lda], vs[j - j0]);
+    }
+    ppart[(int64_t)blockIdx.y * n + i] = acc;
+}
+
+// w = tau*p + alpha v,  alpha = -1/2 tau (x^H v) with x = tau*p
+__global__ void hh_w_kernel(int n, int k, const cplx *A, int64_t lda, const cplx *tau, const cplx *ppart,
+                            int nchunk, cplx *w) {
+    __shared__ double sh[32];
+    const int m = n - k - 1;
+    const cplx t = tau[k];
+    const cplx *v = A + (k + 1) + (int64_t)k * lda;
+    double sr = 0.0, si = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        cplx p = mk(0.0, 0.0);
+        for (int c = 0; c < nchunk; c++) p = cadd(p, ppart[(int64_t)c * n + i]);
+        cplx x = cmul(t, p);
+        w[i] = x;
+        cplx xv = cmul(cconj(x), v[i]);
+        sr += xv.x;
+        si += xv.y;
+    }
+    sr = eig_block_sum(sr, sh);
+    si = eig_block_sum(si, sh);
+    cplx alpha = cmul(mk(-0.5, 0.0), cmul(t, mk(sr, si)));
+    for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = cadd(w[i], cmul(alpha, v[i]));
+}
+
+// A(k+1:, k+1:) -= v w^H + w v^H
+__global__ void hh_update_kernel(int n, int k, cplx *A, int64_t lda, const cplx *w) {
+    const int m = n - k - 1;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y;
+    if (i >= m || j >= m) return;
+    const cplx *v = A + (k + 1) + (int64_t)k * lda;
+    cplx vi = v[i], vj = v[j], wi = w[i], wj = w[j];
+    int64_t o = (k + 1 + i) + (int64_t)(k + 1 + j) * lda;
+    cplx a = A[o];
+    a = csub(a, cmulc(vi, wj));
+    a = csub(a, cmulc(wi, vj));
+    if (i == j) a.y = 0.0;
+    A[o] = a;
+}
+
+__global__ void hh_last_kernel(int n, const cplx *A, int64_t lda, double *d) {
+    d[n - 1] = A[(n - 1) + (int64_t)(n - 1) * lda].x;
+}
+
+// ---- persistent form: one cooperative launch for all columns, two grid barriers per column.
+// Every block recomputes the reflector of column k (identical arithmetic in every block) and
+// stages v in shared memory; a warp per column computes p = A22 v (A22 Hermitian, so
+// p_i = column i of A22, conjugated, dotted with v); after the first barrier every block
+// forms w = tau p + alpha v and applies A22 -= v w^H + w v^H to its columns.  Data written by
+// other blocks is read with ld.global.cg so no stale L1 line is used.
+struct GridBar {
+    unsigned count;
+    unsigned gen;
+    int err;       // 1: a barrier wait exceeded its time limit
+    int pad;
+};
+
+__device__ __forceinline__ uint64_t globaltimer_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid-wide barrier for a cooperative launch.  Each wait is bounded (5 s); a block that
+// gives up sets gb->err and every block then leaves the kernel.
+constexpr uint64_t kBarrierLimitNs = 5000000000ull;
+__device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned nblocks) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned *vgen = &gb->gen;
+        volatile int *verr = &gb->err;
+        const unsigned g = *vgen;
+        __threadfence();
+        if (atomicAdd(&gb->count, 1u) == nblocks - 1) {
+            atomicExch(&gb->count, 0u);
+            __threadfence();
+            atomicAdd(&gb->gen, 1u);
+        } else {
+            const uint64_t t0 = globaltimer_ns();
+            while (*vgen == g && *verr == 0) {
+                if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+                    atomicExch(&gb->err, 1);
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        __threadfence();
+        s_ok = (*verr == 0);
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+__device__ __forceinline__ cplx ldcg(const cplx *p) { return __ldcg(p); }
+
+constexpr int TRD_THREADS = 512;
+constexpr int TRD_UNROLL = 8;
+constexpr int kTridiagPersistentMaxN = 7000;   // v and w staged in shared memory: 32 bytes per row
+
+__global__ void __launch_bounds__(TRD_THREADS) tridiag_persistent_kernel(int n, cplx *A, int64_t lda, double *d,
+                                                                         double *e, cplx *tau, cplx *pbuf,
+                                                                         double2 *part, GridBar *gb) {
+    extern __shared__ cplx tsm[];
+    __shared__ double red[32];
+    __shared__ cplx s_scale, s_tau, s_alpha;
+    __shared__ double s_beta;
+    __shared__ int s_skip;
+    const unsigned nb = gridDim.x;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int gw = blockIdx.x * nwb + wib, nw = nb * nwb;
+    cplx *sv = tsm, *sw = tsm + (n > 1 ? n - 1 : 1);
+    for (int k = 0; k + 1 < n; k++) {
+        const int m = n - k - 1;
+        cplx *x = A + (k + 1) + (int64_t)k * lda;
+        // reflector of column k (same in every block)
+        double ss = 0.0;
+        for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) ss += cabs2(ldcg(x + i));
+        ss = eig_block_sum(ss, red);
+        if (threadIdx.x == 0) {
+            const cplx alpha = ldcg(x);
+            const double xnorm = sqrt(ss);
+            if (xnorm == 0.0 && alpha.y == 0.0) {
+                s_tau = mk(0.0, 0.0);
+                s_beta = alpha.x;
+                s_skip = 1;
+                s_scale = mk(1.0, 0.0);
+            } else {
+                const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+                const double beta = alpha.x >= 0.0 ? -nrm : nrm;
+                s_tau = mk((beta - alpha.x) / beta, -alpha.y / beta);
+                s_beta = beta;
+                s_scale = cdiv(mk(1.0, 0.0), mk(alpha.x - beta, alpha.y));
+                s_skip = 0;
+            }
+        }
+        __syncthreads();
+        const cplx t = s_tau, sc = s_scale;
+        const bool active = !s_skip;
+        for (int i = threadIdx.x; i < m; i += blockDim.x) sv[i] = i == 0 ? mk(1.0, 0.0) : (active ? cmul(ldcg(x + i), sc) : ldcg(x + i));
+        __syncthreads();
+        // p = tau * A22 v (warp per column), partial x^H v with x = tau p
+        double pr = 0.0, pim = 0.0;
+        if (active) {
+            for (int i = gw; i < m; i += nw) {
+                const cplx *col = A + (k + 1) + (int64_t)(k + 1 + i) * lda;
+                // conj(column) . v with TRD_UNROLL loads in flight per lane (the loop is L2-latency bound)
+                double arr[TRD_UNROLL], aii[TRD_UNROLL];
+#pragma unroll
+                for (int u = 0; u < TRD_UNROLL; u++) arr[u] = aii[u] = 0.0;
+                int j = lane;
+                for (; j + 32 * (TRD_UNROLL - 1) < m; j += 32 * TRD_UNROLL) {
+                    cplx a[TRD_UNROLL];
+#pragma unroll
+                    for (int u = 0; u < TRD_UNROLL; u++) a[u] = ldcg(col + j + 32 * u);
+#pragma unroll
+                    for (int u = 0; u < TRD_UNROLL; u++) {
+                        const cplx v = sv[j + 32 * u];
+                        arr[u] += a[u].x * v.x + a[u].y * v.y;
+                        aii[u] += a[u].x * v.y - a[u].y * v.x;
+                    }
+                }
+                for (; j < m; j += 32) {
+                    const cplx a = ldcg(col + j), v = sv[j];
+                    arr[0] += a.x * v.x + a.y * v.y;
+                    aii[0] += a.x * v.y - a.y * v.x;
+                }
+                double ar = 0.0, ai = 0.0;
+#pragma unroll
+                for (int u = 0; u < TRD_UNROLL; u++) {
+                    ar += arr[u];
+                    ai += aii[u];
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    ar += __shfl_down_sync(0xffffffffu, ar, o);
+                    ai += __shfl_down_sync(0xffffffffu, ai, o);
+                }
+                if (lane == 0) {
+                    const cplx xp = cmul(t, mk(ar, ai));
+                    pbuf[i] = xp;
+                    const cplx xv = cmul(cconj(xp), sv[i]);
+                    pr += xv.x;
+                    pim += xv.y;
+                }
+            }
+        }
+        pr = eig_block_sum(pr, red);
+        pim = eig_block_sum(pim, red);
+        if (threadIdx.x == 0) part[blockIdx.x] = make_double2(pr, pim);
+        if (!grid_barrier(gb, nb)) return;
+        if (active) {
+            double sr = 0.0, si = 0.0;
+            for (unsigned b = threadIdx.x; b < nb; b += blockDim.x) {
+                const double2 q = __ldcg(part + b);
+                sr += q.x;
+                si += q.y;
+            }
+            sr = eig_block_sum(sr, red);
+            si = eig_block_sum(si, red);
+            if (threadIdx.x == 0) s_alpha = cmul(mk(-0.5, 0.0), cmul(t, mk(sr, si)));
+            __syncthreads();
+            const cplx al = s_alpha;
+            for (int i = threadIdx.x; i < m; i += blockDim.x) sw[i] = cadd(ldcg(pbuf + i), cmul(al, sv[i]));
+            __syncthreads();
+            for (int j = gw; j < m; j += nw) {
+                const cplx vj = sv[j], wj = sw[j];
+                cplx *col = A + (k + 1) + (int64_t)(k + 1 + j) * lda;
+                int i = lane;
+                for (; i + 32 * (TRD_UNROLL - 1) < m; i += 32 * TRD_UNROLL) {
+                    cplx a[TRD_UNROLL];
+#pragma unroll
+                    for (int u = 0; u < TRD_UNROLL; u++) a[u] = ldcg(col + i + 32 * u);
+#pragma unroll
+                    for (int u = 0; u < TRD_UNROLL; u++) {
+                        const int r = i + 32 * u;
+                        cplx x = csub(a[u], cmulc(sv[r], wj));
+                        x = csub(x, cmulc(sw[r], vj));
+                        if (r == j) x.y = 0.0;
+                        col[r] = x;
+                    }
+                }
+                for (; i < m; i += 32) {
+                    cplx a = ldcg(col + i);
+                    a = csub(a, cmulc(sv[i], wj));
+                    a = csub(a, cmulc(sw[i], vj));
+                    if (i == j) a.y = 0.0;
+                    col[i] = a;
+                }
+            }
+        }
+        if (blockIdx.x == 0) {
+            for (int i = threadIdx.x; i < m; i += blockDim.x) x[i] = sv[i];
+            if (threadIdx.x == 0) {
+                d[k] = ldcg(A + k + (int64_t)k * lda).x;
+                e[k] = s_beta;
+                tau[k] = t;
+            }
+        }
+        if (!grid_barrier(gb, nb)) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) d[n - 1] = ldcg(A + (n - 1) + (int64_t)(n - 1) * lda).x;
+}
+
+// ===================================================================== 2. divide and conquer
+// Per-level scratch, every array of length n and sliced by node (a node owns [s, s+N)).
+struct DcBufs {
+    double *lamA, *lamB;      // eigenvalues of the current / next level
+    double *QA, *QB;          // eigenvector matrices (n x n, ld n), block diagonal by node
+    double *U;                // merge eigenvector matrices, block diagonal (n x n, ld n)
+    double *dK, *zK;          // undeflated poles and rank-one components (compact, per node)
+    double *dv;               // deflated eigenvalues (per node)
+    int *Kl, *defl;           // node-local column of each undeflated / deflated entry
+    int *rp, *rn;             // Givens rotation column pairs
+    double *rc, *rs;          // and their cosines / sines
+    int *ord;                 // origin pole of each secular root
+    double *tau, *lamK;       // root offset from its origin, root value
+    double *zh;               // recomputed rank-one vector
+    int *outc;                // output column of each node entry in the next level
+    int *kcnt, *ndef, *nrot;  // per node: undeflated count (-1: pass-through), deflated, rotations
+    double *rho;              // per node
+    int *status;              // nonzero: a merge met an inconsistent pole order
+};
+
+__global__ void dc_leaf_kernel(int n, const double *__restrict__ d, const double *__restrict__ e, double *lam,
+                               double *Q) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    double v = d[i];
+    if (i > 0) v -= fabs(e[i - 1]);
+    if (i < n - 1) v -= fabs(e[i]);
+    lam[i] = v;
+    Q[i + (int64_t)i * n] = 1.0;
+}
+
+// One block per node: rank-one vector, merge order, deflation (thread 0 scans the merged
+// order), rotations applied to the node's eigenvector columns.  Dynamic shared memory:
+// 20 bytes per node column.
+__global__ void dc_prep_kernel(int n, int half, int full, const double *__restrict__ e, DcBufs b) {
+    extern __shared__ double smem[];
+    __shared__ double red[32];
+    const int node = blockIdx.x;
+    const int s = node * full;
+    const int N = min(full, n - s);
+    const int n1 = half, n2 = N - half;
+    if (n2 <= 0) {   // no right sibling at this level: carry the block over
+        for (int i = threadIdx.x; i < N; i += blockDim.x) b.lamB[s + i] = b.lamA[s + i];
+        for (int64_t x = threadIdx.x; x < (int64_t)N * N; x += blockDim.x) {
+            const int r = (int)(x % N), cc = (int)(x / N);
+            b.QB[(s + r) + (int64_t)(s + cc) * n] = b.QA[(s + r) + (int64_t)(s + cc) * n];
+        }
+        if (threadIdx.x == 0) b.kcnt[node] = -1;
+        return;
+    }
+    double *sd = smem, *sz = smem + N;
+    int *sp = reinterpret_cast<int *>(smem + 2 * N);
+    const double beta = e[s + n1 - 1];
+    const double rho = 2.0 * fabs(beta);
+    const double sg = beta < 0.0 ? -1.0 : 1.0;
+    double mx = 0.0;
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        sd[i] = b.lamA[s + i];
+        const double q = i < n1 ? b.QA[(s + n1 - 1) + (int64_t)(s + i) * n] : sg * b.QA[(s + n1) + (int64_t)(s + i) * n];
+        sz[i] = q * 0.70710678118654752440;
+        mx = fmax(mx, fmax(fabs(sd[i]), fabs(sz[i])));
+    }
+    const double tol = 8.0 * kUnitRoundoff * eig_block_max(mx, red);   // syncs the block
+    // stable merge of the two ascending halves
+    for (int i = threadIdx.x; i < N; i += blockDim.x) {
+        const double v = sd[i];
+        int lo, hi;
+        if (i < n1) {   // count right entries strictly below v
+            lo = n1;
+            hi = N;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (sd[mid] < v) lo = mid + 1;
+                else hi = mid;
+            }
+            sp[i + (lo - n1)] = i;
+        } else {        // count left entries at or below v
+            lo = 0;
+            hi = n1;
+            while (lo < hi) {
+                int mid = (lo + hi) >> 1;
+                if (sd[mid] <= v) lo = mid + 1;
+                else hi = mid;
+            }
+            sp[(i - n1) + lo] = i;
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int kc = 0, nd = 0, nr = 0, pj = -1;
+        for (int t = 0; t < N; t++) {
+            const int nj = sp[t];
+            if (rho * fabs(sz[nj]) <= tol) {
+                b.defl[s + nd++] = nj;
+                continue;
+            }
+            if (pj >= 0) {
+                double S = sz[pj], C = sz[nj];
+                const double tt = hypot(C, S);
+                const double T = sd[nj] - sd[pj];
+                C /= tt;
+                S = -S / tt;
+                if (fabs(T * C * S) <= tol) {
+                    sz[nj] = tt;
+                    sz[pj] = 0.0;
+                    b.rp[s + nr] = pj;
+                    b.rn[s + nr] = nj;
+                    b.rc[s + nr] = C;
+                    b.rs[s + nr] = S;
+                    nr++;
+                    const double dp = sd[pj], dn = sd[nj];
+                    sd[pj] = dp * C * C + dn * S * S;
+                    sd[nj] = dp * S * S + dn * C * C;
+                    b.defl[s + nd++] = pj;
+                    kc--;
+                }
+            }
+            b.Kl[s + kc++] = nj;
+            pj = nj;
+        }
+        b.kcnt[node] = kc;
+        b.ndef[node] = nd;
+        b.nrot[node] = nr;
+        b.rho[node] = rho;
+    }
+    __syncthreads();
+    const int kc = b.kcnt[node], nd = b.ndef[node], nr = b.nrot[node];
+    for (int m = threadIdx.x; m < kc; m += blockDim.x) {
+        const int j = b.Kl[s + m];
+        b.dK[s + m] = sd[j];
+        b.zK[s + m] = sz[j];
+    }
+    for (int m = threadIdx.x; m < nd; m += blockDim.x) b.dv[s + m] = sd[b.defl[s + m]];
+    if (nr > 0)
+        for (int r = threadIdx.x; r < N; r += blockDim.x) {
+            double *row = b.QA + (s + r);
+            for (int q = 0; q < nr; q++) {
+                const int64_t op = (int64_t)(s + b.rp[s + q]) * n, on = (int64_t)(s + b.rn[s + q]) * n;
+                const double C = b.rc[s + q], S = b.rs[s + q];
+                const double x = row[op], y = row[on];
+                row[op] = C * x + S * y;
+                row[on] = C * y - S * x;
+            }
+        }
+}
+
+// One warp per secular root: root j of 1/rho + sum_i z_i^2 / (d_i - lambda) = 0 lies in
+// (d_j, d_{j+1}) (the last one in (d_{k-1}, d_{k-1} + rho |z|^2)).  It is found as an offset
+// tau from the nearer pole d_o, so that d_i - lambda = (d_i - d_o) - tau keeps full
+// accuracy.  Each step fits c + s1/(dL - x) + s2/(dR - x) to the value and slope of the two
+// partial sums at tau and takes that model's root; steps leaving the bracket bisect.
+// All lanes hold identical scalars (lane 0's sums are broadcast), so the warp stays uniform.
+__global__ void dc_secular_kernel(int n, int full, DcBufs b) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const int node = w / full, s = node * full, j = w - s;
+    const int k = b.kcnt[node];
+    if (k < 0 || j >= k) return;
+    const double *dk = b.dK + s, *zk = b.zK + s;
+    const double rho = b.rho[node], rhoinv = 1.0 / rho;
+    int o;
+    double lo, hi;
+    if (j < k - 1) {
+        const double dl = dk[j], dr = dk[j + 1];
+        if (!(dr > dl)) {
+            if (lane == 0) {
+                atomicExch(b.status, 1);
+                b.ord[s + j] = j;
+                b.tau[s + j] = 0.0;
+                b.lamK[s + j] = dl;
+            }
+            return;
+        }
+        const double hg = 0.5 * (dr - dl);
+        double p = 0.0;
+        for (int i = lane; i < k; i += 32) p += zk[i] * zk[i] / ((dk[i] - dl) - hg);
+        const double g = rhoinv + eig_warp_sum(p);
+        if (g > 0.0) {
+            o = j;
+            lo = 0.0;
+            hi = hg;
+        } else {
+            o = j + 1;
+            lo = -hg;
+            hi = 0.0;
+        }
+    } else {
+        double p = 0.0;
+        for (int i = lane; i < k; i += 32) p += zk[i] * zk[i];
+        o = j;
+        lo = 0.0;
+        hi = rho * eig_warp_sum(p);
+    }
+    const double d_o = dk[o];
+    const int L = j, R = j + 1;
+    const double dL = dk[L] - d_o, dR = R < k ? dk[R] - d_o : 0.0;
+    double tau = 0.5 * (lo + hi);
+    for (int it = 0; it < kSecularMaxIter; it++) {
+        double ps = 0.0, ph = 0.0, dps = 0.0, dph = 0.0;
+        for (int i = lane; i < k; i += 32) {
+            const double den = (dk[i] - d_o) - tau;
+            const double t = zk[i] * zk[i] / den;
+            if (i <= L) {
+                ps += t;
+                dps += t / den;
+            } else {
+                ph += t;
+                dph += t / den;
+            }
+        }
+        ps = eig_warp_sum(ps);
+        ph = eig_warp_sum(ph);
+        dps = eig_warp_sum(dps);
+        dph = eig_warp_sum(dph);
+        const double g = rhoinv + ps + ph;
+        const double err = 8.0 * (ph - ps) + rhoinv + fabs(tau) * (dps + dph);
+        if (fabs(g) <= 4.0 * kUnitRoundoff * err * k) break;
+        if (hi - lo <= 2.0 * kUnitRoundoff * fmax(fabs(lo), fabs(hi))) break;
+        if (g < 0.0) lo = tau;
+        else hi = tau;
+        const double s1 = dps * (dL - tau) * (dL - tau);
+        double cc = rhoinv + ps - s1 / (dL - tau);
+        double x;
+        if (R < k) {
+            const double s2 = dph * (dR - tau) * (dR - tau);
+            cc += ph - s2 / (dR - tau);
+            const double A = cc, B = cc * (dL + dR) + s1 + s2, C = cc * dL * dR + s1 * dR + s2 * dL;
+            if (A == 0.0) {
+                x = C / B;
+            } else {
+                const double disc = fmax(B * B - 4.0 * A * C, 0.0);
+                const double q = 0.5 * (B + copysign(sqrt(disc), B));
+                const double r1 = q / A;
+                const double r2 = q != 0.0 ? C / q : NAN;
+                x = (r1 > lo && r1 < hi) ? r1 : r2;
+            }
+        } else {
+            x = cc > 0.0 ? dL + s1 / cc : NAN;
+        }
+        if (!(x > lo && x < hi)) x = 0.5 * (lo + hi);
+        tau = x;
+    }
+    if (lane == 0) {
+        b.ord[s + j] = o;
+        b.tau[s + j] = tau;
+        b.lamK[s + j] = d_o + tau;
+    }
+}
+
+// One warp per undeflated entry i: zhat_i^2 = prod_j |d_i - lambda_j| / prod_{j != i} |d_i - d_j|
+// (up to the common factor 1/rho, which the normalisation removes); sign of z_i.
+__global__ void dc_zhat_kernel(int n, int full, DcBufs b) {
+    const int w = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (w >= n) return;
+    const int node = w / full, s = node * full, i = w - s;
+    const int k = b.kcnt[node];
+    if (k < 0 || i >= k) return;
+    const double *dk = b.dK + s;
+    const double di = dk[i];
+    double p = 1.0;
+    for (int j = lane; j < k; j += 32) {
+        const double dl = fabs((di - dk[b.ord[s + j]]) - b.tau[s + j]);
+        p *= (j == i) ? dl : dl / fabs(dk[j] - di);
+    }
+    p = eig_warp_prod(p);
+    if (lane == 0) b.zh[s + i] = copysign(sqrt(p), b.zK[s + i]);
+}
+
+// One thread per node entry: the rank of its eigenvalue in the merged ascending order
+// (ties by entry index) gives its column in the next level.
+__global__ void dc_rank_kernel(int n, int full, DcBufs b) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const int node = g / full, s = node * full, i = g - s;
+    const int k = b.kcnt[node];
+    if (k < 0) return;
+    const int N = k + b.ndef[node];
+    if (i >= N) return;
+    const double v = i < k ? b.lamK[s + i] : b.dv[s + i - k];
+    int r = 0;
+    for (int m = 0; m < N; m++) {
+        const double u = m < k ? b.lamK[s + m] : b.dv[s + m - k];
+        r += (u < v) || (u == v && m < i);
+    }
+    b.lamB[s + r] = v;
+    b.outc[s + i] = s + r;
+}
+
+// One block per node entry: column of the merge eigenvector matrix (undeflated entries),
+// or the copy of a deflated eigenvector into its output column.
+__global__ void dc_vec_kernel(int n, int full, DcBufs b) {
+    __shared__ double red[32];
+    const int g = blockIdx.x;
+    const int node = g / full, s = node * full, i = g - s;
+    const int k = b.kcnt[node];
+    if (k < 0) return;
+    const int N = k + b.ndef[node];
+    if (i >= N) return;
+    if (i < k) {
+        const double *dk = b.dK + s;
+        const double dO = dk[b.ord[s + i]], t = b.tau[s + i];
+        double ss = 0.0;
+        for (int m = threadIdx.x; m < k; m += blockDim.x) {
+            const double u = b.zh[s + m] / ((dk[m] - dO) - t);
+            ss += u * u;
+        }
+        const double inv = 1.0 / sqrt(eig_block_sum(ss, red));
+        for (int m = threadIdx.x; m < k; m += blockDim.x)
+            b.U[(s + m) + (int64_t)(s + i) * n] = b.zh[s + m] / ((dk[m] - dO) - t) * inv;
+    } else {
+        const int64_t src = (int64_t)(s + b.defl[s + i - k]) * n, dst = (int64_t)b.outc[s + i] * n;
+        for (int r = threadIdx.x; r < N; r += blockDim.x) b.QB[(s + r) + dst] = b.QA[(s + r) + src];
+    }
+}
+
+// QB(rows of node, outc[j]) = QA(rows of node, Kl[m]) * U(m, j) for the undeflated entries:
+// one 64x64 output tile per block, batched over nodes (blockIdx.z).
+constexpr int DG_T = 64, DG_K = 16;
+__global__ void __launch_bounds__(256) dc_gemm_kernel(int n, int full, DcBufs b) {
+    __shared__ double As[DG_K][DG_T + 1];
+    __shared__ double Bs[DG_K][DG_T + 1];
+    const int node = blockIdx.z, s = node * full;
+    const int k = b.kcnt[node];
+    if (k <= 0) return;
+    const int N = min(full, n - s);
+    const int r0 = blockIdx.x * DG_T, c0 = blockIdx.y * DG_T;
+    if (r0 >= N || c0 >= k) return;
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    double acc[4][4] = {};
+    for (int m0 = 0; m0 < k; m0 += DG_K) {
+        for (int x = threadIdx.x; x < DG_T * DG_K; x += 256) {
+            const int rr = x % DG_T, kk = x / DG_T;
+            const int gr = r0 + rr, gm = m0 + kk;
+            As[kk][rr] = (gr < N && gm < k) ? b.QA[(s + gr) + (int64_t)(s + b.Kl[s + gm]) * n] : 0.0;
+        }
+        for (int x = threadIdx.x; x < DG_T * DG_K; x += 256) {
+            const int kk = x % DG_K, cc = x / DG_K;
+            const int gm = m0 + kk, gc = c0 + cc;
+            Bs[kk][cc] = (gm < k && gc < k) ? b.U[(s + gm) + (int64_t)(s + gc) * n] : 0.0;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int kk = 0; kk < DG_K; kk++) {
+            double a[4], bb[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                a[q] = As[kk][ty + 16 * q];
+                bb[q] = Bs[kk][tx + 16 * q];
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) acc[p][q] = fma(a[p], bb[q], acc[p][q]);
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int gc = c0 + tx + 16 * q;
+        if (gc >= k) continue;
+        const int64_t col = (int64_t)b.outc[s + gc] * n;
+#pragma unroll
+        for (int p = 0; p < 4; p++) {
+            const int gr = r0 + ty + 16 * p;
+            if (gr < N) b.QB[(s + gr) + col] = acc[p][q];
+        }
+    }
+}
+
+// Largest divide-and-conquer dimension: the merge scan keeps 20 bytes per column in shared
+// memory (227 KB per block).
+constexpr int kDcMaxN = 11264;
+
+static DcBufs dc_bufs(Context &c, int n) {
+    DcBufs b;
+    const size_t nn = (size_t)n * n;
+    b.QA = wsget<double>(c, "dc.QA", nn);
+    b.QB = wsget<double>(c, "dc.QB", nn);
+    b.U = wsget<double>(c, "dc.U", nn);
+    b.lamA = wsget<double>(c, "dc.lamA", n);
+    b.lamB = wsget<double>(c, "dc.lamB", n);
+    b.dK = wsget<double>(c, "dc.dK", n);
+    b.zK = wsget<double>(c, "dc.zK", n);
+    b.dv = wsget<double>(c, "dc.dv", n);
+    b.Kl = wsget<int>(c, "dc.Kl", n);
+    b.defl = wsget<int>(c, "dc.defl", n);
+    b.rp = wsget<int>(c, "dc.rp", n);
+    b.rn = wsget<int>(c, "dc.rn", n);
+    b.rc = wsget<double>(c, "dc.rc", n);
+    b.rs = wsget<double>(c, "dc.rs", n);
+    b.ord = wsget<int>(c, "dc.ord", n);
+    b.tau = wsget<double>(c, "dc.tau", n);
+    b.lamK = wsget<double>(c, "dc.lamK", n);
+    b.zh = wsget<double>(c, "dc.zh", n);
+    b.outc = wsget<int>(c, "dc.outc", n);
+    b.kcnt = wsget<int>(c, "dc.kcnt", n);
+    b.ndef = wsget<int>(c, "dc.ndef", n);
+    b.nrot = wsget<int>(c, "dc.nrot", n);
+    b.rho = wsget<double>(c, "dc.rho", n);
+    b.status = wsget<int>(c, "dc.status", 1);
+    return b;
+}
+
+// Eigenvalues (ascending, into w) and eigenvectors (n x n, ld n, returned) of the
+// symmetric tridiagonal (d, e).  d and e are device arrays; e has n-1 entries.
+static const double *tridiag_dc(Context &c, int n, const double *d, const double *e, double *w) {
+    if (n > kDcMaxN)
+        throw Error{DCG_E_ARG, "eigensolver dimension " + std::to_string(n) + " exceeds " + std::to_string(kDcMaxN)};
+    DcBufs b = dc_bufs(c, n);
+    // Both buffers start at zero: a merge reads whole columns of its node block, including the
+    // cross blocks between its two children, which no earlier level writes.
+    DCG_CUDA(cudaMemsetAsync(b.QA, 0, sizeof(double) * (size_t)n * n, c.stream));
+    DCG_CUDA(cudaMemsetAsync(b.QB, 0, sizeof(double) * (size_t)n * n, c.stream));
+    DCG_CUDA(cudaMemsetAsync(b.status, 0, sizeof(int), c.stream));
+    dc_leaf_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, d, e, b.lamA, b.QA);
+    DCG_LAUNCHED(c);
+    static bool attr_set = false;
+    if (!attr_set) {
+        DCG_CUDA(cudaFuncSetAttribute(dc_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * kDcMaxN));
+        attr_set = true;
+    }
+    for (int half = 1; half < n; half *= 2) {
+        const int full = 2 * half;
+        const int nodes = (n + full - 1) / full;
+        const int nmax = std::min(full, n);
+        dc_prep_kernel<<<nodes, 256, 20 * (size_t)nmax, c.stream>>>(n, half, full, e, b);
+        DCG_LAUNCHED(c);
+        dc_secular_kernel<<<grid1d((int64_t)n * 32, 256), 256, 0, c.stream>>>(n, full, b);
+        DCG_LAUNCHED(c);
+        dc_zhat_kernel<<<grid1d((int64_t)n * 32, 256), 256, 0, c.stream>>>(n, full, b);
+        DCG_LAUNCHED(c);
+        dc_rank_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, full, b);
+        DCG_LAUNCHED(c);
+        dc_vec_kernel<<<n, 128, 0, c.stream>>>(n, full, b);
+        DCG_LAUNCHED(c);
+        dim3 gg(grid1d(nmax, DG_T), grid1d(nmax, DG_T), nodes);
+        dc_gemm_kernel<<<gg, 256, 0, c.stream>>>(n, full, b);
+        DCG_LAUNCHED(c);
+        std::swap(b.QA, b.QB);
+        std::swap(b.lamA, b.lamB);
+    }
+    DCG_CUDA(cudaMemcpyAsync(w, b.lamA, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
+    // record which buffer holds the result for heev_vectors_only
+    c.eig_Q = b.QA;
+    c.eig_n = n;
+    c.eig_status = b.status;
+    return b.QA;
+}
+
+// ===================================================================== 3. back-transformation
+// Z = H_0 H_1 ... H_{n-2} Qt(:, vlo:vhi), applied in panels of WY_NB reflectors: the product
+// of a panel H_k0 ... H_{k0+nb-1} is I - V T V^H with T upper triangular (the compact WY form
+// of Schreiber & Van Loan, SIAM J. Sci. Stat. Comput. 10 (1989) 53), built by the forward
+// recurrence T(0:i, i) = -tau_i T(0:i, 0:i) (V(:, 0:i)^H v_i).  Each panel costs three GEMMs.
+constexpr int WY_NB = 32;
+
+__global__ void z_from_real_kernel(int n, const double *__restrict__ Qt, int vlo, int nvec, cplx *Z, int64_t ldz) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)n * nvec) return;
+    const int i = (int)(idx % n), c = (int)(idx / n);
+    Z[i + (int64_t)c * ldz] = mk(Qt[i + (int64_t)(vlo + c) * n], 0.0);
+}
+
+// Panel reflectors k0..k0+nbp-1 as a dense (m0 x nbp) matrix, m0 = n-k0-1, row r = global
+// row k0+1+r: zero above each reflector's unit entry.
+__global__ void wy_extract_kernel(int n, int k0, int nbp, const cplx *__restrict__ A, int64_t lda, cplx *Vp) {
+    const int m0 = n - k0 - 1;
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (idx >= (int64_t)m0 * nbp) return;
+    const int r = (int)(idx % m0), jj = (int)(idx / m0);
+    cplx v = mk(0.0, 0.0);
+    if (r == jj) v = mk(1.0, 0.0);
+    else if (r > jj) v = A[(k0 + 1 + r) + (int64_t)(k0 + jj) * lda];
+    Vp[r + (int64_t)jj * m0] = v;
+}
+
+// T (nbp x nbp, ld WY_NB) from G = Vp^H Vp and tau[k0..]; one block of WY_NB threads.
+__global__ void wy_tfactor_kernel(int nbp, const cplx *__restrict__ G, const cplx *__restrict__ tau, int k0, cplx *T) {
+    const int j = threadIdx.x;
+    for (int x = j; x < WY_NB * WY_NB; x += blockDim.x) T[x] = mk(0.0, 0.0);
+    __syncthreads();
+    for (int i = 0; i < nbp; i++) {
+        const cplx ti = tau[k0 + i];
+        cplx acc = mk(0.0, 0.0);
+        if (j < i)
+            for (int l = j; l < i; l++) cfma(acc, T[j + l * WY_NB], G[l + i * nbp]);
+        __syncthreads();
+        if (j < i) T[j + i * WY_NB] = cmul(mk(-ti.x, -ti.y), acc);
+        if (j == i) T[i + i * WY_NB] = ti;
+        __syncthreads();
+    }
+}
+
+// ===================================================================== driver
+struct HeevWork {
+    double *d, *e;
+    cplx *tau, *ppart, *w;
+};
+
+static HeevWork heev_work(Context &c, int n) {
+    HeevWork h;
+    h.d = wsget<double>(c, "heev.d", n + 1);
+    h.e = wsget<double>(c, "heev.e", n + 1);
+    h.tau = wsget<cplx>(c, "heev.tau", n + 1);
+    int nchunk = (n + HH_CHUNK - 1) / HH_CHUNK;
+    h.ppart = wsget<cplx>(c, "heev.ppart", (size_t)nchunk * (n + 1));
+    h.w = wsget<cplx>(c, "heev.w", n + 1);
+    return h;
+}
+
+static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
+    const size_t smem = 2 * sizeof(cplx) * (size_t)std::max(n - 1, 1);
+    DCG_CUDA(cudaFuncSetAttribute(tridiag_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    DCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_persistent_kernel, TRD_THREADS, smem));
+    if (per_sm < 1) throw Error{DCG_E_CUDA, "tridiagonalisation kernel does not fit on an SM"};
+    // one warp per trailing column at most; never more blocks than can be co-resident
+    const int want = std::max(1, (n + (TRD_THREADS / 32) - 1) / (TRD_THREADS / 32));
+    const int nblocks = std::min({want, per_sm * std::max(1, c.num_sms), 2 * std::max(1, c.num_sms)});
+    cplx *pbuf = wsget<cplx>(c, "trd.p", (size_t)n + 1);
+    double2 *part = wsget<double2>(c, "trd.part", (size_t)nblocks + 1);
+    GridBar *gb = wsget<GridBar>(c, "trd.bar", 1);
+    DCG_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBar), c.stream));
+    void *args[] = {&n, &A, &lda, &h.d, &h.e, &h.tau, &pbuf, &part, &gb};
+    DCG_CUDA(cudaLaunchCooperativeKernel((const void *)tridiag_persistent_kernel, dim3(nblocks), dim3(TRD_THREADS),
+                                         args, smem, c.stream));
+    DCG_LAUNCHED(c);
+    GridBar hb;
+    DCG_CUDA(cudaMemcpyAsync(&hb, gb, sizeof(GridBar), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    if (hb.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
+}
+
+// Reduce A to tridiagonal form; d, e, tau in the named workspace, reflectors in A.
+static void tridiag(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
+    if (n <= kTridiagPersistentMaxN) {
+        tridiag_persistent(c, n, A, lda, h);
+        return;
+    }
+    for (int k = 0; k + 1 < n; k++) {
+        const int m = n - k - 1;
+        hh_gen_kernel<<<1, 256, 0, c.stream>>>(n, k, A, lda, h.d, h.e, h.tau);
+        DCG_LAUNCHED(c);
+        const int nchunk = (m + HH_CHUNK - 1) / HH_CHUNK;
+        dim3 g1(grid1d(m, 128), nchunk);
+        hh_matvec_kernel<<<g1, 128, 0, c.stream>>>(n, k, A, lda, h.tau, h.ppart);
+        DCG_LAUNCHED(c);
+        hh_w_kernel<<<1, 512, 0, c.stream>>>(n, k, A, lda, h.tau, h.ppart, nchunk, h.w);
+        DCG_LAUNCHED(c);
+        dim3 g2(grid1d(m, 128), m);
+        hh_update_kernel<<<g2, 128, 0, c.stream>>>(n, k, A, lda, h.w);
+        DCG_LAUNCHED(c);
+    }
+    hh_last_kernel<<<1, 1, 0, c.stream>>>(n, A, lda, h.d);
+    DCG_LAUNCHED(c);
+}
+
+static void check_dc_status(Context &c) {
+    if (!c.eig_status) return;
+    int st = 0;
+    DCG_CUDA(cudaMemcpyAsync(&st, c.eig_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    if (st) throw Error{DCG_E_NUMERIC, "divide-and-conquer merge met coincident undeflated poles"};
+}
+
+void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
+    if (n <= 0) return;
+    FamScope fs(c, DCG_FAM_EIG, (16.0 / 3.0) * (double)n * n * n);
+    HeevWork h = heev_work(c, n);
+    {
+        FamScope f1(c, DCG_FAM_EIG_TRI, (16.0 / 3.0) * (double)n * n * n);
+        tridiag(c, n, A, lda, h);
+    }
+    {
+        FamScope f2(c, DCG_FAM_EIG_VAL, 4.0 / 3.0 * (double)n * n * n);
+        tridiag_dc(c, n, h.d, h.e, w);
+    }
+    check_dc_status(c);
+    heev_vectors_only(c, n, A, lda, w, vlo, vhi, Z, ldz);
+}
+
+// Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (its reflectors are
+// still in A and the tridiagonal eigenvectors in the divide-and-conquer workspace).
+void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
+                       int64_t ldz) {
+    (void)w;
+    const int nvec = vhi - vlo;
+    if (nvec <= 0 || n <= 0 || Z == nullptr) return;
+    if (c.eig_Q == nullptr || c.eig_n != n) throw Error{DCG_E_STATE, "heev_vectors_only without a matching heev"};
+    HeevWork h = heev_work(c, n);
+    FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nvec);
+    FamScope f4(c, DCG_FAM_EIG_BACK, 8.0 * (double)n * n * nvec);
+    z_from_real_kernel<<<grid1d((int64_t)n * nvec, 256), 256, 0, c.stream>>>(n, c.eig_Q, vlo, nvec, Z, ldz);
+    DCG_LAUNCHED(c);
+    if (n < 2) return;
+    cplx *Vp = wsget<cplx>(c, "wy.V", (size_t)n * WY_NB);
+    cplx *G = wsget<cplx>(c, "wy.G", WY_NB * WY_NB);
+    cplx *T = wsget<cplx>(c, "wy.T", WY_NB * WY_NB);
+    cplx *W1 = wsget<cplx>(c, "wy.W1", (size_t)WY_NB * nvec);
+    cplx *W2 = wsget<cplx>(c, "wy.W2", (size_t)WY_NB * nvec);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
+    const int nref = n - 1;
+    const int npanel = (nref + WY_NB - 1) / WY_NB;
+    for (int p = npanel - 1; p >= 0; p--) {
+        const int k0 = p * WY_NB;
+        const int nbp = std::min(WY_NB, nref - k0);
+        const int m0 = n - k0 - 1;
+        wy_extract_kernel<<<grid1d((int64_t)m0 * nbp, 256), 256, 0, c.stream>>>(n, k0, nbp, A, lda, Vp);
+        DCG_LAUNCHED(c);
+        zgemm(c, OP_C, OP_N, nbp, nbp, m0, one, Vp, m0, 0, Vp, m0, 0, zero, G, nbp, 0, 1);
+        wy_tfactor_kernel<<<1, WY_NB, 0, c.stream>>>(nbp, G, h.tau, k0, T);
+        DCG_LAUNCHED(c);
+        cplx *Zs = Z + (k0 + 1);
+        zgemm(c, OP_C, OP_N, nbp, nvec, m0, one, Vp, m0, 0, Zs, ldz, 0, zero, W1, nbp, 0, 1);
+        zgemm(c, OP_N, OP_N, nbp, nvec, nbp, one, T, WY_NB, 0, W1, nbp, 0, zero, W2, nbp, 0, 1);
+        zgemm(c, OP_N, OP_N, m0, nvec, nbp, mone, Vp, m0, 0, W2, nbp, 0, one, Zs, ldz, 0, 1);
+    }
+}
+
+// Symmetric tridiagonal eigendecomposition (the divide-and-conquer stage alone): d (n),
+// e (n-1) device arrays; ascending eigenvalues into w (device) and eigenvectors returned
+// (device, n x n, ld n; valid until the next eigensolver call).
+const double *stedc(Context &c, int n, const double *d, const double *e, double *w) {
+    if (n <= 0) return nullptr;
+    const double *Q = tridiag_dc(c, n, d, e, w);
+    check_dc_status(c);
+    return Q;
+}
+
+}  // namespace dcg

@@ -13,6 +13,12 @@ void launch_occ_energy(Context &c, int na, int64_t M, const uint64_t *full, cons
 void launch_embed(Context &c, int ndet, const int64_t *pos, const cplx *cvec, cplx *psi, int64_t M);
 void launch_detsc(Context &c, const uint64_t *dets, int ndet, const cplx *Uact, cplx *ds);
 
+// Gram factor G (Mp x dimn) of the A (create = 1) or C (create = 0) overlap matrix
+void launch_gram(Context &c, int na, int64_t Mp, const uint64_t *dets_p, int64_t M, const cplx *Y, const int *ind,
+                 int dimn, int create, cplx *G);
+// A(i, j) *= s[soff + i] (or /= when inv)
+void launch_scale_rows(Context &c, int m, int n, cplx *A, int64_t lda, const double *s, int soff, bool inv);
+
 // ---- dcg_ints.cu
 // Dense class tensors of the two-electron integrals in the original spinor basis.
 enum ClassId {

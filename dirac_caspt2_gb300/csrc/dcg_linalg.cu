@@ -1,14 +1,7 @@
-// Dense FP64 complex linear algebra on the device: GEMM, Hermitian eigensolver and LU
-// solve.  Written from the textbook algorithms:
-//   - Householder reduction of a Hermitian matrix to real symmetric tridiagonal form
-//     (Golub & Van Loan, Matrix Computations, 4th ed., 8.3.1), with the complex
-//     reflector of LAPACK's documented xLARFG definition (beta real);
-//   - eigenvalues by Sturm-count bisection (GVL 8.4.1);
-//   - eigenvectors by inverse iteration on the tridiagonal with partial-pivoting LU
-//     (GVL 8.2.2), followed by modified Gram-Schmidt inside clusters of close eigenvalues;
-//   - back-transformation by the stored reflectors.
-// Eigenvalues come out ascending, as the reference's ZHEEV/DSYEV calls
-// (src/diag.F90:43,109) return them.
+// Dense FP64 complex linear algebra on the device: workspace, GEMM, Hermitian fill,
+// deterministic sums and the LU solve (Golub & Van Loan, Matrix Computations, 4th ed.,
+// 3.4: partial pivoting).  The Hermitian eigensolver lives in dcg_eig.cu.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 
@@ -157,6 +150,128 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx al
     }
 }
 
+// ---- small-dimension GEMMs of the 4-index transformation.  When the contracted index
+// and the small output index are at most SMALL_D (an active or inactive orbital dimension),
+// the GEMM is memory-bound: the small matrix is staged in shared memory and the large
+// operand is streamed once.  Each thread owns one row (right-small) or one column
+// (left-small) and SMALL_G consecutive outputs of it.
+constexpr int SMALL_D = 32, SMALL_G = 8;
+
+// C(m x n) = alpha * A(m x k) * op(B)(k x n) + beta * C, op(B) = B or conj(B); k, n <= SMALL_D.
+template <int OPB>
+__global__ void __launch_bounds__(256) zgemm_rsmall_kernel(int m, int n, int k, cplx alpha, const cplx *__restrict__ A,
+                                                           int64_t lda, int64_t sa, const cplx *__restrict__ B,
+                                                           int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc,
+                                                           int64_t sc, int z0) {
+    __shared__ cplx Bs[SMALL_D][SMALL_D];
+    const int z = z0 + blockIdx.z;
+    A += (int64_t)z * sa;
+    B += (int64_t)z * sb;
+    C += (int64_t)z * sc;
+    for (int x = threadIdx.x + blockDim.x * threadIdx.y; x < k * n; x += blockDim.x * blockDim.y) {
+        const int kk = x % k, j = x / k;
+        cplx v = B[kk + (int64_t)j * ldb];
+        if (OPB == OP_R) v = cconj(v);
+        Bs[kk][j] = v;
+    }
+    __syncthreads();
+    const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int j0 = threadIdx.y * SMALL_G;
+    if (i >= m || j0 >= n) return;
+    cplx acc[SMALL_G];
+#pragma unroll
+    for (int q = 0; q < SMALL_G; q++) acc[q] = mk(0.0, 0.0);
+    for (int kk = 0; kk < k; kk++) {
+        const cplx a = A[i + (int64_t)kk * lda];
+#pragma unroll
+        for (int q = 0; q < SMALL_G; q++)
+            if (j0 + q < n) cfma(acc[q], a, Bs[kk][j0 + q]);
+    }
+    const bool use_beta = (beta.x != 0.0 || beta.y != 0.0);
+#pragma unroll
+    for (int q = 0; q < SMALL_G; q++) {
+        if (j0 + q >= n) break;
+        const int64_t o = i + (int64_t)(j0 + q) * ldc;
+        cplx r = cmul(alpha, acc[q]);
+        if (use_beta) r = cadd(r, cmul(beta, C[o]));
+        C[o] = r;
+    }
+}
+
+// C(m x n) = alpha * A^H(m x k) * B(k x n) + beta * C with A (k x m); m, k <= SMALL_D.
+__global__ void __launch_bounds__(256) zgemm_lsmall_kernel(int m, int n, int k, cplx alpha, const cplx *__restrict__ A,
+                                                           int64_t lda, int64_t sa, const cplx *__restrict__ B,
+                                                           int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc,
+                                                           int64_t sc, int z0) {
+    __shared__ cplx As[SMALL_D][SMALL_D];   // As[kk][i] = conj(A(kk, i))
+    const int z = z0 + blockIdx.z;
+    A += (int64_t)z * sa;
+    B += (int64_t)z * sb;
+    C += (int64_t)z * sc;
+    for (int x = threadIdx.x + blockDim.x * threadIdx.y; x < k * m; x += blockDim.x * blockDim.y) {
+        const int kk = x % k, i = x / k;
+        As[kk][i] = cconj(A[kk + (int64_t)i * lda]);
+    }
+    __syncthreads();
+    const int64_t j = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const int i0 = threadIdx.y * SMALL_G;
+    if (j >= n || i0 >= m) return;
+    cplx acc[SMALL_G];
+#pragma unroll
+    for (int q = 0; q < SMALL_G; q++) acc[q] = mk(0.0, 0.0);
+    for (int kk = 0; kk < k; kk++) {
+        const cplx b = B[kk + j * ldb];
+#pragma unroll
+        for (int q = 0; q < SMALL_G; q++)
+            if (i0 + q < m) cfma(acc[q], As[kk][i0 + q], b);
+    }
+    const bool use_beta = (beta.x != 0.0 || beta.y != 0.0);
+#pragma unroll
+    for (int q = 0; q < SMALL_G; q++) {
+        if (i0 + q >= m) break;
+        const int64_t o = (i0 + q) + j * ldc;
+        cplx r = cmul(alpha, acc[q]);
+        if (use_beta) r = cadd(r, cmul(beta, C[o]));
+        C[o] = r;
+    }
+}
+
+// Small-dimension dispatch; returns false when the shape is not one of the two forms.
+static bool zgemm_small(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda,
+                        int64_t sa, const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
+                        int batch) {
+    if (k < 1 || k > SMALL_D) return false;
+    if (opa == OP_N && (opb == OP_N || opb == OP_R) && n <= SMALL_D && m >= 64) {
+        const int gy = (n + SMALL_G - 1) / SMALL_G;
+        const int bx = 256 / gy;   // gy <= 4, bx >= 64
+        for (int z0 = 0; z0 < batch; z0 += 65535) {
+            const int nz = std::min(65535, batch - z0);
+            dim3 grid(grid1d(m, bx), 1, nz), block(bx, gy);
+            if (opb == OP_N)
+                zgemm_rsmall_kernel<OP_N><<<grid, block, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C,
+                                                                        ldc, sc, z0);
+            else
+                zgemm_rsmall_kernel<OP_R><<<grid, block, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C,
+                                                                        ldc, sc, z0);
+            DCG_LAUNCHED(c);
+        }
+        return true;
+    }
+    if (opa == OP_C && opb == OP_N && m <= SMALL_D && n >= 64) {
+        const int gy = (m + SMALL_G - 1) / SMALL_G;
+        const int bx = 256 / gy;
+        for (int z0 = 0; z0 < batch; z0 += 65535) {
+            const int nz = std::min(65535, batch - z0);
+            dim3 grid(grid1d(n, bx), 1, nz), block(bx, gy);
+            zgemm_lsmall_kernel<<<grid, block, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc,
+                                                              z0);
+            DCG_LAUNCHED(c);
+        }
+        return true;
+    }
+    return false;
+}
+
 template <int OPA, int OPB>
 static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
                          const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
@@ -170,14 +285,65 @@ static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx
     }
 }
 
+// C = alpha * sum_s P_s + beta * C over nsplit partial products (fixed summation order).
+__global__ void splitk_reduce_kernel(int m, int n, int nsplit, const cplx *__restrict__ P, cplx alpha, cplx beta,
+                                     cplx *C, int64_t ldc) {
+    const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t mn = (int64_t)m * n;
+    if (idx >= mn) return;
+    cplx acc = mk(0.0, 0.0);
+    for (int s = 0; s < nsplit; s++) acc = cadd(acc, P[s * mn + idx]);
+    const int i = (int)(idx % m), j = (int)(idx / m);
+    const int64_t o = i + (int64_t)j * ldc;
+    cplx r = cmul(alpha, acc);
+    if (beta.x != 0.0 || beta.y != 0.0) r = cadd(r, cmul(beta, C[o]));
+    C[o] = r;
+}
+
+template <int OPA, int OPB>
+static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
+                         const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
+                         int batch);
+
+// Split-K for a single GEMM whose output has too few 64x64 tiles to occupy every SM (a GB300
+// SM retires only about two FP64 FMAs per clock, so a GEMM on a handful of SMs runs at a
+// small fraction of the GPU): K is cut into equal chunks (at least 64 long) computed as one
+// batched GEMM into partial products, then reduced in a fixed order.  Returns false when
+// the shape does not qualify.
+template <int OPA, int OPB>
+static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B,
+                         int64_t ldb, cplx beta, cplx *C, int64_t ldc) {
+    const int64_t tiles = (int64_t)((m + 63) / 64) * ((n + 63) / 64);
+    const int sms = std::max(1, c.num_sms);
+    if (tiles >= sms || k < 128) return false;
+    int nsplit = (int)std::min<int64_t>((2 * sms + tiles - 1) / tiles, k / 64);
+    if (nsplit < 2) return false;
+    const int kc = (k + nsplit - 1) / nsplit;
+    nsplit = (k + kc - 1) / kc;
+    const int nfull = k / kc;             // chunks of exactly kc
+    const int rem = k - nfull * kc;       // last, shorter chunk
+    const int64_t mn = (int64_t)m * n;
+    cplx *P = wsget<cplx>(c, "gemm.splitk", (size_t)mn * nsplit);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    // K-chunk strides: A is m x k (OP_N/OP_R, chunk = columns) or k x m (OP_T/OP_C, chunk = rows)
+    const int64_t sa = (OPA == OP_N || OPA == OP_R) ? (int64_t)kc * lda : kc;
+    const int64_t sb = (OPB == OP_N || OPB == OP_R) ? kc : (int64_t)kc * ldb;
+    zgemm_launch<OPA, OPB>(c, m, n, kc, one, A, lda, sa, B, ldb, sb, zero, P, m, mn, nfull);
+    if (rem > 0)
+        zgemm_launch<OPA, OPB>(c, m, n, rem, one, A + nfull * sa, lda, 0, B + nfull * sb, ldb, 0, zero, P + nfull * mn,
+                               m, 0, 1);
+    splitk_reduce_kernel<<<grid1d(mn, 256), 256, 0, c.stream>>>(m, n, nsplit, P, alpha, beta, C, ldc);
+    DCG_LAUNCHED(c);
+    return true;
+}
+
 void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
            const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc, int batch) {
     if (m <= 0 || n <= 0 || batch <= 0) return;
-    if (k <= 0) {
-        // C = beta*C : run with k=0 through the kernel (acc stays zero)
-    }
+    if (zgemm_small(c, opa, opb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch)) return;
 #define DCG_ZG(a, b)                                                                                   \
     if (opa == a && opb == b) {                                                                        \
+        if (batch == 1 && zgemm_splitk<a, b>(c, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)) return;  \
         zgemm_launch<a, b>(c, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch);        \
         return;                                                                                        \
     }
@@ -218,384 +384,6 @@ void dsum(Context &c, const double *x, int64_t n, double *out) {
     DCG_LAUNCHED(c);
 }
 
-// ===================================================================== tridiagonalisation
-// Step k: reflector for column k (rows k+1..n-1), v stored in A(k+1:n-1, k) with v0 = 1.
-__global__ void hh_gen_kernel(int n, int k, cplx *A, int64_t lda, double *d, double *e, cplx *tau) {
-    __shared__ double sh[32];
-    __shared__ cplx s_scale;
-    __shared__ int s_skip;
-    const int m = n - k - 1;
-    cplx *x = A + (k + 1) + (int64_t)k * lda;
-    double s = 0.0;
-    for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) s += cabs2(x[i]);
-    s = block_sum(s, sh);
-    if (threadIdx.x == 0) {
-        cplx alpha = x[0];
-        double xnorm = sqrt(s);
-        cplx t;
-        double beta;
-        if (xnorm == 0.0 && alpha.y == 0.0) {
-            t = mk(0.0, 0.0);
-            beta = alpha.x;
-            s_skip = 1;
-        } else {
-            double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
-            beta = alpha.x >= 0.0 ? -nrm : nrm;
-            t = mk((beta - alpha.x) / beta, -alpha.y / beta);
-            s_scale = cdiv(mk(1.0, 0.0), mk(alpha.x - beta, alpha.y));
-            s_skip = 0;
-        }
-        tau[k] = t;
-        e[k] = beta;
-        d[k] = A[k + (int64_t)k * lda].x;
-    }
-    __syncthreads();
-    if (!s_skip)
-        for (int i = 1 + threadIdx.x; i < m; i += blockDim.x) x[i] = cmul(x[i], s_scale);
-    __syncthreads();
-    if (threadIdx.x == 0) x[0] = mk(1.0, 0.0);
-}
-
-// partial p(i) = sum_{j in chunk} A(k+1+i, k+1+j) v(j)
-constexpr int HH_CHUNK = 256;
-__global__ void hh_matvec_kernel(int n, int k, const cplx *__restrict__ A, int64_t lda, const cplx *__restrict__ tau,
-                                 cplx *ppart) {
-    __shared__ cplx vs[HH_CHUNK];
-    const int m = n - k - 1;
-    const cplx t = tau[k];
-    const int j0 = blockIdx.y * HH_CHUNK;
-    const int j1 = min(m, j0 + HH_CHUNK);
-    const cplx *v = A + (k + 1) + (int64_t)k * lda;
-    for (int j = threadIdx.x; j < j1 - j0; j += blockDim.x) vs[j] = v[j0 + j];
-    __syncthreads();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= m) return;
-    cplx acc = mk(0.0, 0.0);
-    if (t.x != 0.0 || t.y != 0.0) {
-        const cplx *Ai = A + (k + 1 + i) + (int64_t)(k + 1) * lda;
-        for (int j = j0; j < j1; j++) cfma(acc, Ai[(int64_t)j * lda], vs[j - j0]);
-    }
-    ppart[(int64_t)blockIdx.y * n + i] = acc;
-}
-
-// w = tau*p + alpha v,  alpha = -1/2 tau (x^H v) with x = tau*p
-__global__ void hh_w_kernel(int n, int k, const cplx *A, int64_t lda, const cplx *tau, const cplx *ppart,
-                            int nchunk, cplx *w) {
-    __shared__ double sh[32];
-    const int m = n - k - 1;
-    const cplx t = tau[k];
-    const cplx *v = A + (k + 1) + (int64_t)k * lda;
-    double sr = 0.0, si = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        cplx p = mk(0.0, 0.0);
-        for (int c = 0; c < nchunk; c++) p = cadd(p, ppart[(int64_t)c * n + i]);
-        cplx x = cmul(t, p);
-        w[i] = x;
-        cplx xv = cmul(cconj(x), v[i]);
-        sr += xv.x;
-        si += xv.y;
-    }
-    sr = block_sum(sr, sh);
-    si = block_sum(si, sh);
-    cplx alpha = cmul(mk(-0.5, 0.0), cmul(t, mk(sr, si)));
-    for (int i = threadIdx.x; i < m; i += blockDim.x) w[i] = cadd(w[i], cmul(alpha, v[i]));
-}
-
-// A(k+1:, k+1:) -= v w^H + w v^H
-__global__ void hh_update_kernel(int n, int k, cplx *A, int64_t lda, const cplx *w) {
-    const int m = n - k - 1;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y;
-    if (i >= m || j >= m) return;
-    const cplx *v = A + (k + 1) + (int64_t)k * lda;
-    cplx vi = v[i], vj = v[j], wi = w[i], wj = w[j];
-    int64_t o = (k + 1 + i) + (int64_t)(k + 1 + j) * lda;
-    cplx a = A[o];
-    a = csub(a, cmulc(vi, wj));
-    a = csub(a, cmulc(wi, vj));
-    if (i == j) a.y = 0.0;
-    A[o] = a;
-}
-
-__global__ void hh_last_kernel(int n, const cplx *A, int64_t lda, double *d) {
-    d[n - 1] = A[(n - 1) + (int64_t)(n - 1) * lda].x;
-}
-
-// Gershgorin interval of the tridiagonal -> bounds[0..1]; also max |T| in bounds[2]
-__global__ void gersh_kernel(int n, const double *d, const double *e, double *bounds) {
-    __shared__ double lo_s[1024], hi_s[1024];
-    double lo = 1e300, hi = -1e300;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        double r = 0.0;
-        if (i > 0) r += fabs(e[i - 1]);
-        if (i < n - 1) r += fabs(e[i]);
-        lo = fmin(lo, d[i] - r);
-        hi = fmax(hi, d[i] + r);
-    }
-    lo_s[threadIdx.x] = lo;
-    hi_s[threadIdx.x] = hi;
-    __syncthreads();
-    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
-        if (threadIdx.x < s) {
-            lo_s[threadIdx.x] = fmin(lo_s[threadIdx.x], lo_s[threadIdx.x + s]);
-            hi_s[threadIdx.x] = fmax(hi_s[threadIdx.x], hi_s[threadIdx.x + s]);
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-        double L = lo_s[0], H = hi_s[0];
-        double tn = fmax(fabs(L), fabs(H));
-        double pad = 2.2e-16 * tn * 4.0 + 1e-300;
-        bounds[0] = L - pad;
-        bounds[1] = H + pad;
-        bounds[2] = tn;
-    }
-}
-
-// number of eigenvalues of T strictly below x (Sturm count of the LDL^T of T - xI)
-__device__ int sturm_count(int n, const double *__restrict__ d, const double *__restrict__ e, double x,
-                           double pivmin) {
-    int cnt = 0;
-    double q = d[0] - x;
-    if (fabs(q) < pivmin) q = -pivmin;
-    if (q < 0.0) cnt++;
-    for (int i = 1; i < n; i++) {
-        double ei = e[i - 1];
-        q = d[i] - x - ei * ei / q;
-        if (fabs(q) < pivmin) q = -pivmin;
-        if (q < 0.0) cnt++;
-    }
-    return cnt;
-}
-
-__global__ void bisect_kernel(int n, const double *d, const double *e, const double *bounds, double *w) {
-    int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    double lo = bounds[0], hi = bounds[1];
-    double tn = bounds[2];
-    double pivmin = 1e-290 * fmax(1.0, tn * tn);
-    for (int it = 0; it < 128; it++) {
-        double mid = 0.5 * (lo + hi);
-        if (mid <= lo || mid >= hi) break;
-        if (hi - lo <= 2.0 * 2.2e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300) break;
-        int c = sturm_count(n, d, e, mid, pivmin);
-        if (c <= j) lo = mid;
-        else hi = mid;
-    }
-    w[j] = 0.5 * (lo + hi);
-}
-
-__device__ __forceinline__ double hash_unit(uint32_t a, uint32_t b) {
-    uint32_t h = a * 0x9E3779B1u ^ (b + 0x7F4A7C15u) * 0x85EBCA77u;
-    h ^= h >> 15;
-    h *= 0x2C1B3C6Du;
-    h ^= h >> 12;
-    h *= 0x297A2D39u;
-    h ^= h >> 15;
-    return ((double)h / 4294967296.0) * 2.0 - 1.0;
-}
-
-// Inverse iteration, one thread per eigenvector; factorisation scratch laid out
-// [array][row][vector] so that consecutive threads touch consecutive addresses.
-__global__ void invit_kernel(int n, const double *__restrict__ d, const double *__restrict__ e,
-                             const double *__restrict__ w, const double *__restrict__ bounds, int vlo, int nvec,
-                             double *scr, double *z) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= nvec) return;
-    const double lam = w[vlo + t];
-    const int64_t N = nvec;
-    double *DL = scr, *DD = scr + (int64_t)n * N, *DU = scr + 2 * (int64_t)n * N, *DU2 = scr + 3 * (int64_t)n * N;
-    unsigned char *PV = reinterpret_cast<unsigned char *>(scr + 4 * (int64_t)n * N);
-#define IX(i) ((int64_t)(i) * N + t)
-    const double tn = fmax(bounds[2], 1e-300);
-    const double tiny = 2.2e-16 * tn;
-    for (int i = 0; i < n; i++) {
-        DD[IX(i)] = d[i] - lam;
-        if (i < n - 1) {
-            DL[IX(i)] = e[i];
-            DU[IX(i)] = e[i];
-        }
-        if (i < n - 2) DU2[IX(i)] = 0.0;
-    }
-    // LU with partial pivoting (tridiagonal, fill-in in DU2)
-    for (int i = 0; i < n - 1; i++) {
-        double di = DD[IX(i)], li = DL[IX(i)];
-        if (fabs(di) >= fabs(li)) {
-            if (di == 0.0) di = tiny;
-            DD[IX(i)] = di;
-            double f = li / di;
-            DL[IX(i)] = f;
-            DD[IX(i + 1)] -= f * DU[IX(i)];
-            PV[IX(i)] = 0;
-        } else {
-            double f = di / li;
-            DD[IX(i)] = li;
-            DL[IX(i)] = f;
-            double tmp = DU[IX(i)];
-            DU[IX(i)] = DD[IX(i + 1)];
-            DD[IX(i + 1)] = tmp - f * DD[IX(i + 1)];
-            if (i < n - 2) {
-                DU2[IX(i)] = DU[IX(i + 1)];
-                DU[IX(i + 1)] = -f * DU[IX(i + 1)];
-            }
-            PV[IX(i)] = 1;
-        }
-    }
-    if (DD[IX(n - 1)] == 0.0) DD[IX(n - 1)] = tiny;
-    for (int i = 0; i < n; i++) z[IX(i)] = hash_unit(i, vlo + t) + 0.5 * hash_unit(i + 7919, t + 104729);
-    for (int it = 0; it < 3; it++) {
-        // forward: apply L^-1 P
-        for (int i = 0; i < n - 1; i++) {
-            double bi = z[IX(i)], bn = z[IX(i + 1)];
-            if (PV[IX(i)]) {
-                z[IX(i)] = bn;
-                z[IX(i + 1)] = bi - DL[IX(i)] * bn;
-            } else {
-                z[IX(i + 1)] = bn - DL[IX(i)] * bi;
-            }
-        }
-        // back substitution with U (diag DD, super DU, second super DU2)
-        double mx = 0.0;
-        z[IX(n - 1)] /= DD[IX(n - 1)];
-        if (n > 1) z[IX(n - 2)] = (z[IX(n - 2)] - DU[IX(n - 2)] * z[IX(n - 1)]) / DD[IX(n - 2)];
-        for (int i = n - 3; i >= 0; i--)
-            z[IX(i)] = (z[IX(i)] - DU[IX(i)] * z[IX(i + 1)] - DU2[IX(i)] * z[IX(i + 2)]) / DD[IX(i)];
-        for (int i = 0; i < n; i++) mx = fmax(mx, fabs(z[IX(i)]));
-        double inv = mx > 0.0 ? 1.0 / mx : 1.0;
-        double s2 = 0.0;
-        for (int i = 0; i < n; i++) {
-            double v = z[IX(i)] * inv;
-            z[IX(i)] = v;
-            s2 += v * v;
-        }
-        double nrm = 1.0 / sqrt(s2);
-        for (int i = 0; i < n; i++) z[IX(i)] *= nrm;
-    }
-#undef IX
-}
-
-// Modified Gram-Schmidt inside clusters of close eigenvalues (one block per cluster head)
-__global__ void cluster_mgs_kernel(int n, const double *w, const double *bounds, int vlo, int nvec, double *z,
-                                   double rel_tol) {
-    __shared__ double sh[32];
-    const int j = blockIdx.x;
-    const double tol = rel_tol * fmax(bounds[2], 1e-300);
-    if (j > 0 && w[vlo + j] - w[vlo + j - 1] <= tol) return;   // not a cluster head
-    int len = 1;
-    while (j + len < nvec && w[vlo + j + len] - w[vlo + j + len - 1] <= tol) len++;
-    if (len == 1) return;
-    const int64_t N = nvec;
-    for (int c = 1; c < len; c++) {
-        for (int pass = 0; pass < 2; pass++) {
-            for (int p = 0; p < c; p++) {
-                double s = 0.0;
-                for (int i = threadIdx.x; i < n; i += blockDim.x) s += z[(int64_t)i * N + j + p] * z[(int64_t)i * N + j + c];
-                s = block_sum(s, sh);
-                for (int i = threadIdx.x; i < n; i += blockDim.x) z[(int64_t)i * N + j + c] -= s * z[(int64_t)i * N + j + p];
-                __syncthreads();
-            }
-            double s2 = 0.0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                double v = z[(int64_t)i * N + j + c];
-                s2 += v * v;
-            }
-            s2 = block_sum(s2, sh);
-            double inv = s2 > 0.0 ? 1.0 / sqrt(s2) : 0.0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) z[(int64_t)i * N + j + c] *= inv;
-            __syncthreads();
-        }
-    }
-}
-
-// Z(:, c) = Q z(:, c) with Q = H_0 H_1 ... H_{n-2};  each block owns BT_COLS columns.
-constexpr int BT_COLS = 4;
-__global__ void backtransform_kernel(int n, const cplx *__restrict__ A, int64_t lda, const cplx *__restrict__ tau,
-                                     const double *__restrict__ z, int nvec, cplx *Z, int64_t ldz) {
-    __shared__ double sh[32];
-    const int c0 = blockIdx.x * BT_COLS;
-    const int nc = min(BT_COLS, nvec - c0);
-    for (int c = 0; c < nc; c++)
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-            Z[i + (int64_t)(c0 + c) * ldz] = mk(z[(int64_t)i * nvec + c0 + c], 0.0);
-    __syncthreads();
-    for (int k = n - 2; k >= 0; k--) {
-        const cplx t = tau[k];
-        if (t.x == 0.0 && t.y == 0.0) continue;
-        const int m = n - k - 1;
-        const cplx *v = A + (k + 1) + (int64_t)k * lda;
-        double pr[BT_COLS], pi[BT_COLS];
-#pragma unroll
-        for (int c = 0; c < BT_COLS; c++) pr[c] = pi[c] = 0.0;
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            cplx vi = cconj(v[i]);
-#pragma unroll
-            for (int c = 0; c < BT_COLS; c++) {
-                if (c < nc) {
-                    cplx zz = Z[(k + 1 + i) + (int64_t)(c0 + c) * ldz];
-                    cplx p = cmul(vi, zz);
-                    pr[c] += p.x;
-                    pi[c] += p.y;
-                }
-            }
-        }
-        cplx s[BT_COLS];
-#pragma unroll
-        for (int c = 0; c < BT_COLS; c++) {
-            double a = block_sum(pr[c], sh);
-            double b = block_sum(pi[c], sh);
-            s[c] = cmul(t, mk(a, b));
-        }
-        for (int i = threadIdx.x; i < m; i += blockDim.x) {
-            cplx vi = v[i];
-#pragma unroll
-            for (int c = 0; c < BT_COLS; c++) {
-                if (c < nc) {
-                    int64_t o = (k + 1 + i) + (int64_t)(c0 + c) * ldz;
-                    Z[o] = csub(Z[o], cmul(vi, s[c]));
-                }
-            }
-        }
-        __syncthreads();
-    }
-}
-
-struct HeevWork {
-    double *d, *e, *bounds;
-    cplx *tau, *ppart, *w;
-};
-
-static HeevWork heev_work(Context &c, int n) {
-    HeevWork h;
-    h.d = wsget<double>(c, "heev.d", n + 1);
-    h.e = wsget<double>(c, "heev.e", n + 1);
-    h.bounds = wsget<double>(c, "heev.bounds", 4);
-    h.tau = wsget<cplx>(c, "heev.tau", n + 1);
-    int nchunk = (n + HH_CHUNK - 1) / HH_CHUNK;
-    h.ppart = wsget<cplx>(c, "heev.ppart", (size_t)nchunk * (n + 1));
-    h.w = wsget<cplx>(c, "heev.w", n + 1);
-    return h;
-}
-
-// Reduce A to tridiagonal form; d, e, tau in the named workspace, reflectors in A.
-static void tridiag(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
-    for (int k = 0; k + 1 < n; k++) {
-        const int m = n - k - 1;
-        hh_gen_kernel<<<1, 256, 0, c.stream>>>(n, k, A, lda, h.d, h.e, h.tau);
-        DCG_LAUNCHED(c);
-        const int nchunk = (m + HH_CHUNK - 1) / HH_CHUNK;
-        dim3 g1(grid1d(m, 128), nchunk);
-        hh_matvec_kernel<<<g1, 128, 0, c.stream>>>(n, k, A, lda, h.tau, h.ppart);
-        DCG_LAUNCHED(c);
-        hh_w_kernel<<<1, 512, 0, c.stream>>>(n, k, A, lda, h.tau, h.ppart, nchunk, h.w);
-        DCG_LAUNCHED(c);
-        dim3 g2(grid1d(m, 128), m);
-        hh_update_kernel<<<g2, 128, 0, c.stream>>>(n, k, A, lda, h.w);
-        DCG_LAUNCHED(c);
-    }
-    hh_last_kernel<<<1, 1, 0, c.stream>>>(n, A, lda, h.d);
-    DCG_LAUNCHED(c);
-}
-
 void fam_collect(Context &c) {
     for (auto &pr : c.fam_ev) {
         cudaEventSynchronize(pr.second);
@@ -606,46 +394,6 @@ void fam_collect(Context &c) {
         cudaEventDestroy(pr.second);
     }
     c.fam_ev.clear();
-}
-
-void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
-    if (n <= 0) return;
-    FamScope fs(c, DCG_FAM_EIG, (16.0 / 3.0) * (double)n * n * n);
-    HeevWork h = heev_work(c, n);
-    {
-        FamScope f1(c, DCG_FAM_EIG_TRI, (16.0 / 3.0) * (double)n * n * n);
-        tridiag(c, n, A, lda, h);
-    }
-    {
-        FamScope f2(c, DCG_FAM_EIG_VAL, (double)n * n);
-        gersh_kernel<<<1, 1024, 0, c.stream>>>(n, h.d, h.e, h.bounds);
-        DCG_LAUNCHED(c);
-        bisect_kernel<<<grid1d(n, 128), 128, 0, c.stream>>>(n, h.d, h.e, h.bounds, w);
-        DCG_LAUNCHED(c);
-    }
-    heev_vectors_only(c, n, A, lda, w, vlo, vhi, Z, ldz);
-}
-
-// Eigenvectors [vlo, vhi) of the matrix most recently reduced by heev() (its reflectors
-// are still in A and its tridiagonal in the heev.* workspace).
-void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
-                       int64_t ldz) {
-    int nvec = vhi - vlo;
-    if (nvec <= 0 || n <= 0) return;
-    HeevWork h = heev_work(c, n);
-    double *scr = wsget<double>(c, "heev.scr", (size_t)n * nvec * 5 + 16);
-    double *zt = wsget<double>(c, "heev.z", (size_t)n * nvec + 16);
-    FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nvec);
-    {
-        FamScope f3(c, DCG_FAM_EIG_VEC, 10.0 * (double)n * nvec);
-        invit_kernel<<<grid1d(nvec, 64), 64, 0, c.stream>>>(n, h.d, h.e, w, h.bounds, vlo, nvec, scr, zt);
-        DCG_LAUNCHED(c);
-        cluster_mgs_kernel<<<nvec, 256, 0, c.stream>>>(n, w, h.bounds, vlo, nvec, zt, 1e-7);
-        DCG_LAUNCHED(c);
-    }
-    FamScope f4(c, DCG_FAM_EIG_BACK, 8.0 * (double)n * n * nvec);
-    backtransform_kernel<<<grid1d(nvec, BT_COLS), 256, 0, c.stream>>>(n, A, lda, h.tau, zt, nvec, Z, ldz);
-    DCG_LAUNCHED(c);
 }
 
 // ===================================================================== LU solve

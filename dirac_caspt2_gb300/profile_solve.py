@@ -1,0 +1,62 @@
+"""Run CASCI/CASPT2 solves of one synthetic workload, for profilers.
+
+A named workload (``--workload cas_20_12_300``) or explicit sizes
+(``--ninact 16 --nact 8 --nsec 240 --nelec 4``) is generated with the seeded synthetic
+generator, uploaded once, and solved ``--warmup + --solves`` times through the C ABI.
+The library marks each stage with an NVTX range (``ints``, ``casci_eig``, ``A`` ... ``H``,
+``transformation``) and each transformed integral class with ``tr_<class>``, so a profiler
+can select the launches of one stage, e.g.
+
+    ncu --nvtx --nvtx-include "tr_H/" -k regex:zgemm -c 3 ... \\
+        python -m dirac_caspt2_gb300.profile_solve --ninact 16 --nact 8 --nsec 240 --nelec 4
+
+Prints the total energy and per-stage device times of the last solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import sys
+import time
+
+from . import api, synth
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--workload", default=None, choices=sorted(synth.CONFIGS))
+    ap.add_argument("--ninact", type=int, default=8)
+    ap.add_argument("--nact", type=int, default=6)
+    ap.add_argument("--nsec", type=int, default=40)
+    ap.add_argument("--nelec", type=int, default=4)
+    ap.add_argument("--real", action="store_true")
+    ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--warmup", type=int, default=0)
+    ap.add_argument("--solves", type=int, default=1)
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    a = ap.parse_args(argv)
+    if a.workload:
+        cfg = synth.CONFIGS[a.workload]
+    else:
+        cfg = synth.SynthConfig(a.ninact, a.nact, a.nsec, a.nelec, realonly=a.real, seed=a.seed,
+                                name=f"cas_{a.ninact}_{a.nact}_{a.nsec}")
+    t0 = time.time()
+    system = api.SystemInput.from_synth(synth.make_system(cfg))
+    t1 = time.time()
+    prec = api.DCG_PREC_SPLIT if a.precision == "split" else api.DCG_PREC_FP64
+    ses = api.Caspt2Session(0, precision=prec)
+    res = None
+    for _ in range(a.warmup + a.solves):
+        res = ses.solve(system)
+    t2 = time.time()
+    print(json.dumps({
+        "workload": cfg.name, "generate_s": round(t1 - t0, 2), "solve_wall_s": round(t2 - t1, 3),
+        "solves": a.warmup + a.solves, "total_energy": res.total_energy,
+        "e2": res.e2, "kernel_launches": res.kernel_launches,
+        "stage_ms": {k: round(v, 3) for k, v in res.stage_ms.items()},
+    }))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

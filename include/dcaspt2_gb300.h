@@ -142,6 +142,20 @@ const char *dcg_version(void);
  * against the library's. */
 void *dcg_stream(const dcg_ctx *ctx);
 
+/* Hermitian eigendecomposition on the device, the solver behind every ZHEEV/DSYEV call of
+ * the path (src/diag.F90:43,109): ascending eigenvalues w_out[n] and, when z_re is not
+ * NULL, the eigenvectors as columns of z_re/z_im (n x n, column-major; z_im may be NULL to
+ * drop the imaginary plane).  The upper triangle of a_re/a_im (column-major; a_im NULL for a
+ * real symmetric matrix) is read, as ZHEEV with uplo='U' reads it. */
+int dcg_heev(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, double *w_out, double *z_re,
+             double *z_im);
+
+/* Symmetric tridiagonal eigendecomposition (the divide-and-conquer stage of dcg_heev; the
+ * role of LAPACK's DSTEDC): diagonal d[n], off-diagonal e[n-1] (host arrays), ascending
+ * eigenvalues w_out[n] and, when z_out is not NULL, eigenvectors as the columns of z_out
+ * (n x n, column-major). */
+int dcg_stedc(dcg_ctx *ctx, int32_t n, const double *d, const double *e, double *w_out, double *z_out);
+
 /* Kernel families whose launches can be timed with CUDA events on the context stream. */
 #define DCG_FAM_NONE 0
 #define DCG_FAM_TRANSFORM 1   /* 4-index transformation GEMMs; work = FLOPs (complex MAC = 8)  */
@@ -150,8 +164,8 @@ void *dcg_stream(const dcg_ctx *ctx);
 #define DCG_FAM_SCATTER 4     /* record expansion; work = record bytes read                      */
 #define DCG_FAM_EIG 5         /* Hermitian eigensolver launches; work = nominal FLOPs 16/3 n^3   */
 #define DCG_FAM_EIG_TRI 6     /* eigensolver phases: tridiagonal reduction (FLOPs 16/3 n^3)      */
-#define DCG_FAM_EIG_VAL 7     /*   bisection for the eigenvalues (Sturm steps)                   */
-#define DCG_FAM_EIG_VEC 8     /*   tridiagonal eigenvectors (inverse iteration + cluster MGS)    */
+#define DCG_FAM_EIG_VAL 7     /*   tridiagonal divide and conquer (values and vectors; 4/3 n^3)  */
+#define DCG_FAM_EIG_VEC 8     /*   reserved (no launches)                                          */
 #define DCG_FAM_EIG_BACK 9    /*   back-transformation (FLOPs 8 n^2 m)                            */
 
 /* Select the family timed during subsequent calls (DCG_FAM_NONE disables; resets stats). */
