@@ -88,6 +88,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_stream.restype = ctypes.c_void_p
     lib.dcg_time_family.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_family_stats.argtypes = [ctypes.c_void_p, P(ctypes.c_double), P(ctypes.c_int64), P(ctypes.c_double)]
+    lib.dcg_zgemm.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
+                              ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
+                              ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64,
+                              ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]
     lib.dcg_stedc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p]
     lib.dcg_heev.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -99,7 +103,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
-                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_stedc"]
+                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_stedc", "dcg_zgemm"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9}
 
@@ -348,6 +352,13 @@ class Caspt2Session:
         ptr = lambda x: None if x is None else x.ctypes.data
         self._check(self.lib.dcg_heev(self.h, n, ptr(are), ptr(aim), ptr(w), ptr(zr), ptr(zi)))
         return (w, zr + 1j * zi) if vectors else w
+
+    def zgemm(self, precision: int, M: int, N: int, K: int, batch: int, A_ptr: int, a_si: int, a_sk: int, a_sb: int,
+              B_ptr: int, ldb: int, conj_b: bool, C_ptr: int, c_si: int, c_sj: int, c_sb: int,
+              accumulate: bool = False):
+        """Complex GEMM on device buffers (dcg_zgemm); strides in complex elements."""
+        self._check(self.lib.dcg_zgemm(self.h, precision, M, N, K, batch, A_ptr, a_si, a_sk, a_sb, B_ptr, ldb,
+                                       int(conj_b), C_ptr, c_si, c_sj, c_sb, int(accumulate)))
 
     def stedc(self, d: np.ndarray, e: np.ndarray, vectors: bool = True):
         """Symmetric tridiagonal eigendecomposition on the device (dcg_stedc)."""

@@ -12,6 +12,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -283,22 +284,46 @@ static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double
 // ------------------------------------------------------------------------- 4-index transformation
 // (i'j'|k'l') = sum conj(U_ii') U_jj' conj(U_kk') U_ll' (ij|kl)   (module_intra.F90:130-277),
 // index l first, then k, j, i, as four GEMMs.
+// Quarters whose contracted orbital dimension exceeds this run on the split-precision tensor
+// cores when the context asks for DCG_PREC_SPLIT; smaller ones are memory-bound and stay on
+// the exact FP64 small-dimension kernels.
+constexpr int kSplitMinK = 32;
+
 static void transform4(Context &c, const cplx *in, cplx *out, cplx *tmp, const int dm[4], const cplx *U[4]) {
     const int64_t d0 = dm[0], d1 = dm[1], d2 = dm[2], d3 = dm[3];
     const int64_t tot = d0 * d1 * d2 * d3;
     if (tot == 0) return;
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    const bool split = c.precision == DCG_PREC_SPLIT;
+    const int lb = c.split_lbo, sb = c.split_sbo;
     // l: tmp = in * U4
-    zgemm(c, OP_N, OP_N, (int)(d0 * d1 * d2), (int)d3, (int)d3, one, in, d0 * d1 * d2, 0, U[3], d3, 0, zero, tmp,
-          d0 * d1 * d2, 0, 1);
+    if (split && d3 > kSplitMinK)
+        zgemm_split(c, (int)(d0 * d1 * d2), (int)d3, (int)d3, 1, in, 1, d0 * d1 * d2, 0, U[3], d3, 0, tmp, 1,
+                    d0 * d1 * d2, 0, false, lb, sb);
+    else
+        zgemm(c, OP_N, OP_N, (int)(d0 * d1 * d2), (int)d3, (int)d3, one, in, d0 * d1 * d2, 0, U[3], d3, 0, zero, tmp,
+              d0 * d1 * d2, 0, 1);
     // k: out_l = tmp_l * conj(U3)
-    zgemm(c, OP_N, OP_R, (int)(d0 * d1), (int)d2, (int)d2, one, tmp, d0 * d1, d0 * d1 * d2, U[2], d2, 0, zero, out,
-          d0 * d1, d0 * d1 * d2, (int)d3);
+    if (split && d2 > kSplitMinK)
+        zgemm_split(c, (int)(d0 * d1), (int)d2, (int)d2, (int)d3, tmp, 1, d0 * d1, d0 * d1 * d2, U[2], d2, 1, out, 1,
+                    d0 * d1, d0 * d1 * d2, false, lb, sb);
+    else
+        zgemm(c, OP_N, OP_R, (int)(d0 * d1), (int)d2, (int)d2, one, tmp, d0 * d1, d0 * d1 * d2, U[2], d2, 0, zero,
+              out, d0 * d1, d0 * d1 * d2, (int)d3);
     // j: tmp_kl = out_kl * U2
-    zgemm(c, OP_N, OP_N, (int)d0, (int)d1, (int)d1, one, out, d0, d0 * d1, U[1], d1, 0, zero, tmp, d0, d0 * d1,
-          (int)(d2 * d3));
-    // i: out = U1^H * tmp
-    zgemm(c, OP_C, OP_N, (int)d0, (int)(d1 * d2 * d3), (int)d0, one, U[0], d0, 0, tmp, d0, 0, zero, out, d0, 0, 1);
+    if (split && d1 > kSplitMinK)
+        zgemm_split(c, (int)d0, (int)d1, (int)d1, (int)(d2 * d3), out, 1, d0, d0 * d1, U[1], d1, 0, tmp, 1, d0,
+                    d0 * d1, false, lb, sb);
+    else
+        zgemm(c, OP_N, OP_N, (int)d0, (int)d1, (int)d1, one, out, d0, d0 * d1, U[1], d1, 0, zero, tmp, d0, d0 * d1,
+              (int)(d2 * d3));
+    // i: out = U1^H * tmp, as out^T = tmp^T conj(U1) on the split path
+    if (split && d0 > kSplitMinK)
+        zgemm_split(c, (int)(d1 * d2 * d3), (int)d0, (int)d0, 1, tmp, d0, 1, 0, U[0], d0, 1, out, d0, 1, 0, false, lb,
+                    sb);
+    else
+        zgemm(c, OP_C, OP_N, (int)d0, (int)(d1 * d2 * d3), (int)d0, one, U[0], d0, 0, tmp, d0, 0, zero, out, d0, 0,
+              1);
 }
 
 // ------------------------------------------------------------------------- subspace block solve
@@ -600,6 +625,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     for (int k = 0; k < 8; k++) { e2_sub[k] = 0.0; sc2_sub[k] = 0.0; }
     if (ni == 0 && ns == 0) throw Error{DCG_E_ARG, "CASPT2 energy undefined for ninact = 0 and nsec = 0"};
+    if (c.precision == DCG_PREC_SPLIT) split_reset(c);
 
     // full N-electron space and the CI-space positions inside it
     std::vector<uint64_t> full = gosper_all(na, c.ne);
@@ -977,6 +1003,8 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         sc2_sub[7] = hr[1];
     });
 
+    if (c.precision == DCG_PREC_SPLIT && split_error(c))
+        throw Error{DCG_E_NUMERIC, "split-precision GEMM: a pipeline wait timed out"};
     double e2all = 0.0, sumc2 = 0.0;
     for (int k = 0; k < 8; k++) { e2all += e2_sub[k]; sumc2 += sc2_sub[k]; }
     fam_collect(c);
@@ -1026,6 +1054,14 @@ int dcg_create(int device, int precision, dcg_ctx **out) {
         for (int k = 0; k <= dcg::ST_COUNT; k++) DCG_CUDA(cudaEventCreate(&c.ev[k]));
         c.ev_init = true;
         DCG_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
+        if (const char *ds = getenv("DCG_SPLIT_DESC_STRIDES")) {   // diagnostic: "lbo,sbo"
+            int l = 0, s = 0;
+            if (sscanf(ds, "%d,%d", &l, &s) == 2 && l > 0 && s > 0 && l % 16 == 0 && s % 16 == 0 && l <= 4096 &&
+                s <= 4096) {
+                c.split_lbo = l;
+                c.split_sbo = s;
+            }
+        }
         dcg::upload_binomials(c);
         DCG_CUDA(cudaStreamSynchronize(c.stream));
     } catch (const Error &e) {
@@ -1093,6 +1129,33 @@ int64_t dcg_kernel_launches(const dcg_ctx *ctx) { return ctx ? ctx->c.launches :
 const char *dcg_version(void) { return "dcaspt2_gb300 0.1 (sm_103a, FP64 path)"; }
 
 void *dcg_stream(const dcg_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }
+
+int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int32_t batch, const void *A, int64_t a_si,
+              int64_t a_sk, int64_t a_sb, const void *B, int64_t ldb, int32_t conj_b, void *C, int64_t c_si,
+              int64_t c_sj, int64_t c_sb, int32_t accumulate) {
+    if (M < 0 || N < 0 || K < 0 || batch < 0 || (M * (int64_t)N * batch > 0 && (!A || !B || !C))) return DCG_E_ARG;
+    if (precision != DCG_PREC_FP64 && precision != DCG_PREC_SPLIT) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        if ((int64_t)M * N * batch == 0) return DCG_OK;
+        const dcg::cplx *a = static_cast<const dcg::cplx *>(A);
+        const dcg::cplx *b = static_cast<const dcg::cplx *>(B);
+        dcg::cplx *cc = static_cast<dcg::cplx *>(C);
+        if (precision == DCG_PREC_SPLIT) {
+            dcg::split_reset(c_);
+            dcg::zgemm_split(c_, M, N, K, batch, a, a_si, a_sk, a_sb, b, ldb, conj_b ? 1 : 0, cc, c_si, c_sj, c_sb,
+                             accumulate != 0, c_.split_lbo, c_.split_sbo);
+            if (dcg::split_error(c_)) throw(Error{DCG_E_NUMERIC, "split GEMM: a pipeline wait timed out"});
+        } else {
+            if (a_si != 1 || c_si != 1) throw(Error{DCG_E_ARG, "FP64 dcg_zgemm needs column-major A and C"});
+            const dcg::cplx one = dcg::mk(1.0, 0.0);
+            const dcg::cplx beta = accumulate ? one : dcg::mk(0.0, 0.0);
+            dcg::zgemm(c_, dcg::OP_N, conj_b ? dcg::OP_R : dcg::OP_N, M, N, K, one, a, a_sk, a_sb, b, ldb, 0, beta, cc,
+                       c_sj, c_sb, batch);
+        }
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        return DCG_OK;
+    });
+}
 
 int dcg_stedc(dcg_ctx *ctx, int32_t n, const double *d, const double *e, double *w_out, double *z_out) {
     if (n < 0 || (n > 0 && (!d || !w_out || (n > 1 && !e)))) return DCG_E_ARG;

@@ -89,6 +89,8 @@ struct Context {
     int fam = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> fam_ev;
     double fam_ms = 0.0, fam_work = 0.0;
+    // tcgen05 shared-memory descriptor strides of the split GEMM (leading, stride byte offset)
+    int split_lbo = 128, split_sbo = 256;
     // tridiagonal eigenvectors of the last heev (device, n x n), for heev_vectors_only
     const double *eig_Q = nullptr;
     int eig_n = 0;
@@ -188,6 +190,15 @@ void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, 
 // Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (same A, w).
 void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
                        int64_t ldz);
+
+// Split-precision (BF16 tensor core, FP64 recombination) complex GEMM, dcg_split.cu:
+// C[z*c_sb + i*c_si + j*c_sj] (+)= sum_k A[z*a_sb + i*a_si + k*a_sk] * op(B)(k, j),
+// op(B)(k, j) = B[k + j*ldb] (conj_b 0) or its conjugate (conj_b 1).
+void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int64_t a_si, int64_t a_sk, int64_t a_sb,
+                 const cplx *B, int64_t ldb, int opb, cplx *C, int64_t c_si, int64_t c_sj, int64_t c_sb,
+                 bool accumulate, int lbo, int sbo);
+void split_reset(Context &c);
+int split_error(Context &c);
 
 // Symmetric tridiagonal eigendecomposition by divide and conquer (d: n, e: n-1, device);
 // ascending eigenvalues into w, eigenvectors returned (n x n, ld n, workspace-owned).

@@ -156,6 +156,16 @@ int dcg_heev(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, do
  * (n x n, column-major). */
 int dcg_stedc(dcg_ctx *ctx, int32_t n, const double *d, const double *e, double *w_out, double *z_out);
 
+/* Complex GEMM on device buffers at a chosen precision (the contraction kernel of the
+ * 4-index transformation): for z < batch, i < M, j < N
+ *   C[z*c_sb + i*c_si + j*c_sj] (+)= sum_{k<K} A[z*a_sb + i*a_si + k*a_sk] * op(B)(k, j)
+ * with op(B)(k, j) = B[k + j*ldb], conjugated when conj_b; strides count complex elements
+ * (double2).  DCG_PREC_SPLIT runs the BF16 tensor-core path with FP64 recombination (any
+ * strides); DCG_PREC_FP64 needs a_si = c_si = 1.  accumulate != 0 adds to C. */
+int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int32_t batch, const void *A, int64_t a_si,
+              int64_t a_sk, int64_t a_sb, const void *B, int64_t ldb, int32_t conj_b, void *C, int64_t c_si,
+              int64_t c_sj, int64_t c_sb, int32_t accumulate);
+
 /* Kernel families whose launches can be timed with CUDA events on the context stream. */
 #define DCG_FAM_NONE 0
 #define DCG_FAM_TRANSFORM 1   /* 4-index transformation GEMMs; work = FLOPs (complex MAC = 8)  */
