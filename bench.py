@@ -6,7 +6,9 @@ transformation and the eight subspaces A-H) of the seeded synthetic system
 20 inactive / 12 active (6 electrons) / 300 secondary Kramers-paired complex spinors,
 CASCI root 1.
 
-  value  : solves/s with the MDCINTNEW records already resident in HBM (device pointers)
+  value  : solves/s of the split-precision path (transformation on BF16 tensor cores, FP64
+           recombination) with the MDCINTNEW records already resident in HBM (device pointers)
+  fp64_gpu : the plain FP64 GPU path on the same system, and |dE2| between the two paths
   e2e    : solves/s through the public C-ABI call with pinned host buffers; every step
            copies the records and one-electron data host->device and reads the energies back
   cpu_baseline / --impl reference : the CPU restatement of the reference algorithm
@@ -35,6 +37,7 @@ CONFIG = "cas_20_12_300"
 ROOFLINE_FAMILY = "transform"
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 FALLBACK_PEAKS = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}
+REF_BUDGET_S = 150.0   # reference arm: stop adding CPU solves past this much time
 
 
 def _dist():
@@ -116,7 +119,10 @@ def cpu_oracle_solve(S, cfg):
 
 
 def run_reference(args, cfg_name):
-    """Reference arm: the CPU restatement of the reference's FP64 algorithm on the host cores."""
+    """Reference arm: the CPU restatement of the reference's FP64 algorithm (oracle/) on the
+    host cores.  One step is one full solve of the workload.  A CPU solve has no warm-up state,
+    so the warm-up steps are not run, and steps stop once REF_BUDGET_S of solves have
+    accumulated (at least one); the line states how many ran."""
     rank, world, local = _dist()
     if rank != 0:
         return 0
@@ -124,22 +130,26 @@ def run_reference(args, cfg_name):
     cfg = synth.CONFIGS[cfg_name]
     S = synth.make_system(cfg)
     times = []
-    for k in range(args.warmup + args.steps):
+    r = None
+    for k in range(max(1, args.steps)):
         dt, r = cpu_oracle_solve(S, cfg)
-        if k >= args.warmup:
-            times.append(dt)
+        times.append(dt)
+        if sum(times) > REF_BUDGET_S:
+            break
     mean = sum(times) / len(times)
     cores = os.cpu_count()
     value = 1.0 / mean
     line = {"impl": "reference", "metric": "caspt2_solves_per_s", "value": value, "unit": "solves/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": mean * 1e3,
+            "n_gpus": args.gpus, "steps": len(times), "steps_requested": args.steps, "warmup": 0,
+            "warmup_requested": args.warmup, "ms_per_step": mean * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128 (f64)",
             "data": "synthetic (seeded Kramers-paired complex spinor system)",
             "config": {"workload": cfg_name, "ninact": cfg.ninact, "nact": cfg.nact, "nsec": cfg.nsec,
                        "nelec": cfg.nelec, "root": 1, "l2": "inputs larger than L2"},
             "cpu_baseline": {"value": value, "unit": "solves/s", "cores": cores, "kind": "port",
-                             "sample": f"full CASCI+CASPT2 solve of {cfg_name} by the numpy restatement "
-                                       "of the reference (oracle/), host BLAS threads = all cores"},
+                             "sample": f"{len(times)} full CASCI+CASPT2 solve(s) of {cfg_name} by the numpy "
+                                       "restatement of the reference (oracle/); host BLAS threads = all cores; "
+                                       "the reference's Fortran needs a Fortran compiler absent here"},
             "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "p50_ms": float(np.percentile(np.array(times) * 1e3, 50)),
             "p99_ms": float(np.percentile(np.array(times) * 1e3, 99)),
@@ -161,6 +171,7 @@ def run_ours(args, cfg_name):
     S = synth.make_system(cfg)
     sin = api.SystemInput.from_synth(S)
     prec = api.DCG_PREC_SPLIT if args.precision == "split" else api.DCG_PREC_FP64
+    family = args.roofline_family or ("split_mma" if prec == api.DCG_PREC_SPLIT else "transform")
     ses = api.Caspt2Session(local, prec)
     stream = torch.cuda.ExternalStream(ses.stream_ptr, device=local)
 
@@ -178,22 +189,18 @@ def run_ours(args, cfg_name):
     hb_dev = api.HostBuffers(sin)
     hb_dev.use_device_records(dev["ijkl"].data_ptr(), dev["re"].data_ptr(),
                               dev["im"].data_ptr() if "im" in dev else 0)
-    hb = hb_host
 
-    def one(bufs):
-        ses.set_system(sin, bufs)
-        ses.casci(1)
-        return ses.caspt2(0)
+    def one(session, bufs):
+        session.set_system(sin, bufs)
+        eig, _ = session.casci(1)
+        e2, sc2, e0, etot = session.caspt2(0)
+        return eig[0], e2, etot
 
-    # warm-up (allocations, module load)
-    for _ in range(args.warmup):
-        ref = one(hb_dev)
-    e_ref = ref[3]
-
-    def timed(bufs, family=None):
-        if family:
-            ses.time_family(family)
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    def timed(session, bufs, steps, fam=None):
+        strm = torch.cuda.ExternalStream(session.stream_ptr, device=local)
+        if fam:
+            session.time_family(fam)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         launches = 0
         if world > 1:
             import torch.distributed as dist
@@ -201,27 +208,46 @@ def run_ours(args, cfg_name):
         torch.cuda.synchronize()
         clk = ClockSampler(local)
         clk.start()
-        energies = []
-        t0 = time.perf_counter()
-        for k in range(args.steps):
-            ev[k][0].record(stream)
-            r = one(bufs)
-            ev[k][1].record(stream)
-            launches += ses.kernel_launches()
-            energies.append(r[3])
+        results = []
+        for k in range(steps):
+            ev[k][0].record(strm)
+            results.append(one(session, bufs))
+            ev[k][1].record(strm)
+            launches += session.kernel_launches()
         torch.cuda.synchronize()
-        wall = time.perf_counter() - t0
         clocks = clk.stop()
-        per = [a.elapsed_time(b) for a, b in ev]
-        fam = ses.family_stats() if family else None
-        if family:
-            ses.time_family("none")
-        return per, wall, launches, clocks, energies, fam
+        per = [x.elapsed_time(y) for x, y in ev]
+        stats = session.family_stats() if fam else None
+        if fam:
+            session.time_family("none")
+        return per, launches, clocks, results, stats
 
-    per_v, wall_v, launches_v, clocks_v, en_v, fam = timed(hb_dev, ROOFLINE_FAMILY)
-    per_e, wall_e, launches_e, clocks_e, en_e, _ = timed(hb_host)
+    for _ in range(args.warmup):          # allocations, module load
+        one(ses, hb_dev)
+    per_v, launches_v, clocks_v, res_v, fam = timed(ses, hb_dev, args.steps, family)
+    per_e, _, clocks_e, res_e, _ = timed(ses, hb_host, args.steps)
+    stage = ses.stage_ms()
     tot_v = sum(per_v) / 1e3
     tot_e = sum(per_e) / 1e3
+
+    # plain FP64 GPU path on the same system: the comparison the metric names
+    fp64 = None
+    if prec == api.DCG_PREC_SPLIT and not args.no_fp64_compare:
+        s64 = api.Caspt2Session(local, api.DCG_PREC_FP64)
+        for _ in range(max(1, min(args.warmup, 2))):
+            one(s64, hb_dev)
+        n64 = max(3, min(args.steps, 5))
+        per_64, _, _, res_64, _ = timed(s64, hb_dev, n64)
+        s64.close()
+        e_s, e2_s, t_s = res_v[-1]
+        e_d, e2_d, t_d = res_64[-1]
+        fp64 = {"value": n64 / (sum(per_64) / 1e3), "unit": "solves/s", "ms_per_step": sum(per_64) / n64,
+                "p50_ms": float(np.percentile(per_64, 50)), "p99_ms": float(np.percentile(per_64, 99)),
+                "max_abs_dE2_subspace": max(abs(e2_s[k] - e2_d[k]) for k in e2_s),
+                "abs_dE2_total": abs(sum(e2_s.values()) - sum(e2_d.values())),
+                "abs_dE_casci": abs(e_s - e_d), "abs_dE_total": abs(t_s - t_d),
+                "dE2_by_subspace": {k: e2_s[k] - e2_d[k] for k in e2_s}}
+
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([tot_v, tot_e], dtype=torch.float64)
@@ -229,44 +255,54 @@ def run_ours(args, cfg_name):
         tot_v, tot_e = float(t[0]), float(t[1])
     value = world * args.steps / tot_v
     e2e = world * args.steps / tot_e
-    stage = ses.stage_ms()
     peaks, src = _peaks()
-    # roofline of the dominant kernel family
     fam_ms, fam_launch, fam_work = fam
-    per_launch_ms = fam_ms / max(1, fam_launch)
-    if ROOFLINE_FAMILY in ("hstream", "scatter"):
+    if family in ("hstream", "scatter"):
         achieved = fam_work / (fam_ms * 1e-3) / 1e9
         roof = {"bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                 "frac": achieved / peaks["hbm_gbs"]}
-    else:
+    elif family == "split_mma":
         achieved = fam_work / (fam_ms * 1e-3) / 1e12
         pk = peaks["bf16_tflops_sustained"]
-        roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk}
-    roof.update({"traffic": None, "kernel_family": ROOFLINE_FAMILY, "launches_timed": fam_launch,
-                 "mean_launch_ms": per_launch_ms, "peak_source": f"{src} ({'sustained' if roof['unit'] == 'TFLOP/s' else 'burst'})"})
+        roof = {"bound": "tensor", "achieved": achieved, "peak": pk, "unit": "TFLOP/s", "frac": achieved / pk,
+                "work": "BF16 tensor FLOPs of the 15 slice products (15 x 8 M N K per complex M x N x K GEMM)"}
+    else:
+        achieved = fam_work / (fam_ms * 1e-3) / 1e12
+        roof = {"bound": "fp64", "achieved": achieved, "peak": None, "unit": "TFLOP/s", "frac": None,
+                "work": "FP64 FLOPs; GB300 has no FP64 tensor rate to compare against"}
+    roof.update({"traffic": None, "kernel_family": family, "launches_timed": fam_launch,
+                 "mean_launch_ms": fam_ms / max(1, fam_launch),
+                 "peak_source": f"{src} MEASURED_PEAKS.json ({'sustained' if roof['unit'] == 'TFLOP/s' else 'burst'})"})
+    e_casci, e2_last, e_tot = res_v[-1]
+    energies = [r[2] for r in res_v + res_e]
     line = {"metric": "caspt2_solves_per_s", "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": tot_v / args.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "c128 (f64)" if prec == api.DCG_PREC_FP64 else "c128 (split bf16 -> f64)",
+            "dtype": ("c128 (f64)" if prec == api.DCG_PREC_FP64 else
+                      "c128: transformation on BF16 tensor cores as 5-slice split products with FP64 "
+                      "recombination; eigensolvers, densities and E2 in f64"),
             "data": "synthetic (seeded Kramers-paired complex spinor system; replicas only)",
             "config": {"workload": cfg_name, "ninact": cfg.ninact, "nact": cfg.nact, "nsec": cfg.nsec,
                        "nelec": cfg.nelec, "root": 1, "records": int(len(S.rec_val)),
                        "precision": args.precision, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (1 GB of records, 0.6 GB H class per step)"},
             "p50_ms": float(np.percentile(per_v, 50)), "p99_ms": float(np.percentile(per_v, 99)),
-            "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": hb.h2d_bytes,
+            "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": hb_host.h2d_bytes,
                     "d2h_bytes_per_step": 8 * (1 + 8 + 8 + 2), "p50_ms": float(np.percentile(per_e, 50)),
                     "p99_ms": float(np.percentile(per_e, 99))},
             "gpu_launches": int(launches_v),
             "clocks": clocks_v, "roofline": roof,
             "stage_ms_last_step": {k: round(v, 3) for k, v in stage.items()},
-            "total_energy": e_ref, "energy_spread": float(max(en_v + en_e) - min(en_v + en_e))}
+            "total_energy": e_tot, "energy_spread": float(max(energies) - min(energies))}
+    if fp64 is not None:
+        line["fp64_gpu"] = fp64
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         dt, r = cpu_oracle_solve(S, cfg)
         line["cpu_baseline"] = {"value": 1.0 / dt, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
                                 "sample": f"one full CASCI+CASPT2 solve of {cfg_name} by the numpy restatement "
                                           "(oracle/), host BLAS threads = all cores",
-                                "abs_diff_total_energy": abs(r.total_energy - e_ref)}
+                                "abs_diff_total_energy": abs(r.total_energy - e_tot),
+                                "max_abs_dE2_subspace": max(abs(r.e2[k] - e2_last[k]) for k in r.e2)}
     if rank == 0:
         print(json.dumps(line), flush=True)
     ses.close()
@@ -280,7 +316,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--config", default=CONFIG)
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--precision", default="split", choices=["fp64", "split"])
+    ap.add_argument("--roofline-family", default=None,
+                    help="kernel family timed live for the roofline (default: split_mma, or transform for fp64)")
+    ap.add_argument("--no-fp64-compare", action="store_true", help="skip the plain FP64 GPU comparison leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":

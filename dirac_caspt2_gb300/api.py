@@ -105,7 +105,7 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
                     "dcg_solve_h_noalloc", "dcg_heev", "dcg_stedc", "dcg_zgemm"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
-            "eig_val": 7, "eig_vec": 8, "eig_back": 9}
+            "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
 
 def _ptr(a: Optional[np.ndarray], ct):

@@ -415,7 +415,14 @@ static RdmBufs rdm_build(Context &c, const uint64_t *full, int64_t M, const cplx
     r.g1 = wsget<cplx>(c, "rdm.g1", (size_t)nv * na2);
     zgemm(c, OP_C, OP_N, 1, (int)(nv * na2), (int)M, one, psi, M, 0, YZ, M, 0, zero, r.g1, 1, 0, 1);
     r.gall = wsget<cplx>(c, "rdm.gall", (size_t)na2 * ncol);
-    zgemm(c, OP_C, OP_N, (int)na2, (int)ncol, (int)M, one, YZ, M, 0, YZ, M, 0, zero, r.gall, na2, 0, 1);
+    if (c.precision == DCG_PREC_SPLIT && M > 32 && ncol >= 128) {
+        // gall^T = [Y|Z]^T conj(Y) on the split-precision tensor cores (rows of [Y|Z]^T are
+        // its columns, contiguous along the determinant index)
+        zgemm_split(c, (int)ncol, (int)na2, (int)M, 1, YZ, M, 1, 0, YZ, M, 1, r.gall, na2, 1, 0, false, c.split_lbo,
+                    c.split_sbo);
+    } else {
+        zgemm(c, OP_C, OP_N, (int)na2, (int)ncol, (int)M, one, YZ, M, 0, YZ, M, 0, zero, r.gall, na2, 0, 1);
+    }
     r.Y = YZ;
     r.M = M;
     r.view.na = na;
@@ -1224,7 +1231,7 @@ int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, 
 }
 
 int dcg_time_family(dcg_ctx *ctx, int32_t family) {
-    if (!ctx || family < 0 || family > DCG_FAM_EIG_BACK) return DCG_E_ARG;
+    if (!ctx || family < 0 || family > DCG_FAM_SPLIT_MMA) return DCG_E_ARG;
     Context &c = ctx->c;
     dcg::fam_collect(c);
     c.fam = family;

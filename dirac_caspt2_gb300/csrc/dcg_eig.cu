@@ -202,36 +202,72 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
     return t;
 }
 
-// Grid-wide barrier for a cooperative launch.  Each wait is bounded (5 s); a block that
-// gives up sets gb->err and every block then leaves the kernel.
+// Grid-wide barrier for a cooperative launch: one monotonically increasing arrival counter
+// (count), so a barrier costs one fence, one atomic and an acquire poll.  Each wait is bounded
+// (5 s); a block that gives up sets gb->err and every waiting block then leaves the kernel.
 constexpr uint64_t kBarrierLimitNs = 5000000000ull;
 __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned nblocks) {
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        volatile unsigned *vgen = &gb->gen;
-        volatile int *verr = &gb->err;
-        const unsigned g = *vgen;
+        int ok = 1;
         __threadfence();
-        if (atomicAdd(&gb->count, 1u) == nblocks - 1) {
-            atomicExch(&gb->count, 0u);
-            __threadfence();
-            atomicAdd(&gb->gen, 1u);
-        } else {
+        const unsigned arrive = atomicAdd(&gb->count, 1u);
+        const unsigned target = (arrive / nblocks + 1u) * nblocks;
+        unsigned cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->count) : "memory");
+        if ((int)(cur - target) < 0) {
             const uint64_t t0 = globaltimer_ns();
-            while (*vgen == g && *verr == 0) {
-                if (globaltimer_ns() - t0 > kBarrierLimitNs) {
-                    atomicExch(&gb->err, 1);
-                    break;
+            unsigned spins = 0;
+            while (true) {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->count) : "memory");
+                if ((int)(cur - target) >= 0) break;
+                if ((++spins & 255u) == 0) {
+                    if (*(volatile int *)&gb->err) {
+                        ok = 0;
+                        break;
+                    }
+                    if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+                        atomicExch(&gb->err, 1);
+                        ok = 0;
+                        break;
+                    }
                 }
-                __nanosleep(100);
             }
         }
-        __threadfence();
-        s_ok = (*verr == 0);
+        s_ok = ok;
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// Two deterministic block sums in one pass (sh >= 64 doubles); every thread gets both.
+__device__ void eig_block_sum2(double &a, double &b, double *sh) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    __syncthreads();
+    if (lane == 0) {
+        sh[wid] = a;
+        sh[32 + wid] = b;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double x = lane < nw ? sh[lane] : 0.0, y = lane < nw ? sh[32 + lane] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) {
+            x += __shfl_down_sync(0xffffffffu, x, o);
+            y += __shfl_down_sync(0xffffffffu, y, o);
+        }
+        if (lane == 0) {
+            sh[0] = x;
+            sh[32] = y;
+        }
+    }
+    __syncthreads();
+    a = sh[0];
+    b = sh[32];
 }
 
 __device__ __forceinline__ cplx ldcg(const cplx *p) { return __ldcg(p); }
@@ -381,6 +417,156 @@ __global__ void __launch_bounds__(TRD_THREADS) tridiag_persistent_kernel(int n, 
         if (!grid_barrier(gb, nb)) return;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) d[n - 1] = ldcg(A + (n - 1) + (int64_t)(n - 1) * lda).x;
+}
+
+// ---- shared-memory-resident form (n up to kTridiagSmemMaxN): the matrix lives in the blocks'
+// shared memory for the whole reduction, block b owning columns b, b + nb, ...  Per column k
+// the global traffic is the reflector v (written by the owner of column k), the all-gathered
+// p = tau A22 v (one entry per column, from its owner) and one partial dot per block; the
+// matvec and the rank-2 update run from shared memory.  The warp that updates column k+1
+// forms the next reflector from it right away.  Two grid barriers per column.
+constexpr int kTridiagSmemMaxN = 1400;
+
+// reflector of x[0..m) (x[0] = alpha), by one warp; returns tau, beta, the scale for x[1:]
+__device__ __forceinline__ void warp_reflector(const cplx *x, int m, cplx &tau, double &beta, cplx &scale,
+                                               bool &skip) {
+    const int lane = threadIdx.x & 31;
+    double ss = 0.0;
+    for (int i = 1 + lane; i < m; i += 32) ss += cabs2(x[i]);
+    ss = eig_warp_sum(ss);
+    const cplx alpha = x[0];
+    const double xnorm = sqrt(ss);
+    if (xnorm == 0.0 && alpha.y == 0.0) {
+        tau = mk(0.0, 0.0);
+        beta = alpha.x;
+        scale = mk(1.0, 0.0);
+        skip = true;
+    } else {
+        const double nrm = sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xnorm * xnorm);
+        beta = alpha.x >= 0.0 ? -nrm : nrm;
+        tau = mk((beta - alpha.x) / beta, -alpha.y / beta);
+        scale = cdiv(mk(1.0, 0.0), mk(alpha.x - beta, alpha.y));
+        skip = false;
+    }
+}
+
+// Column k+1 is in this block's shared memory (local slot c): write its reflector (rows k+2..)
+// to A(k+2:, k+1), and d[k+1], e[k+1], tau[k+1].  One warp.
+__device__ __forceinline__ void publish_reflector(int n, int k1, const cplx *col, cplx *A, int64_t lda, double *d,
+                                                  double *e, cplx *tau) {
+    const int lane = threadIdx.x & 31;
+    const int m = n - k1 - 1;
+    const cplx *x = col + k1 + 1;
+    cplx t, sc;
+    double beta;
+    bool skip;
+    warp_reflector(x, m, t, beta, sc, skip);
+    cplx *g = A + (k1 + 1) + (int64_t)k1 * lda;
+    for (int i = lane; i < m; i += 32) g[i] = i == 0 ? mk(1.0, 0.0) : (skip ? x[i] : cmul(x[i], sc));
+    if (lane == 0) {
+        tau[k1] = t;
+        e[k1] = beta;
+        d[k1] = col[k1].x;
+    }
+}
+
+__global__ void __launch_bounds__(TRD_THREADS) tridiag_smem_kernel(int n, cplx *A, int64_t lda, double *d, double *e,
+                                                                    cplx *tau, cplx *pbuf, double2 *part,
+                                                                    GridBar *gb) {
+    extern __shared__ cplx tsm2[];
+    __shared__ double red[64];
+    const unsigned nb = gridDim.x;
+    const int b = blockIdx.x;
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
+    const int nown = (n - b + (int)nb - 1) / (int)nb;   // columns b, b+nb, ...
+    cplx *cols = tsm2;                                    // nown x n
+    cplx *sv = cols + (size_t)nown * n, *sw = sv + n;
+    for (int64_t x = threadIdx.x; x < (int64_t)nown * n; x += blockDim.x) {
+        const int c = (int)(x / n), r = (int)(x % n);
+        cols[x] = A[r + (int64_t)(b + c * (int)nb) * lda];
+    }
+    __syncthreads();
+    if (b == 0 && wib == 0) {
+        if (n >= 2) publish_reflector(n, 0, cols, A, lda, d, e, tau);
+        else if (lane == 0) d[0] = cols[0].x;
+    }
+    if (!grid_barrier(gb, nb)) return;
+    for (int k = 0; k + 1 < n; k++) {
+        const cplx t = ldcg(tau + k);
+        const bool active = (t.x != 0.0 || t.y != 0.0);
+        for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sv[r] = ldcg(A + r + (int64_t)k * lda);
+        __syncthreads();
+        // first owned column index > k
+        const int c0 = k + 1 > b ? (k + 1 - b + (int)nb - 1) / (int)nb : 0;
+        double pr = 0.0, pim = 0.0;
+        if (active) {
+            for (int c = c0 + wib; c < nown; c += nwb) {
+                const int j = b + c * (int)nb;
+                const cplx *col = cols + (size_t)c * n;
+                double ar = 0.0, ai = 0.0;
+                for (int r = k + 1 + lane; r < n; r += 32) {
+                    const cplx a = col[r], v = sv[r];
+                    ar += a.x * v.x + a.y * v.y;
+                    ai += a.x * v.y - a.y * v.x;
+                }
+                for (int o = 16; o > 0; o >>= 1) {
+                    ar += __shfl_down_sync(0xffffffffu, ar, o);
+                    ai += __shfl_down_sync(0xffffffffu, ai, o);
+                }
+                if (lane == 0) {
+                    const cplx xp = cmul(t, mk(ar, ai));
+                    pbuf[j] = xp;
+                    const cplx xv = cmul(cconj(xp), sv[j]);
+                    pr += xv.x;
+                    pim += xv.y;
+                }
+            }
+        }
+        eig_block_sum2(pr, pim, red);
+        if (threadIdx.x == 0) part[b] = make_double2(pr, pim);
+        if (!grid_barrier(gb, nb)) return;
+        if (active) {
+            double sr = 0.0, si = 0.0;
+            for (unsigned q = threadIdx.x; q < nb; q += blockDim.x) {
+                const double2 v = __ldcg(part + q);
+                sr += v.x;
+                si += v.y;
+            }
+            eig_block_sum2(sr, si, red);
+            const cplx al = cmul(mk(-0.5, 0.0), cmul(t, mk(sr, si)));
+            for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sw[r] = cadd(ldcg(pbuf + r), cmul(al, sv[r]));
+            __syncthreads();
+        }
+        // update owned columns > k; the warp that owns column k+1 then publishes its reflector
+        for (int c = c0 + wib; c < nown; c += nwb) {
+            const int j = b + c * (int)nb;
+            cplx *col = cols + (size_t)c * n;
+            if (active) {
+                const cplx vj = sv[j], wj = sw[j];
+                for (int r = k + 1 + lane; r < n; r += 32) {
+                    // a -= v_r conj(w_j) + w_r conj(v_j), as eight FMAs
+                    const cplx vr = sv[r], wr = sw[r];
+                    cplx a = col[r];
+                    a.x = fma(-vr.x, wj.x, a.x);
+                    a.x = fma(-vr.y, wj.y, a.x);
+                    a.x = fma(-wr.x, vj.x, a.x);
+                    a.x = fma(-wr.y, vj.y, a.x);
+                    a.y = fma(-vr.y, wj.x, a.y);
+                    a.y = fma(vr.x, wj.y, a.y);
+                    a.y = fma(-wr.y, vj.x, a.y);
+                    a.y = fma(wr.x, vj.y, a.y);
+                    if (r == j) a.y = 0.0;
+                    col[r] = a;
+                }
+                __syncwarp();
+            }
+            if (j == k + 1) {
+                if (k + 2 < n) publish_reflector(n, k + 1, col, A, lda, d, e, tau);
+                else if (lane == 0) d[k + 1] = col[k + 1].x;
+            }
+        }
+        if (!grid_barrier(gb, nb)) return;
+    }
 }
 
 // ===================================================================== 2. divide and conquer
@@ -839,7 +1025,7 @@ static const double *tridiag_dc(Context &c, int n, const double *d, const double
 // of a panel H_k0 ... H_{k0+nb-1} is I - V T V^H with T upper triangular (the compact WY form
 // of Schreiber & Van Loan, SIAM J. Sci. Stat. Comput. 10 (1989) 53), built by the forward
 // recurrence T(0:i, i) = -tau_i T(0:i, 0:i) (V(:, 0:i)^H v_i).  Each panel costs three GEMMs.
-constexpr int WY_NB = 32;
+constexpr int WY_NB = 64;
 
 __global__ void z_from_real_kernel(int n, const double *__restrict__ Qt, int vlo, int nvec, cplx *Z, int64_t ldz) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -861,21 +1047,105 @@ __global__ void wy_extract_kernel(int n, int k0, int nbp, const cplx *__restrict
     Vp[r + (int64_t)jj * m0] = v;
 }
 
-// T (nbp x nbp, ld WY_NB) from G = Vp^H Vp and tau[k0..]; one block of WY_NB threads.
+// T (nbp x nbp, ld WY_NB) from G = Vp^H Vp and tau[k0..]; one block of WY_NB threads with
+// G and T staged in shared memory (the recurrence is sequential in i).
 __global__ void wy_tfactor_kernel(int nbp, const cplx *__restrict__ G, const cplx *__restrict__ tau, int k0, cplx *T) {
+    extern __shared__ cplx wy_sm[];
+    cplx *Gs = wy_sm, *Ts = wy_sm + WY_NB * WY_NB;
     const int j = threadIdx.x;
-    for (int x = j; x < WY_NB * WY_NB; x += blockDim.x) T[x] = mk(0.0, 0.0);
+    for (int x = j; x < WY_NB * WY_NB; x += blockDim.x) {
+        Ts[x] = mk(0.0, 0.0);
+        const int r = x % WY_NB, cc = x / WY_NB;
+        Gs[x] = (r < nbp && cc < nbp) ? G[r + cc * nbp] : mk(0.0, 0.0);
+    }
     __syncthreads();
     for (int i = 0; i < nbp; i++) {
         const cplx ti = tau[k0 + i];
         cplx acc = mk(0.0, 0.0);
         if (j < i)
-            for (int l = j; l < i; l++) cfma(acc, T[j + l * WY_NB], G[l + i * nbp]);
+            for (int l = j; l < i; l++) cfma(acc, Ts[j + l * WY_NB], Gs[l + i * WY_NB]);
         __syncthreads();
-        if (j < i) T[j + i * WY_NB] = cmul(mk(-ti.x, -ti.y), acc);
-        if (j == i) T[i + i * WY_NB] = ti;
+        if (j < i) Ts[j + i * WY_NB] = cmul(mk(-ti.x, -ti.y), acc);
+        if (j == i) Ts[i + i * WY_NB] = ti;
         __syncthreads();
     }
+    for (int x = j; x < WY_NB * WY_NB; x += blockDim.x) T[x] = Ts[x];
+}
+
+// Register-resident back-transformation (n <= 32 R): one warp per eigenvector column, the
+// column held in registers (lane owns rows lane + 32 i), the reflectors applied from the last
+// to the first and read straight from L1/L2 (they are read-only here and shared by every warp
+// of an SM).  Columns are independent: no block or grid synchronisation, and the FP64 work,
+// written as explicit FMAs (8 per row and reflector), spreads over every SM.
+template <int R>
+__global__ void __launch_bounds__(64) backtransform_reg_kernel(int n, const cplx *__restrict__ A, int64_t lda,
+                                                                const cplx *__restrict__ tau,
+                                                                const double *__restrict__ Qt, int vlo, int nvec,
+                                                                cplx *Z, int64_t ldz) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int col = blockIdx.x * nwarp + warp;
+    if (col >= nvec) return;   // whole warp
+    const int rmax = (n + 31) >> 5;
+    cplx z[R];
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int r = lane + 32 * i;
+        z[i] = (i < rmax && r < n) ? mk(Qt[r + (int64_t)(vlo + col) * n], 0.0) : mk(0.0, 0.0);
+    }
+    for (int k = n - 2; k >= 0; k--) {
+        const cplx t = __ldg(tau + k);
+        if (t.x == 0.0 && t.y == 0.0) continue;
+        const cplx *v = A + (int64_t)k * lda;   // v(r) for r in [k+1, n), v(k+1) = 1
+        const int i0 = (k + 1) >> 5;
+        double s0r = 0.0, s0i = 0.0, s1r = 0.0, s1i = 0.0;
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            if (i < i0 || i >= rmax) continue;
+            const int r = lane + 32 * i;
+            const cplx vv = (r > k && r < n) ? __ldg(v + r) : mk(0.0, 0.0);
+            if (i & 1) {   // conj(v) z, two accumulator chains
+                s1r = fma(vv.x, z[i].x, s1r);
+                s1r = fma(vv.y, z[i].y, s1r);
+                s1i = fma(vv.x, z[i].y, s1i);
+                s1i = fma(-vv.y, z[i].x, s1i);
+            } else {
+                s0r = fma(vv.x, z[i].x, s0r);
+                s0r = fma(vv.y, z[i].y, s0r);
+                s0i = fma(vv.x, z[i].y, s0i);
+                s0i = fma(-vv.y, z[i].x, s0i);
+            }
+        }
+        double sr = s0r + s1r, si = s0i + s1i;
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_down_sync(0xffffffffu, sr, o);
+            si += __shfl_down_sync(0xffffffffu, si, o);
+        }
+        sr = __shfl_sync(0xffffffffu, sr, 0);
+        si = __shfl_sync(0xffffffffu, si, 0);
+        const double fr = t.x * sr - t.y * si, fi = t.x * si + t.y * sr;   // f = tau (v^H z)
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            if (i < i0 || i >= rmax) continue;
+            const int r = lane + 32 * i;
+            const cplx vv = (r > k && r < n) ? __ldg(v + r) : mk(0.0, 0.0);
+            z[i].x = fma(-vv.x, fr, z[i].x);   // z -= v f
+            z[i].x = fma(vv.y, fi, z[i].x);
+            z[i].y = fma(-vv.x, fi, z[i].y);
+            z[i].y = fma(-vv.y, fr, z[i].y);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int r = lane + 32 * i;
+        if (i < rmax && r < n) Z[r + (int64_t)col * ldz] = z[i];
+    }
+}
+
+template <int R>
+static void launch_bt_reg(Context &c, int n, const cplx *A, int64_t lda, const cplx *tau, const double *Qt, int vlo,
+                          int nvec, cplx *Z, int64_t ldz) {
+    backtransform_reg_kernel<R><<<grid1d(nvec, 2), 64, 0, c.stream>>>(n, A, lda, tau, Qt, vlo, nvec, Z, ldz);
+    DCG_LAUNCHED(c);
 }
 
 // ===================================================================== driver
@@ -918,8 +1188,51 @@ static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork
     if (hb.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
 }
 
+// Returns false (nothing launched) when the matrix does not fit the blocks' shared memory.
+static bool tridiag_smem(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
+    const int sms = std::max(1, c.num_sms);
+    int optin = 0;
+    DCG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
+    const size_t limit = (size_t)std::max(0, optin - 1024);   // static shared memory of the kernel
+    // Block count: the FP64 work (about 4 n^3 FMAs; a GB300 SM retires ~2 FP64 FMAs per clock)
+    // spreads over the blocks while every grid barrier (2 per column) costs more with more
+    // blocks; take the cheapest count among those whose owned columns fit shared memory.
+    auto bytes_for = [&](int nbk) { return (size_t)(((n + nbk - 1) / nbk) + 2) * n * sizeof(cplx); };
+    int nblocks = 0;
+    double best = 1e300;
+    for (int nbk = 1; nbk <= std::min(sms, n); nbk++) {
+        if (bytes_for(nbk) > limit) continue;
+        const double fp64_s = 4.0 * (double)n * n * n / (nbk * 4.0e9);
+        const double bar_s = 2.0 * n * (3.0e-6 + 0.02e-6 * nbk);
+        if (fp64_s + bar_s < best) {
+            best = fp64_s + bar_s;
+            nblocks = nbk;
+        }
+    }
+    if (nblocks == 0) return false;
+    const size_t smem = bytes_for(nblocks);
+    DCG_CUDA(cudaFuncSetAttribute(tridiag_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    DCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_smem_kernel, TRD_THREADS, smem));
+    if (per_sm < 1 || nblocks > per_sm * sms) return false;
+    cplx *pbuf = wsget<cplx>(c, "trd.p", (size_t)n + 1);
+    double2 *part = wsget<double2>(c, "trd.part", (size_t)nblocks + 1);
+    GridBar *gb = wsget<GridBar>(c, "trd.bar", 1);
+    DCG_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBar), c.stream));
+    void *args[] = {&n, &A, &lda, &h.d, &h.e, &h.tau, &pbuf, &part, &gb};
+    DCG_CUDA(cudaLaunchCooperativeKernel((const void *)tridiag_smem_kernel, dim3(nblocks), dim3(TRD_THREADS), args,
+                                         smem, c.stream));
+    DCG_LAUNCHED(c);
+    GridBar hb;
+    DCG_CUDA(cudaMemcpyAsync(&hb, gb, sizeof(GridBar), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    if (hb.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
+    return true;
+}
+
 // Reduce A to tridiagonal form; d, e, tau in the named workspace, reflectors in A.
 static void tridiag(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
+    if (n <= kTridiagSmemMaxN && tridiag_smem(c, n, A, lda, h)) return;
     if (n <= kTridiagPersistentMaxN) {
         tridiag_persistent(c, n, A, lda, h);
         return;
@@ -952,18 +1265,20 @@ static void check_dc_status(Context &c) {
 
 void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
     if (n <= 0) return;
-    FamScope fs(c, DCG_FAM_EIG, (16.0 / 3.0) * (double)n * n * n);
     HeevWork h = heev_work(c, n);
     {
-        FamScope f1(c, DCG_FAM_EIG_TRI, (16.0 / 3.0) * (double)n * n * n);
-        tridiag(c, n, A, lda, h);
+        FamScope fs(c, DCG_FAM_EIG, (16.0 / 3.0) * (double)n * n * n);
+        {
+            FamScope f1(c, DCG_FAM_EIG_TRI, (16.0 / 3.0) * (double)n * n * n);
+            tridiag(c, n, A, lda, h);
+        }
+        {
+            FamScope f2(c, DCG_FAM_EIG_VAL, 4.0 / 3.0 * (double)n * n * n);
+            tridiag_dc(c, n, h.d, h.e, w);
+        }
+        check_dc_status(c);
     }
-    {
-        FamScope f2(c, DCG_FAM_EIG_VAL, 4.0 / 3.0 * (double)n * n * n);
-        tridiag_dc(c, n, h.d, h.e, w);
-    }
-    check_dc_status(c);
-    heev_vectors_only(c, n, A, lda, w, vlo, vhi, Z, ldz);
+    heev_vectors_only(c, n, A, lda, w, vlo, vhi, Z, ldz);   // own EIG / EIG_BACK scopes
 }
 
 // Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (its reflectors are
@@ -977,9 +1292,14 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
     HeevWork h = heev_work(c, n);
     FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nvec);
     FamScope f4(c, DCG_FAM_EIG_BACK, 8.0 * (double)n * n * nvec);
+    if (n <= 1024) {
+        if (n <= 256) launch_bt_reg<8>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        else if (n <= 512) launch_bt_reg<16>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        else launch_bt_reg<32>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        return;
+    }
     z_from_real_kernel<<<grid1d((int64_t)n * nvec, 256), 256, 0, c.stream>>>(n, c.eig_Q, vlo, nvec, Z, ldz);
     DCG_LAUNCHED(c);
-    if (n < 2) return;
     cplx *Vp = wsget<cplx>(c, "wy.V", (size_t)n * WY_NB);
     cplx *G = wsget<cplx>(c, "wy.G", WY_NB * WY_NB);
     cplx *T = wsget<cplx>(c, "wy.T", WY_NB * WY_NB);
@@ -988,6 +1308,8 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     const int nref = n - 1;
     const int npanel = (nref + WY_NB - 1) / WY_NB;
+    DCG_CUDA(cudaFuncSetAttribute(wy_tfactor_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  2 * WY_NB * WY_NB * (int)sizeof(cplx)));
     for (int p = npanel - 1; p >= 0; p--) {
         const int k0 = p * WY_NB;
         const int nbp = std::min(WY_NB, nref - k0);
@@ -995,7 +1317,7 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
         wy_extract_kernel<<<grid1d((int64_t)m0 * nbp, 256), 256, 0, c.stream>>>(n, k0, nbp, A, lda, Vp);
         DCG_LAUNCHED(c);
         zgemm(c, OP_C, OP_N, nbp, nbp, m0, one, Vp, m0, 0, Vp, m0, 0, zero, G, nbp, 0, 1);
-        wy_tfactor_kernel<<<1, WY_NB, 0, c.stream>>>(nbp, G, h.tau, k0, T);
+        wy_tfactor_kernel<<<1, WY_NB, 2 * WY_NB * WY_NB * sizeof(cplx), c.stream>>>(nbp, G, h.tau, k0, T);
         DCG_LAUNCHED(c);
         cplx *Zs = Z + (k0 + 1);
         zgemm(c, OP_C, OP_N, nbp, nvec, m0, one, Vp, m0, 0, Zs, ldz, 0, zero, W1, nbp, 0, 1);

@@ -511,8 +511,12 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     sa.accumulate = accumulate ? 1 : 0;
     sa.err = err;
     dim3 grid(nrb, nnb, batch);
-    sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(sa);
-    DCG_LAUNCHED(c);
+    {
+        // tensor work: 15 slice products, each a real GEMM of M x 2N x 2K
+        FamScope fs(c, DCG_FAM_SPLIT_MMA, 15.0 * 8.0 * (double)M * N * K * batch);
+        sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(sa);
+        DCG_LAUNCHED(c);
+    }
 }
 
 void split_reset(Context &c) {

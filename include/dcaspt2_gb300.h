@@ -177,6 +177,7 @@ int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int3
 #define DCG_FAM_EIG_VAL 7     /*   tridiagonal divide and conquer (values and vectors; 4/3 n^3)  */
 #define DCG_FAM_EIG_VEC 8     /*   reserved (no launches)                                          */
 #define DCG_FAM_EIG_BACK 9    /*   back-transformation (FLOPs 8 n^2 m)                            */
+#define DCG_FAM_SPLIT_MMA 10  /* tcgen05 split-precision GEMM kernel; work = BF16 tensor FLOPs      */
 
 /* Select the family timed during subsequent calls (DCG_FAM_NONE disables; resets stats). */
 int dcg_time_family(dcg_ctx *ctx, int32_t family);

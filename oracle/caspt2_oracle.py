@@ -71,14 +71,18 @@ class System:
     def nmoc(self) -> int:
         return self.ninact + self.nact
 
+    @functools.cached_property
+    def _space_lut(self) -> np.ndarray:
+        n = max(self.nmo, self.ninact + self.nact + self.nsec)
+        lut = np.full(n + 1, 4, dtype=np.int8)
+        lut[:self.ninact + self.nact + self.nsec] = 3
+        lut[:self.ninact + self.nact] = 2
+        lut[:self.ninact] = 1
+        return lut
+
     def space_of(self, g: np.ndarray) -> np.ndarray:
         """1 inactive, 2 active, 3 secondary, 4 beyond (read_mrconee.F90:311-315)."""
-        g = np.asarray(g)
-        s = np.full(g.shape, 4, dtype=np.int64)
-        s[g < self.ninact + self.nact + self.nsec] = 3
-        s[g < self.ninact + self.nact] = 2
-        s[g < self.ninact] = 1
-        return s
+        return self._space_lut[np.asarray(g)]
 
     # multiplication tables (read_mrconee.F90:368-453)
     @functools.cached_property
@@ -180,12 +184,12 @@ class Integrals:
             P, V = expand_partners(sysm.rec_idx[c0:c0 + chunk], sysm.rec_val[c0:c0 + chunk])
             P = P.reshape(-1, 4)
             V = V.reshape(-1)
-            m = np.all(P < nmoc, axis=1)
+            sp = sysm.space_of(P).astype(np.int16)
+            code = sp[:, 0] * 1000 + sp[:, 1] * 100 + sp[:, 2] * 10 + sp[:, 3]
+            m = (sp <= 2).all(axis=1)              # every index inactive or active
             if np.any(m):
                 q = P[m]
                 self._occ[q[:, 0], q[:, 1], q[:, 2], q[:, 3]] = V[m]
-            sp = sysm.space_of(P)
-            code = sp[:, 0] * 1000 + sp[:, 1] * 100 + sp[:, 2] * 10 + sp[:, 3]
             for cd, pat in codes.items():
                 mm = code == cd
                 if not np.any(mm):
@@ -396,8 +400,8 @@ class FullSpace:
         """y = E_pq x (x may carry trailing columns)."""
         src, dst, sg = self.ops[(p, q)]
         y = np.zeros_like(x)
-        if len(src):
-            np.add.at(y, dst, x[src] * sg.reshape((-1,) + (1,) * (x.ndim - 1)))
+        if len(src):   # E_pq maps determinants one to one: a plain scatter
+            y[dst] = x[src] * sg.reshape((-1,) + (1,) * (x.ndim - 1))
         return y
 
     def project(self, x: np.ndarray) -> np.ndarray:
@@ -568,13 +572,15 @@ def fock_diag(s: System, f: np.ndarray):
 def ci_rotate(s: System, dets: List[int], U_act: np.ndarray, c: np.ndarray) -> np.ndarray:
     """tracic (trac.F90:76-156) with detsc (sdet.F90:58-110): ds(k,k~) = det(U[occ_k, occ_k~]),
     then solve ds c' = c (ZGESV)."""
-    occ = [[t for t in range(s.nact) if (I >> t) & 1] for I in dets]
     nd = len(dets)
+    if s.nelec == 0:
+        return np.linalg.solve(np.ones((nd, nd), dtype=np.complex128), c)
+    occ = np.array([[t for t in range(s.nact) if (I >> t) & 1] for I in dets], dtype=np.int64)   # (nd, ne)
     ds = np.zeros((nd, nd), dtype=np.complex128)
     for a in range(nd):
-        oa = occ[a]
-        for b in range(nd):
-            ds[a, b] = np.linalg.det(U_act[np.ix_(oa, occ[b])]) if s.nelec else 1.0
+        # U[occ_a, occ_b] for every b at once: (nd, ne, ne)
+        sub = U_act[occ[a][None, :, None], occ[:, None, :]]
+        ds[a] = np.linalg.det(sub)
     return np.linalg.solve(ds, c)
 
 
