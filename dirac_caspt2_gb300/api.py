@@ -94,6 +94,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]
     lib.dcg_stedc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p]
+    lib.dcg_heev_range.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_heev.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p, ctypes.c_void_p]
     _lib = lib
@@ -103,7 +105,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
-                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_stedc", "dcg_zgemm"]
+                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_stedc", "dcg_zgemm"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
@@ -359,6 +361,19 @@ class Caspt2Session:
         """Complex GEMM on device buffers (dcg_zgemm); strides in complex elements."""
         self._check(self.lib.dcg_zgemm(self.h, precision, M, N, K, batch, A_ptr, a_si, a_sk, a_sb, B_ptr, ldb,
                                        int(conj_b), C_ptr, c_si, c_sj, c_sb, int(accumulate)))
+
+    def heev_range(self, a: np.ndarray, vlo: int):
+        """Eigenvalues (all) and the eigenvectors of eigenvalues vlo..n-1 (dcg_heev_range)."""
+        a = np.asarray(a)
+        n = a.shape[0]
+        are = np.asfortranarray(a.real, dtype=np.float64)
+        aim = np.asfortranarray(a.imag, dtype=np.float64) if np.iscomplexobj(a) else None
+        w = np.zeros(n)
+        zr = np.zeros((n, n - vlo), order="F")
+        zi = np.zeros((n, n - vlo), order="F")
+        self._check(self.lib.dcg_heev_range(self.h, n, are.ctypes.data, None if aim is None else aim.ctypes.data,
+                                            w.ctypes.data, vlo, zr.ctypes.data, zi.ctypes.data))
+        return w, zr + 1j * zi
 
     def stedc(self, d: np.ndarray, e: np.ndarray, vectors: bool = True):
         """Symmetric tridiagonal eigendecomposition on the device (dcg_stedc)."""

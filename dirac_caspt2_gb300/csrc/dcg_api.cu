@@ -285,9 +285,10 @@ static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double
 // (i'j'|k'l') = sum conj(U_ii') U_jj' conj(U_kk') U_ll' (ij|kl)   (module_intra.F90:130-277),
 // index l first, then k, j, i, as four GEMMs.
 // Quarters whose contracted orbital dimension exceeds this run on the split-precision tensor
-// cores when the context asks for DCG_PREC_SPLIT; smaller ones are memory-bound and stay on
-// the exact FP64 small-dimension kernels.
-constexpr int kSplitMinK = 32;
+// cores when the context asks for DCG_PREC_SPLIT.  Even a quarter over 12 or 20 orbitals is
+// FP64-bound on a GB300 (8 M K^2 flops at ~1.2 TF/s against one pass over the class), so
+// only trivial dimensions stay on the FP64 kernels.
+constexpr int kSplitMinK = 4;
 
 static void transform4(Context &c, const cplx *in, cplx *out, cplx *tmp, const int dm[4], const cplx *U[4]) {
     const int64_t d0 = dm[0], d1 = dm[1], d2 = dm[2], d3 = dm[3];
@@ -466,6 +467,9 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
                                  int nouter, const double *alpha) {
     BlockOut r;
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    // K is the overlap metric itself: its small eigenvalues (down to the 1e-8 cutoff) set X through
+    // Lambda^-1, and a 2^-36-relative error in K moves their eigenvectors by |dK| / gap.  On the
+    // 20/12/300 system the split product shifted e2c by 1.2e-9 Eh, so K stays in FP64.
     cplx *K = wsget<cplx>(c, "gram.K", (size_t)Mp * Mp);
     zgemm(c, OP_N, OP_C, Mp, Mp, dimn, one, G, Mp, 0, G, Mp, 0, zero, K, Mp, 0, 1);
     herm_from_upper(c, Mp, K, Mp);
@@ -689,11 +693,25 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         DCG_CUDA(cudaMemcpy2DAsync(Uact, na * sizeof(cplx), U + ni + (size_t)c.nmo * ni, c.nmo * sizeof(cplx),
                                    na * sizeof(cplx), na, cudaMemcpyDeviceToDevice, c.stream));
     cplx *ds = wsget<cplx>(c, "pt.ds", (size_t)d.ndet * d.ndet);
-    launch_detsc(c, d.dets, d.ndet, Uact, ds);
     cplx *c1 = wsget<cplx>(c, "pt.c1", d.ndet);
-    DCG_CUDA(cudaMemcpyAsync(c1, d.c0, sizeof(cplx) * d.ndet, cudaMemcpyDeviceToDevice, c.stream));
-    const int info = zgesv(c, d.ndet, ds, d.ndet, c1);
-    if (info != 0) throw Error{info, "CI rotation: singular determinant-overlap matrix (ZGESV info " + std::to_string(info) + ")"};
+    if ((int64_t)d.ndet == M && na > 0) {
+        // Full determinant space: ds(U)(k, l) = det U[occ_k, occ_l] is the ne-th exterior power
+        // of the unitary U, and exterior powers multiply (Cauchy-Binet), so ds(U)^-1 = ds(U^H):
+        // c1 = ds(U^H) c0 solves the reference's ZGESV system without a factorisation.
+        std::vector<cplx> uh = download(c, Uact, (size_t)na * na), uht((size_t)na * na);
+        for (int i = 0; i < na; i++)
+            for (int j = 0; j < na; j++) uht[j + (size_t)na * i] = cconj(uh[i + (size_t)na * j]);
+        cplx *UactH = upload(c, "pt.UactH", uht);
+        launch_detsc(c, d.dets, d.ndet, UactH, ds);
+        zgemm(c, OP_N, OP_N, d.ndet, 1, d.ndet, one, ds, d.ndet, 0, d.c0, d.ndet, 0, zero, c1, d.ndet, 0, 1);
+    } else {
+        // restricted (RAS or symmetry) determinant list: the reference's linear solve
+        launch_detsc(c, d.dets, d.ndet, Uact, ds);
+        DCG_CUDA(cudaMemcpyAsync(c1, d.c0, sizeof(cplx) * d.ndet, cudaMemcpyDeviceToDevice, c.stream));
+        const int info = zgesv(c, d.ndet, ds, d.ndet, c1);
+        if (info != 0)
+            throw Error{info, "CI rotation: singular determinant-overlap matrix (ZGESV info " + std::to_string(info) + ")"};
+    }
     stage_end(c, ST_CIROT);
 
     // ---- densities of the rotated state and e0 (calce0.F90:4-50)
@@ -844,7 +862,13 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         cplx *P3 = wsget<cplx>(c, "v.P3", (size_t)n3 * n3 + 1);
         cplx *P2 = wsget<cplx>(c, "v.P2", (size_t)na * n3 + 1);
         launch_perm_C2(c, sc.rv, P3, P2);
-        zgemm(c, OP_N, OP_N, ns, (int)n3, (int)n3, one, C1, ns, 0, P3, n3, 0, zero, V, ns, 0, 1);
+        // V = C1 P3 + effh P2: its errors stay relative through X^H V, so the large product may
+        // run on the split-precision tensor cores
+        if (c.precision == DCG_PREC_SPLIT)
+            zgemm_split(c, ns, (int)n3, (int)n3, 1, C1, 1, ns, 0, P3, n3, 0, V, 1, ns, 0, false, c.split_lbo,
+                        c.split_sbo);
+        else
+            zgemm(c, OP_N, OP_N, ns, (int)n3, (int)n3, one, C1, ns, 0, P3, n3, 0, zero, V, ns, 0, 1);
         zgemm(c, OP_N, OP_N, ns, (int)n3, na, one, effC, ns, 0, P2, na, 0, one, V, ns, 0, 1);
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
@@ -938,7 +962,11 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         cplx *V = wsget<cplx>(c, "v.F", (size_t)ns2 * na2 + 1);
         launch_F_pack(c, Fc, ns, na, Fp);
         launch_perm_F(c, sc.rv, P2, nullptr);
-        zgemm(c, OP_N, OP_N, (int)ns2, (int)na2, (int)na2, one, Fp, ns2, 0, P2, na2, 0, zero, V, ns2, 0, 1);
+        if (c.precision == DCG_PREC_SPLIT)
+            zgemm_split(c, (int)ns2, (int)na2, (int)na2, 1, Fp, 1, ns2, 0, P2, na2, 0, V, 1, ns2, 0, false,
+                        c.split_lbo, c.split_sbo);
+        else
+            zgemm(c, OP_N, OP_N, (int)ns2, (int)na2, (int)na2, one, Fp, ns2, 0, P2, na2, 0, zero, V, ns2, 0, 1);
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
@@ -1178,6 +1206,34 @@ int dcg_stedc(dcg_ctx *ctx, int32_t n, const double *d, const double *e, double 
         if (z_out)
             DCG_CUDA(cudaMemcpyAsync(z_out, Q, (size_t)n * n * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
         DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        return DCG_OK;
+    });
+}
+
+int dcg_heev_range(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, double *w_out, int32_t vlo,
+                   double *z_re, double *z_im) {
+    if (n < 0 || vlo < 0 || vlo > n || (n > 0 && (!a_re || !w_out))) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        if (n == 0) return DCG_OK;
+        const size_t nn = (size_t)n * n;
+        const size_t nv = (size_t)n * (n - vlo);
+        std::vector<dcg::cplx> h(nn);
+        for (size_t x = 0; x < nn; x++) h[x] = dcg::mk(a_re[x], a_im ? a_im[x] : 0.0);
+        dcg::cplx *A = dcg::wsget<dcg::cplx>(c_, "abi.heev.A", nn);
+        dcg::cplx *Z = dcg::wsget<dcg::cplx>(c_, "abi.heev.Z", nv + 1);
+        double *w = dcg::wsget<double>(c_, "abi.heev.w", n);
+        DCG_CUDA(cudaMemcpyAsync(A, h.data(), nn * sizeof(dcg::cplx), cudaMemcpyHostToDevice, c_.stream));
+        dcg::herm_from_upper(c_, n, A, n);
+        dcg::heev(c_, n, A, n, w, vlo, z_re ? n : vlo, z_re ? Z : nullptr, n);
+        DCG_CUDA(cudaMemcpyAsync(w_out, w, n * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+        std::vector<dcg::cplx> zh(nv + 1);
+        if (z_re && nv) DCG_CUDA(cudaMemcpyAsync(zh.data(), Z, nv * sizeof(dcg::cplx), cudaMemcpyDeviceToHost, c_.stream));
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        if (z_re)
+            for (size_t x = 0; x < nv; x++) {
+                z_re[x] = zh[x].x;
+                if (z_im) z_im[x] = zh[x].y;
+            }
         return DCG_OK;
     });
 }

@@ -1072,79 +1072,122 @@ __global__ void wy_tfactor_kernel(int nbp, const cplx *__restrict__ G, const cpl
     for (int x = j; x < WY_NB * WY_NB; x += blockDim.x) T[x] = Ts[x];
 }
 
-// Register-resident back-transformation (n <= 32 R): one warp per eigenvector column, the
-// column held in registers (lane owns rows lane + 32 i), the reflectors applied from the last
-// to the first and read straight from L1/L2 (they are read-only here and shared by every warp
-// of an SM).  Columns are independent: no block or grid synchronisation, and the FP64 work,
-// written as explicit FMAs (8 per row and reflector), spreads over every SM.
-template <int R>
+// Register-resident back-transformation (n <= 32 R WPC): WPC warps per eigenvector column,
+// the column held in registers (warp w, lane l owns rows l + 32 (WPC i + w)), the reflectors
+// applied from the last to the first.  Reflector k-1 is loaded into registers while reflector
+// k is applied, so the per-reflector chain is FMAs and shuffles only; this matters most for a
+// single column (a CASCI root: n-1 strictly sequential reflections).  With two warps per
+// column their partial dot products meet in double-buffered shared memory, summed in a fixed
+// order.  Columns are independent, and the FP64 work (8 FMAs per row and reflector) spreads
+// over every SM.
+template <int R, int WPC, bool PF>
 __global__ void __launch_bounds__(64) backtransform_reg_kernel(int n, const cplx *__restrict__ A, int64_t lda,
                                                                 const cplx *__restrict__ tau,
                                                                 const double *__restrict__ Qt, int vlo, int nvec,
                                                                 cplx *Z, int64_t ldz) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const int col = blockIdx.x * nwarp + warp;
-    if (col >= nvec) return;   // whole warp
-    const int rmax = (n + 31) >> 5;
-    cplx z[R];
+    __shared__ double part[2][2][2];   // [parity][warp][re, im]
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int wsub = warp % WPC;                               // warp within its column
+    const int col = blockIdx.x * (2 / WPC) + warp / WPC;       // 64 threads: 2 / WPC columns
+    const bool have = col < nvec;
+    cplx z[R], vc[PF ? R : 1], vn[PF ? R : 1];
 #pragma unroll
     for (int i = 0; i < R; i++) {
-        const int r = lane + 32 * i;
-        z[i] = (i < rmax && r < n) ? mk(Qt[r + (int64_t)(vlo + col) * n], 0.0) : mk(0.0, 0.0);
+        const int r = lane + 32 * (WPC * i + wsub);
+        z[i] = (have && r < n) ? mk(Qt[r + (int64_t)(vlo + col) * n], 0.0) : mk(0.0, 0.0);
     }
+#define BT_LOAD(kk, dst)                                                                     \
+    {                                                                                        \
+        const cplx *v_ = A + (int64_t)(kk) * lda;                                            \
+        _Pragma("unroll") for (int i = 0; i < R; i++) {                                      \
+            const int r = lane + 32 * (WPC * i + wsub);                                      \
+            dst[i] = (have && r > (kk) && r < n) ? __ldg(v_ + r) : mk(0.0, 0.0);             \
+        }                                                                                    \
+    }
+    if (PF && n >= 2) BT_LOAD(n - 2, vc);
     for (int k = n - 2; k >= 0; k--) {
+        if (PF && k >= 1) BT_LOAD(k - 1, vn);
         const cplx t = __ldg(tau + k);
-        if (t.x == 0.0 && t.y == 0.0) continue;
-        const cplx *v = A + (int64_t)k * lda;   // v(r) for r in [k+1, n), v(k+1) = 1
-        const int i0 = (k + 1) >> 5;
-        double s0r = 0.0, s0i = 0.0, s1r = 0.0, s1i = 0.0;
+        if (t.x != 0.0 || t.y != 0.0) {   // uniform over the block
+            const int i0 = (k + 1) / (32 * WPC);   // row chunks below k+1 hold v = 0 in every lane
+            double s0r = 0.0, s0i = 0.0, s1r = 0.0, s1i = 0.0;
+            const cplx *vk = A + (int64_t)k * lda;
 #pragma unroll
-        for (int i = 0; i < R; i++) {
-            if (i < i0 || i >= rmax) continue;
-            const int r = lane + 32 * i;
-            const cplx vv = (r > k && r < n) ? __ldg(v + r) : mk(0.0, 0.0);
-            if (i & 1) {   // conj(v) z, two accumulator chains
-                s1r = fma(vv.x, z[i].x, s1r);
-                s1r = fma(vv.y, z[i].y, s1r);
-                s1i = fma(vv.x, z[i].y, s1i);
-                s1i = fma(-vv.y, z[i].x, s1i);
+            for (int i = 0; i < R; i++) {
+                if (i < i0) continue;
+                cplx vv;
+                if (PF) {
+                    vv = vc[i];
+                } else {   // read from L1/L2 (shared by the SM's warps) instead of holding it
+                    const int r = lane + 32 * (WPC * i + wsub);
+                    vv = (have && r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
+                }
+                if (i & 1) {   // conj(v) z, two accumulator chains
+                    s1r = fma(vv.x, z[i].x, s1r);
+                    s1r = fma(vv.y, z[i].y, s1r);
+                    s1i = fma(vv.x, z[i].y, s1i);
+                    s1i = fma(-vv.y, z[i].x, s1i);
+                } else {
+                    s0r = fma(vv.x, z[i].x, s0r);
+                    s0r = fma(vv.y, z[i].y, s0r);
+                    s0i = fma(vv.x, z[i].y, s0i);
+                    s0i = fma(-vv.y, z[i].x, s0i);
+                }
+            }
+            double sr = s0r + s1r, si = s0i + s1i;
+            for (int o = 16; o > 0; o >>= 1) {
+                sr += __shfl_down_sync(0xffffffffu, sr, o);
+                si += __shfl_down_sync(0xffffffffu, si, o);
+            }
+            if (WPC == 2) {
+                if (lane == 0) {
+                    part[k & 1][wsub][0] = sr;
+                    part[k & 1][wsub][1] = si;
+                }
+                __syncthreads();
+                sr = part[k & 1][0][0] + part[k & 1][1][0];
+                si = part[k & 1][0][1] + part[k & 1][1][1];
             } else {
-                s0r = fma(vv.x, z[i].x, s0r);
-                s0r = fma(vv.y, z[i].y, s0r);
-                s0i = fma(vv.x, z[i].y, s0i);
-                s0i = fma(-vv.y, z[i].x, s0i);
+                sr = __shfl_sync(0xffffffffu, sr, 0);
+                si = __shfl_sync(0xffffffffu, si, 0);
+            }
+            const double fr = t.x * sr - t.y * si, fi = t.x * si + t.y * sr;   // f = tau (v^H z)
+#pragma unroll
+            for (int i = 0; i < R; i++) {
+                if (i < i0) continue;
+                cplx vv;
+                if (PF) {
+                    vv = vc[i];
+                } else {
+                    const int r = lane + 32 * (WPC * i + wsub);
+                    vv = (have && r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
+                }
+                z[i].x = fma(-vv.x, fr, z[i].x);   // z -= v f
+                z[i].x = fma(vv.y, fi, z[i].x);
+                z[i].y = fma(-vv.x, fi, z[i].y);
+                z[i].y = fma(-vv.y, fr, z[i].y);
             }
         }
-        double sr = s0r + s1r, si = s0i + s1i;
-        for (int o = 16; o > 0; o >>= 1) {
-            sr += __shfl_down_sync(0xffffffffu, sr, o);
-            si += __shfl_down_sync(0xffffffffu, si, o);
-        }
-        sr = __shfl_sync(0xffffffffu, sr, 0);
-        si = __shfl_sync(0xffffffffu, si, 0);
-        const double fr = t.x * sr - t.y * si, fi = t.x * si + t.y * sr;   // f = tau (v^H z)
+        if (PF) {
 #pragma unroll
-        for (int i = 0; i < R; i++) {
-            if (i < i0 || i >= rmax) continue;
-            const int r = lane + 32 * i;
-            const cplx vv = (r > k && r < n) ? __ldg(v + r) : mk(0.0, 0.0);
-            z[i].x = fma(-vv.x, fr, z[i].x);   // z -= v f
-            z[i].x = fma(vv.y, fi, z[i].x);
-            z[i].y = fma(-vv.x, fi, z[i].y);
-            z[i].y = fma(-vv.y, fr, z[i].y);
+            for (int i = 0; i < R; i++) vc[i] = vn[i];
         }
     }
+#undef BT_LOAD
+    if (have) {
 #pragma unroll
-    for (int i = 0; i < R; i++) {
-        const int r = lane + 32 * i;
-        if (i < rmax && r < n) Z[r + (int64_t)col * ldz] = z[i];
+        for (int i = 0; i < R; i++) {
+            const int r = lane + 32 * (WPC * i + wsub);
+            if (r < n) Z[r + (int64_t)col * ldz] = z[i];
+        }
     }
 }
 
-template <int R>
+template <int R, int WPC, bool PF>
 static void launch_bt_reg(Context &c, int n, const cplx *A, int64_t lda, const cplx *tau, const double *Qt, int vlo,
                           int nvec, cplx *Z, int64_t ldz) {
-    backtransform_reg_kernel<R><<<grid1d(nvec, 2), 64, 0, c.stream>>>(n, A, lda, tau, Qt, vlo, nvec, Z, ldz);
+    backtransform_reg_kernel<R, WPC, PF><<<grid1d(nvec, 2 / WPC), 64, 0, c.stream>>>(n, A, lda, tau, Qt, vlo, nvec,
+                                                                                       Z, ldz);
     DCG_LAUNCHED(c);
 }
 
@@ -1292,10 +1335,21 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
     HeevWork h = heev_work(c, n);
     FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nvec);
     FamScope f4(c, DCG_FAM_EIG_BACK, 8.0 * (double)n * n * nvec);
+    // Many columns: the FP64 pipe is the limit, one warp per column without prefetch (fewest
+    // registers).  Few columns: the n-1 sequential reflections are the limit, prefetch the next
+    // reflector (two warps per column above 512 rows to keep it in registers).
     if (n <= 1024) {
-        if (n <= 256) launch_bt_reg<8>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
-        else if (n <= 512) launch_bt_reg<16>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
-        else launch_bt_reg<32>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        const bool many = nvec >= 64;
+        if (n <= 256) {
+            if (many) launch_bt_reg<8, 1, false>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+            else launch_bt_reg<8, 1, true>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        } else if (n <= 512) {
+            if (many) launch_bt_reg<16, 1, false>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+            else launch_bt_reg<16, 1, true>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        } else {
+            if (many) launch_bt_reg<32, 1, false>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+            else launch_bt_reg<16, 2, true>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+        }
         return;
     }
     z_from_real_kernel<<<grid1d((int64_t)n * nvec, 256), 256, 0, c.stream>>>(n, c.eig_Q, vlo, nvec, Z, ldz);

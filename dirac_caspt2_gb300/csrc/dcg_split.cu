@@ -165,14 +165,15 @@ __global__ void sp_slice_a_kernel(int M, int K, const cplx *__restrict__ A, int6
 }
 
 // B' slices (N'-major tiles: tile (q, nb, ks) at (q*nnb + nb)*nks + ks) and column exponents.
-// op(B)(k, j): opb 0 = B[k + j ldb], 1 = conj(B[k + j ldb]).  One block per complex column j.
+// op(B)(k, j) = B[k + j ldb], or B[j + k ldb] when opb & 2 (B stored transposed), conjugated
+// when opb & 1.  One block per complex column j.
 __global__ void sp_slice_b_kernel(int K, int N, const cplx *__restrict__ B, int64_t ldb, int opb, int nnb, int nks,
                                   __nv_bfloat16 *Bs, int *fexp) {
     __shared__ long long red[32];
     const int j = blockIdx.x;
     long long mb = 0;
     for (int k = threadIdx.x; k < K; k += blockDim.x) {
-        const cplx v = B[k + (int64_t)j * ldb];
+        const cplx v = (opb & 2) ? B[j + (int64_t)k * ldb] : B[k + (int64_t)j * ldb];
         mb = max(mb, max(sp_absbits(v.x), sp_absbits(v.y)));
     }
     for (int o = 16; o > 0; o >>= 1) mb = max(mb, __shfl_down_sync(0xffffffffu, mb, o));
@@ -191,8 +192,8 @@ __global__ void sp_slice_b_kernel(int K, int N, const cplx *__restrict__ B, int6
         const int k = kr >> 1, part = kr & 1;   // real row 2k (Re) or 2k+1 (Im) of B'
         cplx v = mk(0.0, 0.0);
         if (k < K) {
-            v = B[k + (int64_t)j * ldb];
-            if (opb == 1) v = cconj(v);
+            v = (opb & 2) ? B[j + (int64_t)k * ldb] : B[k + (int64_t)j * ldb];
+            if (opb & 1) v = cconj(v);
         }
         // column 2j: (Re, -Im) down the real rows; column 2j+1: (Im, Re)
         const double c0 = part == 0 ? v.x : -v.y;
@@ -436,7 +437,8 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
 // ------------------------------------------------------------------------- host driver
 // C = A * op(B) (+ C when accumulate), complex FP64 in and out, through the split path.
 // Large operand: element (i, k) of batch z at A[z*a_sb + i*a_si + k*a_sk], i < M, k < K.
-// Small operand: op(B)(k, j) = B[k + j ldb] (opb 0) or its conjugate (opb 1), j < N.
+// Small operand: op(B)(k, j) = B[k + j ldb], or B[j + k ldb] when opb & 2; conjugated when
+// opb & 1; j < N.
 // Output: C[z*c_sb + i*c_si + j*c_sj].
 void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int64_t a_si, int64_t a_sk, int64_t a_sb,
                  const cplx *B, int64_t ldb, int opb, cplx *C, int64_t c_si, int64_t c_sj, int64_t c_sb,
@@ -452,7 +454,8 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     if (K > kmax) {   // exact FP32 groups need K' <= SP_KMAX: chain K chunks through C
         for (int k0 = 0; k0 < K; k0 += kmax) {
             const int kc = std::min(kmax, K - k0);
-            zgemm_split(c, M, N, kc, batch, A + k0 * a_sk, a_si, a_sk, a_sb, B + k0, ldb, opb, C, c_si, c_sj, c_sb,
+            zgemm_split(c, M, N, kc, batch, A + k0 * a_sk, a_si, a_sk, a_sb, (opb & 2) ? B + k0 * ldb : B + k0, ldb, opb,
+                        C, c_si, c_sj, c_sb,
                         accumulate || k0 > 0, lbo, sbo);
         }
         return;

@@ -149,6 +149,11 @@ void *dcg_stream(const dcg_ctx *ctx);
  * real symmetric matrix) is read, as ZHEEV with uplo='U' reads it. */
 int dcg_heev(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, double *w_out, double *z_re,
              double *z_im);
+/* dcg_heev returning only the eigenvectors of eigenvalues vlo..n-1 (ascending), as the
+ * columns of z_re/z_im (n x (n - vlo)): the S-matrix use, which keeps the eigenvectors above
+ * the linear-dependence cutoff, and the CASCI use, which keeps the lowest roots. */
+int dcg_heev_range(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, double *w_out, int32_t vlo,
+                   double *z_re, double *z_im);
 
 /* Symmetric tridiagonal eigendecomposition (the divide-and-conquer stage of dcg_heev; the
  * role of LAPACK's DSTEDC): diagonal d[n], off-diagonal e[n-1] (host arrays), ascending

@@ -100,3 +100,19 @@ def test_stedc_matches_lapack(session, n):
     assert np.abs(w - wr).max() <= TOL * scale
     assert np.abs(t @ q - q * w).max() <= TOL * scale
     assert np.abs(q.T @ q - np.eye(n)).max() <= TOL
+
+
+@pytest.mark.parametrize("n,nvec", [(100, 3), (300, 5), (700, 1), (700, 10), (900, 70)])
+def test_heev_range_few_vectors(session, n, nvec):
+    """Eigenvectors of the top nvec eigenvalues only: the few-column back-transformation (a
+    CASCI root) and the many-column one, on both sides of 512 rows."""
+    rng = np.random.default_rng(n + nvec)
+    a = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    a = a + a.conj().T
+    w, z = session.heev_range(a, n - nvec)
+    wr = np.linalg.eigvalsh(a)
+    scale = max(1.0, np.abs(wr).max())
+    assert np.abs(w - wr).max() <= TOL * scale
+    ws = w[n - nvec:]
+    assert np.abs(a @ z - z * ws).max() <= TOL * scale
+    assert np.abs(z.conj().T @ z - np.eye(nvec)).max() <= TOL
