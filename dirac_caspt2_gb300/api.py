@@ -28,7 +28,7 @@ DCG_PREC_FP64 = 0
 DCG_PREC_SPLIT = 1
 SUBSPACES = "ABCDEFGH"
 STAGES = ["ints", "casci_matrix", "casci_eig", "fock", "ci_rotation", "rdm", "transformation",
-          "A", "B", "C", "D", "E", "F", "G", "H"]
+          "A", "B", "C", "D", "E", "F", "G", "H", "AC"]
 
 
 class DcgError(RuntimeError):
@@ -94,6 +94,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                               ctypes.c_int64, ctypes.c_int64, ctypes.c_int32]
     lib.dcg_stedc.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                               ctypes.c_void_p]
+    lib.dcg_heev_batch.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_heev_range.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_heev.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -105,7 +107,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
-                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_stedc", "dcg_zgemm"]
+                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
@@ -361,6 +363,25 @@ class Caspt2Session:
         """Complex GEMM on device buffers (dcg_zgemm); strides in complex elements."""
         self._check(self.lib.dcg_zgemm(self.h, precision, M, N, K, batch, A_ptr, a_si, a_sk, a_sb, B_ptr, ldb,
                                        int(conj_b), C_ptr, c_si, c_sj, c_sb, int(accumulate)))
+
+    def heev_batch(self, mats):
+        """Batched Hermitian eigendecompositions (dcg_heev_batch): list of (w, Z)."""
+        k = len(mats)
+        n = (ctypes.c_int32 * k)(*[m.shape[0] for m in mats])
+        keep = []
+        def arr(x):
+            keep.append(x)
+            return x.ctypes.data
+        re = (ctypes.c_void_p * k)(*[arr(np.asfortranarray(m.real, dtype=np.float64)) for m in mats])
+        im = (ctypes.c_void_p * k)(*[arr(np.asfortranarray(m.imag, dtype=np.float64)) for m in mats])
+        ws = [np.zeros(m.shape[0]) for m in mats]
+        zr = [np.zeros(m.shape, order="F") for m in mats]
+        zi = [np.zeros(m.shape, order="F") for m in mats]
+        wp = (ctypes.c_void_p * k)(*[w.ctypes.data for w in ws])
+        zrp = (ctypes.c_void_p * k)(*[z.ctypes.data for z in zr])
+        zip_ = (ctypes.c_void_p * k)(*[z.ctypes.data for z in zi])
+        self._check(self.lib.dcg_heev_batch(self.h, k, n, re, im, wp, zrp, zip_))
+        return [(w, a + 1j * b) for w, a, b in zip(ws, zr, zi)]
 
     def heev_range(self, a: np.ndarray, vlo: int):
         """Eigenvalues (all) and the eigenvectors of eigenvalues vlo..n-1 (dcg_heev_range)."""

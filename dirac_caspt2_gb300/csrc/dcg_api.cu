@@ -108,7 +108,8 @@ static std::vector<T> download(Context &c, const T *p, size_t n) {
 
 // Stage names double as NVTX range names, so a profiler can select one stage's launches.
 static const char *const kStageName[ST_COUNT] = {"ints", "casci_matrix", "casci_eig", "fock", "ci_rotation",
-                                                 "rdm", "transformation", "A", "B", "C", "D", "E", "F", "G", "H"};
+                                                 "rdm", "transformation", "A", "B", "C", "D", "E", "F", "G", "H",
+                                                 "AC"};
 static void stage_begin(Context &c, int st) {
     nvtxRangePushA(kStageName[st]);
     DCG_CUDA(cudaEventRecord(c.ev[st], c.stream));
@@ -445,6 +446,8 @@ struct SubCtx {
     double e0;
     const cplx *Y = nullptr;   // E_pq psi over the full nelec-electron space (M x na^2)
     int64_t M = 0;
+    struct GramJob *defer = nullptr;   // when set, Gram-route blocks are queued here (see GramJob)
+    std::vector<struct GramJob> *jobs = nullptr;
 };
 
 struct BlockSpec {
@@ -471,7 +474,7 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     // Lambda^-1, and a 2^-36-relative error in K moves their eigenvectors by |dK| / gap.  On the
     // 20/12/300 system the split product shifted e2c by 1.2e-9 Eh, so K stays in FP64.
     cplx *K = wsget<cplx>(c, "gram.K", (size_t)Mp * Mp);
-    zgemm(c, OP_N, OP_C, Mp, Mp, dimn, one, G, Mp, 0, G, Mp, 0, zero, K, Mp, 0, 1);
+    zherk_upper(c, Mp, dimn, G, Mp, K, Mp);
     herm_from_upper(c, Mp, K, Mp);
     double *wk = wsget<double>(c, "gram.wk", Mp);
     heev(c, Mp, K, Mp, wk, Mp, Mp, nullptr, Mp);   // values first (cutoff count)
@@ -514,6 +517,108 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     return r;
 }
 
+// A Gram-route block (subspace A or C) queued for the joint solve: the blocks of A and C are
+// independent, so their K and B' eigenproblems are reduced together in batched launches.
+struct GramJob {
+    int Mp = 0, dimn = 0, nouter = 0;
+    cplx *G = nullptr, *Vsel = nullptr;
+    const double *Dd = nullptr;
+    double *alpha = nullptr;
+    int sub = 0;   // index into e2_sub / sc2_sub (0 = A, 2 = C)
+};
+
+// Solve queued Gram blocks (same algebra as solve_gram_block), at most 16 per pass so that the
+// K and B' matrices of a pass take distinct eigensolver slots.
+static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub[8], double sc2_sub[8]) {
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    for (size_t p0 = 0; p0 < all.size(); p0 += 16) {
+        const size_t np = std::min<size_t>(16, all.size() - p0);
+        auto nm = [](const char *b, size_t j) { return std::string(b) + "#" + std::to_string(j); };
+        std::vector<cplx *> K(np), P(np, nullptr), VC0(np, nullptr), Bp(np, nullptr);
+        std::vector<double *> wk(np), wb(np, nullptr), red(np);
+        std::vector<int> vlo(np, 0), dimm(np, 0);
+        std::vector<EigJob> ek;
+        for (size_t j = 0; j < np; j++) {
+            GramJob &g = all[p0 + j];
+            K[j] = wsget<cplx>(c, nm("gj.K", j), (size_t)g.Mp * g.Mp);
+            zherk_upper(c, g.Mp, g.dimn, g.G, g.Mp, K[j], g.Mp);   // K = G G^H, FP64 (the metric)
+            herm_from_upper(c, g.Mp, K[j], g.Mp);
+            wk[j] = wsget<double>(c, nm("gj.wk", j), g.Mp);
+            EigJob e;
+            e.n = g.Mp;
+            e.A = K[j];
+            e.lda = g.Mp;
+            e.w = wk[j];
+            e.slot = (int)j;
+            ek.push_back(e);
+        }
+        heev_values_batched(c, ek);
+        std::vector<std::vector<double>> wh(np);
+        for (size_t j = 0; j < np; j++) {
+            wh[j].resize(all[p0 + j].Mp);
+            DCG_CUDA(cudaMemcpyAsync(wh[j].data(), wk[j], sizeof(double) * wh[j].size(), cudaMemcpyDeviceToHost,
+                                     c.stream));
+        }
+        DCG_CUDA(cudaStreamSynchronize(c.stream));
+        std::vector<EigJob> eb;
+        for (size_t j = 0; j < np; j++) {
+            GramJob &g = all[p0 + j];
+            vlo[j] = g.Mp;
+            for (int q = 0; q < g.Mp; q++)
+                if (wh[j][q] >= 1.0e-8) { vlo[j] = q; break; }   // cutoff.F90:37-70
+            dimm[j] = g.Mp - vlo[j];
+            if (dimm[j] == 0 || g.nouter == 0) continue;
+            const int dm = dimm[j], Mp = g.Mp;
+            P[j] = wsget<cplx>(c, nm("gj.P", j), (size_t)Mp * dm);
+            heev_vectors_slot(c, (int)j, Mp, K[j], Mp, vlo[j], Mp, P[j], Mp);
+            cplx *GV = wsget<cplx>(c, nm("gj.GV", j), (size_t)Mp * g.nouter);
+            zgemm(c, OP_N, OP_N, Mp, g.nouter, g.dimn, one, g.G, Mp, 0, g.Vsel, g.dimn, 0, zero, GV, Mp, 0, 1);
+            VC0[j] = wsget<cplx>(c, nm("gj.VC0", j), (size_t)dm * g.nouter);
+            zgemm(c, OP_C, OP_N, dm, g.nouter, Mp, one, P[j], Mp, 0, GV, Mp, 0, zero, VC0[j], dm, 0, 1);
+            launch_scale_rows(c, dm, g.nouter, VC0[j], dm, wk[j], vlo[j], true);   // Lambda^-1 P^H G v
+            cplx *PD = wsget<cplx>(c, nm("gj.PD", j), (size_t)Mp * dm);
+            DCG_CUDA(cudaMemcpyAsync(PD, P[j], sizeof(cplx) * (size_t)Mp * dm, cudaMemcpyDeviceToDevice, c.stream));
+            launch_scale_rows(c, Mp, dm, PD, Mp, g.Dd, 0, false);
+            Bp[j] = wsget<cplx>(c, nm("gj.Bp", j), (size_t)dm * dm);
+            zgemm(c, OP_C, OP_N, dm, dm, Mp, one, P[j], Mp, 0, PD, Mp, 0, zero, Bp[j], dm, 0, 1);   // P^H D P
+            herm_from_upper(c, dm, Bp[j], dm);
+            wb[j] = wsget<double>(c, nm("gj.wb", j), dm);
+            EigJob e;
+            e.n = dm;
+            e.A = Bp[j];
+            e.lda = dm;
+            e.w = wb[j];
+            e.slot = (int)(16 + j);
+            eb.push_back(e);
+        }
+        heev_values_batched(c, eb);
+        for (size_t j = 0; j < np; j++) {
+            GramJob &g = all[p0 + j];
+            red[j] = nullptr;
+            if (dimm[j] == 0 || g.nouter == 0) continue;
+            const int dm = dimm[j];
+            cplx *W = wsget<cplx>(c, nm("gj.W", j), (size_t)dm * dm);
+            heev_vectors_slot(c, (int)(16 + j), dm, Bp[j], dm, 0, dm, W, dm);
+            cplx *VC1 = wsget<cplx>(c, nm("gj.VC1", j), (size_t)dm * g.nouter);
+            zgemm(c, OP_C, OP_N, dm, g.nouter, dm, one, W, dm, 0, VC0[j], dm, 0, zero, VC1, dm, 0, 1);
+            double *e2o = wsget<double>(c, nm("gj.e2o", j), g.nouter);
+            double *sco = wsget<double>(c, nm("gj.sco", j), g.nouter);
+            launch_e2(c, VC1, dm, g.nouter, g.alpha, wb[j], e2o, sco);
+            red[j] = wsget<double>(c, nm("gj.red", j), 2);
+            dsum(c, e2o, g.nouter, red[j]);
+            dsum(c, sco, g.nouter, red[j] + 1);
+        }
+        std::vector<double> hr(2 * np, 0.0);
+        for (size_t j = 0; j < np; j++)
+            if (red[j]) DCG_CUDA(cudaMemcpyAsync(&hr[2 * j], red[j], 2 * sizeof(double), cudaMemcpyDeviceToHost, c.stream));
+        DCG_CUDA(cudaStreamSynchronize(c.stream));
+        for (size_t j = 0; j < np; j++) {
+            e2_sub[all[p0 + j].sub] += hr[2 * j];
+            sc2_sub[all[p0 + j].sub] += hr[2 * j + 1];
+        }
+    }
+}
+
 // run the per-isym blocks of one subspace; V is the full V tensor on the device
 static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpec> &blocks, double &e2, double &sc2) {
     Context &c = *sc.c;
@@ -528,6 +633,7 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
     const int Mp = (int)dets_p.size();
     uint64_t *d_dets_p = nullptr;
     double *d_Dp = nullptr;
+    const std::string sfx(1, sub);
     for (size_t bi = 0; bi < blocks.size(); bi++) {
         BlockSpec &b = blocks[bi];
         if (b.dimn == 0) continue;
@@ -542,8 +648,27 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
                         if ((dets_p[r] >> w) & 1ull) e += sc.eps[c.ni + w];
                     Dp[r] = e;
                 }
-                d_dets_p = upload(c, "gram.dets", dets_p);
-                d_Dp = upload(c, "gram.D", Dp);
+                d_dets_p = upload(c, "gram.dets" + sfx, dets_p);
+                d_Dp = upload(c, "gram.D" + sfx, Dp);
+            }
+            if (sc.jobs) {   // queue for the joint A/C solve: buffers named per job
+                const std::string jn = sfx + std::to_string(bi);
+                int *ind = upload(c, "gq.ind" + jn, b.ind);
+                GramJob g;
+                g.Mp = Mp;
+                g.dimn = b.dimn;
+                g.nouter = nouter;
+                g.G = wsget<cplx>(c, "gq.G" + jn, (size_t)Mp * b.dimn);
+                launch_gram(c, c.na, Mp, d_dets_p, sc.M, sc.Y, ind, b.dimn, sub == 'A' ? 1 : 0, g.G);
+                int64_t *oo = upload(c, "gq.oo" + jn, b.outer_off);
+                int64_t *io = upload(c, "gq.io" + jn, b.inner_off);
+                g.alpha = upload(c, "gq.alpha" + jn, b.alpha);
+                g.Vsel = wsget<cplx>(c, "gq.Vsel" + jn, (size_t)b.dimn * nouter);
+                launch_gather_v(c, V, oo, nouter, io, b.dimn, g.Vsel);
+                g.Dd = d_Dp;
+                g.sub = sub == 'A' ? 0 : 2;
+                sc.jobs->push_back(g);
+                continue;
             }
             int *ind = upload(c, "blk.ind", b.ind);
             cplx *G = wsget<cplx>(c, "gram.G", (size_t)Mp * b.dimn);
@@ -785,6 +910,9 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
     const bool c1sym = (c.nsym == 1);
     auto timed = [&](int st, auto fn) { stage_begin(c, st); fn(); stage_end(c, st); };
 
+    std::vector<GramJob> gjobs;   // A and C Gram blocks, solved together after C's build
+    sc.jobs = &gjobs;
+
     // ================= A: E_ti E_uv|0>  (solve_A_subspace.F90:26-678)
     if (ni > 0 && !(skip & 1u)) timed(ST_A, [&] {
         stage_begin(c, ST_TRANS);
@@ -890,6 +1018,9 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         }
         run_blocks(sc, 'C', V, blocks, e2_sub[2], sc2_sub[2]);
     });
+    // joint solve of the queued A and C Gram blocks (their eigenproblems batched)
+    if (!gjobs.empty()) timed(ST_AC, [&] { solve_gram_jobs(c, gjobs, e2_sub, sc2_sub); });
+    sc.jobs = nullptr;
 
     // ================= D: E_ai E_tu|0>  (solve_D_subspace.F90:25-609)
     if (ni > 0 && ns > 0 && !(skip & 8u)) timed(ST_D, [&] {
@@ -1234,6 +1365,55 @@ int dcg_heev_range(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_
                 z_re[x] = zh[x].x;
                 if (z_im) z_im[x] = zh[x].y;
             }
+        return DCG_OK;
+    });
+}
+
+int dcg_heev_batch(dcg_ctx *ctx, int32_t nmat, const int32_t *n, const double *const *a_re,
+                   const double *const *a_im, double *const *w_out, double *const *z_re, double *const *z_im) {
+    if (nmat < 0 || nmat > dcg::kEigSlots || (nmat > 0 && (!n || !a_re || !w_out))) return DCG_E_ARG;
+    for (int q = 0; q < nmat; q++)
+        if (n[q] < 0 || (n[q] > 0 && (!a_re[q] || !w_out[q]))) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        std::vector<dcg::EigJob> jobs;
+        std::vector<dcg::cplx *> As;
+        std::vector<double *> ws;
+        for (int q = 0; q < nmat; q++) {
+            const size_t nn = (size_t)n[q] * n[q];
+            std::vector<dcg::cplx> h(nn);
+            for (size_t x = 0; x < nn; x++) h[x] = dcg::mk(a_re[q][x], (a_im && a_im[q]) ? a_im[q][x] : 0.0);
+            dcg::cplx *A = dcg::wsget<dcg::cplx>(c_, "abi.batch.A" + std::to_string(q), nn + 1);
+            double *w = dcg::wsget<double>(c_, "abi.batch.w" + std::to_string(q), (size_t)n[q] + 1);
+            if (nn) DCG_CUDA(cudaMemcpyAsync(A, h.data(), nn * sizeof(dcg::cplx), cudaMemcpyHostToDevice, c_.stream));
+            dcg::herm_from_upper(c_, n[q], A, n[q]);
+            dcg::EigJob j;
+            j.n = n[q];
+            j.A = A;
+            j.lda = n[q];
+            j.w = w;
+            j.slot = q;
+            jobs.push_back(j);
+            As.push_back(A);
+            ws.push_back(w);
+        }
+        dcg::heev_values_batched(c_, jobs);
+        for (int q = 0; q < nmat; q++) {
+            const size_t nn = (size_t)n[q] * n[q];
+            if (n[q] == 0) continue;
+            DCG_CUDA(cudaMemcpyAsync(w_out[q], ws[q], n[q] * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
+            if (z_re && z_re[q]) {
+                dcg::cplx *Z = dcg::wsget<dcg::cplx>(c_, "abi.batch.Z", nn);
+                dcg::heev_vectors_slot(c_, q, n[q], As[q], n[q], 0, n[q], Z, n[q]);
+                std::vector<dcg::cplx> zh(nn);
+                DCG_CUDA(cudaMemcpyAsync(zh.data(), Z, nn * sizeof(dcg::cplx), cudaMemcpyDeviceToHost, c_.stream));
+                DCG_CUDA(cudaStreamSynchronize(c_.stream));
+                for (size_t x = 0; x < nn; x++) {
+                    z_re[q][x] = zh[x].x;
+                    if (z_im && z_im[q]) z_im[q][x] = zh[x].y;
+                }
+            }
+        }
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
         return DCG_OK;
     });
 }

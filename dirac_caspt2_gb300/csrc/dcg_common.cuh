@@ -72,7 +72,7 @@ class Workspace {
 // Stage indices of dcg_stage_times
 enum Stage {
     ST_INTS = 0, ST_CASMAT, ST_CASEIG, ST_FOCK, ST_CIROT, ST_RDM, ST_TRANS,
-    ST_A, ST_B, ST_C, ST_D, ST_E, ST_F, ST_G, ST_H, ST_COUNT
+    ST_A, ST_B, ST_C, ST_D, ST_E, ST_F, ST_G, ST_H, ST_AC, ST_COUNT
 };
 
 struct Context {
@@ -91,10 +91,12 @@ struct Context {
     double fam_ms = 0.0, fam_work = 0.0;
     // tcgen05 shared-memory descriptor strides of the split GEMM (leading, stride byte offset)
     int split_lbo = 128, split_sbo = 256;
-    // tridiagonal eigenvectors of the last heev (device, n x n), for heev_vectors_only
-    const double *eig_Q = nullptr;
-    int eig_n = 0;
-    int *eig_status = nullptr;
+    // per eigensolver slot: tridiagonal eigenvectors of the last value stage (device, n x n),
+    // their dimension and the divide-and-conquer status word
+    static constexpr int kSlots = 32;
+    const double *eig_Q[kSlots] = {};
+    int eig_n[kSlots] = {};
+    int *eig_status[kSlots] = {};
     int64_t fam_launches = 0;
 
     // ---- system (host copies)
@@ -187,6 +189,20 @@ void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cp
 // columns 0..n-vlo-1.  A is destroyed.  Pass vlo = n for eigenvalues only.
 void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz);
 
+// Batched Hermitian eigensolver: job = one matrix (A, n x n, lda; destroyed), its eigenvalues
+// w (device, ascending) and a workspace slot (0 .. kEigSlots-1, distinct within a batch; slot 0
+// is the one heev() uses).
+constexpr int kEigSlots = Context::kSlots;
+struct EigJob {
+    int n = 0;
+    cplx *A = nullptr;
+    int64_t lda = 0;
+    double *w = nullptr;
+    int slot = 0;
+};
+void heev_values_batched(Context &c, const std::vector<EigJob> &jobs);
+void heev_vectors_slot(Context &c, int slot, int n, cplx *A, int64_t lda, int vlo, int vhi, cplx *Z, int64_t ldz);
+
 // Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (same A, w).
 void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
                        int64_t ldz);
@@ -206,6 +222,9 @@ const double *stedc(Context &c, int n, const double *d, const double *e, double 
 
 // Solve A x = b (n x n, LU with partial pivoting), b overwritten.  Returns info.
 int zgesv(Context &c, int n, cplx *A, int64_t lda, cplx *b);
+
+// Upper triangle of C = A A^H (n x n from A n x k); the strictly lower part is left undefined.
+void zherk_upper(Context &c, int n, int k, const cplx *A, int64_t lda, cplx *C, int64_t ldc);
 
 // Hermitian fill from the upper triangle (ZHEEV uplo='U' semantics): A(j,i) = conj(A(i,j))
 // for i < j, Im A(i,i) = 0.

@@ -470,13 +470,22 @@ __device__ __forceinline__ void publish_reflector(int n, int k1, const cplx *col
     }
 }
 
-__global__ void __launch_bounds__(TRD_THREADS) tridiag_smem_kernel(int n, cplx *A, int64_t lda, double *d, double *e,
-                                                                    cplx *tau, cplx *pbuf, double2 *part,
-                                                                    GridBar *gb) {
+// One problem of a batched launch: its matrix, outputs, scratch and the block range
+// [b0, b0 + nb) that reduces it (with its own grid barrier).
+struct TrdJob {
+    cplx *A;
+    int64_t lda;
+    double *d, *e;
+    cplx *tau, *pbuf;
+    double2 *part;
+    GridBar *gb;
+    int n, b0, nb;
+};
+
+__device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double *e, cplx *tau, cplx *pbuf,
+                                  double2 *part, GridBar *gb, const int b, const unsigned nb) {
     extern __shared__ cplx tsm2[];
     __shared__ double red[64];
-    const unsigned nb = gridDim.x;
-    const int b = blockIdx.x;
     const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, nwb = blockDim.x >> 5;
     const int nown = (n - b + (int)nb - 1) / (int)nb;   // columns b, b+nb, ...
     cplx *cols = tsm2;                                    // nown x n
@@ -567,6 +576,18 @@ __global__ void __launch_bounds__(TRD_THREADS) tridiag_smem_kernel(int n, cplx *
         }
         if (!grid_barrier(gb, nb)) return;
     }
+}
+
+// Batched tridiagonalisation: several Hermitian matrices in one cooperative launch, each
+// reduced by its own group of blocks, so the barrier-bound column loops of independent
+// problems overlap instead of running one after another.
+__global__ void __launch_bounds__(TRD_THREADS) tridiag_smem_batched_kernel(const TrdJob *__restrict__ jobs,
+                                                                            int njobs) {
+    int j = 0;
+    while (j + 1 < njobs && (int)blockIdx.x >= jobs[j + 1].b0) j++;
+    const TrdJob J = jobs[j];
+    tridiag_smem_body(J.n, J.A, J.lda, J.d, J.e, J.tau, J.pbuf, J.part, J.gb, (int)blockIdx.x - J.b0,
+                      (unsigned)J.nb);
 }
 
 // ===================================================================== 2. divide and conquer
@@ -944,42 +965,45 @@ __global__ void __launch_bounds__(256) dc_gemm_kernel(int n, int full, DcBufs b)
 // memory (227 KB per block).
 constexpr int kDcMaxN = 11264;
 
-static DcBufs dc_bufs(Context &c, int n) {
+static std::string slot_name(const char *base, int slot) { return std::string(base) + "#" + std::to_string(slot); }
+
+static DcBufs dc_bufs(Context &c, int n, int slot) {
     DcBufs b;
     const size_t nn = (size_t)n * n;
-    b.QA = wsget<double>(c, "dc.QA", nn);
-    b.QB = wsget<double>(c, "dc.QB", nn);
-    b.U = wsget<double>(c, "dc.U", nn);
-    b.lamA = wsget<double>(c, "dc.lamA", n);
-    b.lamB = wsget<double>(c, "dc.lamB", n);
-    b.dK = wsget<double>(c, "dc.dK", n);
-    b.zK = wsget<double>(c, "dc.zK", n);
-    b.dv = wsget<double>(c, "dc.dv", n);
-    b.Kl = wsget<int>(c, "dc.Kl", n);
-    b.defl = wsget<int>(c, "dc.defl", n);
-    b.rp = wsget<int>(c, "dc.rp", n);
-    b.rn = wsget<int>(c, "dc.rn", n);
-    b.rc = wsget<double>(c, "dc.rc", n);
-    b.rs = wsget<double>(c, "dc.rs", n);
-    b.ord = wsget<int>(c, "dc.ord", n);
-    b.tau = wsget<double>(c, "dc.tau", n);
-    b.lamK = wsget<double>(c, "dc.lamK", n);
-    b.zh = wsget<double>(c, "dc.zh", n);
-    b.outc = wsget<int>(c, "dc.outc", n);
-    b.kcnt = wsget<int>(c, "dc.kcnt", n);
-    b.ndef = wsget<int>(c, "dc.ndef", n);
-    b.nrot = wsget<int>(c, "dc.nrot", n);
-    b.rho = wsget<double>(c, "dc.rho", n);
-    b.status = wsget<int>(c, "dc.status", 1);
+    auto nm = [&](const char *x) { return slot_name(x, slot); };
+    b.QA = wsget<double>(c, nm("dc.QA"), nn);
+    b.QB = wsget<double>(c, nm("dc.QB"), nn);
+    b.U = wsget<double>(c, nm("dc.U"), nn);
+    b.lamA = wsget<double>(c, nm("dc.lamA"), n);
+    b.lamB = wsget<double>(c, nm("dc.lamB"), n);
+    b.dK = wsget<double>(c, nm("dc.dK"), n);
+    b.zK = wsget<double>(c, nm("dc.zK"), n);
+    b.dv = wsget<double>(c, nm("dc.dv"), n);
+    b.Kl = wsget<int>(c, nm("dc.Kl"), n);
+    b.defl = wsget<int>(c, nm("dc.defl"), n);
+    b.rp = wsget<int>(c, nm("dc.rp"), n);
+    b.rn = wsget<int>(c, nm("dc.rn"), n);
+    b.rc = wsget<double>(c, nm("dc.rc"), n);
+    b.rs = wsget<double>(c, nm("dc.rs"), n);
+    b.ord = wsget<int>(c, nm("dc.ord"), n);
+    b.tau = wsget<double>(c, nm("dc.tau"), n);
+    b.lamK = wsget<double>(c, nm("dc.lamK"), n);
+    b.zh = wsget<double>(c, nm("dc.zh"), n);
+    b.outc = wsget<int>(c, nm("dc.outc"), n);
+    b.kcnt = wsget<int>(c, nm("dc.kcnt"), n);
+    b.ndef = wsget<int>(c, nm("dc.ndef"), n);
+    b.nrot = wsget<int>(c, nm("dc.nrot"), n);
+    b.rho = wsget<double>(c, nm("dc.rho"), n);
+    b.status = wsget<int>(c, nm("dc.status"), 1);
     return b;
 }
 
 // Eigenvalues (ascending, into w) and eigenvectors (n x n, ld n, returned) of the
 // symmetric tridiagonal (d, e).  d and e are device arrays; e has n-1 entries.
-static const double *tridiag_dc(Context &c, int n, const double *d, const double *e, double *w) {
+static const double *tridiag_dc(Context &c, int n, const double *d, const double *e, double *w, int slot) {
     if (n > kDcMaxN)
         throw Error{DCG_E_ARG, "eigensolver dimension " + std::to_string(n) + " exceeds " + std::to_string(kDcMaxN)};
-    DcBufs b = dc_bufs(c, n);
+    DcBufs b = dc_bufs(c, n, slot);
     // Both buffers start at zero: a merge reads whole columns of its node block, including the
     // cross blocks between its two children, which no earlier level writes.
     DCG_CUDA(cudaMemsetAsync(b.QA, 0, sizeof(double) * (size_t)n * n, c.stream));
@@ -1013,10 +1037,10 @@ static const double *tridiag_dc(Context &c, int n, const double *d, const double
         std::swap(b.lamA, b.lamB);
     }
     DCG_CUDA(cudaMemcpyAsync(w, b.lamA, sizeof(double) * n, cudaMemcpyDeviceToDevice, c.stream));
-    // record which buffer holds the result for heev_vectors_only
-    c.eig_Q = b.QA;
-    c.eig_n = n;
-    c.eig_status = b.status;
+    // record which buffer holds the result for the vector stage of this slot
+    c.eig_Q[slot] = b.QA;
+    c.eig_n[slot] = n;
+    c.eig_status[slot] = b.status;
     return b.QA;
 }
 
@@ -1197,14 +1221,14 @@ struct HeevWork {
     cplx *tau, *ppart, *w;
 };
 
-static HeevWork heev_work(Context &c, int n) {
+static HeevWork heev_work(Context &c, int n, int slot) {
     HeevWork h;
-    h.d = wsget<double>(c, "heev.d", n + 1);
-    h.e = wsget<double>(c, "heev.e", n + 1);
-    h.tau = wsget<cplx>(c, "heev.tau", n + 1);
+    h.d = wsget<double>(c, slot_name("heev.d", slot), n + 1);
+    h.e = wsget<double>(c, slot_name("heev.e", slot), n + 1);
+    h.tau = wsget<cplx>(c, slot_name("heev.tau", slot), n + 1);
     int nchunk = (n + HH_CHUNK - 1) / HH_CHUNK;
-    h.ppart = wsget<cplx>(c, "heev.ppart", (size_t)nchunk * (n + 1));
-    h.w = wsget<cplx>(c, "heev.w", n + 1);
+    h.ppart = wsget<cplx>(c, slot_name("heev.ppart", slot), (size_t)nchunk * (n + 1));
+    h.w = wsget<cplx>(c, slot_name("heev.w", slot), n + 1);
     return h;
 }
 
@@ -1231,51 +1255,77 @@ static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork
     if (hb.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
 }
 
-// Returns false (nothing launched) when the matrix does not fit the blocks' shared memory.
-static bool tridiag_smem(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
+// Shared-memory tridiagonalisation of several matrices in one cooperative launch (one job = one
+// block group).  Block counts come from a cost model: a job's FP64 work (about 4 n^3 FMAs; a
+// GB300 SM retires ~2 FP64 FMAs per clock) spreads over its blocks while every grid barrier (2
+// per column) costs more with more blocks; the jobs share the SMs, and blocks go to the job that
+// is currently the slowest.  Returns false (nothing launched) when the jobs do not fit.
+static double trd_cost(int n, int nb) {
+    return 4.0 * (double)n * n * n / (nb * 4.0e9) + 2.0 * n * (3.0e-6 + 0.02e-6 * nb);
+}
+
+static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
     const int sms = std::max(1, c.num_sms);
     int optin = 0;
     DCG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
     const size_t limit = (size_t)std::max(0, optin - 1024);   // static shared memory of the kernel
-    // Block count: the FP64 work (about 4 n^3 FMAs; a GB300 SM retires ~2 FP64 FMAs per clock)
-    // spreads over the blocks while every grid barrier (2 per column) costs more with more
-    // blocks; take the cheapest count among those whose owned columns fit shared memory.
-    auto bytes_for = [&](int nbk) { return (size_t)(((n + nbk - 1) / nbk) + 2) * n * sizeof(cplx); };
-    int nblocks = 0;
-    double best = 1e300;
-    for (int nbk = 1; nbk <= std::min(sms, n); nbk++) {
-        if (bytes_for(nbk) > limit) continue;
-        const double fp64_s = 4.0 * (double)n * n * n / (nbk * 4.0e9);
-        const double bar_s = 2.0 * n * (3.0e-6 + 0.02e-6 * nbk);
-        if (fp64_s + bar_s < best) {
-            best = fp64_s + bar_s;
-            nblocks = nbk;
-        }
+    auto bytes_for = [](int n, int nbk) { return (size_t)(((n + nbk - 1) / nbk) + 2) * n * sizeof(cplx); };
+    int total = 0;
+    for (TrdJob &j : jobs) {
+        if (j.n > kTridiagSmemMaxN) return false;
+        int nb = 1;
+        while (nb < std::min(sms, j.n) && bytes_for(j.n, nb) > limit) nb++;
+        if (bytes_for(j.n, nb) > limit) return false;
+        j.nb = nb;
+        total += nb;
     }
-    if (nblocks == 0) return false;
-    const size_t smem = bytes_for(nblocks);
-    DCG_CUDA(cudaFuncSetAttribute(tridiag_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    if (total > sms) return false;
+    while (total < sms) {   // give the next block to the slowest job that it helps
+        int best = -1;
+        double worst = -1.0;
+        for (size_t q = 0; q < jobs.size(); q++) {
+            const TrdJob &j = jobs[q];
+            if (j.nb >= j.n || trd_cost(j.n, j.nb + 1) >= trd_cost(j.n, j.nb)) continue;
+            const double cst = trd_cost(j.n, j.nb);
+            if (cst > worst) {
+                worst = cst;
+                best = (int)q;
+            }
+        }
+        if (best < 0) break;
+        jobs[best].nb++;
+        total++;
+    }
+    size_t smem = 0;
+    int b0 = 0;
+    for (TrdJob &j : jobs) {
+        smem = std::max(smem, bytes_for(j.n, j.nb));
+        j.b0 = b0;
+        b0 += j.nb;
+    }
+    DCG_CUDA(cudaFuncSetAttribute(tridiag_smem_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
-    DCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_smem_kernel, TRD_THREADS, smem));
-    if (per_sm < 1 || nblocks > per_sm * sms) return false;
-    cplx *pbuf = wsget<cplx>(c, "trd.p", (size_t)n + 1);
-    double2 *part = wsget<double2>(c, "trd.part", (size_t)nblocks + 1);
-    GridBar *gb = wsget<GridBar>(c, "trd.bar", 1);
-    DCG_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBar), c.stream));
-    void *args[] = {&n, &A, &lda, &h.d, &h.e, &h.tau, &pbuf, &part, &gb};
-    DCG_CUDA(cudaLaunchCooperativeKernel((const void *)tridiag_smem_kernel, dim3(nblocks), dim3(TRD_THREADS), args,
-                                         smem, c.stream));
+    DCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_smem_batched_kernel, TRD_THREADS, smem));
+    if (per_sm < 1 || total > per_sm * sms) return false;
+    for (size_t q = 0; q < jobs.size(); q++) DCG_CUDA(cudaMemsetAsync(jobs[q].gb, 0, sizeof(GridBar), c.stream));
+    TrdJob *dj = wsget<TrdJob>(c, "trd.jobs", jobs.size());
+    DCG_CUDA(cudaMemcpyAsync(dj, jobs.data(), jobs.size() * sizeof(TrdJob), cudaMemcpyHostToDevice, c.stream));
+    int nj = (int)jobs.size();
+    void *args[] = {&dj, &nj};
+    DCG_CUDA(cudaLaunchCooperativeKernel((const void *)tridiag_smem_batched_kernel, dim3(total), dim3(TRD_THREADS),
+                                         args, smem, c.stream));
     DCG_LAUNCHED(c);
-    GridBar hb;
-    DCG_CUDA(cudaMemcpyAsync(&hb, gb, sizeof(GridBar), cudaMemcpyDeviceToHost, c.stream));
+    std::vector<GridBar> hb(jobs.size());
+    for (size_t q = 0; q < jobs.size(); q++)
+        DCG_CUDA(cudaMemcpyAsync(&hb[q], jobs[q].gb, sizeof(GridBar), cudaMemcpyDeviceToHost, c.stream));
     DCG_CUDA(cudaStreamSynchronize(c.stream));
-    if (hb.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
+    for (const GridBar &g : hb)
+        if (g.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
     return true;
 }
 
-// Reduce A to tridiagonal form; d, e, tau in the named workspace, reflectors in A.
-static void tridiag(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
-    if (n <= kTridiagSmemMaxN && tridiag_smem(c, n, A, lda, h)) return;
+// One matrix: the L2-resident persistent kernel, or one kernel launch per column beyond it.
+static void tridiag_single(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
     if (n <= kTridiagPersistentMaxN) {
         tridiag_persistent(c, n, A, lda, h);
         return;
@@ -1298,41 +1348,80 @@ static void tridiag(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
     DCG_LAUNCHED(c);
 }
 
-static void check_dc_status(Context &c) {
-    if (!c.eig_status) return;
+static void check_dc_status(Context &c, int slot) {
+    if (!c.eig_status[slot]) return;
     int st = 0;
-    DCG_CUDA(cudaMemcpyAsync(&st, c.eig_status, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaMemcpyAsync(&st, c.eig_status[slot], sizeof(int), cudaMemcpyDeviceToHost, c.stream));
     DCG_CUDA(cudaStreamSynchronize(c.stream));
     if (st) throw Error{DCG_E_NUMERIC, "divide-and-conquer merge met coincident undeflated poles"};
 }
 
-void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
-    if (n <= 0) return;
-    HeevWork h = heev_work(c, n);
-    {
-        FamScope fs(c, DCG_FAM_EIG, (16.0 / 3.0) * (double)n * n * n);
-        {
-            FamScope f1(c, DCG_FAM_EIG_TRI, (16.0 / 3.0) * (double)n * n * n);
-            tridiag(c, n, A, lda, h);
-        }
-        {
-            FamScope f2(c, DCG_FAM_EIG_VAL, 4.0 / 3.0 * (double)n * n * n);
-            tridiag_dc(c, n, h.d, h.e, w);
-        }
-        check_dc_status(c);
+// Eigenvalues of every job's matrix (ascending, into job.w); the reflectors stay in job.A and
+// the tridiagonal eigenvectors in the job's slot for heev_vectors_slot.  Jobs that fit the
+// shared-memory tridiagonalisation are reduced together in one launch.
+void heev_values_batched(Context &c, const std::vector<EigJob> &jobs) {
+    if (jobs.empty()) return;
+    double work = 0.0;
+    for (const EigJob &j : jobs) {
+        if (j.slot < 0 || j.slot >= kEigSlots) throw Error{DCG_E_ARG, "eigensolver slot out of range"};
+        work += (16.0 / 3.0) * (double)j.n * j.n * j.n;
     }
-    heev_vectors_only(c, n, A, lda, w, vlo, vhi, Z, ldz);   // own EIG / EIG_BACK scopes
+    std::vector<HeevWork> hw;
+    for (const EigJob &j : jobs) hw.push_back(heev_work(c, std::max(j.n, 1), j.slot));
+    FamScope fs(c, DCG_FAM_EIG, work);
+    {
+        FamScope f1(c, DCG_FAM_EIG_TRI, work);
+        std::vector<TrdJob> tj;
+        std::vector<size_t> who;
+        for (size_t q = 0; q < jobs.size(); q++) {
+            const EigJob &j = jobs[q];
+            if (j.n <= 0 || j.n > kTridiagSmemMaxN) continue;
+            TrdJob t;
+            t.A = j.A;
+            t.lda = j.lda;
+            t.d = hw[q].d;
+            t.e = hw[q].e;
+            t.tau = hw[q].tau;
+            t.pbuf = wsget<cplx>(c, slot_name("trd.p", j.slot), (size_t)j.n + 1);
+            t.part = wsget<double2>(c, slot_name("trd.part", j.slot), (size_t)std::max(1, c.num_sms) + 1);
+            t.gb = wsget<GridBar>(c, slot_name("trd.bar", j.slot), 1);
+            t.n = j.n;
+            t.b0 = t.nb = 0;
+            tj.push_back(t);
+            who.push_back(q);
+        }
+        std::vector<bool> done(jobs.size(), false);
+        if (!tj.empty()) {
+            if (tridiag_smem_batched(c, tj)) {
+                for (size_t q : who) done[q] = true;
+            } else if (tj.size() > 1) {   // too many for one launch: each on its own
+                for (size_t k = 0; k < tj.size(); k++) {
+                    std::vector<TrdJob> one(1, tj[k]);
+                    if (tridiag_smem_batched(c, one)) done[who[k]] = true;
+                }
+            }
+        }
+        for (size_t q = 0; q < jobs.size(); q++)
+            if (!done[q] && jobs[q].n > 0) tridiag_single(c, jobs[q].n, jobs[q].A, jobs[q].lda, hw[q]);
+    }
+    {
+        FamScope f2(c, DCG_FAM_EIG_VAL, work / 4.0);
+        for (size_t q = 0; q < jobs.size(); q++)
+            if (jobs[q].n > 0) tridiag_dc(c, jobs[q].n, hw[q].d, hw[q].e, jobs[q].w, jobs[q].slot);
+    }
+    for (const EigJob &j : jobs)
+        if (j.n > 0) check_dc_status(c, j.slot);
 }
 
-// Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (its reflectors are
-// still in A and the tridiagonal eigenvectors in the divide-and-conquer workspace).
-void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
-                       int64_t ldz) {
-    (void)w;
+// Eigenvectors [vlo, vhi) of the matrix reduced in slot `slot` by heev_values_batched (its
+// reflectors still in A, its tridiagonal eigenvectors in the slot).
+void heev_vectors_slot(Context &c, int slot, int n, cplx *A, int64_t lda, int vlo, int vhi, cplx *Z, int64_t ldz) {
     const int nvec = vhi - vlo;
     if (nvec <= 0 || n <= 0 || Z == nullptr) return;
-    if (c.eig_Q == nullptr || c.eig_n != n) throw Error{DCG_E_STATE, "heev_vectors_only without a matching heev"};
-    HeevWork h = heev_work(c, n);
+    if (slot < 0 || slot >= kEigSlots || c.eig_Q[slot] == nullptr || c.eig_n[slot] != n)
+        throw Error{DCG_E_STATE, "eigenvectors requested without a matching eigenvalue stage"};
+    HeevWork h = heev_work(c, n, slot);
+    const double *Qt = c.eig_Q[slot];
     FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nvec);
     FamScope f4(c, DCG_FAM_EIG_BACK, 8.0 * (double)n * n * nvec);
     // Many columns: the FP64 pipe is the limit, one warp per column without prefetch (fewest
@@ -1341,18 +1430,18 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
     if (n <= 1024) {
         const bool many = nvec >= 64;
         if (n <= 256) {
-            if (many) launch_bt_reg<8, 1, false>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
-            else launch_bt_reg<8, 1, true>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+            if (many) launch_bt_reg<8, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            else launch_bt_reg<8, 1, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
         } else if (n <= 512) {
-            if (many) launch_bt_reg<16, 1, false>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
-            else launch_bt_reg<16, 1, true>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+            if (many) launch_bt_reg<16, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            else launch_bt_reg<16, 1, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
         } else {
-            if (many) launch_bt_reg<32, 1, false>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
-            else launch_bt_reg<16, 2, true>(c, n, A, lda, h.tau, c.eig_Q, vlo, nvec, Z, ldz);
+            if (many) launch_bt_reg<32, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            else launch_bt_reg<16, 2, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
         }
         return;
     }
-    z_from_real_kernel<<<grid1d((int64_t)n * nvec, 256), 256, 0, c.stream>>>(n, c.eig_Q, vlo, nvec, Z, ldz);
+    z_from_real_kernel<<<grid1d((int64_t)n * nvec, 256), 256, 0, c.stream>>>(n, Qt, vlo, nvec, Z, ldz);
     DCG_LAUNCHED(c);
     cplx *Vp = wsget<cplx>(c, "wy.V", (size_t)n * WY_NB);
     cplx *G = wsget<cplx>(c, "wy.G", WY_NB * WY_NB);
@@ -1380,13 +1469,32 @@ void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w,
     }
 }
 
+void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
+    if (n <= 0) return;
+    EigJob j;
+    j.n = n;
+    j.A = A;
+    j.lda = lda;
+    j.w = w;
+    j.slot = 0;
+    heev_values_batched(c, std::vector<EigJob>(1, j));
+    heev_vectors_slot(c, 0, n, A, lda, vlo, vhi, Z, ldz);
+}
+
+// Eigenvectors [vlo, vhi) of the matrix most recently passed to heev() (slot 0).
+void heev_vectors_only(Context &c, int n, cplx *A, int64_t lda, const double *w, int vlo, int vhi, cplx *Z,
+                       int64_t ldz) {
+    (void)w;
+    heev_vectors_slot(c, 0, n, A, lda, vlo, vhi, Z, ldz);
+}
+
 // Symmetric tridiagonal eigendecomposition (the divide-and-conquer stage alone): d (n),
 // e (n-1) device arrays; ascending eigenvalues into w (device) and eigenvectors returned
 // (device, n x n, ld n; valid until the next eigensolver call).
 const double *stedc(Context &c, int n, const double *d, const double *e, double *w) {
     if (n <= 0) return nullptr;
-    const double *Q = tridiag_dc(c, n, d, e, w);
-    check_dc_status(c);
+    const double *Q = tridiag_dc(c, n, d, e, w, 0);
+    check_dc_status(c, 0);
     return Q;
 }
 

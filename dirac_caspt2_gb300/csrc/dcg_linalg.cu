@@ -67,7 +67,7 @@ template <int OPA, int OPB>
 __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx alpha, const cplx *__restrict__ A,
                                                     int64_t lda, int64_t sa, const cplx *__restrict__ B,
                                                     int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc,
-                                                    int64_t sc, int zoff) {
+                                                    int64_t sc, int zoff, int upper) {
     constexpr int BM = 64, BN = 64, BK = 16;
     __shared__ cplx As[BK][BM + 1];
     __shared__ cplx Bs[BK][BN + 1];
@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx al
     B += bz * sb;
     C += bz * sc;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+    if (upper && m0 >= n0 + BN) return;   // tile strictly below the diagonal (Hermitian product, upper half)
     const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
     cplx acc[4][4];
 #pragma unroll
@@ -275,25 +276,26 @@ static bool zgemm_small(Context &c, Op opa, Op opb, int m, int n, int k, cplx al
 template <int OPA, int OPB>
 static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
                          const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
-                         int batch) {
+                         int batch, int upper) {
     for (int z0 = 0; z0 < batch; z0 += 65535) {
         int nz = batch - z0 < 65535 ? batch - z0 : 65535;
         dim3 grid(grid1d(m, 64), grid1d(n, 64), nz);
         zgemm_kernel<OPA, OPB><<<grid, 256, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc,
-                                                           sc, z0);
+                                                           sc, z0, upper);
         DCG_LAUNCHED(c);
     }
 }
 
 // C = alpha * sum_s P_s + beta * C over nsplit partial products (fixed summation order).
 __global__ void splitk_reduce_kernel(int m, int n, int nsplit, const cplx *__restrict__ P, cplx alpha, cplx beta,
-                                     cplx *C, int64_t ldc) {
+                                     cplx *C, int64_t ldc, int upper) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const int64_t mn = (int64_t)m * n;
     if (idx >= mn) return;
+    const int i = (int)(idx % m), j = (int)(idx / m);
+    if (upper && i > j) return;
     cplx acc = mk(0.0, 0.0);
     for (int s = 0; s < nsplit; s++) acc = cadd(acc, P[s * mn + idx]);
-    const int i = (int)(idx % m), j = (int)(idx / m);
     const int64_t o = i + (int64_t)j * ldc;
     cplx r = cmul(alpha, acc);
     if (beta.x != 0.0 || beta.y != 0.0) r = cadd(r, cmul(beta, C[o]));
@@ -303,7 +305,7 @@ __global__ void splitk_reduce_kernel(int m, int n, int nsplit, const cplx *__res
 template <int OPA, int OPB>
 static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
                          const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
-                         int batch);
+                         int batch, int upper);
 
 // Split-K for a single GEMM whose output has too few 64x64 tiles to occupy every SM (a GB300
 // SM retires only about two FP64 FMAs per clock, so a GEMM on a handful of SMs runs at a
@@ -312,8 +314,10 @@ static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx
 // the shape does not qualify.
 template <int OPA, int OPB>
 static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B,
-                         int64_t ldb, cplx beta, cplx *C, int64_t ldc) {
-    const int64_t tiles = (int64_t)((m + 63) / 64) * ((n + 63) / 64);
+                         int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper = 0) {
+    const int64_t tm = (m + 63) / 64, tn = (n + 63) / 64;
+    // tiles on or above the diagonal only, for a Hermitian product's upper half
+    const int64_t tiles = upper ? (tn * (tn + 1)) / 2 : tm * tn;
     const int sms = std::max(1, c.num_sms);
     if (tiles >= sms || k < 128) return false;
     int nsplit = (int)std::min<int64_t>((2 * sms + tiles - 1) / tiles, k / 64);
@@ -328,11 +332,11 @@ static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx
     // K-chunk strides: A is m x k (OP_N/OP_R, chunk = columns) or k x m (OP_T/OP_C, chunk = rows)
     const int64_t sa = (OPA == OP_N || OPA == OP_R) ? (int64_t)kc * lda : kc;
     const int64_t sb = (OPB == OP_N || OPB == OP_R) ? kc : (int64_t)kc * ldb;
-    zgemm_launch<OPA, OPB>(c, m, n, kc, one, A, lda, sa, B, ldb, sb, zero, P, m, mn, nfull);
+    zgemm_launch<OPA, OPB>(c, m, n, kc, one, A, lda, sa, B, ldb, sb, zero, P, m, mn, nfull, upper);
     if (rem > 0)
         zgemm_launch<OPA, OPB>(c, m, n, rem, one, A + nfull * sa, lda, 0, B + nfull * sb, ldb, 0, zero, P + nfull * mn,
-                               m, 0, 1);
-    splitk_reduce_kernel<<<grid1d(mn, 256), 256, 0, c.stream>>>(m, n, nsplit, P, alpha, beta, C, ldc);
+                               m, 0, 1, upper);
+    splitk_reduce_kernel<<<grid1d(mn, 256), 256, 0, c.stream>>>(m, n, nsplit, P, alpha, beta, C, ldc, upper);
     DCG_LAUNCHED(c);
     return true;
 }
@@ -344,7 +348,7 @@ void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cp
 #define DCG_ZG(a, b)                                                                                   \
     if (opa == a && opb == b) {                                                                        \
         if (batch == 1 && zgemm_splitk<a, b>(c, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)) return;  \
-        zgemm_launch<a, b>(c, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch);        \
+        zgemm_launch<a, b>(c, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, 0);     \
         return;                                                                                        \
     }
     DCG_ZG(OP_N, OP_N) DCG_ZG(OP_N, OP_T) DCG_ZG(OP_N, OP_C) DCG_ZG(OP_N, OP_R)
@@ -353,6 +357,17 @@ void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cp
     DCG_ZG(OP_R, OP_N) DCG_ZG(OP_R, OP_T) DCG_ZG(OP_R, OP_C) DCG_ZG(OP_R, OP_R)
 #undef DCG_ZG
     throw Error{DCG_E_ARG, "zgemm: bad op"};
+}
+
+// Upper triangle of C = A A^H (n x n, A n x k, column-major): only the 64 x 64 tiles on or
+// above the diagonal are computed (half the work of the full product), split along k when
+// those tiles alone cannot fill the GPU.  The strictly lower part of C is left undefined; a
+// Hermitian fill from the upper triangle completes it.
+void zherk_upper(Context &c, int n, int k, const cplx *A, int64_t lda, cplx *C, int64_t ldc) {
+    if (n <= 0) return;
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    if (zgemm_splitk<OP_N, OP_C>(c, n, n, k, one, A, lda, A, lda, zero, C, ldc, 1)) return;
+    zgemm_launch<OP_N, OP_C>(c, n, n, k, one, A, lda, 0, A, lda, 0, zero, C, ldc, 0, 1, 1);
 }
 
 // ===================================================================== Hermitian fill

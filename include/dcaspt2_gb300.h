@@ -129,7 +129,9 @@ int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n);
 
 /* Per-stage device times of the last dcg_casci/dcg_caspt2 (ms), in the order:
  * 0 integral expansion, 1 CASCI matrix, 2 CASCI eigensolve, 3 Fock build+diag,
- * 4 CI rotation, 5 RDMs, 6 transformation, 7..14 subspaces A..H.  Returns the count. */
+ * 4 CI rotation, 5 RDMs, 6 transformation, 7..14 subspaces A..H (their builds and own
+ * solves), 15 the joint eigensolves of the A and C blocks that go through the Gram factor.
+ * Returns the count. */
 int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n);
 
 /* Device kernel launches issued by the last dcg_set_system+dcg_casci+dcg_caspt2. */
@@ -149,6 +151,13 @@ void *dcg_stream(const dcg_ctx *ctx);
  * real symmetric matrix) is read, as ZHEEV with uplo='U' reads it. */
 int dcg_heev(dcg_ctx *ctx, int32_t n, const double *a_re, const double *a_im, double *w_out, double *z_re,
              double *z_im);
+/* Several Hermitian eigendecompositions in one batch (nmat <= 32): their tridiagonal reductions
+ * run together in one launch, as the subspace solvers batch their S and B' matrices.  Per
+ * matrix q: dimension n[q], upper triangle of a_re[q]/a_im[q] (a_im or a_im[q] NULL: real),
+ * eigenvalues w_out[q] (ascending) and, when z_re and z_re[q] are not NULL, all eigenvectors. */
+int dcg_heev_batch(dcg_ctx *ctx, int32_t nmat, const int32_t *n, const double *const *a_re,
+                   const double *const *a_im, double *const *w_out, double *const *z_re, double *const *z_im);
+
 /* dcg_heev returning only the eigenvectors of eigenvalues vlo..n-1 (ascending), as the
  * columns of z_re/z_im (n x (n - vlo)): the S-matrix use, which keeps the eigenvectors above
  * the linear-dependence cutoff, and the CASCI use, which keeps the lowest roots. */

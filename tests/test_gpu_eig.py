@@ -116,3 +116,22 @@ def test_heev_range_few_vectors(session, n, nvec):
     ws = w[n - nvec:]
     assert np.abs(a @ z - z * ws).max() <= TOL * scale
     assert np.abs(z.conj().T @ z - np.eye(nvec)).max() <= TOL
+
+
+def test_heev_batch_mixed_sizes(session):
+    """The batched eigensolver on matrices of mixed size reduced together (the S and B'
+    matrices of several subspace blocks): each result against LAPACK."""
+    rng = np.random.default_rng(77)
+    mats = []
+    for n in (792, 496, 144, 66, 12, 1):
+        a = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+        mats.append(a + a.conj().T)
+    mats.append(CASES["gram_rank120_400"])
+    mats.append(CASES["kramers_200"])
+    for a, (w, z) in zip(mats, session.heev_batch(mats)):
+        n = a.shape[0]
+        wr = np.linalg.eigvalsh(a)
+        scale = max(1.0, np.abs(wr).max())
+        assert np.abs(w - wr).max() <= TOL * scale
+        assert np.abs(a @ z - z * w).max() <= TOL * scale
+        assert np.abs(z.conj().T @ z - np.eye(n)).max() <= TOL
