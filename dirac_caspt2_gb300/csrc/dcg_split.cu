@@ -307,7 +307,9 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
     __shared__ uint32_t s_tmem;
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rb = blockIdx.x, nb = blockIdx.y, z = blockIdx.z;
+    // linear (row block, column block) index with the column blocks of a row block adjacent,
+    // so the CTAs that share an A tile run together and find it in L2
+    const int rb = (int)(blockIdx.x / (unsigned)a.nnb), nb = (int)(blockIdx.x % (unsigned)a.nnb), z = blockIdx.z;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < SP_STAGES; s++) {
@@ -513,7 +515,7 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     sa.sbo = sbo;
     sa.accumulate = accumulate ? 1 : 0;
     sa.err = err;
-    dim3 grid(nrb, nnb, batch);
+    dim3 grid((unsigned)((int64_t)nrb * nnb), 1, batch);
     {
         // tensor work: 15 slice products, each a real GEMM of M x 2N x 2K
         FamScope fs(c, DCG_FAM_SPLIT_MMA, 15.0 * 8.0 * (double)M * N * K * batch);

@@ -10,7 +10,8 @@ can select the launches of one stage, e.g.
     ncu --nvtx --nvtx-include "tr_H/" -k regex:zgemm -c 3 ... \\
         python -m dirac_caspt2_gb300.profile_solve --ninact 16 --nact 8 --nsec 240 --nelec 4
 
-Prints the total energy and per-stage device times of the last solve.
+Prints the total energy and per-stage device times of the last solve.  With ``--heev N`` it
+runs the Hermitian eigensolver alone on a seeded random N x N matrix instead.
 """
 from __future__ import annotations
 
@@ -34,7 +35,22 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=0)
     ap.add_argument("--solves", type=int, default=1)
     ap.add_argument("--precision", default="fp64", choices=["fp64", "split"])
+    ap.add_argument("--heev", type=int, default=0,
+                    help="instead of a solve: dcg_heev (all eigenpairs) of a seeded random Hermitian matrix "
+                         "of this size, --warmup + --solves times")
     a = ap.parse_args(argv)
+    if a.heev > 0:
+        import numpy as np
+        rng = np.random.default_rng(a.seed)
+        m = rng.normal(size=(a.heev, a.heev)) + 1j * rng.normal(size=(a.heev, a.heev))
+        m = m + m.conj().T
+        ses = api.Caspt2Session(0)
+        t0 = time.time()
+        for _ in range(a.warmup + a.solves):
+            w, _ = ses.heev(m)
+        print(json.dumps({"heev": a.heev, "calls": a.warmup + a.solves, "wall_s": round(time.time() - t0, 3),
+                          "max_abs_eig_error": float(np.abs(w - np.linalg.eigvalsh(m)).max())}))
+        return 0
     if a.workload:
         cfg = synth.CONFIGS[a.workload]
     else:
