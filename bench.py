@@ -165,7 +165,7 @@ def run_ours(args, cfg_name):
         import torch.distributed as dist
         dist.init_process_group(backend="gloo")
     torch.cuda.set_device(local)
-    from dirac_caspt2_gb300 import api, build, synth
+    from dirac_caspt2_gb300 import api, build, replicas, synth
     build.build()
     cfg = synth.CONFIGS[cfg_name]
     S = synth.make_system(cfg)
@@ -202,9 +202,7 @@ def run_ours(args, cfg_name):
             session.time_family(fam)
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
         launches = 0
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier()
         torch.cuda.synchronize()
         clk = ClockSampler(local)
         clk.start()
@@ -248,13 +246,9 @@ def run_ours(args, cfg_name):
                 "abs_dE_casci": abs(e_s - e_d), "abs_dE_total": abs(t_s - t_d),
                 "dE2_by_subspace": {k: e2_s[k] - e2_d[k] for k in e2_s}}
 
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([tot_v, tot_e], dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        tot_v, tot_e = float(t[0]), float(t[1])
-    value = world * args.steps / tot_v
-    e2e = world * args.steps / tot_e
+    # replicas: every rank solves its own copy; the slowest rank bounds the job
+    tot_v, tot_e = replicas.max_over_ranks([tot_v, tot_e])
+    value, e2e = world * args.steps / tot_v, world * args.steps / tot_e
     peaks, src = _peaks()
     fam_ms, fam_launch, fam_work = fam
     if family in ("hstream", "scatter"):
