@@ -54,6 +54,17 @@ class _System(ctypes.Structure):
     ]
 
 
+class _RequestResult(ctypes.Structure):
+    """dcg_request_result of the serving loop."""
+    _fields_ = [
+        ("request_id", ctypes.c_uint64), ("status", ctypes.c_int32), ("ndet", ctypes.c_int32),
+        ("casci_energy", ctypes.c_double), ("e2", ctypes.c_double * 8), ("sumc2", ctypes.c_double * 8),
+        ("e0", ctypes.c_double), ("etotal", ctypes.c_double), ("t_submit", ctypes.c_double),
+        ("t_start", ctypes.c_double), ("t_end", ctypes.c_double), ("slot", ctypes.c_int32),
+        ("attempts", ctypes.c_int32),
+    ]
+
+
 _lib = None
 
 
@@ -100,6 +111,21 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_heev.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p, ctypes.c_void_p]
+    lib.dcg_device_bytes.argtypes = [ctypes.c_void_p]
+    lib.dcg_device_bytes.restype = ctypes.c_int64
+    lib.dcg_trim.argtypes = [ctypes.c_void_p]
+    lib.dcg_footprint_estimate.argtypes = [P(_System)]
+    lib.dcg_footprint_estimate.restype = ctypes.c_int64
+    lib.dcg_server_create.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_int32, ctypes.c_int64,
+                                      P(ctypes.c_void_p)]
+    lib.dcg_server_submit.argtypes = [ctypes.c_void_p, P(_System), ctypes.c_uint64]
+    lib.dcg_server_poll.argtypes = [ctypes.c_void_p, ctypes.c_int32, P(_RequestResult)]
+    lib.dcg_server_pending.argtypes = [ctypes.c_void_p, P(ctypes.c_int32), P(ctypes.c_int32)]
+    lib.dcg_server_clock.argtypes = [ctypes.c_void_p]
+    lib.dcg_server_clock.restype = ctypes.c_double
+    lib.dcg_server_device_bytes.argtypes = [ctypes.c_void_p]
+    lib.dcg_server_device_bytes.restype = ctypes.c_int64
+    lib.dcg_server_destroy.argtypes = [ctypes.c_void_p]
     _lib = lib
     return lib
 
@@ -107,7 +133,10 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
-                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm"]
+                    "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm",
+                    "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
+                    "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
+                    "dcg_server_device_bytes", "dcg_server_destroy"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
@@ -343,6 +372,14 @@ class Caspt2Session:
     def kernel_launches(self) -> int:
         return int(self.lib.dcg_kernel_launches(self.h))
 
+    def device_bytes(self) -> int:
+        """Device bytes the context holds (dcg_device_bytes)."""
+        return int(self.lib.dcg_device_bytes(self.h))
+
+    def trim(self) -> None:
+        """Release the context's device workspace (dcg_trim)."""
+        self._check(self.lib.dcg_trim(self.h))
+
     def heev(self, a: np.ndarray, vectors: bool = True):
         """Hermitian eigendecomposition on the device (dcg_heev): ascending eigenvalues and,
         when ``vectors``, the eigenvectors as columns.  Reads the upper triangle of ``a``."""
@@ -438,6 +475,112 @@ class Caspt2Session:
         e2, sc2, e0, et = self.caspt2(skip_mask)
         return Caspt2Result(casci_energies=eig, ndet=ndet, e2=e2, sumc2=sc2, e0=e0, total_energy=et,
                             stage_ms=self.stage_ms(), kernel_launches=self.kernel_launches())
+
+
+def footprint_estimate(bufs: "HostBuffers") -> int:
+    """dcg_footprint_estimate: upper estimate of one solve's device bytes in a fresh context."""
+    return int(load_library().dcg_footprint_estimate(ctypes.byref(bufs.struct)))
+
+
+@dataclasses.dataclass
+class ServedResult:
+    """One finished request of a ``Caspt2Server`` (times in seconds on the server clock)."""
+    request_id: int
+    status: int
+    ndet: int
+    casci_energy: float
+    e2: Dict[str, float]
+    sumc2: Dict[str, float]
+    e0: float
+    total_energy: float
+    t_submit: float
+    t_start: float
+    t_end: float
+    slot: int
+    attempts: int
+
+    @property
+    def latency(self) -> float:
+        return self.t_end - self.t_submit
+
+    @property
+    def e2_total(self) -> float:
+        return float(sum(self.e2.values()))
+
+
+class Caspt2Server:
+    """The library's serving loop (dcg_server_*): ``slots`` contexts with a worker thread and a
+    CUDA stream each, admission of queued requests by an HBM budget, results polled as they
+    finish.  A request is one (system, selectroot) entry run as set_system + casci + caspt2.
+
+    ``submit`` keeps the request's HostBuffers (and, through them, any device records) alive
+    until its result has been polled."""
+
+    def __init__(self, device: int = 0, precision: int = DCG_PREC_FP64, slots: int = 4, hbm_budget: int = 0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        rc = self.lib.dcg_server_create(device, precision, slots, int(hbm_budget), ctypes.byref(h))
+        if rc != 0:
+            raise DcgError(rc, "dcg_server_create failed")
+        self.h = h
+        self.slots = slots
+        self._inflight: Dict[int, HostBuffers] = {}
+
+    def submit(self, request_id: int, system, selectroot: Optional[int] = None) -> None:
+        bufs = system if isinstance(system, HostBuffers) else HostBuffers(system)
+        if selectroot is not None:
+            bufs.struct.selectroot = int(selectroot)
+        self._inflight[int(request_id)] = bufs
+        rc = self.lib.dcg_server_submit(self.h, ctypes.byref(bufs.struct), ctypes.c_uint64(int(request_id)))
+        if rc != 0:
+            del self._inflight[int(request_id)]
+            raise DcgError(rc, "request does not fit the server's device-memory budget" if rc == -5 else
+                           "dcg_server_submit failed")
+
+    def poll(self, timeout_ms: int = 0) -> Optional[ServedResult]:
+        r = _RequestResult()
+        rc = self.lib.dcg_server_poll(self.h, int(timeout_ms), ctypes.byref(r))
+        if rc == 1:
+            return None
+        if rc != 0:
+            raise DcgError(rc, "dcg_server_poll failed")
+        self._inflight.pop(int(r.request_id), None)
+        return ServedResult(request_id=int(r.request_id), status=int(r.status), ndet=int(r.ndet),
+                            casci_energy=float(r.casci_energy),
+                            e2={k: float(r.e2[i]) for i, k in enumerate(SUBSPACES)},
+                            sumc2={k: float(r.sumc2[i]) for i, k in enumerate(SUBSPACES)}, e0=float(r.e0),
+                            total_energy=float(r.etotal), t_submit=float(r.t_submit), t_start=float(r.t_start),
+                            t_end=float(r.t_end), slot=int(r.slot), attempts=int(r.attempts))
+
+    def pending(self) -> Tuple[int, int]:
+        q = ctypes.c_int32(0)
+        r = ctypes.c_int32(0)
+        self.lib.dcg_server_pending(self.h, ctypes.byref(q), ctypes.byref(r))
+        return q.value, r.value
+
+    def clock(self) -> float:
+        return float(self.lib.dcg_server_clock(self.h))
+
+    def device_bytes(self) -> int:
+        return int(self.lib.dcg_server_device_bytes(self.h))
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.dcg_server_destroy(self.h)
+            self.h = None
+            self._inflight.clear()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def format_reference_lines(r: Caspt2Result, s: SystemInput) -> List[str]:

@@ -14,7 +14,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdcaspt2_gb300.so")
-SOURCES = ["dcg_linalg.cu", "dcg_eig.cu", "dcg_split.cu", "dcg_ci.cu", "dcg_ints.cu", "dcg_pt2.cu", "dcg_api.cu"]
+SOURCES = ["dcg_linalg.cu", "dcg_eig.cu", "dcg_split.cu", "dcg_ci.cu", "dcg_ints.cu", "dcg_pt2.cu", "dcg_api.cu",
+           "dcg_serve.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-Xptxas", "-O3"]
@@ -51,7 +52,7 @@ def build(force: bool = False, extra_flags: list | None = None, verbose: bool = 
             return LIB
     with concurrent.futures.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", LIB + ".tmp", "-lcudart", "-ldl"]
+    cmd = [nvcc(), *ARCH, "-shared", "-Xcompiler", "-fPIC", *objs, "-o", LIB + ".tmp", "-lcudart", "-ldl", "-lpthread"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stderr}")

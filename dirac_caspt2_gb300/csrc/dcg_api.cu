@@ -1292,6 +1292,25 @@ int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n) {
 
 int64_t dcg_kernel_launches(const dcg_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
 
+int64_t dcg_device_bytes(const dcg_ctx *ctx) { return ctx ? (int64_t)ctx->c.ws.bytes_in_use() : -1; }
+
+int dcg_trim(dcg_ctx *ctx) {
+    DCG_API_BODY(ctx, {
+        DCG_CUDA(cudaStreamSynchronize(c_.stream));
+        c_.ws.release_all();
+        delete static_cast<dcg::DevSystem *>(c_.dev_state);
+        c_.dev_state = nullptr;
+        for (int s = 0; s < Context::kSlots; s++) {
+            c_.eig_Q[s] = nullptr;
+            c_.eig_n[s] = 0;
+            c_.eig_status[s] = nullptr;
+        }
+        c_.have_system = false;
+        c_.have_casci = false;
+    });
+    return DCG_OK;
+}
+
 const char *dcg_version(void) { return "dcaspt2_gb300 0.1 (sm_103a, FP64 path)"; }
 
 void *dcg_stream(const dcg_ctx *ctx) { return ctx ? (void *)ctx->c.stream : nullptr; }

@@ -15,13 +15,23 @@ namespace dcg {
 
 __constant__ int64_t c_binom[65][65];
 
-void upload_binomials(Context &c) {
-    static int64_t tab[65][65];
-    for (int n = 0; n <= 64; n++) {
-        tab[n][0] = 1;
-        for (int k = 1; k <= 64; k++) tab[n][k] = (n == 0) ? 0 : tab[n - 1][k - 1] + (k <= n - 1 ? tab[n - 1][k] : 0);
+namespace {
+struct BinomTable {
+    int64_t t[65][65];
+    BinomTable() {
+        for (int n = 0; n <= 64; n++) {
+            t[n][0] = 1;
+            for (int k = 1; k <= 64; k++) t[n][k] = (n == 0) ? 0 : t[n - 1][k - 1] + (k <= n - 1 ? t[n - 1][k] : 0);
+        }
     }
-    DCG_CUDA(cudaMemcpyToSymbolAsync(c_binom, tab, sizeof(tab), 0, cudaMemcpyHostToDevice, c.stream));
+};
+}  // namespace
+
+// The table is the same for every context; contexts created from several host threads write
+// identical bytes (the static is initialised once, thread-safely).
+void upload_binomials(Context &c) {
+    static const BinomTable tab;
+    DCG_CUDA(cudaMemcpyToSymbolAsync(c_binom, tab.t, sizeof(tab.t), 0, cudaMemcpyHostToDevice, c.stream));
 }
 
 __device__ __forceinline__ int64_t colex_rank(uint64_t I) {

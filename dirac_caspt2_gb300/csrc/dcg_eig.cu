@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 
 #include "dcg_common.cuh"
 
@@ -1011,11 +1012,7 @@ static const double *tridiag_dc(Context &c, int n, const double *d, const double
     DCG_CUDA(cudaMemsetAsync(b.status, 0, sizeof(int), c.stream));
     dc_leaf_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, d, e, b.lamA, b.QA);
     DCG_LAUNCHED(c);
-    static bool attr_set = false;
-    if (!attr_set) {
-        DCG_CUDA(cudaFuncSetAttribute(dc_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * kDcMaxN));
-        attr_set = true;
-    }
+    DCG_CUDA(cudaFuncSetAttribute(dc_prep_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 20 * kDcMaxN));
     for (int half = 1; half < n; half *= 2) {
         const int full = 2 * half;
         const int nodes = (n + full - 1) / full;
@@ -1232,7 +1229,13 @@ static HeevWork heev_work(Context &c, int n, int slot) {
     return h;
 }
 
+// Cooperative launches from different contexts (a serving process runs one context per
+// slot, each on its own stream) are serialised from launch to completion: two grid-synchronised
+// kernels must never wait for each other's SMs.
+static std::mutex g_coop_mutex;
+
 static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
+    std::lock_guard<std::mutex> coop(g_coop_mutex);
     const size_t smem = 2 * sizeof(cplx) * (size_t)std::max(n - 1, 1);
     DCG_CUDA(cudaFuncSetAttribute(tridiag_persistent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int per_sm = 0;
@@ -1265,6 +1268,7 @@ static double trd_cost(int n, int nb) {
 }
 
 static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
+    std::lock_guard<std::mutex> coop(g_coop_mutex);
     const int sms = std::max(1, c.num_sms);
     int optin = 0;
     DCG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));

@@ -491,11 +491,7 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     }
     sp_slice_b_kernel<<<N, 128, 0, c.stream>>>(K, N, B, ldb, opb, nnb, nks, Bs, fexp);
     DCG_LAUNCHED(c);
-    static bool attr = false;
-    if (!attr) {
-        DCG_CUDA(cudaFuncSetAttribute(sp_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SP_SMEM));
-        attr = true;
-    }
+    DCG_CUDA(cudaFuncSetAttribute(sp_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SP_SMEM));
     SplitArgs sa;
     sa.As = As;
     sa.Bs = Bs;

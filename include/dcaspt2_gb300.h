@@ -198,6 +198,54 @@ int dcg_time_family(dcg_ctx *ctx, int32_t family);
 /* Accumulated device time (ms), launch count and algorithmic work of the timed family. */
 int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work);
 
+/* Device bytes the context holds: its grow-only workspace (integral classes, CI vectors,
+ * densities, subspace matrices, solver scratch), which stays resident between solves. */
+int64_t dcg_device_bytes(const dcg_ctx *ctx);
+/* Release the context's device workspace and system; the next solve starts with
+ * dcg_set_system again. */
+int dcg_trim(dcg_ctx *ctx);
+/* Upper estimate of the device bytes one set_system + casci + caspt2 of sys needs in a fresh
+ * context (the admission size of the serving loop; host pointers of sys are not read). */
+int64_t dcg_footprint_estimate(const dcg_system *sys);
+
+/* ------------------------------------------------------------------------ serving loop
+ * A server runs independent CASCI/CASPT2 solves (each one .caspt2_ciroots entry of one
+ * system: dcg_set_system + dcg_casci(selectroot roots) + dcg_caspt2) from a request queue on
+ * one GPU.  It owns `slots` contexts, one host worker thread and one CUDA stream each, so the
+ * solves of different requests overlap on the device.  A free slot takes the first queued
+ * request whose dcg_footprint_estimate fits the HBM budget beside the bytes the other slots
+ * hold (the running requests' estimates and the idle slots' resident workspaces; an idle slot
+ * releases its workspace when a queued request does not fit).  The host arrays a request's
+ * dcg_system points at must stay valid until its result has been polled. */
+typedef struct dcg_server dcg_server;
+
+typedef struct dcg_request_result {
+    uint64_t request_id;
+    int32_t status;          /* DCG_OK or the failing call's status                       */
+    int32_t ndet;            /* CASCI determinants                                        */
+    double casci_energy;     /* energy of the selected root (casci.F90 root selectroot)   */
+    double e2[8], sumc2[8];  /* subspaces A..H                                            */
+    double e0, etotal;       /* as dcg_caspt2                                              */
+    double t_submit, t_start, t_end;   /* seconds on the server clock (dcg_server_clock)  */
+    int32_t slot;            /* worker slot that ran the request                          */
+    int32_t attempts;        /* 1, or 2 when a first attempt ran out of device memory     */
+} dcg_request_result;
+
+/* slots in 1..64; hbm_budget_bytes <= 0 takes 90% of the device's free memory at creation. */
+int dcg_server_create(int device, int precision, int32_t slots, int64_t hbm_budget_bytes, dcg_server **out);
+/* Queue one request (DCG_E_NOMEM when its estimate exceeds the whole budget). */
+int dcg_server_submit(dcg_server *srv, const dcg_system *sys, uint64_t request_id);
+/* Take one finished request, waiting up to timeout_ms; returns 1 when none finished in time. */
+int dcg_server_poll(dcg_server *srv, int32_t timeout_ms, dcg_request_result *out);
+/* Requests waiting in the queue and running on the slots. */
+int dcg_server_pending(dcg_server *srv, int32_t *queued, int32_t *running);
+/* The server clock (seconds, monotonic) of the result stamps. */
+double dcg_server_clock(const dcg_server *srv);
+/* Device bytes held by the server's slots now (their contexts' workspaces). */
+int64_t dcg_server_device_bytes(dcg_server *srv);
+/* Drop queued requests, finish the running ones, join the workers and free the contexts. */
+int dcg_server_destroy(dcg_server *srv);
+
 #ifdef __cplusplus
 }
 #endif
