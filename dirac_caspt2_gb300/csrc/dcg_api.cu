@@ -240,6 +240,18 @@ static void set_system(Context &c, const dcg_system *s) {
 }
 
 // ------------------------------------------------------------------------- CASCI
+// The dense eigensolver below kDavidsonMinDet determinants or for many roots; block Davidson
+// on the resident Hamiltonian above it.
+constexpr int kDavidsonMinDet = 400;
+constexpr int kDavidsonMaxRoots = 12;
+
+static bool use_davidson(const Context &c, int ndet, int nvec) {
+    if (c.casci_solver == DCG_CASCI_DENSE) return false;
+    const bool fits = nvec <= kDavidsonMaxRoots && ndet >= nvec + 5;
+    if (c.casci_solver == DCG_CASCI_DAVIDSON) return fits;
+    return fits && ndet >= kDavidsonMinDet;
+}
+
 static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double *ci_im, int32_t *ndet_out) {
     if (!c.have_system) throw Error{DCG_E_STATE, "dcg_casci before dcg_set_system"};
     DevSystem &d = dev(c);
@@ -259,7 +271,13 @@ static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double
     const int nvec = std::max(nr, c.selectroot);
     double *w = wsget<double>(c, "ci.w", ndet);
     cplx *Z = wsget<cplx>(c, "ci.Z", (size_t)ndet * nvec);
-    heev(c, ndet, H, ndet, w, 0, nvec, Z, ndet);
+    c.casci_iters = 0;
+    if (use_davidson(c, ndet, nvec)) {
+        // |r| <= 1e-13 max(1, max |H_ii|): eigenvalue errors ~|r|^2/gap, vector errors ~|r|/gap
+        davidson_lowest(c, ndet, H, nvec, w, Z, 1e-13, 400);
+    } else {
+        heev(c, ndet, H, ndet, w, 0, nvec, Z, ndet);
+    }
     stage_end(c, ST_CASEIG);
     std::vector<double> wh = download(c, w, ndet);
     c.ecas.assign(wh.begin(), wh.begin() + nvec);
@@ -1291,6 +1309,14 @@ int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n) {
 }
 
 int64_t dcg_kernel_launches(const dcg_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
+
+int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver) {
+    if (!ctx || solver < DCG_CASCI_AUTO || solver > DCG_CASCI_DAVIDSON) return DCG_E_ARG;
+    ctx->c.casci_solver = solver;
+    return DCG_OK;
+}
+
+int32_t dcg_casci_iterations(const dcg_ctx *ctx) { return ctx ? ctx->c.casci_iters : -1; }
 
 int64_t dcg_device_bytes(const dcg_ctx *ctx) { return ctx ? (int64_t)ctx->c.ws.bytes_in_use() : -1; }
 

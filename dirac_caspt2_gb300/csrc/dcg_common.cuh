@@ -98,6 +98,9 @@ struct Context {
     int eig_n[kSlots] = {};
     int *eig_status[kSlots] = {};
     int64_t fam_launches = 0;
+    // CASCI eigensolver: DCG_CASCI_AUTO, _DENSE or _DAVIDSON (dcg_set_casci_solver)
+    int casci_solver = 0;
+    int casci_iters = 0;   // Davidson iterations of the last CASCI (0: dense solver)
 
     // ---- system (host copies)
     bool have_system = false;
@@ -232,5 +235,11 @@ void herm_from_upper(Context &c, int n, cplx *A, int64_t lda);
 
 // deterministic sum of n doubles on the device into *out (device)
 void dsum(Context &c, const double *x, int64_t n, double *out);
+
+// Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
+void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);
+// Lowest nwant eigenpairs of the full-storage Hermitian H (n x n, left intact) by block
+// Davidson: eigenvalues to w (device), vectors to Z (n x nwant); |r| <= tol_rel max(1, max|H_ii|).
+void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cplx *Z, double tol_rel, int maxit);
 
 }  // namespace dcg

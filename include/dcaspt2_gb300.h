@@ -198,6 +198,17 @@ int dcg_time_family(dcg_ctx *ctx, int32_t family);
 /* Accumulated device time (ms), launch count and algorithmic work of the timed family. */
 int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work);
 
+/* CASCI eigensolver of dcg_casci.  AUTO: dense Householder + divide-and-conquer (the ZHEEV
+ * of diag.F90:66-128) below 400 determinants or for more than 12 roots, block Davidson on the
+ * resident Hamiltonian otherwise (residual norms <= 1e-13 max(1, max |H_ii|) for every
+ * returned root).  DENSE / DAVIDSON force one of them (DAVIDSON needs ndet >= roots + 5). */
+#define DCG_CASCI_AUTO 0
+#define DCG_CASCI_DENSE 1
+#define DCG_CASCI_DAVIDSON 2
+int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver);
+/* Davidson iterations of the last dcg_casci (0 when the dense solver ran). */
+int32_t dcg_casci_iterations(const dcg_ctx *ctx);
+
 /* Device bytes the context holds: its grow-only workspace (integral classes, CI vectors,
  * densities, subspace matrices, solver scratch), which stays resident between solves. */
 int64_t dcg_device_bytes(const dcg_ctx *ctx);
