@@ -352,6 +352,32 @@ struct BlockOut {
     int dimm = 0;
 };
 
+// Per outer index o: e2o = -sum_m |(W^H VC)_m,o|^2 / (alpha_o + w_m) and sco = sum_m
+// |(W^H VC)_m,o|^2 / (alpha_o + w_m)^2 over the eigenpairs (w, W) of B' (dimm x dimm, destroyed;
+// VC: dimm x nouter), as the reference's solve_X_subspace evaluates them.  Up to
+// kTridiagE2MaxN they come from the tridiagonal form of B' (tridiag_e2: no eigenvectors).
+static void e2_from_bprime(Context &c, int dimm, cplx *Bp, const cplx *VC, int nouter, const double *alpha,
+                           double *e2o, double *sco) {
+    if (dimm <= kTridiagE2MaxN) {
+        EigJob e;
+        e.n = dimm;
+        e.A = Bp;
+        e.lda = dimm;
+        e.slot = 0;
+        e.tridiag_only = true;
+        heev_values_batched(c, std::vector<EigJob>(1, e));
+        tridiag_e2(c, 0, dimm, Bp, dimm, VC, dimm, nouter, alpha, e2o, sco);
+        return;
+    }
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    double *wb = wsget<double>(c, "blk.wb", dimm);
+    cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
+    heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
+    cplx *VC1 = wsget<cplx>(c, "blk.VC1", (size_t)dimm * nouter);
+    zgemm(c, OP_C, OP_N, dimm, nouter, dimm, one, W, dimm, 0, VC, dimm, 0, zero, VC1, dimm, 0, 1);
+    launch_e2(c, VC1, dimm, nouter, alpha, wb, e2o, sco);
+}
+
 // S,B (dimn x dimn) already assembled; Vsel (dimn x nouter); alphas on device.
 static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *Vsel, int nouter, const double *alpha) {
     BlockOut r;
@@ -380,17 +406,11 @@ static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *
     zgemm(c, OP_N, OP_N, dimn, dimm, dimn, one, B, dimn, 0, X, dimn, 0, zero, BX, dimn, 0, 1);
     zgemm(c, OP_C, OP_N, dimm, dimm, dimn, one, X, dimn, 0, BX, dimn, 0, zero, Bp, dimm, 0, 1);
     herm_from_upper(c, dimm, Bp, dimm);
-    double *wb = wsget<double>(c, "blk.wb", dimm);
-    cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
-    heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
-    // VC = W^H X^H Vsel
     cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
-    cplx *VC1 = wsget<cplx>(c, "blk.VC1", (size_t)dimm * nouter);
     zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, X, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
-    zgemm(c, OP_C, OP_N, dimm, nouter, dimm, one, W, dimm, 0, VC0, dimm, 0, zero, VC1, dimm, 0, 1);
     double *e2o = wsget<double>(c, "blk.e2o", nouter);
     double *sco = wsget<double>(c, "blk.sco", nouter);
-    launch_e2(c, VC1, dimm, nouter, alpha, wb, e2o, sco);
+    e2_from_bprime(c, dimm, Bp, VC0, nouter, alpha, e2o, sco);
     double *red = wsget<double>(c, "blk.red", 2);
     dsum(c, e2o, nouter, red);
     dsum(c, sco, nouter, red + 1);
@@ -518,14 +538,9 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     cplx *Bp = wsget<cplx>(c, "blk.Bp", (size_t)dimm * dimm);
     zgemm(c, OP_C, OP_N, dimm, dimm, Mp, one, P, Mp, 0, PD, Mp, 0, zero, Bp, dimm, 0, 1);
     herm_from_upper(c, dimm, Bp, dimm);
-    double *wb = wsget<double>(c, "blk.wb", dimm);
-    cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
-    heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
-    cplx *VC1 = wsget<cplx>(c, "blk.VC1", (size_t)dimm * nouter);
-    zgemm(c, OP_C, OP_N, dimm, nouter, dimm, one, W, dimm, 0, VC0, dimm, 0, zero, VC1, dimm, 0, 1);
     double *e2o = wsget<double>(c, "blk.e2o", nouter);
     double *sco = wsget<double>(c, "blk.sco", nouter);
-    launch_e2(c, VC1, dimm, nouter, alpha, wb, e2o, sco);
+    e2_from_bprime(c, dimm, Bp, VC0, nouter, alpha, e2o, sco);
     double *red = wsget<double>(c, "blk.red", 2);
     dsum(c, e2o, nouter, red);
     dsum(c, sco, nouter, red + 1);
@@ -607,6 +622,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             e.lda = dm;
             e.w = wb[j];
             e.slot = (int)(16 + j);
+            e.tridiag_only = dm <= kTridiagE2MaxN;   // E2 from the tridiagonal form
             eb.push_back(e);
         }
         heev_values_batched(c, eb);
@@ -615,13 +631,17 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             red[j] = nullptr;
             if (dimm[j] == 0 || g.nouter == 0) continue;
             const int dm = dimm[j];
-            cplx *W = wsget<cplx>(c, nm("gj.W", j), (size_t)dm * dm);
-            heev_vectors_slot(c, (int)(16 + j), dm, Bp[j], dm, 0, dm, W, dm);
-            cplx *VC1 = wsget<cplx>(c, nm("gj.VC1", j), (size_t)dm * g.nouter);
-            zgemm(c, OP_C, OP_N, dm, g.nouter, dm, one, W, dm, 0, VC0[j], dm, 0, zero, VC1, dm, 0, 1);
             double *e2o = wsget<double>(c, nm("gj.e2o", j), g.nouter);
             double *sco = wsget<double>(c, nm("gj.sco", j), g.nouter);
-            launch_e2(c, VC1, dm, g.nouter, g.alpha, wb[j], e2o, sco);
+            if (dm <= kTridiagE2MaxN) {
+                tridiag_e2(c, (int)(16 + j), dm, Bp[j], dm, VC0[j], dm, g.nouter, g.alpha, e2o, sco);
+            } else {
+                cplx *W = wsget<cplx>(c, nm("gj.W", j), (size_t)dm * dm);
+                heev_vectors_slot(c, (int)(16 + j), dm, Bp[j], dm, 0, dm, W, dm);
+                cplx *VC1 = wsget<cplx>(c, nm("gj.VC1", j), (size_t)dm * g.nouter);
+                zgemm(c, OP_C, OP_N, dm, g.nouter, dm, one, W, dm, 0, VC0[j], dm, 0, zero, VC1, dm, 0, 1);
+                launch_e2(c, VC1, dm, g.nouter, g.alpha, wb[j], e2o, sco);
+            }
             red[j] = wsget<double>(c, nm("gj.red", j), 2);
             dsum(c, e2o, g.nouter, red[j]);
             dsum(c, sco, g.nouter, red[j] + 1);

@@ -202,6 +202,7 @@ struct EigJob {
     int64_t lda = 0;
     double *w = nullptr;
     int slot = 0;
+    bool tridiag_only = false;   // stop after the reduction: for tridiag_e2 (w is not written)
 };
 void heev_values_batched(Context &c, const std::vector<EigJob> &jobs);
 void heev_vectors_slot(Context &c, int slot, int n, cplx *A, int64_t lda, int vlo, int vhi, cplx *Z, int64_t ldz);
@@ -222,6 +223,16 @@ int split_error(Context &c);
 // Symmetric tridiagonal eigendecomposition by divide and conquer (d: n, e: n-1, device);
 // ascending eigenvalues into w, eigenvectors returned (n x n, ld n, workspace-owned).
 const double *stedc(Context &c, int n, const double *d, const double *e, double *w);
+
+// Largest B' dimension that tridiag_e2 takes (the reflections hold a column in registers).
+constexpr int kTridiagE2MaxN = 1024;
+// E2 terms of a B' matrix reduced to tridiagonal form T (B' = Q T Q^H) in `slot` by a
+// tridiag_only job, without its eigendecomposition: with y_o = Q^H VC[:, o] (VC: n x nouter),
+//   e2o[o] = -Re y_o^H (T + alpha_o)^-1 y_o,   sco[o] = |(T + alpha_o)^-1 y_o|^2,
+// which equal the reference's -sum_m |W^H v|_m^2 / (alpha + w_m) and sum_m |W^H v|_m^2 /
+// (alpha + w_m)^2 over the eigenpairs (w_m, W) of B'.  n <= kTridiagE2MaxN.
+void tridiag_e2(Context &c, int slot, int n, const cplx *A, int64_t lda, const cplx *VC, int64_t ldvc, int nouter,
+                const double *alpha, double *e2o, double *sco);
 
 // Solve A x = b (n x n, LU with partial pivoting), b overwritten.  Returns info.
 int zgesv(Context &c, int n, cplx *A, int64_t lda, cplx *b);

@@ -1411,10 +1411,149 @@ void heev_values_batched(Context &c, const std::vector<EigJob> &jobs) {
     {
         FamScope f2(c, DCG_FAM_EIG_VAL, work / 4.0);
         for (size_t q = 0; q < jobs.size(); q++)
-            if (jobs[q].n > 0) tridiag_dc(c, jobs[q].n, hw[q].d, hw[q].e, jobs[q].w, jobs[q].slot);
+            if (jobs[q].n > 0 && !jobs[q].tridiag_only)
+                tridiag_dc(c, jobs[q].n, hw[q].d, hw[q].e, jobs[q].w, jobs[q].slot);
     }
     for (const EigJob &j : jobs)
-        if (j.n > 0) check_dc_status(c, j.slot);
+        if (j.n > 0 && !j.tridiag_only) check_dc_status(c, j.slot);
+}
+
+// y <- Q^H y for the columns of Y0 (written to Y), Q = H_0 H_1 ... H_{n-2} the reflectors of a
+// tridiagonal reduction (H_k = I - tau_k v_k v_k^H, v_k in column k of A below the diagonal):
+// H_0^H first.  One warp per column, the column in registers (R = ceil(n / 32)).
+template <int R>
+__global__ void __launch_bounds__(64) apply_qh_kernel(int n, const cplx *__restrict__ A, int64_t lda,
+                                                     const cplx *__restrict__ tau, const cplx *__restrict__ Y0,
+                                                     int64_t ldy0, int ncol, cplx *Y, int64_t ldy) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int col = blockIdx.x * 2 + warp;
+    if (col >= ncol) return;   // whole warp
+    cplx z[R];
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int r = lane + 32 * i;
+        z[i] = r < n ? Y0[r + (int64_t)col * ldy0] : mk(0.0, 0.0);
+    }
+    for (int k = 0; k + 1 < n; k++) {
+        const cplx t = __ldg(tau + k);
+        if (t.x == 0.0 && t.y == 0.0) continue;
+        const int i0 = (k + 1) >> 5;
+        const cplx *vk = A + (int64_t)k * lda;
+        double sr = 0.0, si = 0.0;
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            if (i < i0) continue;
+            const int r = lane + 32 * i;
+            const cplx vv = (r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
+            sr = fma(vv.x, z[i].x, fma(vv.y, z[i].y, sr));    // conj(v) z
+            si = fma(vv.x, z[i].y, fma(-vv.y, z[i].x, si));
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            sr += __shfl_xor_sync(0xffffffffu, sr, o);
+            si += __shfl_xor_sync(0xffffffffu, si, o);
+        }
+        const double fr = t.x * sr + t.y * si, fi = t.x * si - t.y * sr;   // f = conj(tau) (v^H z)
+#pragma unroll
+        for (int i = 0; i < R; i++) {
+            if (i < i0) continue;
+            const int r = lane + 32 * i;
+            const cplx vv = (r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
+            z[i].x = fma(-vv.x, fr, fma(vv.y, fi, z[i].x));   // z -= v f
+            z[i].y = fma(-vv.x, fi, fma(-vv.y, fr, z[i].y));
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < R; i++) {
+        const int r = lane + 32 * i;
+        if (r < n) Y[r + (int64_t)col * ldy] = z[i];
+    }
+}
+
+// Per outer index o (one thread): solve (T + alpha_o) z = y_o by Gaussian elimination with
+// partial pivoting on the tridiagonal (Golub & Van Loan, Matrix Computations, 4th ed., 4.3:
+// row interchanges add one superdiagonal of fill-in), then e2o = -Re y^H z, sco = |z|^2.
+// T: diagonal d (n), off-diagonal e (n-1), real.  The eliminated rows go to per-thread scratch
+// laid out [row * nouter + o] (coalesced across threads).
+__global__ void tridiag_solve_e2_kernel(int n, const double *__restrict__ d, const double *__restrict__ e,
+                                        const cplx *__restrict__ Y, int64_t ldy, int nouter,
+                                        const double *__restrict__ alpha, double *D, double *U, double *U2, cplx *B,
+                                        double *e2o, double *sco) {
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= nouter) return;
+    const double al = alpha[o];
+    const cplx *y = Y + (int64_t)o * ldy;
+#define IX(k) ((int64_t)(k) * nouter + o)
+    double dcur = d[0] + al, ucur = n > 1 ? e[0] : 0.0;
+    cplx bcur = y[0];
+    for (int i = 0; i + 1 < n; i++) {
+        double dn = d[i + 1] + al;
+        double un = (i + 2 < n) ? e[i + 1] : 0.0;
+        cplx bn = y[i + 1];
+        const double dl = e[i];
+        double u2 = 0.0;
+        if (fabs(dcur) >= fabs(dl)) {   // pivot on row i
+            const double f = dl / dcur;
+            dn = fma(-f, ucur, dn);
+            bn = mk(fma(-f, bcur.x, bn.x), fma(-f, bcur.y, bn.y));
+        } else {                        // rows i and i+1 exchanged
+            const double f = dcur / dl;
+            const double newu = dn;
+            dn = fma(-f, dn, ucur);
+            u2 = un;
+            un = -f * un;
+            const cplx nb = mk(fma(-f, bn.x, bcur.x), fma(-f, bn.y, bcur.y));
+            bcur = bn;
+            bn = nb;
+            dcur = dl;
+            ucur = newu;
+        }
+        D[IX(i)] = dcur;
+        U[IX(i)] = ucur;
+        U2[IX(i)] = u2;
+        B[IX(i)] = bcur;
+        dcur = dn;
+        ucur = un;
+        bcur = bn;
+    }
+    // back substitution, with the two sums
+    double er = 0.0, s = 0.0;
+    cplx z1 = mk(bcur.x / dcur, bcur.y / dcur), z2 = mk(0.0, 0.0);
+    er += y[n - 1].x * z1.x + y[n - 1].y * z1.y;
+    s += z1.x * z1.x + z1.y * z1.y;
+    for (int i = n - 2; i >= 0; i--) {
+        const double di = D[IX(i)], ui = U[IX(i)], u2i = U2[IX(i)];
+        const cplx bi = B[IX(i)];
+        const cplx zi = mk((bi.x - ui * z1.x - u2i * z2.x) / di, (bi.y - ui * z1.y - u2i * z2.y) / di);
+        er += y[i].x * zi.x + y[i].y * zi.y;
+        s += zi.x * zi.x + zi.y * zi.y;
+        z2 = z1;
+        z1 = zi;
+    }
+#undef IX
+    e2o[o] = -er;
+    sco[o] = s;
+}
+
+void tridiag_e2(Context &c, int slot, int n, const cplx *A, int64_t lda, const cplx *VC, int64_t ldvc, int nouter,
+                const double *alpha, double *e2o, double *sco) {
+    if (n <= 0 || nouter <= 0) return;
+    if (n > kTridiagE2MaxN) throw Error{DCG_E_ARG, "tridiag_e2: dimension above the register limit"};
+    HeevWork h = heev_work(c, n, slot);
+    cplx *Y = wsget<cplx>(c, slot_name("te2.Y", slot), (size_t)n * nouter);
+    FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nouter);
+    const unsigned g = grid1d(nouter, 2);
+    if (n <= 256) apply_qh_kernel<8><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+    else if (n <= 512) apply_qh_kernel<16><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+    else apply_qh_kernel<32><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+    DCG_LAUNCHED(c);
+    const size_t sz = (size_t)n * nouter;
+    double *D = wsget<double>(c, slot_name("te2.D", slot), sz);
+    double *U = wsget<double>(c, slot_name("te2.U", slot), sz);
+    double *U2 = wsget<double>(c, slot_name("te2.U2", slot), sz);
+    cplx *B = wsget<cplx>(c, slot_name("te2.B", slot), sz);
+    tridiag_solve_e2_kernel<<<grid1d(nouter, 64), 64, 0, c.stream>>>(n, h.d, h.e, Y, n, nouter, alpha, D, U, U2, B,
+                                                                      e2o, sco);
+    DCG_LAUNCHED(c);
 }
 
 // Eigenvectors [vlo, vhi) of the matrix reduced in slot `slot` by heev_values_batched (its
