@@ -297,10 +297,67 @@ def run_ours(args, cfg_name):
                                           "(oracle/), host BLAS threads = all cores",
                                 "abs_diff_total_energy": abs(r.total_energy - e_tot),
                                 "max_abs_dE2_subspace": max(abs(r.e2[k] - e2_last[k]) for k in r.e2)}
+    ses.close()
+    del dev, hb_dev
+    torch.cuda.empty_cache()
+    if args.serve_requests > 0:
+        line["serve"] = serve_leg(args, local, world)
     if rank == 0:
         print(json.dumps(line), flush=True)
-    ses.close()
     return 0
+
+
+def serve_leg(args, local, world):
+    """The served-stream configuration: Poisson arrivals (mean args.serve_rate/s) of
+    args.serve_requests independent synthetic systems (per-request seeds; active 4-12 spinors
+    half filled, inactive 4-24, secondary 60-400, complex), generated on the device with their
+    records resident in HBM, run through the library's serving loop (dcg_server, args.serve_slots
+    slots).  Reports solves/s over the stream and the latency percentiles (submit to result),
+    and checks that the first requests give the same energies alone as in the mix."""
+    import torch
+    from dirac_caspt2_gb300 import api, replicas, serve, synth_device as sd
+    prec = api.DCG_PREC_SPLIT if args.precision == "split" else api.DCG_PREC_FP64
+    cfgs = sd.stream_configs(args.serve_requests, seed=0)
+    t0 = time.perf_counter()
+    systems = [sd.make_system_device(c, f"cuda:{local}") for c in cfgs]
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    gen_s = time.perf_counter() - t0
+    bufs = [s.buffers() for s in systems]
+    arrivals = serve.poisson_arrivals(len(bufs), args.serve_rate, seed=1)
+    with api.Caspt2Server(local, prec, args.serve_slots) as srv:
+        nw = min(2 * args.serve_slots, len(bufs))      # untimed: workspaces and module load
+        for k in range(nw):
+            srv.submit(2**40 + k, bufs[k])
+        for _ in range(nw):
+            while srv.poll(1000) is None:
+                pass
+        replicas.barrier()
+        rep = serve.run_stream(srv, list(enumerate(bufs)), arrivals)
+        worst = 0.0
+        nchk = min(8, len(bufs))
+        for k in range(nchk):
+            srv.submit(10**6 + k, bufs[k])
+            r = None
+            while r is None:
+                r = srv.poll(1000)
+            worst = max(worst, serve.max_result_difference(r, rep.results[k]))
+        dev_gb = srv.device_bytes() / 1e9
+    (mk,) = replicas.max_over_ranks([rep.makespan_s])
+    out = {"workload": "poisson stream of independent synthetic systems", "requests": rep.requests,
+           "rate_hz": args.serve_rate, "slots": args.serve_slots, "precision": args.precision,
+           "value": world * (rep.requests - rep.failed) / mk, "unit": "solves/s", "failed": rep.failed,
+           "p50_ms": rep.latency["p50_ms"], "p99_ms": rep.latency["p99_ms"], "mean_ms": rep.latency["mean_ms"],
+           "queue_wait_p50_ms": rep.queue_wait["p50_ms"], "service_p50_ms": rep.service["p50_ms"],
+           "service_p99_ms": rep.service["p99_ms"], "max_concurrent": rep.max_running, "makespan_s": mk,
+           "generate_s": round(gen_s, 2),
+           "resident_record_gb": round(sum(s.record_bytes for s in systems) / 1e9, 2),
+           "server_workspace_gb": round(dev_gb, 2),
+           "alone_vs_mix_max_abs_dE": worst, "alone_checked": nchk,
+           "sizes": "nact in {4,6,8,10,12} (nelec = nact/2), ninact 4-24, nsec 60-400 (even), per-request seeds"}
+    del bufs, systems
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -315,6 +372,10 @@ def main():
                     help="kernel family timed live for the roofline (default: split_mma, or transform for fp64)")
     ap.add_argument("--no-fp64-compare", action="store_true", help="skip the plain FP64 GPU comparison leg")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--serve-requests", type=int, default=256,
+                    help="requests of the served-stream leg (0 skips it)")
+    ap.add_argument("--serve-rate", type=float, default=20.0, help="mean Poisson arrival rate of the stream (1/s)")
+    ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the serving loop")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args, args.config)

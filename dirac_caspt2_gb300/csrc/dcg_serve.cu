@@ -28,12 +28,15 @@ struct Request {
     int attempts = 0;
 };
 
-// Device footprint of one solve (bytes), from its dimensions.  Terms: the record stream
-// (indices, values, packed values), the active/inactive two-electron block, the fourteen
-// integral classes with their transformed copies, the CASCI matrix and CI rotation (ndet^2),
-// the densities of the full determinant space (E_pq psi and E_pq E_rs psi), the subspace
-// matrices (up to na^3 x na^3 for A and C) and Gram factors (C(na, ne+-1) rows), and the
-// eigensolver slots; scaled by a margin measured against dcg_device_bytes.
+// Device footprint of one solve (bytes), from its dimensions, for either precision.  Terms:
+// the record stream (indices, values, packed values), the active/inactive two-electron block,
+// the fourteen integral classes with their transformed copies, the CASCI matrix and CI
+// rotation (ndet^2), the densities of the full determinant space (E_pq psi and E_pq E_rs psi
+// for the state and its orbital-energy-weighted copy), the subspace matrices (up to
+// na^3 x na^3 for A and C), the Gram factors (C(na, ne+-1) rows) and the eigensolver slots; on
+// the split path also the BF16 slices of the largest class and of the density operand.  The
+// 1.25 margin keeps it above dcg_device_bytes of a fresh context on every size measured (4 to
+// 40 inactive, 4 to 14 active, 60 to 800 secondary spinors: 1.15 to 1.7 times the use).
 double binom(int n, int k) {
     if (k < 0 || k > n) return 0.0;
     double r = 1.0;
@@ -44,17 +47,26 @@ double binom(int n, int k) {
 int64_t footprint(const dcg_system &s) {
     const double ni = s.ninact, na = s.nact, ns = s.nsec, nmoc = ni + na;
     const double z = 16.0;   // complex128
-    const double cls = ns * (na * na * na + 2.0 * na * ni * ni + 2.0 * ni * na * na + ni * ni * ni + ni * na * ni) +
-                       ns * ns * (3.0 * na * na + ni * na + ni * ni + 2.0 * ni);
+    const double sizes[] = {ns * na * na * na, ns * na * ni * ni, ns * ni * ni * na, ns * ni * na * na,
+                            ns * na * na * ni, ns * ni * ni * ni, ns * ni * na * ni, ns * na * ns * na,
+                            ns * ni * ns * na, ns * ni * ns * ni, ns * ns * na * na, ns * na * na * ns,
+                            ns * ns * ni, ns * ns * ni};
+    double cls = 0.0, largest = 0.0;
+    for (double x : sizes) {
+        cls += x;
+        largest = std::max(largest, x);
+    }
     const double ndet = binom(s.nact, s.nelec);
     const double mp = std::max(binom(s.nact, s.nelec + 1), binom(s.nact, s.nelec - 1));
-    const double n3 = na * na * na;
+    const double n3 = na * na * na, na2 = na * na;
+    const double dens = z * ndet * 2.0 * (na2 * na2 + na2);   // E_pq psi and E_pq E_rs psi, two vectors
     double b = 48.0 * (double)s.nrec + z * nmoc * nmoc * nmoc * nmoc + 2.0 * z * cls;
-    b += 3.0 * z * ndet * ndet;                              // CASCI matrix, vectors, CI rotation
-    b += z * ndet * (na * na * na * na + 3.0 * na * na);    // densities
-    b += 10.0 * z * n3 * n3;                                 // S, B, X, BX, B', W of the largest block
-    b += 6.0 * z * mp * (mp + n3);                           // Gram factor, metric, P, PD
-    b += 64.0 * 1024.0 * 1024.0;                             // eigensolver slots, reductions
+    b += 3.0 * z * ndet * ndet;         // CASCI matrix, vectors, CI rotation
+    b += dens;
+    b += 10.0 * z * n3 * n3;            // S, B, X, BX, B', W of the largest block
+    b += 6.0 * z * mp * (mp + n3);      // Gram factor, metric, P, PD
+    b += 64.0 * 1024.0 * 1024.0;        // eigensolver slots, reductions
+    b += 1.3 * z * largest + 0.7 * dens;   // split-precision slices
     return (int64_t)(1.25 * b);
 }
 

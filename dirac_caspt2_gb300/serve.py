@@ -135,13 +135,13 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--requests", type=int, default=256)
     ap.add_argument("--rate", type=float, default=20.0, help="mean arrivals per second")
-    ap.add_argument("--slots", type=int, default=4)
-    ap.add_argument("--precision", default="split", choices=["fp64", "split"])
+    ap.add_argument("--slots", default="4", help="slot counts to run the stream with, comma separated")
+    ap.add_argument("--precision", default="split", help="fp64, split or both (comma separated)")
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--hbm-budget-gb", type=float, default=0.0, help="0: 90%% of the free memory after generation")
     ap.add_argument("--max-nsec", type=int, default=400)
     ap.add_argument("--check-alone", type=int, default=0)
-    ap.add_argument("--warmup", type=int, default=4, help="requests run before the stream (untimed)")
+    ap.add_argument("--warmup", type=int, default=2, help="requests per slot run before the stream (untimed)")
     a = ap.parse_args(argv)
     import torch
     from . import synth_device as sd
@@ -149,33 +149,39 @@ def main(argv: Optional[Sequence[str]] = None) -> int:
     t0 = time.perf_counter()
     systems = [sd.make_system_device(c, "cuda") for c in cfgs]
     torch.cuda.synchronize()
+    torch.cuda.empty_cache()
     gen_s = time.perf_counter() - t0
     bufs = [s.buffers() for s in systems]
     rec_gb = sum(s.record_bytes for s in systems) / 1e9
-    prec = api.DCG_PREC_SPLIT if a.precision == "split" else api.DCG_PREC_FP64
-    with api.Caspt2Server(0, prec, a.slots, int(a.hbm_budget_gb * 1e9)) as srv:
-        for k in range(min(a.warmup, len(bufs))):   # warm the slots' workspaces and kernels
-            for w in range(a.slots):
-                srv.submit(2**40 + k * a.slots + w, bufs[k])
-        for _ in range(min(a.warmup, len(bufs)) * a.slots):
-            while srv.poll(1000) is None:
-                pass
-        arrivals = poisson_arrivals(a.requests, a.rate, a.seed + 1)
-        rep = run_stream(srv, list(enumerate(bufs)), arrivals)
-        out = {"stream": "poisson", "rate_hz": a.rate, "slots": a.slots, "precision": a.precision,
-               "generate_s": round(gen_s, 2), "resident_record_gb": round(rec_gb, 2), **rep.summary()}
-        if a.check_alone > 0:
-            worst = 0.0
-            for k in range(min(a.check_alone, a.requests)):
-                srv.submit(10**6 + k, bufs[k])
-                r = None
-                while r is None:
-                    r = srv.poll(1000)
-                worst = max(worst, max_result_difference(r, rep.results[k]))
-            out["alone_vs_mix_max_abs_diff"] = worst
-            out["alone_checked"] = min(a.check_alone, a.requests)
-    print(json.dumps(out))
-    return 0 if rep.failed == 0 else 1
+    arrivals = poisson_arrivals(a.requests, a.rate, a.seed + 1)
+    failed = 0
+    for prec_name in a.precision.split(","):
+        prec = api.DCG_PREC_SPLIT if prec_name == "split" else api.DCG_PREC_FP64
+        for slots in (int(x) for x in a.slots.split(",")):
+            with api.Caspt2Server(0, prec, slots, int(a.hbm_budget_gb * 1e9)) as srv:
+                nw = min(a.warmup * slots, len(bufs))   # warm the slots' workspaces and kernels
+                for k in range(nw):
+                    srv.submit(2**40 + k, bufs[k])
+                for _ in range(nw):
+                    while srv.poll(1000) is None:
+                        pass
+                rep = run_stream(srv, list(enumerate(bufs)), arrivals)
+                out = {"stream": "poisson", "rate_hz": a.rate, "slots": slots, "precision": prec_name,
+                       "generate_s": round(gen_s, 2), "resident_record_gb": round(rec_gb, 2),
+                       "server_device_gb": round(srv.device_bytes() / 1e9, 2), **rep.summary()}
+                if a.check_alone > 0:
+                    worst = 0.0
+                    for k in range(min(a.check_alone, a.requests)):
+                        srv.submit(10**6 + k, bufs[k])
+                        r = None
+                        while r is None:
+                            r = srv.poll(1000)
+                        worst = max(worst, max_result_difference(r, rep.results[k]))
+                    out["alone_vs_mix_max_abs_diff"] = worst
+                    out["alone_checked"] = min(a.check_alone, a.requests)
+            failed += rep.failed
+            print(json.dumps(out), flush=True)
+    return 0 if failed == 0 else 1
 
 
 if __name__ == "__main__":

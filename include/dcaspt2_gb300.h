@@ -216,7 +216,8 @@ int64_t dcg_device_bytes(const dcg_ctx *ctx);
  * dcg_set_system again. */
 int dcg_trim(dcg_ctx *ctx);
 /* Upper estimate of the device bytes one set_system + casci + caspt2 of sys needs in a fresh
- * context (the admission size of the serving loop; host pointers of sys are not read). */
+ * context of either precision (the admission size of the serving loop; host pointers of sys
+ * are not read). */
 int64_t dcg_footprint_estimate(const dcg_system *sys);
 
 /* ------------------------------------------------------------------------ serving loop

@@ -112,6 +112,23 @@ def test_footprint_estimate_bounds(stream):
             assert 0 < used <= est, (s.cfg, used, est)
 
 
+@pytest.mark.parametrize("dims", [(24, 4, 400, 2), (4, 12, 60, 6)])
+def test_footprint_estimate_bounds_larger(gpu_lib, dims):
+    """The same bound on a large secondary space (its split slices) and on 12 active spinors
+    (their densities)."""
+    import torch
+    from dirac_caspt2_gb300 import api, synth, synth_device as sd
+    s = sd.make_system_device(synth.SynthConfig(*dims, seed=3), "cuda")
+    torch.cuda.synchronize()
+    b = s.buffers()
+    est = api.footprint_estimate(b)
+    for prec in (api.DCG_PREC_FP64, api.DCG_PREC_SPLIT):
+        with api.Caspt2Session(0, prec) as ses:
+            ses.solve(s.system_input(), bufs=b)
+            used = ses.device_bytes()
+        assert 0 < used <= est, (dims, prec, used, est)
+
+
 def test_trim_and_resolve(stream, alone):
     from dirac_caspt2_gb300 import api
     prec, ref = alone
