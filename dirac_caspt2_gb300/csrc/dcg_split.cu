@@ -16,8 +16,7 @@
 //     TMEM accumulators by weight p+q = 2, 3, 4 and >= 5.  The first three stay exact (integer
 //     partial sums below 2^24 for K' <= 1024 real); the last one carries only 2^-21-relative
 //     terms, so its rounding is ~2^-45 of the result;
-//   * the epilogue adds the accumulators as 64-bit integers in 2^-28 fixed point and builds the
-//     double of the sum times 2^(e+f-14) with integer instructions (dcg_fixed.cuh).
+//   * the epilogue adds the accumulators in FP64 and applies 2^(e+f-14).
 // The result carries ~2^-36 of max|row of A| * max|column of B| per term.
 //
 // Data movement: the slicing pre-pass writes both operands directly in the tcgen05 canonical
@@ -31,7 +30,6 @@
 #include <cmath>
 
 #include "dcg_common.cuh"
-#include "dcg_fixed.cuh"
 
 namespace dcg {
 
@@ -413,14 +411,16 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
                     const int jr = nb * SP_TN + c0 + q;   // real column (even: Re)
                     const int j = jr >> 1;
                     if (j >= a.N) break;
-                    // the weight 2-4 groups are exact multiples of 2^-14 and add exactly in 2^-28
-                    // fixed point; the weight >= 5 group rounds there (~2^-43 of the result)
-                    const int64_t xr = fx28_from_float_bits(g0[q]) + fx28_from_float_bits(g1[q]) +
-                                       fx28_from_float_bits(g2[q]) + fx28_from_float_bits(g3[q]);
-                    const int64_t xi = fx28_from_float_bits(g0[q + 1]) + fx28_from_float_bits(g1[q + 1]) +
-                                       fx28_from_float_bits(g2[q + 1]) + fx28_from_float_bits(g3[q + 1]);
-                    const int sc = e + a.fexp[j] - 2 * SPLIT_BITS - 28;   // each operand carries 2^-7
-                    cplx v = mk(fx_to_double(xr, sc), fx_to_double(xi, sc));
+                    // weight-2 and -3 groups are exact; the weight >= 4 groups are 2^-14 of them, so
+                    // their FP32 sum costs ~2^-38 of the result
+                    const double re = (double)__uint_as_float(g0[q]) + (double)__uint_as_float(g1[q]) +
+                                      (double)(__uint_as_float(g2[q]) + __uint_as_float(g3[q]));
+                    const double im = (double)__uint_as_float(g0[q + 1]) + (double)__uint_as_float(g1[q + 1]) +
+                                      (double)(__uint_as_float(g2[q + 1]) + __uint_as_float(g3[q + 1]));
+                    const int sc = e + a.fexp[j] - 2 * SPLIT_BITS;   // each operand carries 2^-7
+                    const double p2 = (sc > -1022 && sc < 1023) ? __longlong_as_double((long long)(sc + 1023) << 52)
+                                                                : ldexp(1.0, sc);
+                    cplx v = mk(re * p2, im * p2);
                     cplx *dst = a.C + (int64_t)z * a.c_sb + i * a.c_si + (int64_t)j * a.c_sj;
                     if (a.accumulate) v = cadd(v, *dst);
                     *dst = v;
