@@ -346,7 +346,7 @@ def serve_leg(args, local, world):
     (mk,) = replicas.max_over_ranks([rep.makespan_s])
     out = {"workload": "poisson stream of independent synthetic systems", "requests": rep.requests,
            "rate_hz": args.serve_rate, "slots": args.serve_slots, "precision": args.precision,
-           "value": world * (rep.requests - rep.failed) / mk, "unit": "solves/s", "failed": rep.failed,
+           "value": world * (rep.requests - rep.failed) / mk, "unit": "solves/s", "failed": rep.failed, "failures": rep.failures[:8],
            "p50_ms": rep.latency["p50_ms"], "p99_ms": rep.latency["p99_ms"], "mean_ms": rep.latency["mean_ms"],
            "queue_wait_p50_ms": rep.queue_wait["p50_ms"], "service_p50_ms": rep.service["p50_ms"],
            "service_p99_ms": rep.service["p99_ms"], "max_concurrent": rep.max_running, "makespan_s": mk,

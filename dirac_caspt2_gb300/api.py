@@ -62,7 +62,7 @@ class _RequestResult(ctypes.Structure):
         ("casci_energy", ctypes.c_double), ("e2", ctypes.c_double * 8), ("sumc2", ctypes.c_double * 8),
         ("e0", ctypes.c_double), ("etotal", ctypes.c_double), ("t_submit", ctypes.c_double),
         ("t_start", ctypes.c_double), ("t_end", ctypes.c_double), ("slot", ctypes.c_int32),
-        ("attempts", ctypes.c_int32),
+        ("attempts", ctypes.c_int32), ("error", ctypes.c_char * 96),
     ]
 
 
@@ -510,6 +510,7 @@ class ServedResult:
     t_end: float
     slot: int
     attempts: int
+    error: str = ""
 
     @property
     def latency(self) -> float:
@@ -562,7 +563,8 @@ class Caspt2Server:
                             e2={k: float(r.e2[i]) for i, k in enumerate(SUBSPACES)},
                             sumc2={k: float(r.sumc2[i]) for i, k in enumerate(SUBSPACES)}, e0=float(r.e0),
                             total_energy=float(r.etotal), t_submit=float(r.t_submit), t_start=float(r.t_start),
-                            t_end=float(r.t_end), slot=int(r.slot), attempts=int(r.attempts))
+                            t_end=float(r.t_end), slot=int(r.slot), attempts=int(r.attempts),
+                            error=r.error.decode(errors="replace"))
 
     def pending(self) -> Tuple[int, int]:
         q = ctypes.c_int32(0)

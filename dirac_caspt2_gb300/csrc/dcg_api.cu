@@ -242,7 +242,7 @@ static void set_system(Context &c, const dcg_system *s) {
 // ------------------------------------------------------------------------- CASCI
 // The dense eigensolver below kDavidsonMinDet determinants or for many roots; block Davidson
 // on the resident Hamiltonian above it.
-constexpr int kDavidsonMinDet = 400;
+constexpr int kDavidsonMinDet = 2000;
 constexpr int kDavidsonMaxRoots = 12;
 
 static bool use_davidson(const Context &c, int ndet, int nvec) {
@@ -352,13 +352,18 @@ struct BlockOut {
     int dimm = 0;
 };
 
+// Whether the E2 terms of a B' block come from its tridiagonal form (tridiag_e2) rather than
+// its eigendecomposition: up to kTridiagE2MaxN, and when the outer index is not much longer
+// than B' (the per-outer-index solves stream 5 words per element of VC through scratch; the
+// eigenvector route reads VC once after one GEMM).
+static bool tridiag_e2_pays(int dimm, int nouter) { return dimm <= kTridiagE2MaxN && nouter <= 2 * dimm; }
+
 // Per outer index o: e2o = -sum_m |(W^H VC)_m,o|^2 / (alpha_o + w_m) and sco = sum_m
 // |(W^H VC)_m,o|^2 / (alpha_o + w_m)^2 over the eigenpairs (w, W) of B' (dimm x dimm, destroyed;
-// VC: dimm x nouter), as the reference's solve_X_subspace evaluates them.  Up to
-// kTridiagE2MaxN they come from the tridiagonal form of B' (tridiag_e2: no eigenvectors).
+// VC: dimm x nouter), as the reference's solve_X_subspace evaluates them.
 static void e2_from_bprime(Context &c, int dimm, cplx *Bp, const cplx *VC, int nouter, const double *alpha,
                            double *e2o, double *sco) {
-    if (dimm <= kTridiagE2MaxN) {
+    if (tridiag_e2_pays(dimm, nouter)) {
         EigJob e;
         e.n = dimm;
         e.A = Bp;
@@ -622,7 +627,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             e.lda = dm;
             e.w = wb[j];
             e.slot = (int)(16 + j);
-            e.tridiag_only = dm <= kTridiagE2MaxN;   // E2 from the tridiagonal form
+            e.tridiag_only = tridiag_e2_pays(dm, g.nouter);   // E2 from the tridiagonal form
             eb.push_back(e);
         }
         heev_values_batched(c, eb);
@@ -633,7 +638,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             const int dm = dimm[j];
             double *e2o = wsget<double>(c, nm("gj.e2o", j), g.nouter);
             double *sco = wsget<double>(c, nm("gj.sco", j), g.nouter);
-            if (dm <= kTridiagE2MaxN) {
+            if (tridiag_e2_pays(dm, g.nouter)) {
                 tridiag_e2(c, (int)(16 + j), dm, Bp[j], dm, VC0[j], dm, g.nouter, g.alpha, e2o, sco);
             } else {
                 cplx *W = wsget<cplx>(c, nm("gj.W", j), (size_t)dm * dm);

@@ -150,6 +150,10 @@ void worker_loop(dcg_server *sv, int w) {
         res.t_start = now_s();
         int st = run_request(c, rq, res);
         res.status = st;
+        if (st != DCG_OK) {
+            const char *msg = dcg_last_error(c);
+            std::strncpy(res.error, msg ? msg : "", sizeof(res.error) - 1);
+        }
         res.t_end = now_s();
         if (st == DCG_E_NOMEM) dcg_trim(c);   // the estimate was short or another slot grew: retry once
         {

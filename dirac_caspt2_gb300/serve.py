@@ -63,8 +63,14 @@ class StreamReport:
     max_running: int
     results: Dict[int, api.ServedResult]
 
+    @property
+    def failures(self) -> List[Tuple[int, int, str]]:
+        """(request id, status, message) of every failed request."""
+        return [(r.request_id, r.status, r.error) for r in self.results.values() if r.status != 0]
+
     def summary(self) -> Dict[str, object]:
-        return {"requests": self.requests, "failed": self.failed, "solves_per_s": self.solves_per_s,
+        return {"requests": self.requests, "failed": self.failed, "failures": self.failures[:8],
+                "solves_per_s": self.solves_per_s,
                 "makespan_s": self.makespan_s, **self.latency,
                 "queue_wait_p50_ms": self.queue_wait["p50_ms"], "queue_wait_p99_ms": self.queue_wait["p99_ms"],
                 "service_p50_ms": self.service["p50_ms"], "service_p99_ms": self.service["p99_ms"],

@@ -199,7 +199,7 @@ int dcg_time_family(dcg_ctx *ctx, int32_t family);
 int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work);
 
 /* CASCI eigensolver of dcg_casci.  AUTO: dense Householder + divide-and-conquer (the ZHEEV
- * of diag.F90:66-128) below 400 determinants or for more than 12 roots, block Davidson on the
+ * of diag.F90:66-128) below 2000 determinants or for more than 12 roots, block Davidson on the
  * resident Hamiltonian otherwise (residual norms <= 1e-13 max(1, max |H_ii|) for every
  * returned root).  DENSE / DAVIDSON force one of them (DAVIDSON needs ndet >= roots + 5). */
 #define DCG_CASCI_AUTO 0
@@ -241,6 +241,7 @@ typedef struct dcg_request_result {
     double t_submit, t_start, t_end;   /* seconds on the server clock (dcg_server_clock)  */
     int32_t slot;            /* worker slot that ran the request                          */
     int32_t attempts;        /* 1, or 2 when a first attempt ran out of device memory     */
+    char error[96];          /* the failing call's dcg_last_error (empty on success)      */
 } dcg_request_result;
 
 /* slots in 1..64; hbm_budget_bytes <= 0 takes 90% of the device's free memory at creation. */

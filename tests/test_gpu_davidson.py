@@ -63,17 +63,21 @@ def test_davidson_degenerate_roots(gpu_lib):
     assert abs(ev[0] - ev[1]) <= TOL_E and abs(ev[2] - ev[3]) <= TOL_E
 
 
-def test_auto_uses_davidson_at_924(gpu_lib):
-    """AUTO at 924 determinants takes Davidson and gives the dense result (the route of the
-    20/12/300 solve)."""
+def test_auto_picks_by_size(gpu_lib):
+    """AUTO: dense at 924 determinants (the 20/12/300 CASCI), Davidson at 3003, both equal to
+    the dense roots."""
     from dirac_caspt2_gb300 import api, synth
-    S = synth.make_system(synth.SynthConfig(2, 12, 6, 6, seed=8))
-    s = api.SystemInput.from_synth(S)
-    d = _solve(s, "dense")
-    a = _solve(s, "auto")
-    assert a[6] > 0
-    assert abs(d[0][0] - a[0][0]) <= TOL_E
-    assert abs(d[5] - a[5]) <= TOL_E2
+    for dims, want_dav in (((2, 12, 6, 6), False), ((2, 14, 4, 8), True)):
+        S = synth.make_system(synth.SynthConfig(*dims, seed=8))
+        s = api.SystemInput.from_synth(S)
+        with api.Caspt2Session(0) as ses:
+            ses.set_system(s)
+            ses.set_casci_solver("dense")
+            ed, _ = ses.casci(2)
+            ses.set_casci_solver("auto")
+            ea, _ = ses.casci(2)
+            assert (ses.casci_iterations() > 0) == want_dav
+        assert np.abs(ed - ea).max() <= TOL_E
 
 
 def test_solver_option_rejects_bad_values(gpu_lib):

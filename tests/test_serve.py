@@ -163,7 +163,7 @@ int main(void) {
     P(dcg_request_result, casci_energy); P(dcg_request_result, e2); P(dcg_request_result, sumc2);
     P(dcg_request_result, e0); P(dcg_request_result, etotal); P(dcg_request_result, t_submit);
     P(dcg_request_result, t_start); P(dcg_request_result, t_end); P(dcg_request_result, slot);
-    P(dcg_request_result, attempts);
+    P(dcg_request_result, attempts); P(dcg_request_result, error);
     printf("dcg_system size %zu\n", sizeof(dcg_system));
     P(dcg_system, eshift); P(dcg_system, multb); P(dcg_system, nrec); P(dcg_system, rec_im);
     P(dcg_system, ras1_size); P(dcg_system, rec_on_device);
@@ -191,7 +191,7 @@ def test_abi_layout_matches_header(tmp_path):
         else:
             assert getattr(types[t], f).offset == int(v), line
         checked += 1
-    assert checked == 21
+    assert checked == 22
 
 
 def test_footprint_estimate_host_only():
