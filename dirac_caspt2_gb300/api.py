@@ -27,6 +27,7 @@ LIB_PATH = os.path.join(_HERE, "libdcaspt2_gb300.so")
 DCG_PREC_FP64 = 0
 DCG_PREC_SPLIT = 1
 CASCI_SOLVERS = {"auto": 0, "dense": 1, "davidson": 2}
+METRIC_SOLVERS = {"auto": 0, "eigen": 1}
 SUBSPACES = "ABCDEFGH"
 STAGES = ["ints", "casci_matrix", "casci_eig", "fock", "ci_rotation", "rdm", "transformation",
           "A", "B", "C", "D", "E", "F", "G", "H", "AC"]
@@ -115,6 +116,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_set_casci_solver.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_casci_iterations.argtypes = [ctypes.c_void_p]
     lib.dcg_casci_iterations.restype = ctypes.c_int32
+    lib.dcg_set_metric_solver.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.dcg_gram_cholesky_blocks.argtypes = [ctypes.c_void_p]
+    lib.dcg_gram_cholesky_blocks.restype = ctypes.c_int32
     lib.dcg_device_bytes.argtypes = [ctypes.c_void_p]
     lib.dcg_device_bytes.restype = ctypes.c_int64
     lib.dcg_trim.argtypes = [ctypes.c_void_p]
@@ -138,7 +142,8 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
                     "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm",
-                    "dcg_set_casci_solver", "dcg_casci_iterations", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
+                    "dcg_set_casci_solver", "dcg_casci_iterations", "dcg_set_metric_solver",
+                    "dcg_gram_cholesky_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
                     "dcg_server_device_bytes", "dcg_server_destroy"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
@@ -379,6 +384,15 @@ class Caspt2Session:
     def set_casci_solver(self, solver: str) -> None:
         """CASCI eigensolver: "auto", "dense" or "davidson" (dcg_set_casci_solver)."""
         self._check(self.lib.dcg_set_casci_solver(self.h, CASCI_SOLVERS[solver]))
+
+    def set_metric_solver(self, solver: str) -> None:
+        """Gram-route metric of A and C: "auto" (Cholesky when no eigenvalue falls under the
+        cutoff) or "eigen" (dcg_set_metric_solver)."""
+        self._check(self.lib.dcg_set_metric_solver(self.h, METRIC_SOLVERS[solver]))
+
+    def gram_cholesky_blocks(self) -> int:
+        """Gram blocks of the last caspt2 solved by the Cholesky route."""
+        return int(self.lib.dcg_gram_cholesky_blocks(self.h))
 
     def casci_iterations(self) -> int:
         """Davidson iterations of the last casci (0: dense solver)."""

@@ -509,6 +509,45 @@ struct BlockSpec {
 // The reference's 1e-8 cutoff is applied to the eigenvalues of K.  E2 is invariant to the basis
 // chosen inside the kept space, so this reproduces solve_block on (S, B) with an Mp x Mp
 // eigenproblem instead of a dimn x dimn one.
+// Whether every eigenvalue of the Gram metric K (Mp x Mp) lies above the 1e-8 cutoff
+// (cutoff.F90:37-70): then no eigenvector of S is dropped and X spans the whole range of G^H.
+// Decided by inertia: K - 1e-8 I is positive definite exactly then (its Cholesky succeeds).
+static bool metric_above_cutoff(Context &c, int Mp, const cplx *K, int tag) {
+    const std::string t = "#" + std::to_string(tag);
+    cplx *Kt = wsget<cplx>(c, "gram.Kt" + t, (size_t)Mp * Mp);
+    int *info = wsget<int>(c, "gram.info" + t, 1);
+    DCG_CUDA(cudaMemcpyAsync(Kt, K, sizeof(cplx) * (size_t)Mp * Mp, cudaMemcpyDeviceToDevice, c.stream));
+    shift_diag(c, Mp, Kt, Mp, 1.0e-8);
+    zpotrf_lower(c, Mp, Kt, Mp, info);
+    int h = 0;
+    DCG_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    return h == 0;
+}
+
+// E2 terms of a Gram block whose metric K = G G^H keeps all its eigenvalues: with K = P L P^H
+// unitary, X = G^H P L^-1, B' = P^H D P and Xv = L^-1 P^H G v, so
+//   -v~^H (B' + a)^-1 v~ = -u^H (D + a)^-1 u,   |(B' + a)^-1 v~|^2 = |(D + a)^-1 u|^2,
+// u = P v~ = K^-1 G v: one Cholesky solve with K instead of the eigendecompositions of K and
+// B'.  K is destroyed (overwritten by its factor).  e2o, sco: device, nouter entries.
+static void gram_cholesky_e2(Context &c, int Mp, int dimn, const cplx *G, cplx *K, const double *Dd,
+                             const cplx *Vsel, int nouter, const double *alpha, int tag, const double *&e2o_out,
+                             const double *&sco_out) {
+    const std::string t = "#" + std::to_string(tag);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    int *info = wsget<int>(c, "gram.info2" + t, 1);
+    zpotrf_lower(c, Mp, K, Mp, info);
+    cplx *U = wsget<cplx>(c, "gram.U" + t, (size_t)Mp * nouter);
+    zgemm(c, OP_N, OP_N, Mp, nouter, dimn, one, G, Mp, 0, Vsel, dimn, 0, zero, U, Mp, 0, 1);
+    zpotrs_lower(c, Mp, K, Mp, U, Mp, nouter);
+    double *e2o = wsget<double>(c, "gram.e2o" + t, nouter);
+    double *sco = wsget<double>(c, "gram.sco" + t, nouter);
+    launch_e2(c, U, Mp, nouter, alpha, Dd, e2o, sco);
+    c.gram_cholesky_blocks++;
+    e2o_out = e2o;
+    sco_out = sco;
+}
+
 static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, const double *Dd, const cplx *Vsel,
                                  int nouter, const double *alpha) {
     BlockOut r;
@@ -519,6 +558,18 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     cplx *K = wsget<cplx>(c, "gram.K", (size_t)Mp * Mp);
     zherk_upper(c, Mp, dimn, G, Mp, K, Mp);
     herm_from_upper(c, Mp, K, Mp);
+    if (c.metric_solver == DCG_METRIC_AUTO && metric_above_cutoff(c, Mp, K, 0)) {
+        const double *e2o = nullptr, *sco = nullptr;
+        gram_cholesky_e2(c, Mp, dimn, G, K, Dd, Vsel, nouter, alpha, 0, e2o, sco);
+        double *red = wsget<double>(c, "blk.red", 2);
+        dsum(c, e2o, nouter, red);
+        dsum(c, sco, nouter, red + 1);
+        std::vector<double> hr = download(c, red, 2);
+        r.e2 = hr[0];
+        r.sc2 = hr[1];
+        r.dimm = Mp;
+        return r;
+    }
     double *wk = wsget<double>(c, "gram.wk", Mp);
     heev(c, Mp, K, Mp, wk, Mp, Mp, nullptr, Mp);   // values first (cutoff count)
     std::vector<double> wh = download(c, wk, Mp);
@@ -576,11 +627,38 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         std::vector<double *> wk(np), wb(np, nullptr), red(np);
         std::vector<int> vlo(np, 0), dimm(np, 0);
         std::vector<EigJob> ek;
-        for (size_t j = 0; j < np; j++) {
+        std::vector<bool> chol(np, false);
+        std::vector<int> hinfo(np, 1);
+        for (size_t j = 0; j < np; j++) {   // metrics, and (AUTO) their definiteness above the cutoff
             GramJob &g = all[p0 + j];
             K[j] = wsget<cplx>(c, nm("gj.K", j), (size_t)g.Mp * g.Mp);
             zherk_upper(c, g.Mp, g.dimn, g.G, g.Mp, K[j], g.Mp);   // K = G G^H, FP64 (the metric)
             herm_from_upper(c, g.Mp, K[j], g.Mp);
+            if (c.metric_solver == DCG_METRIC_AUTO && g.nouter > 0) {
+                cplx *Kt = wsget<cplx>(c, nm("gj.Kt", j), (size_t)g.Mp * g.Mp);
+                int *info = wsget<int>(c, nm("gj.info", j), 1);
+                DCG_CUDA(cudaMemcpyAsync(Kt, K[j], sizeof(cplx) * (size_t)g.Mp * g.Mp, cudaMemcpyDeviceToDevice,
+                                         c.stream));
+                shift_diag(c, g.Mp, Kt, g.Mp, 1.0e-8);
+                zpotrf_lower(c, g.Mp, Kt, g.Mp, info);
+                DCG_CUDA(cudaMemcpyAsync(&hinfo[j], info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+            }
+        }
+        DCG_CUDA(cudaStreamSynchronize(c.stream));
+        for (size_t j = 0; j < np; j++) {
+            GramJob &g = all[p0 + j];
+            red[j] = nullptr;
+            if (c.metric_solver != DCG_METRIC_AUTO || g.nouter == 0 || hinfo[j] != 0) continue;
+            chol[j] = true;
+            const double *e2o = nullptr, *sco = nullptr;
+            gram_cholesky_e2(c, g.Mp, g.dimn, g.G, K[j], g.Dd, g.Vsel, g.nouter, g.alpha, (int)j, e2o, sco);
+            red[j] = wsget<double>(c, nm("gj.red", j), 2);
+            dsum(c, e2o, g.nouter, red[j]);
+            dsum(c, sco, g.nouter, red[j] + 1);
+        }
+        for (size_t j = 0; j < np; j++) {
+            GramJob &g = all[p0 + j];
+            if (chol[j]) continue;
             wk[j] = wsget<double>(c, nm("gj.wk", j), g.Mp);
             EigJob e;
             e.n = g.Mp;
@@ -593,6 +671,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         heev_values_batched(c, ek);
         std::vector<std::vector<double>> wh(np);
         for (size_t j = 0; j < np; j++) {
+            if (chol[j]) continue;
             wh[j].resize(all[p0 + j].Mp);
             DCG_CUDA(cudaMemcpyAsync(wh[j].data(), wk[j], sizeof(double) * wh[j].size(), cudaMemcpyDeviceToHost,
                                      c.stream));
@@ -601,6 +680,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         std::vector<EigJob> eb;
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
+            if (chol[j]) continue;
             vlo[j] = g.Mp;
             for (int q = 0; q < g.Mp; q++)
                 if (wh[j][q] >= 1.0e-8) { vlo[j] = q; break; }   // cutoff.F90:37-70
@@ -633,6 +713,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         heev_values_batched(c, eb);
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
+            if (chol[j]) continue;
             red[j] = nullptr;
             if (dimm[j] == 0 || g.nouter == 0) continue;
             const int dm = dimm[j];
@@ -799,6 +880,7 @@ namespace dcg {
 
 static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8], double *e0_out, double *et_out) {
     if (!c.have_casci) throw Error{DCG_E_STATE, "dcg_caspt2 before dcg_casci"};
+    c.gram_cholesky_blocks = 0;
     DevSystem &d = dev(c);
     const int ni = c.ni, na = c.na, ns = c.ns, nmoc = ni + na;
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
@@ -1342,6 +1424,14 @@ int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver) {
 }
 
 int32_t dcg_casci_iterations(const dcg_ctx *ctx) { return ctx ? ctx->c.casci_iters : -1; }
+
+int dcg_set_metric_solver(dcg_ctx *ctx, int32_t solver) {
+    if (!ctx || solver < DCG_METRIC_AUTO || solver > DCG_METRIC_EIGEN) return DCG_E_ARG;
+    ctx->c.metric_solver = solver;
+    return DCG_OK;
+}
+
+int32_t dcg_gram_cholesky_blocks(const dcg_ctx *ctx) { return ctx ? ctx->c.gram_cholesky_blocks : -1; }
 
 int64_t dcg_device_bytes(const dcg_ctx *ctx) { return ctx ? (int64_t)ctx->c.ws.bytes_in_use() : -1; }
 

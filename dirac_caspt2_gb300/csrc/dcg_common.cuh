@@ -101,6 +101,10 @@ struct Context {
     // CASCI eigensolver: DCG_CASCI_AUTO, _DENSE or _DAVIDSON (dcg_set_casci_solver)
     int casci_solver = 0;
     int casci_iters = 0;   // Davidson iterations of the last CASCI (0: dense solver)
+    // Gram-route metric: DCG_METRIC_AUTO (Cholesky solve when K - 1e-8 I is positive
+    // definite, else eigendecomposition) or DCG_METRIC_EIGEN (dcg_set_metric_solver)
+    int metric_solver = 0;
+    int gram_cholesky_blocks = 0;   // Gram blocks of the last dcg_caspt2 solved by Cholesky
 
     // ---- system (host copies)
     bool have_system = false;
@@ -246,6 +250,14 @@ void herm_from_upper(Context &c, int n, cplx *A, int64_t lda);
 
 // deterministic sum of n doubles on the device into *out (device)
 void dsum(Context &c, const double *x, int64_t n, double *out);
+
+// Cholesky A = L L^H of a Hermitian matrix (lower triangle, in place; dcg_chol.cu); *info
+// (device) = index + 1 of the first non-positive pivot, 0 when A is positive definite.
+void zpotrf_lower(Context &c, int n, cplx *A, int64_t lda, int *info);
+// A X = B with the factor of zpotrf_lower; B (n x nrhs, ldb) overwritten by X.
+void zpotrs_lower(Context &c, int n, const cplx *L, int64_t lda, cplx *B, int64_t ldb, int nrhs);
+// A_ii -= s
+void shift_diag(Context &c, int n, cplx *A, int64_t lda, double s);
 
 // Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);

@@ -209,6 +209,18 @@ int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver);
 /* Davidson iterations of the last dcg_casci (0 when the dense solver ran). */
 int32_t dcg_casci_iterations(const dcg_ctx *ctx);
 
+/* Solver of the A and C blocks that go through the (nelec +- 1)-electron Gram factor G
+ * (S = G^H G, metric K = G G^H).  AUTO: when K - 1e-8 I is positive definite (no eigenvalue
+ * of S above zero falls under the 1e-8 cutoff of cutoff.F90:37-70, so X spans the range of
+ * G^H), E2 and c^2 come from one Cholesky solve u = K^-1 G v as -u^H (D + alpha)^-1 u and
+ * |(D + alpha)^-1 u|^2, equal to the reference's eigenvector sums; otherwise, and always
+ * with EIGEN, from the eigendecompositions of K and B'. */
+#define DCG_METRIC_AUTO 0
+#define DCG_METRIC_EIGEN 1
+int dcg_set_metric_solver(dcg_ctx *ctx, int32_t solver);
+/* Gram blocks the last dcg_caspt2 solved by the Cholesky route. */
+int32_t dcg_gram_cholesky_blocks(const dcg_ctx *ctx);
+
 /* Device bytes the context holds: its grow-only workspace (integral classes, CI vectors,
  * densities, subspace matrices, solver scratch), which stays resident between solves. */
 int64_t dcg_device_bytes(const dcg_ctx *ctx);
