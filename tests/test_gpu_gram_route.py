@@ -18,16 +18,17 @@ def _run(s, metric, prec):
         return r, ses.gram_cholesky_blocks()
 
 
-@pytest.mark.parametrize("dims,realonly", [((4, 8, 20, 4), False), ((6, 6, 24, 3), False), ((4, 8, 16, 4), True),
-                                           ((2, 10, 12, 5), False)])
+# (2, 10, 12, 5): its metrics have eigenvalues under the cutoff, so AUTO keeps the eigen route
+@pytest.mark.parametrize("dims,realonly,chol", [((4, 8, 20, 4), False, True), ((6, 6, 24, 3), False, True),
+                                                ((4, 8, 16, 4), True, True), ((2, 10, 12, 5), False, False)])
 @pytest.mark.parametrize("prec", [0, 1])
-def test_cholesky_route_matches_eigen_route(gpu_lib, dims, realonly, prec):
+def test_cholesky_route_matches_eigen_route(gpu_lib, dims, realonly, chol, prec):
     from dirac_caspt2_gb300 import api, synth
     S = synth.make_system(synth.SynthConfig(*dims, seed=31, realonly=realonly))
     s = api.SystemInput.from_synth(S)
     a, na = _run(s, "auto", prec)
     e, ne = _run(s, "eigen", prec)
-    assert na > 0 and ne == 0
+    assert (na > 0) == chol and ne == 0
     for k in "ABCDEFGH":
         assert abs(a.e2[k] - e.e2[k]) <= TOL, (k, a.e2[k], e.e2[k])
         assert abs(a.sumc2[k] - e.sumc2[k]) <= TOL, k
