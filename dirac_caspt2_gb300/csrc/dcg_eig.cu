@@ -194,7 +194,7 @@ struct GridBar {
     unsigned count;
     unsigned gen;
     int err;       // 1: a barrier wait exceeded its time limit
-    int pad;
+    unsigned pub;  // reflectors published so far (shared-memory tridiagonalisation)
 };
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
@@ -240,6 +240,40 @@ __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned nblocks) {
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// Wait until gb->pub >= want (a point-to-point signal from one block instead of a grid
+// barrier); bounded like grid_barrier.  Ends with __syncthreads.
+__device__ __forceinline__ bool wait_published(GridBar *gb, unsigned want) {
+    __shared__ int s_ok2;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        unsigned cur;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->pub) : "memory");
+        if (cur < want) {
+            const uint64_t t0 = globaltimer_ns();
+            unsigned spins = 0;
+            while (true) {
+                asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->pub) : "memory");
+                if (cur >= want) break;
+                if ((++spins & 255u) == 0) {
+                    if (*(volatile int *)&gb->err) {
+                        ok = 0;
+                        break;
+                    }
+                    if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+                        atomicExch(&gb->err, 1);
+                        ok = 0;
+                        break;
+                    }
+                }
+            }
+        }
+        s_ok2 = ok;
+    }
+    __syncthreads();
+    return s_ok2 != 0;
 }
 
 // Two deterministic block sums in one pass (sh >= 64 doubles); every thread gets both.
@@ -425,7 +459,8 @@ __global__ void __launch_bounds__(TRD_THREADS) tridiag_persistent_kernel(int n, 
 // the global traffic is the reflector v (written by the owner of column k), the all-gathered
 // p = tau A22 v (one entry per column, from its owner) and one partial dot per block; the
 // matvec and the rank-2 update run from shared memory.  The warp that updates column k+1
-// forms the next reflector from it right away.  Two grid barriers per column.
+// forms the next reflector from it right away and signals it; per column one grid barrier
+// (before w) and one wait for the published reflector.
 constexpr int kTridiagSmemMaxN = 1400;
 
 // reflector of x[0..m) (x[0] = alpha), by one warp; returns tau, beta, the scale for x[1:]
@@ -452,9 +487,10 @@ __device__ __forceinline__ void warp_reflector(const cplx *x, int m, cplx &tau, 
 }
 
 // Column k+1 is in this block's shared memory (local slot c): write its reflector (rows k+2..)
-// to A(k+2:, k+1), and d[k+1], e[k+1], tau[k+1].  One warp.
+// to A(k+2:, k+1), and d[k+1], e[k+1], tau[k+1].  One warp.  With pub, the warp then raises
+// the published-reflector count to k1 + 1 (release order after every lane's writes).
 __device__ __forceinline__ void publish_reflector(int n, int k1, const cplx *col, cplx *A, int64_t lda, double *d,
-                                                  double *e, cplx *tau) {
+                                                  double *e, cplx *tau, unsigned *pub = nullptr) {
     const int lane = threadIdx.x & 31;
     const int m = n - k1 - 1;
     const cplx *x = col + k1 + 1;
@@ -468,6 +504,11 @@ __device__ __forceinline__ void publish_reflector(int n, int k1, const cplx *col
         tau[k1] = t;
         e[k1] = beta;
         d[k1] = col[k1].x;
+    }
+    if (pub) {
+        __threadfence();
+        __syncwarp();
+        if (lane == 0) atomicMax(pub, (unsigned)(k1 + 1));
     }
 }
 
@@ -497,11 +538,17 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
     }
     __syncthreads();
     if (b == 0 && wib == 0) {
-        if (n >= 2) publish_reflector(n, 0, cols, A, lda, d, e, tau);
+        if (n >= 2) publish_reflector(n, 0, cols, A, lda, d, e, tau, &gb->pub);
         else if (lane == 0) d[0] = cols[0].x;
     }
-    if (!grid_barrier(gb, nb)) return;
     for (int k = 0; k + 1 < n; k++) {
+        // reflector k, published by the owner of column k (the only dependency on the
+        // previous column): a point-to-point wait instead of a second grid barrier.  The
+        // p / partial buffers alternate by parity, so a block that starts column k+1 early
+        // cannot overwrite what a slower block still reads for column k.
+        if (!wait_published(gb, (unsigned)(k + 1))) return;
+        cplx *pb = pbuf + (size_t)(k & 1) * (n + 1);
+        double2 *pt = part + (size_t)(k & 1) * (nb + 1);
         const cplx t = ldcg(tau + k);
         const bool active = (t.x != 0.0 || t.y != 0.0);
         for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sv[r] = ldcg(A + r + (int64_t)k * lda);
@@ -525,7 +572,7 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
                 }
                 if (lane == 0) {
                     const cplx xp = cmul(t, mk(ar, ai));
-                    pbuf[j] = xp;
+                    pb[j] = xp;
                     const cplx xv = cmul(cconj(xp), sv[j]);
                     pr += xv.x;
                     pim += xv.y;
@@ -533,18 +580,18 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
             }
         }
         eig_block_sum2(pr, pim, red);
-        if (threadIdx.x == 0) part[b] = make_double2(pr, pim);
+        if (threadIdx.x == 0) pt[b] = make_double2(pr, pim);
         if (!grid_barrier(gb, nb)) return;
         if (active) {
             double sr = 0.0, si = 0.0;
             for (unsigned q = threadIdx.x; q < nb; q += blockDim.x) {
-                const double2 v = __ldcg(part + q);
+                const double2 v = __ldcg(pt + q);
                 sr += v.x;
                 si += v.y;
             }
             eig_block_sum2(sr, si, red);
             const cplx al = cmul(mk(-0.5, 0.0), cmul(t, mk(sr, si)));
-            for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sw[r] = cadd(ldcg(pbuf + r), cmul(al, sv[r]));
+            for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sw[r] = cadd(ldcg(pb + r), cmul(al, sv[r]));
             __syncthreads();
         }
         // update owned columns > k; the warp that owns column k+1 then publishes its reflector
@@ -571,11 +618,10 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
                 __syncwarp();
             }
             if (j == k + 1) {
-                if (k + 2 < n) publish_reflector(n, k + 1, col, A, lda, d, e, tau);
+                if (k + 2 < n) publish_reflector(n, k + 1, col, A, lda, d, e, tau, &gb->pub);
                 else if (lane == 0) d[k + 1] = col[k + 1].x;
             }
         }
-        if (!grid_barrier(gb, nb)) return;
     }
 }
 
@@ -1260,11 +1306,11 @@ static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork
 
 // Shared-memory tridiagonalisation of several matrices in one cooperative launch (one job = one
 // block group).  Block counts come from a cost model: a job's FP64 work (about 4 n^3 FMAs; a
-// GB300 SM retires ~2 FP64 FMAs per clock) spreads over its blocks while every grid barrier (2
-// per column) costs more with more blocks; the jobs share the SMs, and blocks go to the job that
+// GB300 SM retires ~2 FP64 FMAs per clock) spreads over its blocks while the per-column grid barrier
+// and reflector wait cost more with more blocks; the jobs share the SMs, and blocks go to the job that
 // is currently the slowest.  Returns false (nothing launched) when the jobs do not fit.
 static double trd_cost(int n, int nb) {
-    return 4.0 * (double)n * n * n / (nb * 4.0e9) + 2.0 * n * (3.0e-6 + 0.02e-6 * nb);
+    return 4.0 * (double)n * n * n / (nb * 4.0e9) + 1.4 * n * (3.0e-6 + 0.02e-6 * nb);   // one barrier + one signal
 }
 
 static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
@@ -1386,8 +1432,8 @@ void heev_values_batched(Context &c, const std::vector<EigJob> &jobs) {
             t.d = hw[q].d;
             t.e = hw[q].e;
             t.tau = hw[q].tau;
-            t.pbuf = wsget<cplx>(c, slot_name("trd.p", j.slot), (size_t)j.n + 1);
-            t.part = wsget<double2>(c, slot_name("trd.part", j.slot), (size_t)std::max(1, c.num_sms) + 1);
+            t.pbuf = wsget<cplx>(c, slot_name("trd.p", j.slot), 2 * ((size_t)j.n + 1));   // two parities
+            t.part = wsget<double2>(c, slot_name("trd.part", j.slot), 2 * ((size_t)std::max(1, c.num_sms) + 1));
             t.gb = wsget<GridBar>(c, slot_name("trd.bar", j.slot), 1);
             t.n = j.n;
             t.b0 = t.nb = 0;
