@@ -509,22 +509,6 @@ struct BlockSpec {
 // The reference's 1e-8 cutoff is applied to the eigenvalues of K.  E2 is invariant to the basis
 // chosen inside the kept space, so this reproduces solve_block on (S, B) with an Mp x Mp
 // eigenproblem instead of a dimn x dimn one.
-// Whether every eigenvalue of the Gram metric K (Mp x Mp) lies above the 1e-8 cutoff
-// (cutoff.F90:37-70): then no eigenvector of S is dropped and X spans the whole range of G^H.
-// Decided by inertia: K - 1e-8 I is positive definite exactly then (its Cholesky succeeds).
-static bool metric_above_cutoff(Context &c, int Mp, const cplx *K, int tag) {
-    const std::string t = "#" + std::to_string(tag);
-    cplx *Kt = wsget<cplx>(c, "gram.Kt" + t, (size_t)Mp * Mp);
-    int *info = wsget<int>(c, "gram.info" + t, 1);
-    DCG_CUDA(cudaMemcpyAsync(Kt, K, sizeof(cplx) * (size_t)Mp * Mp, cudaMemcpyDeviceToDevice, c.stream));
-    shift_diag(c, Mp, Kt, Mp, 1.0e-8);
-    zpotrf_lower(c, Mp, Kt, Mp, info);
-    int h = 0;
-    DCG_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    DCG_CUDA(cudaStreamSynchronize(c.stream));
-    return h == 0;
-}
-
 // E2 terms of a Gram block whose metric K = G G^H keeps all its eigenvalues: with K = P L P^H
 // unitary, X = G^H P L^-1, B' = P^H D P and Xv = L^-1 P^H G v, so
 //   -v~^H (B' + a)^-1 v~ = -u^H (D + a)^-1 u,   |(B' + a)^-1 v~|^2 = |(D + a)^-1 u|^2,
@@ -558,17 +542,10 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     cplx *K = wsget<cplx>(c, "gram.K", (size_t)Mp * Mp);
     zherk_upper(c, Mp, dimn, G, Mp, K, Mp);
     herm_from_upper(c, Mp, K, Mp);
-    if (c.metric_solver == DCG_METRIC_AUTO && metric_above_cutoff(c, Mp, K, 0)) {
-        const double *e2o = nullptr, *sco = nullptr;
-        gram_cholesky_e2(c, Mp, dimn, G, K, Dd, Vsel, nouter, alpha, 0, e2o, sco);
-        double *red = wsget<double>(c, "blk.red", 2);
-        dsum(c, e2o, nouter, red);
-        dsum(c, sco, nouter, red + 1);
-        std::vector<double> hr = download(c, red, 2);
-        r.e2 = hr[0];
-        r.sc2 = hr[1];
-        r.dimm = Mp;
-        return r;
+    cplx *Kc = nullptr;
+    if (c.metric_solver == DCG_METRIC_AUTO && nouter > 0) {   // kept for the Cholesky route
+        Kc = wsget<cplx>(c, "gram.Kc", (size_t)Mp * Mp);
+        DCG_CUDA(cudaMemcpyAsync(Kc, K, sizeof(cplx) * (size_t)Mp * Mp, cudaMemcpyDeviceToDevice, c.stream));
     }
     double *wk = wsget<double>(c, "gram.wk", Mp);
     heev(c, Mp, K, Mp, wk, Mp, Mp, nullptr, Mp);   // values first (cutoff count)
@@ -579,6 +556,17 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     const int dimm = Mp - vlo;
     r.dimm = dimm;
     if (dimm == 0 || nouter == 0) return r;
+    if (vlo == 0 && Kc) {   // nothing under the cutoff: the Cholesky route
+        const double *e2o = nullptr, *sco = nullptr;
+        gram_cholesky_e2(c, Mp, dimn, G, Kc, Dd, Vsel, nouter, alpha, 0, e2o, sco);
+        double *red = wsget<double>(c, "blk.red", 2);
+        dsum(c, e2o, nouter, red);
+        dsum(c, sco, nouter, red + 1);
+        std::vector<double> hr = download(c, red, 2);
+        r.e2 = hr[0];
+        r.sc2 = hr[1];
+        return r;
+    }
     cplx *P = wsget<cplx>(c, "gram.P", (size_t)Mp * dimm);
     heev_vectors_only(c, Mp, K, Mp, wk, vlo, Mp, P, Mp);
     // VC0 = Lambda^-1 P^H (G v)
@@ -628,37 +616,21 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         std::vector<int> vlo(np, 0), dimm(np, 0);
         std::vector<EigJob> ek;
         std::vector<bool> chol(np, false);
-        std::vector<int> hinfo(np, 1);
+        std::vector<cplx *> Kc(np, nullptr);
         for (size_t j = 0; j < np; j++) {   // metrics, and (AUTO) their definiteness above the cutoff
             GramJob &g = all[p0 + j];
             K[j] = wsget<cplx>(c, nm("gj.K", j), (size_t)g.Mp * g.Mp);
             zherk_upper(c, g.Mp, g.dimn, g.G, g.Mp, K[j], g.Mp);   // K = G G^H, FP64 (the metric)
             herm_from_upper(c, g.Mp, K[j], g.Mp);
-            if (c.metric_solver == DCG_METRIC_AUTO && g.nouter > 0) {
-                cplx *Kt = wsget<cplx>(c, nm("gj.Kt", j), (size_t)g.Mp * g.Mp);
-                int *info = wsget<int>(c, nm("gj.info", j), 1);
-                DCG_CUDA(cudaMemcpyAsync(Kt, K[j], sizeof(cplx) * (size_t)g.Mp * g.Mp, cudaMemcpyDeviceToDevice,
+            if (c.metric_solver == DCG_METRIC_AUTO && g.nouter > 0) {   // kept for the Cholesky route
+                Kc[j] = wsget<cplx>(c, nm("gj.Kc", j), (size_t)g.Mp * g.Mp);
+                DCG_CUDA(cudaMemcpyAsync(Kc[j], K[j], sizeof(cplx) * (size_t)g.Mp * g.Mp, cudaMemcpyDeviceToDevice,
                                          c.stream));
-                shift_diag(c, g.Mp, Kt, g.Mp, 1.0e-8);
-                zpotrf_lower(c, g.Mp, Kt, g.Mp, info);
-                DCG_CUDA(cudaMemcpyAsync(&hinfo[j], info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
             }
         }
-        DCG_CUDA(cudaStreamSynchronize(c.stream));
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
             red[j] = nullptr;
-            if (c.metric_solver != DCG_METRIC_AUTO || g.nouter == 0 || hinfo[j] != 0) continue;
-            chol[j] = true;
-            const double *e2o = nullptr, *sco = nullptr;
-            gram_cholesky_e2(c, g.Mp, g.dimn, g.G, K[j], g.Dd, g.Vsel, g.nouter, g.alpha, (int)j, e2o, sco);
-            red[j] = wsget<double>(c, nm("gj.red", j), 2);
-            dsum(c, e2o, g.nouter, red[j]);
-            dsum(c, sco, g.nouter, red[j] + 1);
-        }
-        for (size_t j = 0; j < np; j++) {
-            GramJob &g = all[p0 + j];
-            if (chol[j]) continue;
             wk[j] = wsget<double>(c, nm("gj.wk", j), g.Mp);
             EigJob e;
             e.n = g.Mp;
@@ -671,7 +643,6 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         heev_values_batched(c, ek);
         std::vector<std::vector<double>> wh(np);
         for (size_t j = 0; j < np; j++) {
-            if (chol[j]) continue;
             wh[j].resize(all[p0 + j].Mp);
             DCG_CUDA(cudaMemcpyAsync(wh[j].data(), wk[j], sizeof(double) * wh[j].size(), cudaMemcpyDeviceToHost,
                                      c.stream));
@@ -680,12 +651,20 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         std::vector<EigJob> eb;
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
-            if (chol[j]) continue;
             vlo[j] = g.Mp;
             for (int q = 0; q < g.Mp; q++)
                 if (wh[j][q] >= 1.0e-8) { vlo[j] = q; break; }   // cutoff.F90:37-70
             dimm[j] = g.Mp - vlo[j];
             if (dimm[j] == 0 || g.nouter == 0) continue;
+            if (vlo[j] == 0 && Kc[j]) {   // nothing under the cutoff: the Cholesky route
+                chol[j] = true;
+                const double *e2o = nullptr, *sco = nullptr;
+                gram_cholesky_e2(c, g.Mp, g.dimn, g.G, Kc[j], g.Dd, g.Vsel, g.nouter, g.alpha, (int)j, e2o, sco);
+                red[j] = wsget<double>(c, nm("gj.red", j), 2);
+                dsum(c, e2o, g.nouter, red[j]);
+                dsum(c, sco, g.nouter, red[j] + 1);
+                continue;
+            }
             const int dm = dimm[j], Mp = g.Mp;
             P[j] = wsget<cplx>(c, nm("gj.P", j), (size_t)Mp * dm);
             heev_vectors_slot(c, (int)j, Mp, K[j], Mp, vlo[j], Mp, P[j], Mp);
@@ -714,7 +693,6 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
             if (chol[j]) continue;
-            red[j] = nullptr;
             if (dimm[j] == 0 || g.nouter == 0) continue;
             const int dm = dimm[j];
             double *e2o = wsget<double>(c, nm("gj.e2o", j), g.nouter);

@@ -2,10 +2,8 @@
 // device (Golub & Van Loan, Matrix Computations, 4th ed., 4.2.8-4.2.9: right-looking block
 // form).  Per 48-column panel: the diagonal block is factored in one block's shared memory,
 // the rows below it by a triangular solve against it, and the trailing matrix by one FP64
-// GEMM.  The factorisation also decides definiteness: it records the first non-positive
-// pivot, which is how the Gram-route metric K is tested against the linear-dependence cutoff
-// (Sylvester's law of inertia: K - s I is positive definite exactly when every eigenvalue of
-// K exceeds s).
+// GEMM.  The factorisation records the first non-positive pivot (the matrix is then not
+// positive definite).
 #include "dcg_common.cuh"
 
 namespace dcg {
@@ -111,11 +109,6 @@ __global__ void __launch_bounds__(128) chol_trsv_cols_kernel(int kb, int nrhs, c
     for (int i = 0; i < kb; i++) b[i] = x[i];
 }
 
-__global__ void shift_diag_kernel(int n, cplx *A, int64_t lda, double s) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) A[i + (int64_t)i * lda].x -= s;
-}
-
 }  // namespace
 
 void zpotrf_lower(Context &c, int n, cplx *A, int64_t lda, int *info) {
@@ -157,11 +150,6 @@ void zpotrs_lower(Context &c, int n, const cplx *L, int64_t lda, cplx *B, int64_
         chol_trsv_cols_kernel<<<g, 128, 0, c.stream>>>(kb, nrhs, L11, lda, B + k0, ldb, false);
         DCG_LAUNCHED(c);
     }
-}
-
-void shift_diag(Context &c, int n, cplx *A, int64_t lda, double s) {
-    shift_diag_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, A, lda, s);
-    DCG_LAUNCHED(c);
 }
 
 }  // namespace dcg

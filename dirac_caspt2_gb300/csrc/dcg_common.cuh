@@ -256,8 +256,6 @@ void dsum(Context &c, const double *x, int64_t n, double *out);
 void zpotrf_lower(Context &c, int n, cplx *A, int64_t lda, int *info);
 // A X = B with the factor of zpotrf_lower; B (n x nrhs, ldb) overwritten by X.
 void zpotrs_lower(Context &c, int n, const cplx *L, int64_t lda, cplx *B, int64_t ldb, int nrhs);
-// A_ii -= s
-void shift_diag(Context &c, int n, cplx *A, int64_t lda, double s);
 
 // Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);

@@ -224,7 +224,107 @@ __global__ void normalize_kernel(int n, cplx *x, const double *__restrict__ n2) 
     x[i] = mk(x[i].x * s, x[i].y * s);
 }
 
+// C[i + ldc j] (op)= sum_k conj(A[k + lda i]) B[k + ldb j] for a small i x j output and a long
+// k: one block per output element, fixed-order reduction.  beta: 0 overwrite, 1 accumulate
+// with alpha.
+__global__ void dotc_small_kernel(int n, const cplx *__restrict__ A, int64_t lda, const cplx *__restrict__ B,
+                                  int64_t ldb, cplx *C, int ldc, double alpha, int accumulate) {
+    __shared__ double sh[32];
+    const int i = blockIdx.x, j = blockIdx.y;
+    const cplx *a = A + lda * i, *b = B + ldb * j;
+    double re = 0.0, im = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const cplx x = a[k], y = b[k];
+        re += x.x * y.x + x.y * y.y;
+        im += x.x * y.y - x.y * y.x;
+    }
+    re = block_sum_d(re, sh);
+    im = block_sum_d(im, sh);
+    if (threadIdx.x == 0) {
+        cplx v = mk(alpha * re, alpha * im);
+        if (accumulate) v = cadd(v, C[i + (int64_t)ldc * j]);
+        C[i + (int64_t)ldc * j] = v;
+    }
+}
+
+// C (n x k) = alpha A (n x m) B (m x k) + beta C, m and k small: one thread per row (coalesced
+// over rows), the m x k factor read through the read-only cache.
+__global__ void tall_small_kernel(int n, int m, int k, cplx alpha, const cplx *__restrict__ A, int64_t lda,
+                                  const cplx *__restrict__ B, int ldb, cplx beta, cplx *C, int64_t ldc) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (r >= n) return;
+    cplx acc = mk(0.0, 0.0);
+    for (int q = 0; q < m; q++) acc = cadd(acc, cmul(A[r + lda * q], __ldg(B + q + (int64_t)ldb * c)));
+    cplx v = cmul(alpha, acc);
+    if (beta.x != 0.0 || beta.y != 0.0) v = cadd(v, cmul(beta, C[r + ldc * c]));
+    C[r + ldc * c] = v;
+}
+
+// Partial products of H (n x n, column-major) with k vectors X (n x k): chunk q of the columns
+// of H contributes P[q][c][r] = sum_{j in chunk q} H[r, j] X[j, c] (threads over rows r, so
+// each column of H is read coalesced).
+constexpr int kHxChunk = 64;
+__global__ void hx_partial_kernel(int n, int k, const cplx *__restrict__ H, const cplx *__restrict__ X, int64_t ldx,
+                                  cplx *P) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int q = blockIdx.y;
+    const int j0 = q * kHxChunk, j1 = min(n, j0 + kHxChunk);
+    if (r >= n) return;
+    cplx acc[8];
+#pragma unroll
+    for (int c = 0; c < 8; c++) acc[c] = mk(0.0, 0.0);
+    for (int j = j0; j < j1; j++) {
+        const cplx h = H[r + (int64_t)n * j];
+#pragma unroll
+        for (int c = 0; c < 8; c++)
+            if (c < k) acc[c] = cadd(acc[c], cmul(h, __ldg(X + j + ldx * c)));
+    }
+    const int nq = gridDim.y;
+#pragma unroll
+    for (int c = 0; c < 8; c++)
+        if (c < k) P[((int64_t)c * nq + q) * n + r] = acc[c];
+}
+
+// Y[:, c] = sum over chunks of P (fixed order).
+__global__ void hx_reduce_kernel(int n, int k, int nq, const cplx *__restrict__ P, cplx *Y, int64_t ldy) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int c = blockIdx.y;
+    if (r >= n) return;
+    cplx acc = mk(0.0, 0.0);
+    for (int q = 0; q < nq; q++) acc = cadd(acc, P[((int64_t)c * nq + q) * n + r]);
+    Y[r + ldy * c] = acc;
+}
+
 }  // namespace
+
+// C (mi x mj, ldc) = A^H B over n rows (Davidson inner products).
+static void dotc_small(Context &c, int n, int mi, int mj, const cplx *A, int64_t lda, const cplx *B, int64_t ldb,
+                       cplx *C, int ldc, double alpha = 1.0, bool accumulate = false) {
+    if (mi <= 0 || mj <= 0) return;
+    dotc_small_kernel<<<dim3(mi, mj), 256, 0, c.stream>>>(n, A, lda, B, ldb, C, ldc, alpha, accumulate ? 1 : 0);
+    DCG_LAUNCHED(c);
+}
+
+static void tall_small(Context &c, int n, int m, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B, int ldb,
+                       cplx beta, cplx *C, int64_t ldc) {
+    if (n <= 0 || k <= 0) return;
+    tall_small_kernel<<<dim3(grid1d(n, 128), k), 128, 0, c.stream>>>(n, m, k, alpha, A, lda, B, ldb, beta, C, ldc);
+    DCG_LAUNCHED(c);
+}
+
+// Y (n x k) = H X for up to 8 vectors at a time.
+static void hx_many(Context &c, int n, const cplx *H, const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) {
+    const int nq = (n + kHxChunk - 1) / kHxChunk;
+    cplx *P = wsget<cplx>(c, "dav.hxp", (size_t)8 * nq * n);
+    for (int c0 = 0; c0 < k; c0 += 8) {
+        const int kk = std::min(8, k - c0);
+        hx_partial_kernel<<<dim3(grid1d(n, 128), nq), 128, 0, c.stream>>>(n, kk, H, X + ldx * c0, ldx, P);
+        DCG_LAUNCHED(c);
+        hx_reduce_kernel<<<dim3(grid1d(n, 128), kk), 128, 0, c.stream>>>(n, kk, nq, P, Y + ldy * c0, ldy);
+        DCG_LAUNCHED(c);
+    }
+}
 
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy) {
     if (n < 1 || n > kJacobiMaxN) throw Error{DCG_E_ARG, "small_heev: dimension out of range"};
@@ -232,7 +332,8 @@ void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, i
     const size_t smem = 2 * sizeof(cplx) * (size_t)np * np;
     DCG_CUDA(cudaFuncSetAttribute(jacobi_heev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int *st = wsget<int>(c, "dav.jst", 1);
-    jacobi_heev_kernel<<<1, kJacobiThreads, smem, c.stream>>>(n, G, ldg, w, Y, ldy, st);
+    // two warps: the rounds are short (n/2 rotations), so barrier latency, not work, sets the pace
+    jacobi_heev_kernel<<<1, 64, smem, c.stream>>>(n, G, ldg, w, Y, ldy, st);
     DCG_LAUNCHED(c);
 }
 
@@ -276,17 +377,17 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
     unit_cols_kernel<<<grid1d((int64_t)n * nb, 256), 256, 0, c.stream>>>(n, nb, idx, V, ld);
     DCG_LAUNCHED(c);
     int m = nb;
-    zgemm(c, OP_N, OP_N, n, m, n, one, H, ld, 0, V, ld, 0, zero, W, ld, 0);
+    hx_many(c, n, H, V, ld, m, W, ld);
 
     std::vector<double> h2((size_t)nb);
     bool converged = false;
     c.casci_iters = 0;
     for (int it = 0; it < maxit; it++) {
-        zgemm(c, OP_C, OP_N, m, m, n, one, V, ld, 0, W, ld, 0, zero, G, mmax, 0);
+        dotc_small(c, n, m, m, V, ld, W, ld, G, mmax);
         small_heev(c, m, G, mmax, th, Y, mmax);
         // Ritz vectors of the block and their images
-        zgemm(c, OP_N, OP_N, n, nb, m, one, V, ld, 0, Y, mmax, 0, zero, X, ld, 0);
-        zgemm(c, OP_N, OP_N, n, nb, m, one, W, ld, 0, Y, mmax, 0, zero, HX, ld, 0);
+        tall_small(c, n, m, nb, one, V, ld, Y, mmax, zero, X, ld);
+        tall_small(c, n, m, nb, one, W, ld, Y, mmax, zero, HX, ld);
         residual_kernel<<<nb, 256, 0, c.stream>>>(n, HX, X, ld, th, hd, T, nrm);
         DCG_LAUNCHED(c);
         DCG_CUDA(cudaMemcpyAsync(h2.data(), nrm, sizeof(double) * nb, cudaMemcpyDeviceToHost, c.stream));
@@ -316,8 +417,8 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
             DCG_LAUNCHED(c);
             const int mm = m + cand;
             for (int pass = 0; pass < 2; pass++) {
-                zgemm(c, OP_C, OP_N, mm, 1, n, one, V, ld, 0, dst, ld, 0, zero, cf, mmax, 0);
-                zgemm(c, OP_N, OP_N, n, 1, mm, mone, V, ld, 0, cf, mmax, 0, one, dst, ld, 0);
+                dotc_small(c, n, mm, 1, V, ld, dst, ld, cf, mmax);
+                tall_small(c, n, mm, 1, mone, V, ld, cf, mmax, one, dst, ld);
             }
             norm2_kernel<<<1, 256, 0, c.stream>>>(n, dst, nrm + nb + 2 * cand + 1);
             DCG_LAUNCHED(c);
@@ -334,7 +435,7 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
             while (added < cand && nn[2 * added + 1] > 1e-20 * nn[2 * added] && nn[2 * added + 1] > 0.0) added++;
         }
         if (added == 0) break;   // stagnated: reported below
-        zgemm(c, OP_N, OP_N, n, added, n, one, H, ld, 0, V + ld * m, ld, 0, zero, W + ld * m, ld, 0);
+        hx_many(c, n, H, V + ld * m, ld, added, W + ld * m, ld);
         m += added;
     }
     int jh = 0;

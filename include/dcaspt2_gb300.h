@@ -210,11 +210,11 @@ int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver);
 int32_t dcg_casci_iterations(const dcg_ctx *ctx);
 
 /* Solver of the A and C blocks that go through the (nelec +- 1)-electron Gram factor G
- * (S = G^H G, metric K = G G^H).  AUTO: when K - 1e-8 I is positive definite (no eigenvalue
- * of S above zero falls under the 1e-8 cutoff of cutoff.F90:37-70, so X spans the range of
- * G^H), E2 and c^2 come from one Cholesky solve u = K^-1 G v as -u^H (D + alpha)^-1 u and
- * |(D + alpha)^-1 u|^2, equal to the reference's eigenvector sums; otherwise, and always
- * with EIGEN, from the eigendecompositions of K and B'. */
+ * (S = G^H G, metric K = G G^H).  AUTO: when no eigenvalue of K falls under the 1e-8 cutoff
+ * of cutoff.F90:37-70 (so X spans the range of G^H), E2 and c^2 come from one Cholesky solve
+ * u = K^-1 G v as -u^H (D + alpha)^-1 u and |(D + alpha)^-1 u|^2, equal to the reference's
+ * sums over the eigenpairs of B'; otherwise, and always with EIGEN, from the
+ * eigendecompositions of K and B'. */
 #define DCG_METRIC_AUTO 0
 #define DCG_METRIC_EIGEN 1
 int dcg_set_metric_solver(dcg_ctx *ctx, int32_t solver);
