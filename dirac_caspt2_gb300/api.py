@@ -119,6 +119,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_set_metric_solver.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_gram_cholesky_blocks.argtypes = [ctypes.c_void_p]
     lib.dcg_gram_cholesky_blocks.restype = ctypes.c_int32
+    lib.dcg_gram_deflated_blocks.argtypes = [ctypes.c_void_p]
+    lib.dcg_gram_deflated_blocks.restype = ctypes.c_int32
     lib.dcg_device_bytes.argtypes = [ctypes.c_void_p]
     lib.dcg_device_bytes.restype = ctypes.c_int64
     lib.dcg_trim.argtypes = [ctypes.c_void_p]
@@ -143,7 +145,7 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
                     "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm",
                     "dcg_set_casci_solver", "dcg_casci_iterations", "dcg_set_metric_solver",
-                    "dcg_gram_cholesky_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
+                    "dcg_gram_cholesky_blocks", "dcg_gram_deflated_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
                     "dcg_server_device_bytes", "dcg_server_destroy"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
@@ -393,6 +395,10 @@ class Caspt2Session:
     def gram_cholesky_blocks(self) -> int:
         """Gram blocks of the last caspt2 solved by the Cholesky route."""
         return int(self.lib.dcg_gram_cholesky_blocks(self.h))
+
+    def gram_deflated_blocks(self) -> int:
+        """Gram blocks of the last caspt2 solved on the complement of deflated eigenvectors."""
+        return int(self.lib.dcg_gram_deflated_blocks(self.h))
 
     def casci_iterations(self) -> int:
         """Davidson iterations of the last casci (0: dense solver)."""

@@ -532,6 +532,45 @@ static void gram_cholesky_e2(Context &c, int Mp, int dimn, const cplx *G, cplx *
     sco_out = sco;
 }
 
+// Largest number of metric eigenvalues under the cutoff that the complement route takes.
+constexpr int kWoodburyMaxR = 64;
+
+// E2 terms of a Gram block whose metric K keeps all but its r smallest eigenpairs (Ps, Mp x r,
+// the eigenvectors under the cutoff; lam_max its largest eigenvalue).  With P the kept
+// eigenvectors, u = P v~ = sum_kept p lam^-1 p^H G v = K'^-1 (1 - Ps Ps^H) G v for
+// K' = K + s Ps Ps^H (s = max(1, lam_max): K' keeps the kept eigenpairs and is well
+// conditioned), and B' = P^H D P is the compression of D to the complement of Ps, whose
+// inverse there gives e2 and c^2 per outer index (launch_woodbury_e2).  The reference's
+// eigendecomposition of B' and the back-transformation of every kept vector are replaced by
+// r vectors, one Cholesky solve and an r x r system per outer index.  Kc (a copy of K) is
+// destroyed.
+static void gram_woodbury_e2(Context &c, int Mp, int dimn, const cplx *G, cplx *Kc, const cplx *Ps, int r,
+                             double lam_max, const double *Dd, const cplx *Vsel, int nouter, const double *alpha,
+                             int tag, const double *&e2o_out, const double *&sco_out) {
+    const std::string t = "#" + std::to_string(tag);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
+    const double sh = std::max(1.0, lam_max);
+    zgemm(c, OP_N, OP_C, Mp, Mp, r, mk(sh, 0.0), Ps, Mp, 0, Ps, Mp, 0, one, Kc, Mp, 0, 1);   // K' = K + s Ps Ps^H
+    int *info = wsget<int>(c, "gram.winfo" + t, 1);
+    zpotrf_lower(c, Mp, Kc, Mp, info);
+    cplx *U = wsget<cplx>(c, "gram.U" + t, (size_t)Mp * nouter);
+    zgemm(c, OP_N, OP_N, Mp, nouter, dimn, one, G, Mp, 0, Vsel, dimn, 0, zero, U, Mp, 0, 1);
+    cplx *Q = wsget<cplx>(c, "gram.Q" + t, (size_t)r * nouter);
+    zgemm(c, OP_C, OP_N, r, nouter, Mp, one, Ps, Mp, 0, U, Mp, 0, zero, Q, r, 0, 1);
+    zgemm(c, OP_N, OP_N, Mp, nouter, r, mone, Ps, Mp, 0, Q, r, 0, one, U, Mp, 0, 1);   // (1 - Ps Ps^H) G v
+    zpotrs_lower(c, Mp, Kc, Mp, U, Mp, nouter);
+    double *e2o = wsget<double>(c, "gram.e2o" + t, nouter);
+    double *sco = wsget<double>(c, "gram.sco" + t, nouter);
+    launch_woodbury_e2(c, Mp, r, U, Mp, Ps, Mp, Dd, alpha, nouter, e2o, sco);
+    int h = 0;
+    DCG_CUDA(cudaMemcpyAsync(&h, info, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    if (h != 0) throw Error{DCG_E_NUMERIC, "deflated Gram metric is not positive definite"};
+    c.gram_woodbury_blocks++;
+    e2o_out = e2o;
+    sco_out = sco;
+}
+
 static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, const double *Dd, const cplx *Vsel,
                                  int nouter, const double *alpha) {
     BlockOut r;
@@ -556,9 +595,15 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     const int dimm = Mp - vlo;
     r.dimm = dimm;
     if (dimm == 0 || nouter == 0) return r;
-    if (vlo == 0 && Kc) {   // nothing under the cutoff: the Cholesky route
+    if (Kc && vlo <= kWoodburyMaxR) {   // Cholesky route (none under the cutoff) or its deflated form
         const double *e2o = nullptr, *sco = nullptr;
-        gram_cholesky_e2(c, Mp, dimn, G, Kc, Dd, Vsel, nouter, alpha, 0, e2o, sco);
+        if (vlo == 0) {
+            gram_cholesky_e2(c, Mp, dimn, G, Kc, Dd, Vsel, nouter, alpha, 0, e2o, sco);
+        } else {
+            cplx *Ps = wsget<cplx>(c, "gram.Ps", (size_t)Mp * vlo);
+            heev_vectors_only(c, Mp, K, Mp, wk, 0, vlo, Ps, Mp);
+            gram_woodbury_e2(c, Mp, dimn, G, Kc, Ps, vlo, wh.back(), Dd, Vsel, nouter, alpha, 0, e2o, sco);
+        }
         double *red = wsget<double>(c, "blk.red", 2);
         dsum(c, e2o, nouter, red);
         dsum(c, sco, nouter, red + 1);
@@ -656,10 +701,17 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
                 if (wh[j][q] >= 1.0e-8) { vlo[j] = q; break; }   // cutoff.F90:37-70
             dimm[j] = g.Mp - vlo[j];
             if (dimm[j] == 0 || g.nouter == 0) continue;
-            if (vlo[j] == 0 && Kc[j]) {   // nothing under the cutoff: the Cholesky route
+            if (Kc[j] && vlo[j] <= kWoodburyMaxR) {
                 chol[j] = true;
                 const double *e2o = nullptr, *sco = nullptr;
-                gram_cholesky_e2(c, g.Mp, g.dimn, g.G, Kc[j], g.Dd, g.Vsel, g.nouter, g.alpha, (int)j, e2o, sco);
+                if (vlo[j] == 0) {   // nothing under the cutoff: the Cholesky route
+                    gram_cholesky_e2(c, g.Mp, g.dimn, g.G, Kc[j], g.Dd, g.Vsel, g.nouter, g.alpha, (int)j, e2o, sco);
+                } else {             // a few under it: deflate them, solve on the complement
+                    cplx *Ps = wsget<cplx>(c, nm("gj.Ps", j), (size_t)g.Mp * vlo[j]);
+                    heev_vectors_slot(c, (int)j, g.Mp, K[j], g.Mp, 0, vlo[j], Ps, g.Mp);
+                    gram_woodbury_e2(c, g.Mp, g.dimn, g.G, Kc[j], Ps, vlo[j], wh[j].back(), g.Dd, g.Vsel, g.nouter,
+                                     g.alpha, (int)j, e2o, sco);
+                }
                 red[j] = wsget<double>(c, nm("gj.red", j), 2);
                 dsum(c, e2o, g.nouter, red[j]);
                 dsum(c, sco, g.nouter, red[j] + 1);
@@ -859,6 +911,7 @@ namespace dcg {
 static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8], double *e0_out, double *et_out) {
     if (!c.have_casci) throw Error{DCG_E_STATE, "dcg_caspt2 before dcg_casci"};
     c.gram_cholesky_blocks = 0;
+    c.gram_woodbury_blocks = 0;
     DevSystem &d = dev(c);
     const int ni = c.ni, na = c.na, ns = c.ns, nmoc = ni + na;
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
@@ -1409,7 +1462,11 @@ int dcg_set_metric_solver(dcg_ctx *ctx, int32_t solver) {
     return DCG_OK;
 }
 
-int32_t dcg_gram_cholesky_blocks(const dcg_ctx *ctx) { return ctx ? ctx->c.gram_cholesky_blocks : -1; }
+int32_t dcg_gram_cholesky_blocks(const dcg_ctx *ctx) {
+    return ctx ? ctx->c.gram_cholesky_blocks + ctx->c.gram_woodbury_blocks : -1;
+}
+
+int32_t dcg_gram_deflated_blocks(const dcg_ctx *ctx) { return ctx ? ctx->c.gram_woodbury_blocks : -1; }
 
 int64_t dcg_device_bytes(const dcg_ctx *ctx) { return ctx ? (int64_t)ctx->c.ws.bytes_in_use() : -1; }
 

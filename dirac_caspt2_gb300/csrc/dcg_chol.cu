@@ -153,3 +153,155 @@ void zpotrs_lower(Context &c, int n, const cplx *L, int64_t lda, cplx *B, int64_
 }
 
 }  // namespace dcg
+
+namespace dcg {
+
+namespace {
+
+__device__ __forceinline__ double wsum(double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Per outer index o (one block): with M = D + alpha_o (diagonal over the Mp determinants), the
+// compression of M to the orthogonal complement of the r columns of Ps has, on that complement,
+// the inverse M^-1 - M^-1 Ps C^-1 Ps^H M^-1 with C = Ps^H M^-1 Ps (r x r).  For u (Mp) in the
+// complement: z = a - M^-1 Ps C^-1 b with a = M^-1 u, b = Ps^H a; e2o = -Re u^H z, sco = |z|^2.
+// Dynamic shared memory: C (r x r), b, x (r each), complex.  Fixed-order reductions.
+__global__ void __launch_bounds__(256) woodbury_e2_kernel(int Mp, int r, const cplx *__restrict__ U, int64_t ldu,
+                                                          const cplx *__restrict__ Ps, int64_t ldp,
+                                                          const double *__restrict__ Dd,
+                                                          const double *__restrict__ alpha, double *e2o, double *sco) {
+    extern __shared__ double2 wsm[];
+    cplx *C = wsm, *bv = C + r * r, *xv = bv + r;
+    __shared__ double red[2][8];
+    __shared__ int piv_s;
+    const int o = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    const double al = alpha[o];
+    const cplx *u = U + (int64_t)o * ldu;
+    // b_k = sum_m conj(Ps[m,k]) u_m / M_m and C_kl = sum_m conj(Ps[m,k]) Ps[m,l] / M_m (l >= k)
+    const int npair = r * (r + 1) / 2;
+    for (int t = warp; t < r + npair; t += nw) {
+        double re = 0.0, im = 0.0;
+        if (t < r) {
+            const cplx *pk = Ps + (int64_t)t * ldp;
+            for (int m = lane; m < Mp; m += 32) {
+                const double inv = 1.0 / (Dd[m] + al);
+                const cplx p = pk[m], x = u[m];
+                re += (p.x * x.x + p.y * x.y) * inv;
+                im += (p.x * x.y - p.y * x.x) * inv;
+            }
+        } else {
+            int q = t - r, k = 0;
+            while (q >= r - k) {
+                q -= r - k;
+                k++;
+            }
+            const int l = k + q;
+            const cplx *pk = Ps + (int64_t)k * ldp, *pl = Ps + (int64_t)l * ldp;
+            for (int m = lane; m < Mp; m += 32) {
+                const double inv = 1.0 / (Dd[m] + al);
+                const cplx a = pk[m], b = pl[m];
+                re += (a.x * b.x + a.y * b.y) * inv;
+                im += (a.x * b.y - a.y * b.x) * inv;
+            }
+            re = wsum(re);
+            im = wsum(im);
+            if (lane == 0) {
+                C[k + r * l] = mk(re, im);
+                C[l + r * k] = mk(re, -im);
+            }
+            continue;
+        }
+        re = wsum(re);
+        im = wsum(im);
+        if (lane == 0) {
+            bv[t] = mk(re, im);
+            xv[t] = mk(re, im);
+        }
+    }
+    __syncthreads();
+    // C x = b by Gaussian elimination with partial pivoting (rows updated in parallel)
+    for (int k = 0; k < r; k++) {
+        if (threadIdx.x == 0) {
+            int p = k;
+            double best = cabs2(C[k + r * k]);
+            for (int i = k + 1; i < r; i++) {
+                const double v = cabs2(C[i + r * k]);
+                if (v > best) {
+                    best = v;
+                    p = i;
+                }
+            }
+            piv_s = p;
+        }
+        __syncthreads();
+        const int p = piv_s;
+        if (p != k) {
+            for (int j = threadIdx.x; j < r; j += blockDim.x) {
+                const cplx t = C[k + r * j];
+                C[k + r * j] = C[p + r * j];
+                C[p + r * j] = t;
+            }
+            if (threadIdx.x == 0) {
+                const cplx t = xv[k];
+                xv[k] = xv[p];
+                xv[p] = t;
+            }
+        }
+        __syncthreads();
+        const cplx inv = cdiv(mk(1.0, 0.0), C[k + r * k]);
+        for (int i = k + 1 + threadIdx.x; i < r; i += blockDim.x) {
+            const cplx f = cmul(C[i + r * k], inv);
+            for (int j = k + 1; j < r; j++) C[i + r * j] = csub(C[i + r * j], cmul(f, C[k + r * j]));
+            xv[i] = csub(xv[i], cmul(f, xv[k]));
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0)
+        for (int k = r - 1; k >= 0; k--) {
+            cplx s = xv[k];
+            for (int j = k + 1; j < r; j++) s = csub(s, cmul(C[k + r * j], xv[j]));
+            xv[k] = cdiv(s, C[k + r * k]);
+        }
+    __syncthreads();
+    // z = (u - Ps x) / M; e2 = -Re u^H z, sco = |z|^2
+    double e = 0.0, s2 = 0.0;
+    for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
+        cplx w = u[m];
+        for (int k = 0; k < r; k++) w = csub(w, cmul(Ps[m + ldp * k], xv[k]));
+        const double inv = 1.0 / (Dd[m] + al);
+        const cplx z = mk(w.x * inv, w.y * inv);
+        e += u[m].x * z.x + u[m].y * z.y;
+        s2 += z.x * z.x + z.y * z.y;
+    }
+    e = wsum(e);
+    s2 = wsum(s2);
+    if (lane == 0) {
+        red[0][warp] = e;
+        red[1][warp] = s2;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double te = 0.0, ts = 0.0;
+        for (int w = 0; w < nw; w++) {
+            te += red[0][w];
+            ts += red[1][w];
+        }
+        e2o[o] = -te;
+        sco[o] = ts;
+    }
+}
+
+}  // namespace
+
+void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, const cplx *Ps, int64_t ldp,
+                        const double *Dd, const double *alpha, int nouter, double *e2o, double *sco) {
+    if (nouter <= 0) return;
+    const size_t smem = sizeof(cplx) * ((size_t)r * r + 2 * (size_t)r);
+    DCG_CUDA(cudaFuncSetAttribute(woodbury_e2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    woodbury_e2_kernel<<<nouter, 256, smem, c.stream>>>(Mp, r, U, ldu, Ps, ldp, Dd, alpha, e2o, sco);
+    DCG_LAUNCHED(c);
+}
+
+}  // namespace dcg

@@ -105,6 +105,7 @@ struct Context {
     // definite, else eigendecomposition) or DCG_METRIC_EIGEN (dcg_set_metric_solver)
     int metric_solver = 0;
     int gram_cholesky_blocks = 0;   // Gram blocks of the last dcg_caspt2 solved by Cholesky
+    int gram_woodbury_blocks = 0;   // ... of them with metric eigenvalues under the cutoff deflated
 
     // ---- system (host copies)
     bool have_system = false;
@@ -256,6 +257,11 @@ void dsum(Context &c, const double *x, int64_t n, double *out);
 void zpotrf_lower(Context &c, int n, cplx *A, int64_t lda, int *info);
 // A X = B with the factor of zpotrf_lower; B (n x nrhs, ldb) overwritten by X.
 void zpotrs_lower(Context &c, int n, const cplx *L, int64_t lda, cplx *B, int64_t ldb, int nrhs);
+// Per outer index o: e2o = -Re u^H z, sco = |z|^2, z the solution on the orthogonal complement
+// of the r columns of Ps (Mp x r, orthonormal) of the compression of D + alpha_o (D diagonal),
+// u = U[:, o] in that complement (dcg_chol.cu).
+void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, const cplx *Ps, int64_t ldp,
+                        const double *Dd, const double *alpha, int nouter, double *e2o, double *sco);
 
 // Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);
