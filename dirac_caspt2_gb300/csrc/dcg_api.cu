@@ -242,7 +242,7 @@ static void set_system(Context &c, const dcg_system *s) {
 // ------------------------------------------------------------------------- CASCI
 // The dense eigensolver below kDavidsonMinDet determinants or for many roots; block Davidson
 // on the resident Hamiltonian above it.
-constexpr int kDavidsonMinDet = 2000;
+constexpr int kDavidsonMinDet = 600;
 constexpr int kDavidsonMaxRoots = 12;
 
 static bool use_davidson(const Context &c, int ndet, int nvec) {

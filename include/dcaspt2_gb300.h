@@ -199,7 +199,7 @@ int dcg_time_family(dcg_ctx *ctx, int32_t family);
 int dcg_family_stats(const dcg_ctx *ctx, double *ms, int64_t *launches, double *work);
 
 /* CASCI eigensolver of dcg_casci.  AUTO: dense Householder + divide-and-conquer (the ZHEEV
- * of diag.F90:66-128) below 2000 determinants or for more than 12 roots, block Davidson on the
+ * of diag.F90:66-128) below 600 determinants or for more than 12 roots, block Davidson on the
  * resident Hamiltonian otherwise (residual norms <= 1e-13 max(1, max |H_ii|) for every
  * returned root).  DENSE / DAVIDSON force one of them (DAVIDSON needs ndet >= roots + 5). */
 #define DCG_CASCI_AUTO 0

@@ -64,10 +64,10 @@ def test_davidson_degenerate_roots(gpu_lib):
 
 
 def test_auto_picks_by_size(gpu_lib):
-    """AUTO: dense at 924 determinants (the 20/12/300 CASCI), Davidson at 3003, both equal to
-    the dense roots."""
+    """AUTO: dense at 495 determinants, Davidson at 924 (the 20/12/300 CASCI) and 3003, all
+    equal to the dense roots."""
     from dirac_caspt2_gb300 import api, synth
-    for dims, want_dav in (((2, 12, 6, 6), False), ((2, 14, 4, 8), True)):
+    for dims, want_dav in (((2, 12, 6, 4), False), ((2, 12, 6, 6), True), ((2, 14, 4, 8), True)):
         S = synth.make_system(synth.SynthConfig(*dims, seed=8))
         s = api.SystemInput.from_synth(S)
         with api.Caspt2Session(0) as ses:
