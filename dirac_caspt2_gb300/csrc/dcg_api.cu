@@ -940,28 +940,59 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
     DCG_CUDA(cudaMemsetAsync(U, 0, sizeof(cplx) * (size_t)c.nmo * c.nmo, c.stream));
     c.eps.assign(c.nmo, 0.0);
     const int rng[3][2] = {{0, ni}, {ni, nmoc}, {nmoc, nmoc + ns}};
-    for (int sp = 0; sp < 3; sp++) {
+    // the per-space, per-irrep blocks are independent: their reductions run in batched
+    // launches (at most kEigSlots at a time), then each block's vectors are formed
+    struct FockBlk {
+        int sp;
+        std::vector<int> ind;
+        int *dind;
+        cplx *blk, *vec;
+        double *w;
+    };
+    std::vector<FockBlk> fb;
+    for (int sp = 0; sp < 3; sp++)
         for (int sym = 1; sym <= c.nsym; sym++) {
-            std::vector<int> ind;
+            FockBlk b;
+            b.sp = sp;
             for (int i = rng[sp][0]; i < rng[sp][1]; i++)
-                if (c.irpamo[i] == sym) ind.push_back(i);
-            if (ind.empty()) continue;
-            const int nb = (int)ind.size();
-            int *dind = upload(c, "fd.ind", ind);
-            cplx *blk = wsget<cplx>(c, "fd.blk", (size_t)nb * nb);
-            cplx *vec = wsget<cplx>(c, "fd.vec", (size_t)nb * nb);
-            double *w = wsget<double>(c, "fd.w", nb);
-            launch_gather2(c, f, c.nmo, dind, nb, blk);
-            heev(c, nb, blk, nb, w, 0, nb, vec, nb);
-            std::vector<double> wh = download(c, w, nb);
-            if (sp == 1) {   // active space: canonical vectors inside degenerate pairs
-                std::vector<cplx> vh = download(c, vec, (size_t)nb * nb);
+                if (c.irpamo[i] == sym) b.ind.push_back(i);
+            if (!b.ind.empty()) fb.push_back(b);
+        }
+    for (size_t b0 = 0; b0 < fb.size(); b0 += kEigSlots) {
+        const size_t nbat = std::min<size_t>(kEigSlots, fb.size() - b0);
+        std::vector<EigJob> jobs;
+        for (size_t q = 0; q < nbat; q++) {
+            FockBlk &b = fb[b0 + q];
+            const int nb = (int)b.ind.size();
+            const std::string t = "#" + std::to_string(q);
+            b.dind = upload(c, "fd.ind" + t, b.ind);
+            b.blk = wsget<cplx>(c, "fd.blk" + t, (size_t)nb * nb);
+            b.vec = wsget<cplx>(c, "fd.vec" + t, (size_t)nb * nb);
+            b.w = wsget<double>(c, "fd.w" + t, nb);
+            launch_gather2(c, f, c.nmo, b.dind, nb, b.blk);
+            EigJob e;
+            e.n = nb;
+            e.A = b.blk;
+            e.lda = nb;
+            e.w = b.w;
+            e.slot = (int)q;
+            jobs.push_back(e);
+        }
+        heev_values_batched(c, jobs);
+        for (size_t q = 0; q < nbat; q++) {
+            FockBlk &b = fb[b0 + q];
+            const int nb = (int)b.ind.size();
+            heev_vectors_slot(c, (int)q, nb, b.blk, nb, 0, nb, b.vec, nb);
+            std::vector<double> wh = download(c, b.w, nb);
+            if (b.sp == 1) {   // active space: canonical vectors inside degenerate pairs
+                std::vector<cplx> vh = download(c, b.vec, (size_t)nb * nb);
                 canonical_pairs(nb, wh, vh);
-                DCG_CUDA(cudaMemcpyAsync(vec, vh.data(), sizeof(cplx) * vh.size(), cudaMemcpyHostToDevice, c.stream));
+                DCG_CUDA(cudaMemcpyAsync(b.vec, vh.data(), sizeof(cplx) * vh.size(), cudaMemcpyHostToDevice,
+                                         c.stream));
                 DCG_CUDA(cudaStreamSynchronize(c.stream));
             }
-            launch_scatter2(c, vec, nb, dind, U, c.nmo);
-            for (int q = 0; q < nb; q++) c.eps[ind[q]] = wh[q];
+            launch_scatter2(c, b.vec, nb, b.dind, U, c.nmo);
+            for (int k = 0; k < nb; k++) c.eps[b.ind[k]] = wh[k];
         }
     }
     d.eps = upload(c, "pt.eps", c.eps);
