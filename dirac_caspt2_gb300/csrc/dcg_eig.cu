@@ -1616,9 +1616,7 @@ void heev_vectors_slot(Context &c, int slot, int n, cplx *A, int64_t lda, int vl
     // Many columns: the FP64 pipe is the limit, one warp per column without prefetch (fewest
     // registers).  Few columns: the n-1 sequential reflections are the limit, prefetch the next
     // reflector (two warps per column above 512 rows to keep it in registers).
-    // Above 512 rows with hundreds of columns the reflections run as compact-WY GEMMs (the
-    // FP64 GEMM keeps the pipe busier than one warp per column); otherwise in registers.
-    if (n <= 1024 && !(n > 512 && nvec >= 256)) {
+    if (n <= 1024) {
         const bool many = nvec >= 64;
         if (n <= 256) {
             if (many) launch_bt_reg<8, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
