@@ -163,74 +163,64 @@ __device__ __forceinline__ double wsum(double v) {
     return v;
 }
 
-// Per outer index o (one block): with M = D + alpha_o (diagonal over the Mp determinants), the
-// compression of M to the orthogonal complement of the r columns of Ps has, on that complement,
-// the inverse M^-1 - M^-1 Ps C^-1 Ps^H M^-1 with C = Ps^H M^-1 Ps (r x r).  For u (Mp) in the
-// complement: z = a - M^-1 Ps C^-1 b with a = M^-1 u, b = Ps^H a; e2o = -Re u^H z, sco = |z|^2.
-// Dynamic shared memory: C (r x r), b, x (r each), complex.  Fixed-order reductions.
-__global__ void __launch_bounds__(256) woodbury_e2_kernel(int Mp, int r, const cplx *__restrict__ U, int64_t ldu,
-                                                          const cplx *__restrict__ Ps, int64_t ldp,
-                                                          const double *__restrict__ Dd,
-                                                          const double *__restrict__ alpha, double *e2o, double *sco) {
-    extern __shared__ double2 wsm[];
-    cplx *C = wsm, *bv = C + r * r, *xv = bv + r;
-    __shared__ double red[2][8];
-    __shared__ int piv_s;
-    const int o = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const double al = alpha[o];
-    const cplx *u = U + (int64_t)o * ldu;
-    // b_k = sum_m conj(Ps[m,k]) u_m / M_m and C_kl = sum_m conj(Ps[m,k]) Ps[m,l] / M_m (l >= k)
+// Wm[m + Mp i] = 1 / (D_m + alpha_i) (complex, zero imaginary part); A = U o Wm.
+__global__ void wb_weights_kernel(int Mp, int nouter, const double *__restrict__ Dd, const double *__restrict__ alpha,
+                                  const cplx *__restrict__ U, int64_t ldu, cplx *Wm, cplx *A) {
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)Mp * nouter) return;
+    const int m = (int)(e % Mp), i = (int)(e / Mp);
+    const double w = 1.0 / (Dd[m] + alpha[i]);
+    Wm[e] = mk(w, 0.0);
+    const cplx u = U[m + ldu * i];
+    A[e] = mk(u.x * w, u.y * w);
+}
+
+// Phi[p + npair m] = conj(Ps[m, k]) Ps[m, l] for the packed pairs p = (k <= l) of r columns.
+__global__ void wb_phi_kernel(int Mp, int r, const cplx *__restrict__ Ps, int64_t ldp, cplx *Phi) {
     const int npair = r * (r + 1) / 2;
-    for (int t = warp; t < r + npair; t += nw) {
-        double re = 0.0, im = 0.0;
-        if (t < r) {
-            const cplx *pk = Ps + (int64_t)t * ldp;
-            for (int m = lane; m < Mp; m += 32) {
-                const double inv = 1.0 / (Dd[m] + al);
-                const cplx p = pk[m], x = u[m];
-                re += (p.x * x.x + p.y * x.y) * inv;
-                im += (p.x * x.y - p.y * x.x) * inv;
-            }
-        } else {
-            int q = t - r, k = 0;
-            while (q >= r - k) {
-                q -= r - k;
-                k++;
-            }
-            const int l = k + q;
-            const cplx *pk = Ps + (int64_t)k * ldp, *pl = Ps + (int64_t)l * ldp;
-            for (int m = lane; m < Mp; m += 32) {
-                const double inv = 1.0 / (Dd[m] + al);
-                const cplx a = pk[m], b = pl[m];
-                re += (a.x * b.x + a.y * b.y) * inv;
-                im += (a.x * b.y - a.y * b.x) * inv;
-            }
-            re = wsum(re);
-            im = wsum(im);
-            if (lane == 0) {
-                C[k + r * l] = mk(re, im);
-                C[l + r * k] = mk(re, -im);
-            }
-            continue;
-        }
-        re = wsum(re);
-        im = wsum(im);
-        if (lane == 0) {
-            bv[t] = mk(re, im);
-            xv[t] = mk(re, im);
-        }
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)npair * Mp) return;
+    const int p = (int)(e % npair), m = (int)(e / npair);
+    int q = p, k = 0;
+    while (q >= r - k) {
+        q -= r - k;
+        k++;
     }
+    const int l = k + q;
+    Phi[e] = cmul(cconj(Ps[m + ldp * k]), Ps[m + ldp * l]);
+}
+
+// Per outer index i (one block): C_i (r x r Hermitian, unpacked from column i of Cp) x = b_i by
+// Gaussian elimination with partial pivoting (rows updated in parallel); x to X[:, i].
+__global__ void __launch_bounds__(256) wb_solve_kernel(int r, const cplx *__restrict__ Cp, const cplx *__restrict__ Bv,
+                                                       cplx *X) {
+    extern __shared__ double2 wsm[];
+    cplx *C = wsm, *xv = C + r * r;
+    __shared__ int piv_s;
+    const int i = blockIdx.x, npair = r * (r + 1) / 2;
+    const cplx *cp = Cp + (int64_t)npair * i;
+    for (int p = threadIdx.x; p < npair; p += blockDim.x) {
+        int q = p, k = 0;
+        while (q >= r - k) {
+            q -= r - k;
+            k++;
+        }
+        const int l = k + q;
+        const cplx v = cp[p];
+        C[k + r * l] = v;
+        C[l + r * k] = cconj(v);
+    }
+    for (int k = threadIdx.x; k < r; k += blockDim.x) xv[k] = Bv[k + (int64_t)r * i];
     __syncthreads();
-    // C x = b by Gaussian elimination with partial pivoting (rows updated in parallel)
     for (int k = 0; k < r; k++) {
         if (threadIdx.x == 0) {
             int p = k;
             double best = cabs2(C[k + r * k]);
-            for (int i = k + 1; i < r; i++) {
-                const double v = cabs2(C[i + r * k]);
+            for (int q = k + 1; q < r; q++) {
+                const double v = cabs2(C[q + r * k]);
                 if (v > best) {
                     best = v;
-                    p = i;
+                    p = q;
                 }
             }
             piv_s = p;
@@ -251,10 +241,10 @@ __global__ void __launch_bounds__(256) woodbury_e2_kernel(int Mp, int r, const c
         }
         __syncthreads();
         const cplx inv = cdiv(mk(1.0, 0.0), C[k + r * k]);
-        for (int i = k + 1 + threadIdx.x; i < r; i += blockDim.x) {
-            const cplx f = cmul(C[i + r * k], inv);
-            for (int j = k + 1; j < r; j++) C[i + r * j] = csub(C[i + r * j], cmul(f, C[k + r * j]));
-            xv[i] = csub(xv[i], cmul(f, xv[k]));
+        for (int q = k + 1 + threadIdx.x; q < r; q += blockDim.x) {
+            const cplx f = cmul(C[q + r * k], inv);
+            for (int j = k + 1; j < r; j++) C[q + r * j] = csub(C[q + r * j], cmul(f, C[k + r * j]));
+            xv[q] = csub(xv[q], cmul(f, xv[k]));
         }
         __syncthreads();
     }
@@ -265,14 +255,21 @@ __global__ void __launch_bounds__(256) woodbury_e2_kernel(int Mp, int r, const c
             xv[k] = cdiv(s, C[k + r * k]);
         }
     __syncthreads();
-    // z = (u - Ps x) / M; e2 = -Re u^H z, sco = |z|^2
+    for (int k = threadIdx.x; k < r; k += blockDim.x) X[k + (int64_t)r * i] = xv[k];
+}
+
+// Per outer index i: z = Wm o Zm; e2o = -Re u^H z, sco = |z|^2 (fixed-order block reduction).
+__global__ void __launch_bounds__(256) wb_e2_kernel(int Mp, const cplx *__restrict__ U, int64_t ldu,
+                                                    const cplx *__restrict__ Zm, const cplx *__restrict__ Wm,
+                                                    double *e2o, double *sco) {
+    __shared__ double red[2][8];
+    const int i = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     double e = 0.0, s2 = 0.0;
     for (int m = threadIdx.x; m < Mp; m += blockDim.x) {
-        cplx w = u[m];
-        for (int k = 0; k < r; k++) w = csub(w, cmul(Ps[m + ldp * k], xv[k]));
-        const double inv = 1.0 / (Dd[m] + al);
-        const cplx z = mk(w.x * inv, w.y * inv);
-        e += u[m].x * z.x + u[m].y * z.y;
+        const double w = Wm[m + (int64_t)Mp * i].x;
+        const cplx zz = Zm[m + (int64_t)Mp * i];
+        const cplx z = mk(zz.x * w, zz.y * w), u = U[m + ldu * i];
+        e += u.x * z.x + u.y * z.y;
         s2 += z.x * z.x + z.y * z.y;
     }
     e = wsum(e);
@@ -284,23 +281,50 @@ __global__ void __launch_bounds__(256) woodbury_e2_kernel(int Mp, int r, const c
     __syncthreads();
     if (threadIdx.x == 0) {
         double te = 0.0, ts = 0.0;
-        for (int w = 0; w < nw; w++) {
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
             te += red[0][w];
             ts += red[1][w];
         }
-        e2o[o] = -te;
-        sco[o] = ts;
+        e2o[i] = -te;
+        sco[i] = ts;
     }
 }
 
 }  // namespace
 
+// With M_i = D + alpha_i (diagonal over the Mp determinants), the compression of M_i to the
+// orthogonal complement of the r orthonormal columns of Ps has, on that complement, the inverse
+// M^-1 - M^-1 Ps C^-1 Ps^H M^-1 with C = Ps^H M^-1 Ps (r x r).  For u = U[:, i] in the
+// complement: z = M^-1 (u - Ps C^-1 b) with b = Ps^H M^-1 u, and e2o = -Re u^H z,
+// sco = |z|^2.  The r x r matrices of all outer indices come from one GEMM of the packed pair
+// products of Ps with the weights 1 / (D + alpha); then one pivoted r x r solve per index.
 void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, const cplx *Ps, int64_t ldp,
                         const double *Dd, const double *alpha, int nouter, double *e2o, double *sco) {
     if (nouter <= 0) return;
-    const size_t smem = sizeof(cplx) * ((size_t)r * r + 2 * (size_t)r);
-    DCG_CUDA(cudaFuncSetAttribute(woodbury_e2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    woodbury_e2_kernel<<<nouter, 256, smem, c.stream>>>(Mp, r, U, ldu, Ps, ldp, Dd, alpha, e2o, sco);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
+    const int npair = r * (r + 1) / 2;
+    const size_t mo = (size_t)Mp * nouter;
+    cplx *Wm = wsget<cplx>(c, "wb.W", mo);
+    cplx *A = wsget<cplx>(c, "wb.A", mo);
+    cplx *Phi = wsget<cplx>(c, "wb.Phi", (size_t)npair * Mp);
+    cplx *Cp = wsget<cplx>(c, "wb.C", (size_t)npair * nouter);
+    cplx *Bv = wsget<cplx>(c, "wb.B", (size_t)r * nouter);
+    cplx *X = wsget<cplx>(c, "wb.X", (size_t)r * nouter);
+    cplx *Zm = wsget<cplx>(c, "wb.Z", mo);
+    wb_weights_kernel<<<grid1d((int64_t)mo, 256), 256, 0, c.stream>>>(Mp, nouter, Dd, alpha, U, ldu, Wm, A);
+    DCG_LAUNCHED(c);
+    wb_phi_kernel<<<grid1d((int64_t)npair * Mp, 256), 256, 0, c.stream>>>(Mp, r, Ps, ldp, Phi);
+    DCG_LAUNCHED(c);
+    zgemm(c, OP_N, OP_N, npair, nouter, Mp, one, Phi, npair, 0, Wm, Mp, 0, zero, Cp, npair, 0, 1);   // C_i, packed
+    zgemm(c, OP_C, OP_N, r, nouter, Mp, one, Ps, ldp, 0, A, Mp, 0, zero, Bv, r, 0, 1);            // b_i
+    const size_t smem = sizeof(cplx) * ((size_t)r * r + (size_t)r);
+    DCG_CUDA(cudaFuncSetAttribute(wb_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    wb_solve_kernel<<<nouter, 256, smem, c.stream>>>(r, Cp, Bv, X);
+    DCG_LAUNCHED(c);
+    DCG_CUDA(cudaMemcpy2DAsync(Zm, (size_t)Mp * sizeof(cplx), U, (size_t)ldu * sizeof(cplx), (size_t)Mp * sizeof(cplx),
+                               nouter, cudaMemcpyDeviceToDevice, c.stream));
+    zgemm(c, OP_N, OP_N, Mp, nouter, r, mone, Ps, ldp, 0, X, r, 0, one, Zm, Mp, 0, 1);               // u - Ps x
+    wb_e2_kernel<<<nouter, 256, 0, c.stream>>>(Mp, U, ldu, Zm, Wm, e2o, sco);
     DCG_LAUNCHED(c);
 }
 

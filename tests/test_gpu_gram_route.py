@@ -19,8 +19,8 @@ def _run(s, metric, prec):
         return r, ses.gram_cholesky_blocks()
 
 
-# deflated: the metric has eigenvalues under the cutoff (at 10 and 12 active spinors), which
-# the route projects out instead of falling back to the eigendecompositions
+# deflated: the metric has eigenvalues under the cutoff (at 10 and 12 active spinors: 5 and
+# about 80), which the route projects out instead of falling back to the eigendecompositions
 @pytest.mark.parametrize("dims,realonly,deflated", [((4, 8, 20, 4), False, False), ((6, 6, 24, 3), False, False),
                                                     ((4, 8, 16, 4), True, False), ((2, 10, 12, 5), False, True),
                                                     ((2, 12, 6, 6), False, True)])
