@@ -533,7 +533,7 @@ static void gram_cholesky_e2(Context &c, int Mp, int dimn, const cplx *G, cplx *
 }
 
 // Largest number of metric eigenvalues under the cutoff that the complement route takes.
-constexpr int kWoodburyMaxR = 112;   // its r x r system fits one block's shared memory
+constexpr int kWoodburyMaxR = 256;
 
 // E2 terms of a Gram block whose metric K keeps all but its r smallest eigenpairs (Ps, Mp x r,
 // the eigenvectors under the cutoff; lam_max its largest eigenvalue).  With P the kept

@@ -191,11 +191,14 @@ __global__ void wb_phi_kernel(int Mp, int r, const cplx *__restrict__ Ps, int64_
 }
 
 // Per outer index i (one block): C_i (r x r Hermitian, unpacked from column i of Cp) x = b_i by
-// Gaussian elimination with partial pivoting (rows updated in parallel); x to X[:, i].
+// Gaussian elimination with partial pivoting (rows updated in parallel); x to X[:, i].  C_i
+// lives in shared memory (SMEM) or, for larger r, in the block's slice of Cg (global, r x r).
+template <bool SMEM>
 __global__ void __launch_bounds__(256) wb_solve_kernel(int r, const cplx *__restrict__ Cp, const cplx *__restrict__ Bv,
-                                                       cplx *X) {
+                                                       cplx *X, cplx *Cg) {
     extern __shared__ double2 wsm[];
-    cplx *C = wsm, *xv = C + r * r;
+    cplx *C = SMEM ? wsm : Cg + (size_t)r * r * blockIdx.x;
+    cplx *xv = SMEM ? C + r * r : wsm;
     __shared__ int piv_s;
     const int i = blockIdx.x, npair = r * (r + 1) / 2;
     const cplx *cp = Cp + (int64_t)npair * i;
@@ -304,6 +307,7 @@ void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, c
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     const int npair = r * (r + 1) / 2;
     const size_t mo = (size_t)Mp * nouter;
+    constexpr int kWbSmemMaxR = 112;   // (r^2 + r) complex in one block's shared memory
     cplx *Wm = wsget<cplx>(c, "wb.W", mo);
     cplx *A = wsget<cplx>(c, "wb.A", mo);
     cplx *Phi = wsget<cplx>(c, "wb.Phi", (size_t)npair * Mp);
@@ -315,11 +319,23 @@ void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, c
     DCG_LAUNCHED(c);
     wb_phi_kernel<<<grid1d((int64_t)npair * Mp, 256), 256, 0, c.stream>>>(Mp, r, Ps, ldp, Phi);
     DCG_LAUNCHED(c);
-    zgemm(c, OP_N, OP_N, npair, nouter, Mp, one, Phi, npair, 0, Wm, Mp, 0, zero, Cp, npair, 0, 1);   // C_i, packed
+    // C_i, packed: r(r+1)/2 x nouter x Mp, the largest product of the route.  On the split
+    // path it runs on the tensor cores (C_i enters a well-conditioned r x r solve, not the
+    // metric's inverse).
+    if (c.precision == DCG_PREC_SPLIT && npair >= 128)
+        zgemm_split(c, npair, nouter, Mp, 1, Phi, 1, npair, 0, Wm, Mp, 0, Cp, 1, npair, 0, false, c.split_lbo,
+                    c.split_sbo);
+    else
+        zgemm(c, OP_N, OP_N, npair, nouter, Mp, one, Phi, npair, 0, Wm, Mp, 0, zero, Cp, npair, 0, 1);
     zgemm(c, OP_C, OP_N, r, nouter, Mp, one, Ps, ldp, 0, A, Mp, 0, zero, Bv, r, 0, 1);            // b_i
-    const size_t smem = sizeof(cplx) * ((size_t)r * r + (size_t)r);
-    DCG_CUDA(cudaFuncSetAttribute(wb_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    wb_solve_kernel<<<nouter, 256, smem, c.stream>>>(r, Cp, Bv, X);
+    if (r <= kWbSmemMaxR) {
+        const size_t smem = sizeof(cplx) * ((size_t)r * r + (size_t)r);
+        DCG_CUDA(cudaFuncSetAttribute(wb_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        wb_solve_kernel<true><<<nouter, 256, smem, c.stream>>>(r, Cp, Bv, X, nullptr);
+    } else {
+        cplx *Cg = wsget<cplx>(c, "wb.Cg", (size_t)r * r * nouter);
+        wb_solve_kernel<false><<<nouter, 256, sizeof(cplx) * (size_t)r, c.stream>>>(r, Cp, Bv, X, Cg);
+    }
     DCG_LAUNCHED(c);
     DCG_CUDA(cudaMemcpy2DAsync(Zm, (size_t)Mp * sizeof(cplx), U, (size_t)ldu * sizeof(cplx), (size_t)Mp * sizeof(cplx),
                                nouter, cudaMemcpyDeviceToDevice, c.stream));
