@@ -346,14 +346,10 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
     if (nwant < 1 || nb > mmax || n < 2) throw Error{DCG_E_ARG, "davidson: block does not fit the subspace"};
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     const int64_t ld = n;
-    // V and W are kept in the Ritz basis of the last Rayleigh-Ritz step (rotated by Y each
-    // step, into the second buffer of each pair): the Rayleigh matrix is then diagonal up to
-    // the rows of the newest directions, and its Jacobi solve takes few sweeps.  The first nb
-    // columns are the block's Ritz vectors and their images.
     cplx *V = wsget<cplx>(c, "dav.V", (size_t)n * mmax);
     cplx *W = wsget<cplx>(c, "dav.W", (size_t)n * mmax);
-    cplx *V2 = wsget<cplx>(c, "dav.V2", (size_t)n * mmax);
-    cplx *W2 = wsget<cplx>(c, "dav.W2", (size_t)n * mmax);
+    cplx *X = wsget<cplx>(c, "dav.X", (size_t)n * nb);
+    cplx *HX = wsget<cplx>(c, "dav.HX", (size_t)n * nb);
     cplx *T = wsget<cplx>(c, "dav.T", (size_t)n * nb);
     cplx *G = wsget<cplx>(c, "dav.G", (size_t)mmax * mmax);
     cplx *Y = wsget<cplx>(c, "dav.Y", (size_t)mmax * mmax);
@@ -390,11 +386,9 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
         dotc_small(c, n, m, m, V, ld, W, ld, G, mmax);
         small_heev(c, m, G, mmax, th, Y, mmax);
         // Ritz vectors of the block and their images
-        tall_small(c, n, m, m, one, V, ld, Y, mmax, zero, V2, ld);
-        tall_small(c, n, m, m, one, W, ld, Y, mmax, zero, W2, ld);
-        std::swap(V, V2);
-        std::swap(W, W2);
-        residual_kernel<<<nb, 256, 0, c.stream>>>(n, W, V, ld, th, hd, T, nrm);
+        tall_small(c, n, m, nb, one, V, ld, Y, mmax, zero, X, ld);
+        tall_small(c, n, m, nb, one, W, ld, Y, mmax, zero, HX, ld);
+        residual_kernel<<<nb, 256, 0, c.stream>>>(n, HX, X, ld, th, hd, T, nrm);
         DCG_LAUNCHED(c);
         DCG_CUDA(cudaMemcpyAsync(h2.data(), nrm, sizeof(double) * nb, cudaMemcpyDeviceToHost, c.stream));
         DCG_CUDA(cudaStreamSynchronize(c.stream));
@@ -405,7 +399,11 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
             converged = true;
             break;
         }
-        if (m + nb > mmax) m = nb;   // restart on the block's Ritz vectors (the first nb columns)
+        if (m + nb > mmax) {   // restart on the block's Ritz vectors (orthonormal)
+            DCG_CUDA(cudaMemcpyAsync(V, X, sizeof(cplx) * (size_t)n * nb, cudaMemcpyDeviceToDevice, c.stream));
+            DCG_CUDA(cudaMemcpyAsync(W, HX, sizeof(cplx) * (size_t)n * nb, cudaMemcpyDeviceToDevice, c.stream));
+            m = nb;
+        }
         // new directions: preconditioned residuals of the unconverged Ritz pairs, made
         // orthonormal to V and to each other (classical Gram-Schmidt, twice) on the device; the
         // norms before and after come back in one read, and a direction that has lost all but
@@ -446,7 +444,7 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
     if (!converged || jh != 0)
         throw Error{DCG_E_NUMERIC, "CASCI Davidson did not converge to |r| <= " + std::to_string(tol)};
     DCG_CUDA(cudaMemcpyAsync(w, th, sizeof(double) * nwant, cudaMemcpyDeviceToDevice, c.stream));
-    DCG_CUDA(cudaMemcpyAsync(Z, V, sizeof(cplx) * (size_t)n * nwant, cudaMemcpyDeviceToDevice, c.stream));
+    DCG_CUDA(cudaMemcpyAsync(Z, X, sizeof(cplx) * (size_t)n * nwant, cudaMemcpyDeviceToDevice, c.stream));
 }
 
 }  // namespace dcg
