@@ -533,7 +533,10 @@ static void gram_cholesky_e2(Context &c, int Mp, int dimn, const cplx *G, cplx *
 }
 
 // Largest number of metric eigenvalues under the cutoff that the complement route takes.
-constexpr int kWoodburyMaxR = 256;
+// Up to this many, the deflated route costs less than the eigendecompositions of K and B': its
+// packed-pair GEMM (r^2 Mp nouter / 2) and per-index r x r solves grow as r^2 and r^3 (at
+// 12 active, 792 determinants, r = 162 made the A/C stage 2x slower than the eigen route).
+constexpr int kWoodburyMaxR = 64;
 
 // E2 terms of a Gram block whose metric K keeps all but its r smallest eigenpairs (Ps, Mp x r,
 // the eigenvectors under the cutoff; lam_max its largest eigenvalue).  With P the kept

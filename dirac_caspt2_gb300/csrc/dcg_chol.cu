@@ -190,15 +190,13 @@ __global__ void wb_phi_kernel(int Mp, int r, const cplx *__restrict__ Ps, int64_
     Phi[e] = cmul(cconj(Ps[m + ldp * k]), Ps[m + ldp * l]);
 }
 
-// Per outer index i (one block): C_i (r x r Hermitian, unpacked from column i of Cp) x = b_i by
-// Gaussian elimination with partial pivoting (rows updated in parallel); x to X[:, i].  C_i
-// lives in shared memory (SMEM) or, for larger r, in the block's slice of Cg (global, r x r).
-template <bool SMEM>
+// Per outer index i (one block): C_i (r x r Hermitian, unpacked from column i of Cp into shared
+// memory) x = b_i by Gaussian elimination with partial pivoting (rows updated in parallel);
+// x to X[:, i].
 __global__ void __launch_bounds__(256) wb_solve_kernel(int r, const cplx *__restrict__ Cp, const cplx *__restrict__ Bv,
-                                                       cplx *X, cplx *Cg) {
+                                                       cplx *X) {
     extern __shared__ double2 wsm[];
-    cplx *C = SMEM ? wsm : Cg + (size_t)r * r * blockIdx.x;
-    cplx *xv = SMEM ? C + r * r : wsm;
+    cplx *C = wsm, *xv = C + r * r;
     __shared__ int piv_s;
     const int i = blockIdx.x, npair = r * (r + 1) / 2;
     const cplx *cp = Cp + (int64_t)npair * i;
@@ -307,7 +305,7 @@ void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, c
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     const int npair = r * (r + 1) / 2;
     const size_t mo = (size_t)Mp * nouter;
-    constexpr int kWbSmemMaxR = 112;   // (r^2 + r) complex in one block's shared memory
+    constexpr int kWbMaxR = 112;   // (r^2 + r) complex in one block's shared memory
     cplx *Wm = wsget<cplx>(c, "wb.W", mo);
     cplx *A = wsget<cplx>(c, "wb.A", mo);
     cplx *Phi = wsget<cplx>(c, "wb.Phi", (size_t)npair * Mp);
@@ -328,14 +326,10 @@ void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, c
     else
         zgemm(c, OP_N, OP_N, npair, nouter, Mp, one, Phi, npair, 0, Wm, Mp, 0, zero, Cp, npair, 0, 1);
     zgemm(c, OP_C, OP_N, r, nouter, Mp, one, Ps, ldp, 0, A, Mp, 0, zero, Bv, r, 0, 1);            // b_i
-    if (r <= kWbSmemMaxR) {
-        const size_t smem = sizeof(cplx) * ((size_t)r * r + (size_t)r);
-        DCG_CUDA(cudaFuncSetAttribute(wb_solve_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        wb_solve_kernel<true><<<nouter, 256, smem, c.stream>>>(r, Cp, Bv, X, nullptr);
-    } else {
-        cplx *Cg = wsget<cplx>(c, "wb.Cg", (size_t)r * r * nouter);
-        wb_solve_kernel<false><<<nouter, 256, sizeof(cplx) * (size_t)r, c.stream>>>(r, Cp, Bv, X, Cg);
-    }
+    if (r > kWbMaxR) throw Error{DCG_E_ARG, "deflated Gram route: more eigenvalues under the cutoff than it takes"};
+    const size_t smem = sizeof(cplx) * ((size_t)r * r + (size_t)r);
+    DCG_CUDA(cudaFuncSetAttribute(wb_solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    wb_solve_kernel<<<nouter, 256, smem, c.stream>>>(r, Cp, Bv, X);
     DCG_LAUNCHED(c);
     DCG_CUDA(cudaMemcpy2DAsync(Zm, (size_t)Mp * sizeof(cplx), U, (size_t)ldu * sizeof(cplx), (size_t)Mp * sizeof(cplx),
                                nouter, cudaMemcpyDeviceToDevice, c.stream));

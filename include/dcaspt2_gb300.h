@@ -213,7 +213,7 @@ int32_t dcg_casci_iterations(const dcg_ctx *ctx);
  * (S = G^H G, metric K = G G^H).  AUTO: when no eigenvalue of K falls under the 1e-8 cutoff
  * of cutoff.F90:37-70 (so X spans the range of G^H), E2 and c^2 come from one Cholesky solve
  * u = K^-1 G v as -u^H (D + alpha)^-1 u and |(D + alpha)^-1 u|^2, equal to the reference's
- * sums over the eigenpairs of B'; when r <= 256 eigenvalues fall under it, from the same solve
+ * sums over the eigenpairs of B'; when r <= 64 eigenvalues fall under it, from the same solve
  * on the complement of their r eigenvectors (deflated metric, compression of D + alpha);
  * otherwise, and always with EIGEN, from the eigendecompositions of K and B'. */
 #define DCG_METRIC_AUTO 0
