@@ -574,6 +574,18 @@ static void gram_woodbury_e2(Context &c, int Mp, int dimn, const cplx *G, cplx *
     sco_out = sco;
 }
 
+// B' = P^H (D P) (dm x dm) from P and PD (Mp x dm).  Unlike the metric K and Lambda^-1 P^H G v,
+// B' is not amplified by Lambda^-1 (P is orthonormal and D diagonal), so on the split path it
+// runs on the tensor cores, as its transpose (D P)^T conj(P) written back transposed.
+static void bprime_product(Context &c, int Mp, int dm, const cplx *P, const cplx *PD, cplx *Bp) {
+    if (c.precision == DCG_PREC_SPLIT && dm > kSplitMinK) {
+        zgemm_split(c, dm, dm, Mp, 1, PD, Mp, 1, 0, P, Mp, 1, Bp, dm, 1, 0, false, c.split_lbo, c.split_sbo);
+    } else {
+        const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+        zgemm(c, OP_C, OP_N, dm, dm, Mp, one, P, Mp, 0, PD, Mp, 0, zero, Bp, dm, 0, 1);
+    }
+}
+
 static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, const double *Dd, const cplx *Vsel,
                                  int nouter, const double *alpha) {
     BlockOut r;
@@ -628,7 +640,7 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     DCG_CUDA(cudaMemcpyAsync(PD, P, sizeof(cplx) * (size_t)Mp * dimm, cudaMemcpyDeviceToDevice, c.stream));
     launch_scale_rows(c, Mp, dimm, PD, Mp, Dd, 0, false);
     cplx *Bp = wsget<cplx>(c, "blk.Bp", (size_t)dimm * dimm);
-    zgemm(c, OP_C, OP_N, dimm, dimm, Mp, one, P, Mp, 0, PD, Mp, 0, zero, Bp, dimm, 0, 1);
+    bprime_product(c, Mp, dimm, P, PD, Bp);
     herm_from_upper(c, dimm, Bp, dimm);
     double *e2o = wsget<double>(c, "blk.e2o", nouter);
     double *sco = wsget<double>(c, "blk.sco", nouter);
@@ -732,7 +744,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             DCG_CUDA(cudaMemcpyAsync(PD, P[j], sizeof(cplx) * (size_t)Mp * dm, cudaMemcpyDeviceToDevice, c.stream));
             launch_scale_rows(c, Mp, dm, PD, Mp, g.Dd, 0, false);
             Bp[j] = wsget<cplx>(c, nm("gj.Bp", j), (size_t)dm * dm);
-            zgemm(c, OP_C, OP_N, dm, dm, Mp, one, P[j], Mp, 0, PD, Mp, 0, zero, Bp[j], dm, 0, 1);   // P^H D P
+            bprime_product(c, Mp, dm, P[j], PD, Bp[j]);   // P^H D P
             herm_from_upper(c, dm, Bp[j], dm);
             wb[j] = wsget<double>(c, nm("gj.wb", j), dm);
             EigJob e;
