@@ -16,7 +16,8 @@
 //     TMEM accumulators by weight p+q = 2, 3, 4 and >= 5.  The first three stay exact (integer
 //     partial sums below 2^24 for K' <= 1024 real); the last one carries only 2^-21-relative
 //     terms, so its rounding is ~2^-45 of the result;
-//   * the epilogue adds the accumulators in FP64 and applies 2^(e+f-14).
+//   * the epilogue adds the accumulators (the exact pair kept exact by an FP32 TwoSum) and applies
+//     2^(e+f-14) through the exponent field.
 // The result carries ~2^-36 of max|row of A| * max|column of B| per term.
 //
 // Data movement: the slicing pre-pass writes both operands directly in the tcgen05 canonical
@@ -301,6 +302,25 @@ struct SplitArgs {
     int *err;
 };
 
+// g0 + g1 + g2 + g3 (FP32 bit patterns) as a double: TwoSum (Knuth) keeps g0 + g1 exact as
+// s + t, then g2 + g3 are added to t in FP32.
+__device__ __forceinline__ double recombine(uint32_t b0, uint32_t b1, uint32_t b2, uint32_t b3) {
+    const float g0 = __uint_as_float(b0), g1 = __uint_as_float(b1);
+    const float s = __fadd_rn(g0, g1);
+    const float bb = __fsub_rn(s, g0);
+    const float t = __fadd_rn(__fsub_rn(g0, __fsub_rn(s, bb)), __fsub_rn(g1, bb));
+    const float lo = __fadd_rn(t, __fadd_rn(__uint_as_float(b2), __uint_as_float(b3)));
+    return (double)s + (double)lo;
+}
+
+// v 2^sc: an integer add to the exponent field when v and the result are normal numbers.
+__device__ __forceinline__ double scale_pow2(double v, int sc) {
+    const long long bits = __double_as_longlong(v);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (v != 0.0 && ex > 0 && ex + sc > 0 && ex + sc < 2047) return __longlong_as_double(bits + ((long long)sc << 52));
+    return v * ldexp(1.0, sc);
+}
+
 __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
     extern __shared__ __align__(1024) unsigned char sp_raw[];
     __shared__ __align__(8) uint64_t bar_full[SP_STAGES], bar_empty[SP_STAGES], bar_done;
@@ -411,16 +431,14 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
                     const int jr = nb * SP_TN + c0 + q;   // real column (even: Re)
                     const int j = jr >> 1;
                     if (j >= a.N) break;
-                    // weight-2 and -3 groups are exact; the weight >= 4 groups are 2^-14 of them, so
-                    // their FP32 sum costs ~2^-38 of the result
-                    const double re = (double)__uint_as_float(g0[q]) + (double)__uint_as_float(g1[q]) +
-                                      (double)(__uint_as_float(g2[q]) + __uint_as_float(g3[q]));
-                    const double im = (double)__uint_as_float(g0[q + 1]) + (double)__uint_as_float(g1[q + 1]) +
-                                      (double)(__uint_as_float(g2[q + 1]) + __uint_as_float(g3[q + 1]));
+                    // weight-2 and -3 groups are exact and their sum is kept exact as an FP32 pair
+                    // (s, t); the weight >= 4 groups are 2^-14 of them and join t, rounding at ~2^-38
+                    // of the result.  Two conversions and one FP64 add per value (the FP64 pipe is
+                    // the epilogue's limit); the power-of-two scale goes into the exponent field.
                     const int sc = e + a.fexp[j] - 2 * SPLIT_BITS;   // each operand carries 2^-7
-                    const double p2 = (sc > -1022 && sc < 1023) ? __longlong_as_double((long long)(sc + 1023) << 52)
-                                                                : ldexp(1.0, sc);
-                    cplx v = mk(re * p2, im * p2);
+                    const double re = scale_pow2(recombine(g0[q], g1[q], g2[q], g3[q]), sc);
+                    const double im = scale_pow2(recombine(g0[q + 1], g1[q + 1], g2[q + 1], g3[q + 1]), sc);
+                    cplx v = mk(re, im);
                     cplx *dst = a.C + (int64_t)z * a.c_sb + i * a.c_si + (int64_t)j * a.c_sj;
                     if (a.accumulate) v = cadd(v, *dst);
                     *dst = v;
