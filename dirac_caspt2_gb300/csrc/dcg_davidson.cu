@@ -262,14 +262,13 @@ __global__ void tall_small_kernel(int n, int m, int k, cplx alpha, const cplx *_
 }
 
 // Partial products of H (n x n, column-major) with k vectors X (n x k): chunk q of the columns
-// of H contributes P[q][c][r] = sum_{j in chunk q} H[r, j] X[j, c] (threads over rows r, so
-// each column of H is read coalesced).
-constexpr int kHxChunk = 64;
-__global__ void hx_partial_kernel(int n, int k, const cplx *__restrict__ H, const cplx *__restrict__ X, int64_t ldx,
-                                  cplx *P) {
+// of H (chunk columns each) contributes P[q][c][r] = sum_{j in chunk q} H[r, j] X[j, c]
+// (threads over rows r, so each column of H is read coalesced).
+__global__ void hx_partial_kernel(int n, int k, int chunk, const cplx *__restrict__ H, const cplx *__restrict__ X,
+                                  int64_t ldx, cplx *P) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     const int q = blockIdx.y;
-    const int j0 = q * kHxChunk, j1 = min(n, j0 + kHxChunk);
+    const int j0 = q * chunk, j1 = min(n, j0 + chunk);
     if (r >= n) return;
     cplx acc[8];
 #pragma unroll
@@ -313,13 +312,15 @@ static void tall_small(Context &c, int n, int m, int k, cplx alpha, const cplx *
     DCG_LAUNCHED(c);
 }
 
-// Y (n x k) = H X for up to 8 vectors at a time.
+// Y (n x k) = H X for up to 8 vectors at a time.  The columns of H are cut into at most 64
+// chunks (of at least 64 columns), so the partial sums stay a small multiple of Y.
 static void hx_many(Context &c, int n, const cplx *H, const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) {
-    const int nq = (n + kHxChunk - 1) / kHxChunk;
+    const int chunk = std::max(64, (n + 63) / 64);
+    const int nq = (n + chunk - 1) / chunk;
     cplx *P = wsget<cplx>(c, "dav.hxp", (size_t)8 * nq * n);
     for (int c0 = 0; c0 < k; c0 += 8) {
         const int kk = std::min(8, k - c0);
-        hx_partial_kernel<<<dim3(grid1d(n, 128), nq), 128, 0, c.stream>>>(n, kk, H, X + ldx * c0, ldx, P);
+        hx_partial_kernel<<<dim3(grid1d(n, 128), nq), 128, 0, c.stream>>>(n, kk, chunk, H, X + ldx * c0, ldx, P);
         DCG_LAUNCHED(c);
         hx_reduce_kernel<<<dim3(grid1d(n, 128), kk), 128, 0, c.stream>>>(n, kk, nq, P, Y + ldy * c0, ldy);
         DCG_LAUNCHED(c);

@@ -47,18 +47,21 @@ class DeviceSystem:
         return int(self.rec_idx.numel() * 4 + self.rec_re.numel() * 8 +
                    (self.rec_im.numel() * 8 if self.rec_im is not None else 0))
 
-    def system_input(self, selectroot: int = 1) -> api.SystemInput:
-        """The dcg_system fields with empty host records (the records are on the device)."""
+    def system_input(self, selectroot: int = 1, ras=(0, 0, 0), ras1_max_hole: int = 0,
+                     ras3_max_elec: int = 0) -> api.SystemInput:
+        """The dcg_system fields with empty host records (the records are on the device); a
+        RAS partition of the active spinors is optional."""
         c = self.cfg
         return api.SystemInput(ninact=c.ninact, nact=c.nact, nsec=c.nsec, nelec=c.nelec, nmo=self.nmo,
                                nsymrpa=1, multb=np.array([[2, 1], [1, 2]]), irpamo=np.ones(self.nmo, np.int64),
                                h=self.h, ecore=self.ecore, rec_idx=np.zeros((0, 4), np.int32),
                                rec_val=np.zeros(0, np.complex128), realonly=c.realonly, selectroot=selectroot,
-                               eshift=c.eshift)
+                               eshift=c.eshift, ras=tuple(ras), ras1_max_hole=ras1_max_hole,
+                               ras3_max_elec=ras3_max_elec)
 
-    def buffers(self, selectroot: int = 1) -> api.HostBuffers:
+    def buffers(self, selectroot: int = 1, **ras) -> api.HostBuffers:
         """HostBuffers whose dcg_system points at the device records."""
-        b = api.HostBuffers(self.system_input(selectroot))
+        b = api.HostBuffers(self.system_input(selectroot, **ras))
         b.use_device_records(self.rec_idx.data_ptr(), self.rec_re.data_ptr(),
                              self.rec_im.data_ptr() if self.rec_im is not None else 0)
         b.struct.nrec = self.nrec
