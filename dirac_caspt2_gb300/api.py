@@ -56,6 +56,43 @@ class _System(ctypes.Structure):
     ]
 
 
+class _MdcintRaw(ctypes.Structure):
+    """dcg_mdcint_raw."""
+    _fields_ = [
+        ("nrec", ctypes.c_int64), ("nent", ctypes.c_int64), ("rec_off", ctypes.c_void_p),
+        ("ikr", ctypes.c_void_p), ("jkr", ctypes.c_void_p), ("indk", ctypes.c_void_p), ("indl", ctypes.c_void_p),
+        ("re", ctypes.c_void_p), ("im", ctypes.c_void_p), ("nkr", ctypes.c_int32), ("kr", ctypes.c_void_p),
+        ("nmo", ctypes.c_int32), ("dirac_to_cas", ctypes.c_void_p), ("scheme", ctypes.c_int32),
+        ("realonly", ctypes.c_int32),
+    ]
+
+
+class MdcintBuffers:
+    """A dirac_io.MdcintRaw in the exact layout of dcg_mdcint_raw (arrays kept alive)."""
+
+    def __init__(self, raw):
+        self.arrays = dict(
+            rec_off=np.ascontiguousarray(raw.rec_off, np.int64), ikr=np.ascontiguousarray(raw.rec_ikr, np.int32),
+            jkr=np.ascontiguousarray(raw.rec_jkr, np.int32), indk=np.ascontiguousarray(raw.indk, np.int32),
+            indl=np.ascontiguousarray(raw.indl, np.int32), re=np.ascontiguousarray(raw.re, np.float64),
+            im=np.ascontiguousarray(raw.im, np.float64), kr=np.ascontiguousarray(raw.kr, np.int32),
+            d2c=np.ascontiguousarray(raw.dirac_to_cas, np.int32))
+        a = self.arrays
+        st = _MdcintRaw()
+        st.nrec = len(a["ikr"])
+        st.nent = len(a["re"])
+        for f, k in (("rec_off", "rec_off"), ("ikr", "ikr"), ("jkr", "jkr"), ("indk", "indk"), ("indl", "indl"),
+                     ("re", "re"), ("kr", "kr"), ("dirac_to_cas", "d2c")):
+            setattr(st, f, a[k].ctypes.data)
+        st.im = None if raw.realonly else a["im"].ctypes.data
+        st.nkr = a["kr"].shape[0]
+        st.nmo = int(raw.nmo)
+        st.scheme = int(raw.scheme)
+        st.realonly = int(bool(raw.realonly))
+        self.struct = st
+        self.realonly = bool(raw.realonly)
+
+
 class _RequestResult(ctypes.Structure):
     """dcg_request_result of the serving loop."""
     _fields_ = [
@@ -113,6 +150,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
                                    ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_heev.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                              ctypes.c_void_p, ctypes.c_void_p]
+    lib.dcg_mdcint_canonicalize.argtypes = [ctypes.c_void_p, P(_MdcintRaw), P(ctypes.c_int64)]
+    lib.dcg_mdcint_records.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    lib.dcg_set_system_mdcint.argtypes = [ctypes.c_void_p, P(_System), P(_MdcintRaw)]
     lib.dcg_set_casci_solver.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_casci_iterations.argtypes = [ctypes.c_void_p]
     lib.dcg_casci_iterations.restype = ctypes.c_int32
@@ -144,6 +184,7 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
                     "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
                     "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm",
+                    "dcg_mdcint_canonicalize", "dcg_mdcint_records", "dcg_set_system_mdcint",
                     "dcg_set_casci_solver", "dcg_casci_iterations", "dcg_set_metric_solver",
                     "dcg_gram_cholesky_blocks", "dcg_gram_deflated_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
@@ -382,6 +423,27 @@ class Caspt2Session:
 
     def kernel_launches(self) -> int:
         return int(self.lib.dcg_kernel_launches(self.h))
+
+    def mdcint_canonicalize(self, raw):
+        """MDCINT records -> the MDCINTNEW stream on the device (dcg_mdcint_canonicalize),
+        copied back as a dirac_io.MdcintNew."""
+        from .dirac_io import MdcintNew
+        mb = raw if isinstance(raw, MdcintBuffers) else MdcintBuffers(raw)
+        n = ctypes.c_int64(0)
+        self._check(self.lib.dcg_mdcint_canonicalize(self.h, ctypes.byref(mb.struct), ctypes.byref(n)))
+        idx = np.zeros((n.value, 4), np.int32)
+        re = np.zeros(n.value)
+        im = np.zeros(n.value)
+        self._check(self.lib.dcg_mdcint_records(self.h, idx.ctypes.data, re.ctypes.data, im.ctypes.data))
+        return MdcintNew(idx=idx, val=re + 1j * im, realonly=mb.realonly)
+
+    def set_system_mdcint(self, s: SystemInput, raw) -> None:
+        """dcg_set_system_mdcint: the system with its records built on the device from MDCINT."""
+        mb = raw if isinstance(raw, MdcintBuffers) else MdcintBuffers(raw)
+        self._bufs = HostBuffers(s)
+        self.system = s
+        self._mdcint = mb
+        self._check(self.lib.dcg_set_system_mdcint(self.h, ctypes.byref(self._bufs.struct), ctypes.byref(mb.struct)))
 
     def set_casci_solver(self, solver: str) -> None:
         """CASCI eigensolver: "auto", "dense" or "davidson" (dcg_set_casci_solver)."""

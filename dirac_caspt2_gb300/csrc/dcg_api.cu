@@ -1494,6 +1494,48 @@ int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n) {
 
 int64_t dcg_kernel_launches(const dcg_ctx *ctx) { return ctx ? ctx->c.launches : -1; }
 
+int dcg_mdcint_canonicalize(dcg_ctx *ctx, const dcg_mdcint_raw *raw, int64_t *nrec_out) {
+    if (!raw) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        c_.mdc_n = dcg::mdcint_canonicalize(c_, *raw, &c_.mdc_ijkl, &c_.mdc_re, &c_.mdc_im);
+        c_.mdc_realonly = raw->realonly != 0 || raw->im == nullptr;
+        if (nrec_out) *nrec_out = c_.mdc_n;
+    });
+    return DCG_OK;
+}
+
+int dcg_mdcint_records(const dcg_ctx *ctx, int32_t *ijkl_out, double *re_out, double *im_out) {
+    if (!ctx || ctx->c.mdc_n < 0) return DCG_E_STATE;
+    const Context &c = ctx->c;
+    if (cudaSetDevice(c.device) != cudaSuccess) return DCG_E_CUDA;
+    const size_t n = (size_t)c.mdc_n;
+    if (n == 0) return DCG_OK;
+    if ((ijkl_out && cudaMemcpyAsync(ijkl_out, c.mdc_ijkl, 4 * n * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                     c.stream) != cudaSuccess) ||
+        (re_out && cudaMemcpyAsync(re_out, c.mdc_re, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream) !=
+                       cudaSuccess) ||
+        (im_out && cudaMemcpyAsync(im_out, c.mdc_im, n * sizeof(double), cudaMemcpyDeviceToHost, c.stream) !=
+                       cudaSuccess) ||
+        cudaStreamSynchronize(c.stream) != cudaSuccess)
+        return DCG_E_CUDA;
+    return DCG_OK;
+}
+
+int dcg_set_system_mdcint(dcg_ctx *ctx, const dcg_system *sys, const dcg_mdcint_raw *raw) {
+    if (!sys || !raw) return DCG_E_ARG;
+    int64_t n = 0;
+    int st = dcg_mdcint_canonicalize(ctx, raw, &n);
+    if (st != DCG_OK) return st;
+    dcg_system s2 = *sys;
+    s2.nrec = n;
+    s2.rec_ijkl = ctx->c.mdc_ijkl;
+    s2.rec_re = ctx->c.mdc_re;
+    s2.rec_im = ctx->c.mdc_realonly ? nullptr : ctx->c.mdc_im;
+    s2.realonly = ctx->c.mdc_realonly ? 1 : sys->realonly;
+    s2.rec_on_device = 1;
+    return dcg_set_system(ctx, &s2);
+}
+
 int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver) {
     if (!ctx || solver < DCG_CASCI_AUTO || solver > DCG_CASCI_DAVIDSON) return DCG_E_ARG;
     ctx->c.casci_solver = solver;

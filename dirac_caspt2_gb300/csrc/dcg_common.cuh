@@ -106,6 +106,11 @@ struct Context {
     int metric_solver = 0;
     int gram_cholesky_blocks = 0;   // Gram blocks of the last dcg_caspt2 solved by Cholesky
     int gram_woodbury_blocks = 0;   // ... of them with metric eigenvalues under the cutoff deflated
+    // last MDCINT canonicalisation (device, in the workspace)
+    int64_t mdc_n = -1;
+    int32_t *mdc_ijkl = nullptr;
+    double *mdc_re = nullptr, *mdc_im = nullptr;
+    bool mdc_realonly = false;
 
     // ---- system (host copies)
     bool have_system = false;
@@ -262,6 +267,11 @@ void zpotrs_lower(Context &c, int n, const cplx *L, int64_t lda, cplx *B, int64_
 // u = U[:, o] in that complement (dcg_chol.cu).
 void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, const cplx *Ps, int64_t ldp,
                         const double *Dd, const double *alpha, int nouter, double *e2o, double *sco);
+
+// MDCINT -> MDCINTNEW on the device (dcg_mdcint.cu); returns the record count, the stream
+// (workspace buffers) through the pointers.
+int64_t mdcint_canonicalize(Context &c, const dcg_mdcint_raw &raw, int32_t **ijkl_out, double **re_out,
+                            double **im_out);
 
 // Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);

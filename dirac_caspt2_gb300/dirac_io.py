@@ -421,9 +421,28 @@ def _parse_mdcint_file(recs: List[bytes], is32: bool, realonly: Optional[bool], 
     return out, realonly
 
 
-def read_mdcint_new(directory: str, mrc: MrconeeData, inp: ActiveInput) -> MdcintNew:
-    """Restatement of ``create_newmdcint`` (create_newmdcint.F90:3-321) returning the
-    MDCINTNEW records in memory instead of on disk."""
+@dataclasses.dataclass
+class MdcintRaw:
+    """DIRAC's MDCINT records flattened in file order (the input of create_newmdcint and of
+    the library's dcg_mdcint_canonicalize): per record the signed Kramers-pair indices
+    (ikr, jkr) and the entry range rec_off[r]:rec_off[r+1]; per entry (indk, indl) and the
+    stored value; the header's Kramers table and the DIRAC-to-CAS map."""
+    rec_ikr: np.ndarray        # (nrec,) int32
+    rec_jkr: np.ndarray        # (nrec,) int32
+    rec_off: np.ndarray        # (nrec + 1,) int64
+    indk: np.ndarray           # (nent,) int32
+    indl: np.ndarray           # (nent,) int32
+    re: np.ndarray             # (nent,) float64
+    im: np.ndarray             # (nent,) float64 (zeros when real-only)
+    kr: np.ndarray             # (nkr, 2) int32: kr(i), kr(-i)
+    nmo: int
+    dirac_to_cas: np.ndarray   # (nmo + 1,) int32, 1-based, [0] unused
+    scheme: int
+    realonly: bool
+
+
+def read_mdcint_raw(directory: str, mrc: MrconeeData, inp: ActiveInput) -> MdcintRaw:
+    """Every record of MDCINT, MDCINXXXX1, ... (create_newmdcint.F90:3-171's reads)."""
     files = mdcint_filenames(directory)
     is32 = mrc.dirac_32bit
     it = "<i4" if is32 else "<i8"
@@ -431,84 +450,121 @@ def read_mdcint_new(directory: str, mrc: MrconeeData, inp: ActiveInput) -> Mdcin
     hdr = read_fortran_records(files[0])[0]
     nkr = int(np.frombuffer(hdr, it, 1, 18)[0])
     pairs = np.frombuffer(hdr, it, 2 * nkr, 18 + isz).astype(np.int64).reshape(nkr, 2)
-    nmo = mrc.nmo
-    kr = np.zeros(nmo + 1, dtype=np.int64)          # kr(-nmo/2 : nmo/2) stored at offset nmo//2
-    o = nmo // 2
-    kr[o + np.arange(1, nkr + 1)] = pairs[:, 0]
-    kr[o - np.arange(1, nkr + 1)] = pairs[:, 1]
-    scheme = inp.mdcint_scheme
     realonly: Optional[bool] = None
-    out_i, out_v = [], []
-    cutoff = 0.25e-12
-    d2c = mrc.dirac_to_cas
+    ikr_l, jkr_l, nz_l, k_l, l_l, re_l, im_l = [], [], [], [], [], [], []
     for fname in files:
         recs = read_fortran_records(fname)
         if not recs:
             continue
         parsed, realonly = _parse_mdcint_file(recs, is32, realonly, skip_header=True)
         for (ikr0, jkr0, indk0, indl0, rr0, ri0) in parsed:
-            nz = len(indk0)
-            ikr, jkr, indk, indl, rr, ri = ikr0, jkr0, indk0, indl0, rr0, ri0
-            for n in (1, 2):
-                if n == 2:
-                    ikr, jkr, indk, indl = -ikr, -jkr, -indk, -indl
-                    sgn = np.where(ikr * jkr * indk * indl >= 0, 1.0, -1.0)
-                    rr = -rr * sgn
-                    ri = ri * sgn
-                amplify = (scheme != 6 and abs(ikr) != abs(jkr))
-                reps = 2 if amplify else 1
-                for rep in range(reps):
-                    ci = np.full(nz, ikr, dtype=np.int64)
-                    cj = np.full(nz, jkr, dtype=np.int64)
-                    ck = indk.copy()
-                    cl = indl.copy()
-                    vr = rr.copy()
-                    vi = ri.copy()
-                    if rep == 1:
-                        ci, cj = cj, ci
-                        ck, cl = cl, ck
-                        t23 = (((ci < 0).astype(int) + (cj < 0).astype(int)) == 1) & \
-                              (((ck < 0).astype(int) + (cl < 0).astype(int)) == 1)
-                        ci = np.where(t23, -ci, ci)
-                        cj = np.where(t23, -cj, cj)
-                        ck = np.where(t23, -ck, ck)
-                        cl = np.where(t23, -cl, cl)
-                        if not realonly:
-                            vi = np.where(t23, vi, -vi)
-                    iii = d2c[kr[o + ci]]
-                    jjj = d2c[kr[o + cj]]
-                    kkk = d2c[kr[o + ck]]
-                    lll = d2c[kr[o + cl]]
-
-                    def kr_signed(x):
-                        return np.where(x % 2 == 1, 1, -1) * (x // 2 + x % 2)
-
-                    ikk, jkk, kkk_, lkk = kr_signed(iii), kr_signed(jjj), kr_signed(kkk), kr_signed(lll)
-                    ii, jj, kk, ll = np.abs(ikk), np.abs(jkk), np.abs(kkk_), np.abs(lkk)
-                    if realonly:
-                        big = np.abs(rr) > cutoff
-                    else:
-                        big = (np.abs(rr) > cutoff) | (np.abs(ri) > cutoff)
-                    t1 = (ikk > 0) & (jkk > 0) & (kkk_ > 0) & (lkk > 0)
-                    t2 = (ikk > 0) & (jkk < 0) & (kkk_ > 0) & (lkk < 0)
-                    t3 = (ikk > 0) & (jkk < 0) & (kkk_ < 0) & (lkk > 0)
-                    t4 = (ikk > 0) & (jkk < 0) & (kkk_ < 0) & (lkk < 0)
-                    c1 = ((ii <= jj) & (kk <= ll) & ((ii < kk) | ((ii == kk) & (jj <= ll)))) | \
-                         ((ii <= jj) & (ll <= kk) & ((ii < ll) | ((ii == ll) & (jj <= kk))))
-                    c23 = (ii <= jj) & (kk <= ll) & ((ii < kk) | ((ii == kk) & (jj <= ll)))
-                    c4 = ii <= jj
-                    keep = big & ((t1 & c1) | (t2 & c23) | (t3 & c23) | (t4 & c4))
-                    if not np.any(keep):
-                        continue
-
-                    def swapkr(x):
-                        return np.where(x % 2 == 1, x + 1, x - 1)
-
-                    q = np.stack([swapkr(iii), swapkr(jjj), swapkr(kkk), swapkr(lll)], axis=1)[keep]
-                    out_i.append(q.astype(np.int32))
-                    out_v.append((vr - 1j * vi)[keep] if not realonly else vr[keep] + 0j)
+            ikr_l.append(ikr0)
+            jkr_l.append(jkr0)
+            nz_l.append(len(indk0))
+            k_l.append(indk0)
+            l_l.append(indl0)
+            re_l.append(rr0)
+            im_l.append(ri0)
     if realonly is None:
         realonly = True
+    off = np.zeros(len(nz_l) + 1, dtype=np.int64)
+    off[1:] = np.cumsum(nz_l) if nz_l else []
+    cat = (lambda xs, dt: np.concatenate(xs).astype(dt) if xs else np.zeros(0, dt))
+    return MdcintRaw(rec_ikr=np.array(ikr_l, np.int32), rec_jkr=np.array(jkr_l, np.int32), rec_off=off,
+                     indk=cat(k_l, np.int32), indl=cat(l_l, np.int32), re=cat(re_l, np.float64),
+                     im=cat(im_l, np.float64), kr=pairs.astype(np.int32), nmo=int(mrc.nmo),
+                     dirac_to_cas=np.asarray(mrc.dirac_to_cas, np.int32), scheme=int(inp.mdcint_scheme),
+                     realonly=bool(realonly))
+
+
+def canonicalize_mdcint(raw: MdcintRaw) -> MdcintNew:
+    """Restatement of create_newmdcint's canonicalisation (create_newmdcint.F90:171-321) on
+    the raw records: both Kramers partners of every record, the bra/ket-exchanged copies of
+    schemes other than 6, the TYPE1-4 filter, the 0.25e-12 cutoff, CAS order."""
+    nkr = raw.kr.shape[0]
+    kr = np.zeros(2 * nkr + 1, dtype=np.int64)   # kr(-nkr : nkr) stored at offset nkr
+    o = nkr
+    kr[o + np.arange(1, nkr + 1)] = raw.kr[:, 0]
+    kr[o - np.arange(1, nkr + 1)] = raw.kr[:, 1]
+    scheme = raw.scheme
+    realonly = raw.realonly
+    out_i, out_v = [], []
+    cutoff = 0.25e-12
+    d2c = raw.dirac_to_cas.astype(np.int64)
+    for r in range(len(raw.rec_ikr)):
+        a, b = int(raw.rec_off[r]), int(raw.rec_off[r + 1])
+        nz = b - a
+        if nz <= 0:
+            continue
+        ikr0, jkr0 = int(raw.rec_ikr[r]), int(raw.rec_jkr[r])
+        indk0 = raw.indk[a:b].astype(np.int64)
+        indl0 = raw.indl[a:b].astype(np.int64)
+        rr0, ri0 = raw.re[a:b], raw.im[a:b]
+        ikr, jkr, indk, indl, rr, ri = ikr0, jkr0, indk0, indl0, rr0, ri0
+        for n in (1, 2):
+            if n == 2:
+                ikr, jkr, indk, indl = -ikr, -jkr, -indk, -indl
+                sgn = np.where(ikr * jkr * indk * indl >= 0, 1.0, -1.0)
+                rr = -rr * sgn
+                ri = ri * sgn
+            amplify = (scheme != 6 and abs(ikr) != abs(jkr))
+            reps = 2 if amplify else 1
+            for rep in range(reps):
+                ci = np.full(nz, ikr, dtype=np.int64)
+                cj = np.full(nz, jkr, dtype=np.int64)
+                ck = indk.copy()
+                cl = indl.copy()
+                vr = rr.copy()
+                vi = ri.copy()
+                if rep == 1:
+                    ci, cj = cj, ci
+                    ck, cl = cl, ck
+                    t23 = (((ci < 0).astype(int) + (cj < 0).astype(int)) == 1) & \
+                          (((ck < 0).astype(int) + (cl < 0).astype(int)) == 1)
+                    ci = np.where(t23, -ci, ci)
+                    cj = np.where(t23, -cj, cj)
+                    ck = np.where(t23, -ck, ck)
+                    cl = np.where(t23, -cl, cl)
+                    if not realonly:
+                        vi = np.where(t23, vi, -vi)
+                iii = d2c[kr[o + ci]]
+                jjj = d2c[kr[o + cj]]
+                kkk = d2c[kr[o + ck]]
+                lll = d2c[kr[o + cl]]
+
+                def kr_signed(x):
+                    return np.where(x % 2 == 1, 1, -1) * (x // 2 + x % 2)
+
+                ikk, jkk, kkk_, lkk = kr_signed(iii), kr_signed(jjj), kr_signed(kkk), kr_signed(lll)
+                ii, jj, kk, ll = np.abs(ikk), np.abs(jkk), np.abs(kkk_), np.abs(lkk)
+                if realonly:
+                    big = np.abs(rr) > cutoff
+                else:
+                    big = (np.abs(rr) > cutoff) | (np.abs(ri) > cutoff)
+                t1 = (ikk > 0) & (jkk > 0) & (kkk_ > 0) & (lkk > 0)
+                t2 = (ikk > 0) & (jkk < 0) & (kkk_ > 0) & (lkk < 0)
+                t3 = (ikk > 0) & (jkk < 0) & (kkk_ < 0) & (lkk > 0)
+                t4 = (ikk > 0) & (jkk < 0) & (kkk_ < 0) & (lkk < 0)
+                c1 = ((ii <= jj) & (kk <= ll) & ((ii < kk) | ((ii == kk) & (jj <= ll)))) | \
+                     ((ii <= jj) & (ll <= kk) & ((ii < ll) | ((ii == ll) & (jj <= kk))))
+                c23 = (ii <= jj) & (kk <= ll) & ((ii < kk) | ((ii == kk) & (jj <= ll)))
+                c4 = ii <= jj
+                keep = big & ((t1 & c1) | (t2 & c23) | (t3 & c23) | (t4 & c4))
+                if not np.any(keep):
+                    continue
+
+                def swapkr(x):
+                    return np.where(x % 2 == 1, x + 1, x - 1)
+
+                q = np.stack([swapkr(iii), swapkr(jjj), swapkr(kkk), swapkr(lll)], axis=1)[keep]
+                out_i.append(q.astype(np.int32))
+                out_v.append((vr - 1j * vi)[keep] if not realonly else vr[keep] + 0j)
     idx = np.concatenate(out_i) if out_i else np.zeros((0, 4), np.int32)
     val = np.concatenate(out_v) if out_v else np.zeros(0, np.complex128)
     return MdcintNew(idx=idx, val=val, realonly=bool(realonly))
+
+
+def read_mdcint_new(directory: str, mrc: MrconeeData, inp: ActiveInput) -> MdcintNew:
+    """Restatement of ``create_newmdcint`` (create_newmdcint.F90:3-321) returning the
+    MDCINTNEW records in memory instead of on disk."""
+    return canonicalize_mdcint(read_mdcint_raw(directory, mrc, inp))

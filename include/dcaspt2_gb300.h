@@ -69,6 +69,25 @@ typedef struct dcg_system {
                                             context's device (already resident in HBM)           */
 } dcg_system;
 
+/* DIRAC's MDCINT file(s) as read record by record (MDCINT, MDCINXXXX1, ...: header
+ * `datex, timex, nkr, (kr(i), kr(-i), i = 1..nkr)`, then records `ikr, jkr, nz, (indk, indl),
+ * values`; read_mrconee.F90 / create_newmdcint.F90:3-171), flattened: the caller's input to
+ * dcg_mdcint_canonicalize / dcg_set_system_mdcint, which replace create_newmdcint. */
+typedef struct dcg_mdcint_raw {
+    int64_t nrec;                        /* records (ikr, jkr) over all files, in file order   */
+    int64_t nent;                        /* entries (sum of nz)                                 */
+    const int64_t *rec_off;              /* nrec + 1: entries of record r are rec_off[r] ..     */
+    const int32_t *ikr, *jkr;            /* per record, signed Kramers-pair indices             */
+    const int32_t *indk, *indl;          /* per entry, signed                                   */
+    const double *re, *im;               /* per entry, as stored; im NULL when real-only        */
+    int32_t nkr;                         /* header: number of Kramers pairs                     */
+    const int32_t *kr;                   /* header: (kr(i), kr(-i)) for i = 1..nkr, 2 x nkr     */
+    int32_t nmo;                         /* MRCONEE NMO                                          */
+    const int32_t *dirac_to_cas;         /* nmo + 1 (entry 0 unused): DIRAC spinor -> CAS index */
+    int32_t scheme;                      /* .mdcint_scheme of the input (6: both orders stored) */
+    int32_t realonly;                    /* MDCINT real-only (module_realonly.F90:29-77)         */
+} dcg_mdcint_raw;
+
 /* Create a context on CUDA device `device`.  precision: DCG_PREC_*. */
 int dcg_create(int device, int precision, dcg_ctx **out);
 int dcg_destroy(dcg_ctx *ctx);
@@ -78,6 +97,20 @@ const char *dcg_last_error(const dcg_ctx *ctx);
  * src/module_2integrals.F90:26-588, and divide_2_elec_integral_into_subspaces,
  * src/divide_2_elec_integral_into_subspaces.F90:3-409). */
 int dcg_set_system(dcg_ctx *ctx, const dcg_system *sys);
+
+/* The MDCINTNEW record stream of create_newmdcint (create_newmdcint.F90:3-321) built on the
+ * device from the raw MDCINT records: both Kramers partners of every record, bra/ket-exchanged
+ * copies for schemes other than 6, the TYPE1-4 canonical filter, the 0.25e-12 cutoff, CAS
+ * order, in the reference's output order.  The stream stays in the context (device); *nrec_out
+ * receives its length. */
+int dcg_mdcint_canonicalize(dcg_ctx *ctx, const dcg_mdcint_raw *raw, int64_t *nrec_out);
+/* Copy the last canonicalised stream to host arrays: ijkl_out (4 x nrec, 1-based CAS indices
+ * (i, j, k, l) of (ij|kl)), re_out and im_out (nrec; im_out may be NULL). */
+int dcg_mdcint_records(const dcg_ctx *ctx, int32_t *ijkl_out, double *re_out, double *im_out);
+/* dcg_mdcint_canonicalize then dcg_set_system on the device-resident stream (the record fields
+ * of sys are ignored): MDCINT to expanded integrals without a scratch file or a host copy of
+ * MDCINTNEW. */
+int dcg_set_system_mdcint(dcg_ctx *ctx, const dcg_system *sys, const dcg_mdcint_raw *raw);
 
 /* CASCI (replaces casci, src/casci.F90:3-163: search_cas_configuration, casmat,
  * cdiag/rdiag).  Writes min(nroot, ndet) total energies eigen(i) = ecas(i) + ecore

@@ -5,7 +5,8 @@ this reads ``active.inp``, ``MRCONEE`` and ``MDCINT*`` with the package's reader
 (restatements of read_mrconee / create_newmdcint) and stores the resulting system in
 ``<case>.npz`` together with the energies printed in ``reference.<case>.out``:
 the CASCI total energy of the selected root, the per-subspace ``e2X`` and ``sumc2,X`` and
-the total CASPT2 energy.
+the total CASPT2 energy.  For the cases with small MDCINT files it also stores the raw MDCINT
+records (``<case>_mdcint_raw.npz``), the input of the MDCINT canonicalisation.
 
 Usage:  python tests/golden/make_golden_fixtures.py /path/to/reference/test/dev
 """
@@ -21,6 +22,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from dirac_caspt2_gb300 import dirac_io  # noqa: E402
 
 CASES = ["c2_h2o_dev", "check_minelecras3_dev", "ninact_0_h2_dev", "mdcint_scheme_6_dirac23_c32h_n2_dev"]
+RAW_CASES = ["check_minelecras3_dev", "ninact_0_h2_dev"]   # MDCINT small enough to keep (28 / 48 KB)
 
 
 def parse_output(path: str, selectroot: int):
@@ -67,6 +69,13 @@ def main(devdir: str):
             out["rec_im"] = new.val.imag
         np.savez_compressed(os.path.join(HERE, f"{case}.npz"), **out)
         print(case, "records", len(new), "total", total)
+        if case in RAW_CASES:   # the MDCINT records themselves, for the device canonicalisation
+            raw = dirac_io.read_mdcint_raw(d, mrc, inp)
+            np.savez_compressed(os.path.join(HERE, f"{case}_mdcint_raw.npz"), rec_ikr=raw.rec_ikr,
+                                rec_jkr=raw.rec_jkr, rec_off=raw.rec_off, indk=raw.indk, indl=raw.indl, re=raw.re,
+                                im=raw.im, kr=raw.kr, nmo=raw.nmo, dirac_to_cas=raw.dirac_to_cas,
+                                scheme=raw.scheme, realonly=raw.realonly)
+            print(case, "raw entries", len(raw.re))
 
 
 if __name__ == "__main__":
