@@ -262,20 +262,26 @@ static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double
     if (c.selectroot > ndet) throw Error{DCG_E_ARG, "selectroot exceeds the number of CASCI configurations"};
     d.ndet = ndet;
     d.dets = upload(c, "ci.dets", c.dets);
-    stage_begin(c, ST_CASMAT);
-    cplx *H = wsget<cplx>(c, "ci.H", (size_t)ndet * ndet);
-    launch_casmat(c, d.dets, ndet, d.h, d.inttw, H);
-    stage_end(c, ST_CASMAT);
-    stage_begin(c, ST_CASEIG);
     const int nr = std::max(1, std::min(nroot, ndet));
     const int nvec = std::max(nr, c.selectroot);
     double *w = wsget<double>(c, "ci.w", ndet);
     cplx *Z = wsget<cplx>(c, "ci.Z", (size_t)ndet * nvec);
     c.casci_iters = 0;
     if (use_davidson(c, ndet, nvec)) {
+        // the Hamiltonian as CSR (singles and doubles of each determinant), never dense
+        stage_begin(c, ST_CASMAT);
+        CsrMatrix Hs;
+        build_casmat_csr(c, d.dets, ndet, d.h, d.inttw, Hs);
+        stage_end(c, ST_CASMAT);
+        stage_begin(c, ST_CASEIG);
         // |r| <= 1e-13 max(1, max |H_ii|): eigenvalue errors ~|r|^2/gap, vector errors ~|r|/gap
-        davidson_lowest(c, ndet, H, nvec, w, Z, 1e-13, 400);
+        davidson_lowest_csr(c, Hs, nvec, w, Z, 1e-13, 400);
     } else {
+        stage_begin(c, ST_CASMAT);
+        cplx *H = wsget<cplx>(c, "ci.H", (size_t)ndet * ndet);
+        launch_casmat(c, d.dets, ndet, d.h, d.inttw, H);
+        stage_end(c, ST_CASMAT);
+        stage_begin(c, ST_CASEIG);
         heev(c, ndet, H, ndet, w, 0, nvec, Z, ndet);
     }
     stage_end(c, ST_CASEIG);

@@ -182,6 +182,218 @@ __global__ void casmat_kernel(int ni, int na, int ne, const uint64_t *__restrict
 #undef GIDX
 }
 
+// ------------------------------------------------------------------------- sparse CASCI matrix
+// The same Slater-Condon elements (casmat.F90:3-222), as a CSR matrix for the Davidson route:
+// row i holds its diagonal and every single and double excitation of det i that lies in the
+// CI space (RAS restrictions included), each element computed from row i's determinant.
+// Candidates of a row: q < ne nv singles, then the ne(ne-1)/2 x nv(nv-1)/2 doubles.
+struct CsrRow {
+    int occ[64], vir[64];
+};
+
+__device__ bool casmat_candidate(int ni, int na, int ne, const uint64_t *__restrict__ dets, int ndet,
+                                 const cplx *__restrict__ h, int nmo, const cplx *__restrict__ g, uint64_t I,
+                                 const CsrRow &rw, int64_t q, int64_t &jout, cplx &vout) {
+    const int nmoc = ni + na, nv = na - ne, nocc = ni + ne;
+#define GIDX(p, q_, r, s) ((int64_t)(p) + (int64_t)nmoc * ((q_) + (int64_t)nmoc * ((r) + (int64_t)nmoc * (s))))
+#define OCCG(x) ((x) < ni ? (x) : ni + rw.occ[(x) - ni])
+    const int64_t nsing = (int64_t)ne * nv;
+    if (q < nsing) {
+        const int ro = rw.occ[q / nv], av = rw.vir[q % nv];
+        uint64_t J;
+        int ph;
+        if (!exct(I, av, ro, na, J, ph)) return false;
+        const int64_t j = find_sorted(dets, ndet, J);
+        if (j < 0) return false;
+        const int ir = ni + ro, ia = ni + av;
+        cplx v = h[ir + (int64_t)nmo * ia];
+        for (int x = 0; x < nocc; x++) {
+            const int s2 = OCCG(x);
+            v = cadd(v, g[GIDX(ir, ia, s2, s2)]);
+            v = csub(v, g[GIDX(ir, s2, s2, ia)]);
+        }
+        if (ph & 1) v = mk(-v.x, -v.y);
+        jout = j;
+        vout = v;
+        return true;
+    }
+    q -= nsing;
+    const int npv = nv * (nv - 1) / 2;
+    const int po = (int)(q / npv), pv = (int)(q % npv);
+    int x = 0, y = 0, u = 0, w2 = 0;
+    {
+        int cnt = po;
+        for (x = 0; x < ne; x++) {
+            const int rem = ne - 1 - x;
+            if (cnt < rem) {
+                y = x + 1 + cnt;
+                break;
+            }
+            cnt -= rem;
+        }
+    }
+    {
+        int cnt = pv;
+        for (u = 0; u < nv; u++) {
+            const int rem = nv - 1 - u;
+            if (cnt < rem) {
+                w2 = u + 1 + cnt;
+                break;
+            }
+            cnt -= rem;
+        }
+    }
+    const int r_ = rw.occ[x], s_ = rw.occ[y], a_ = rw.vir[u], b_ = rw.vir[w2];
+    uint64_t J1, J2;
+    int p1, p2;
+    if (!exct(I, a_, r_, na, J1, p1)) return false;
+    if (!exct(J1, b_, s_, na, J2, p2)) return false;
+    const int64_t j = find_sorted(dets, ndet, J2);
+    if (j < 0) return false;
+    const int ir = ni + r_, is = ni + s_, ia = ni + a_, ib = ni + b_;
+    cplx v = csub(g[GIDX(ir, ia, is, ib)], g[GIDX(ir, ib, is, ia)]);
+    if ((p1 + p2) & 1) v = mk(-v.x, -v.y);
+    jout = j;
+    vout = v;
+    return true;
+#undef OCCG
+#undef GIDX
+}
+
+__device__ void casmat_row_setup(int na, uint64_t I, CsrRow &rw) {
+    if (threadIdx.x == 0) {
+        int no = 0, nv = 0;
+        for (int t = 0; t < na; t++) {
+            if ((I >> t) & 1ull) rw.occ[no++] = t;
+            else rw.vir[nv++] = t;
+        }
+    }
+    __syncthreads();
+}
+
+// Diagonal of row i (block reduction), as casmat_kernel.
+__device__ double casmat_diag(int ni, int na, int ne, const cplx *__restrict__ h, int nmo, const cplx *__restrict__ g,
+                              const CsrRow &rw, double *red) {
+    const int nmoc = ni + na, nocc = ni + ne;
+#define GIDX(p, q_, r, s) ((int64_t)(p) + (int64_t)nmoc * ((q_) + (int64_t)nmoc * ((r) + (int64_t)nmoc * (s))))
+#define OCCG(x) ((x) < ni ? (x) : ni + rw.occ[(x) - ni])
+    double acc = 0.0;
+    const int64_t npair = (int64_t)nocc * nocc;
+    for (int64_t q = threadIdx.x; q < npair; q += blockDim.x) {
+        const int x = (int)(q % nocc), y = (int)(q / nocc);
+        if (y <= x) continue;
+        const int r = OCCG(x), s2 = OCCG(y);
+        acc += g[GIDX(r, r, s2, s2)].x - g[GIDX(r, s2, s2, r)].x;
+    }
+    for (int x = threadIdx.x; x < nocc; x += blockDim.x) {
+        const int r = OCCG(x);
+        acc += h[r + (int64_t)nmo * r].x;
+    }
+#undef OCCG
+#undef GIDX
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[wid] = acc;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < (int)((blockDim.x + 31) >> 5); w++) s += red[w];
+    __syncthreads();
+    return s;
+}
+
+__global__ void __launch_bounds__(256) casmat_csr_count_kernel(int ni, int na, int ne, const uint64_t *__restrict__ dets,
+                                                               int ndet, const cplx *__restrict__ h, int nmo,
+                                                               const cplx *__restrict__ g, int64_t *counts) {
+    __shared__ CsrRow rw;
+    __shared__ int64_t red[8];
+    const int i = blockIdx.x;
+    const uint64_t I = dets[i];
+    casmat_row_setup(na, I, rw);
+    const int nv = na - ne;
+    const int64_t ncand = (int64_t)ne * nv + (int64_t)(ne * (ne - 1) / 2) * (nv * (nv - 1) / 2);
+    int64_t cnt = 0;
+    for (int64_t q = threadIdx.x; q < ncand; q += blockDim.x) {
+        int64_t j;
+        cplx v;
+        cnt += casmat_candidate(ni, na, ne, dets, ndet, h, nmo, g, I, rw, q, j, v) ? 1 : 0;
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int64_t t = 1;   // the diagonal
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += red[w];
+        counts[i] = t;
+    }
+}
+
+__global__ void __launch_bounds__(256) casmat_csr_fill_kernel(int ni, int na, int ne, const uint64_t *__restrict__ dets,
+                                                              int ndet, const cplx *__restrict__ h, int nmo,
+                                                              const cplx *__restrict__ g, const int64_t *rowptr,
+                                                              int *cols, cplx *vals, double *hdiag) {
+    __shared__ CsrRow rw;
+    __shared__ double red[8];
+    __shared__ int wsum[8];
+    __shared__ int64_t run;
+    const int i = blockIdx.x;
+    const uint64_t I = dets[i];
+    casmat_row_setup(na, I, rw);
+    const double dg = casmat_diag(ni, na, ne, h, nmo, g, rw, red);
+    if (threadIdx.x == 0) {
+        cols[rowptr[i]] = i;
+        vals[rowptr[i]] = mk(dg, 0.0);
+        hdiag[i] = dg;
+        run = rowptr[i] + 1;
+    }
+    __syncthreads();
+    const int nv = na - ne;
+    const int64_t ncand = (int64_t)ne * nv + (int64_t)(ne * (ne - 1) / 2) * (nv * (nv - 1) / 2);
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int64_t q0 = 0; q0 < ncand; q0 += blockDim.x) {
+        const int64_t q = q0 + threadIdx.x;
+        int64_t j = 0;
+        cplx v = mk(0.0, 0.0);
+        const bool kept = q < ncand && casmat_candidate(ni, na, ne, dets, ndet, h, nmo, g, I, rw, q, j, v);
+        const unsigned bal = __ballot_sync(0xffffffffu, kept);
+        if (lane == 0) wsum[warp] = __popc(bal);
+        __syncthreads();
+        int before = 0, total = 0;
+        for (int w = 0; w < nw; w++) {
+            if (w < warp) before += wsum[w];
+            total += wsum[w];
+        }
+        before += __popc(bal & ((1u << lane) - 1u));
+        if (kept) {
+            cols[run + before] = (int)j;
+            vals[run + before] = v;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) run += total;
+        __syncthreads();
+    }
+}
+
+void build_casmat_csr(Context &c, const uint64_t *dets, int ndet, const cplx *h, const cplx *g, CsrMatrix &m) {
+    if (c.na > 64) throw Error{DCG_E_ARG, "casmat: more than 64 active spinors"};
+    int64_t *counts = wsget<int64_t>(c, "csr.cnt", (size_t)ndet + 1);
+    casmat_csr_count_kernel<<<ndet, 256, 0, c.stream>>>(c.ni, c.na, c.ne, dets, ndet, h, c.nmo, g, counts);
+    DCG_LAUNCHED(c);
+    std::vector<int64_t> hc(ndet), rp((size_t)ndet + 1, 0);
+    DCG_CUDA(cudaMemcpyAsync(hc.data(), counts, sizeof(int64_t) * ndet, cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    for (int i = 0; i < ndet; i++) rp[i + 1] = rp[i] + hc[i];
+    m.n = ndet;
+    m.nnz = rp[ndet];
+    m.rowptr = wsget<int64_t>(c, "csr.rp", (size_t)ndet + 1);
+    DCG_CUDA(cudaMemcpyAsync(m.rowptr, rp.data(), sizeof(int64_t) * (ndet + 1), cudaMemcpyHostToDevice, c.stream));
+    m.cols = wsget<int>(c, "csr.col", (size_t)m.nnz + 1);
+    m.vals = wsget<cplx>(c, "csr.val", (size_t)m.nnz + 1);
+    m.diag = wsget<double>(c, "csr.diag", (size_t)ndet + 1);
+    casmat_csr_fill_kernel<<<ndet, 256, 0, c.stream>>>(c.ni, c.na, c.ne, dets, ndet, h, c.nmo, g, m.rowptr, m.cols,
+                                                        m.vals, m.diag);
+    DCG_LAUNCHED(c);
+}
+
 void launch_casmat(Context &c, const uint64_t *dets, int ndet, const cplx *h, const cplx *g, cplx *H) {
     DCG_CUDA(cudaMemsetAsync(H, 0, sizeof(cplx) * (size_t)ndet * ndet, c.stream));
     casmat_kernel<<<ndet, 256, 0, c.stream>>>(c.ni, c.na, c.ne, dets, ndet, h, c.nmo, g, H);

@@ -273,10 +273,22 @@ void launch_woodbury_e2(Context &c, int Mp, int r, const cplx *U, int64_t ldu, c
 int64_t mdcint_canonicalize(Context &c, const dcg_mdcint_raw &raw, int32_t **ijkl_out, double **re_out,
                             double **im_out);
 
+// Sparse CASCI Hamiltonian (CSR, rows in CI order, diagonal first in each row).
+struct CsrMatrix {
+    int n = 0;
+    int64_t nnz = 0;
+    int64_t *rowptr = nullptr;
+    int *cols = nullptr;
+    cplx *vals = nullptr;
+    double *diag = nullptr;
+};
+// The Slater-Condon elements of the CI space as CSR (dcg_ci.cu).
+void build_casmat_csr(Context &c, const uint64_t *dets, int ndet, const cplx *h, const cplx *g, CsrMatrix &m);
+// Lowest nwant eigenpairs of the CSR Hamiltonian by block Davidson (dcg_davidson.cu):
+// eigenvalues to w (device), vectors to Z (n x nwant); |r| <= tol_rel max(1, max|H_ii|).
+void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, cplx *Z, double tol_rel, int maxit);
+
 // Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);
-// Lowest nwant eigenpairs of the full-storage Hermitian H (n x n, left intact) by block
-// Davidson: eigenvalues to w (device), vectors to Z (n x nwant); |r| <= tol_rel max(1, max|H_ii|).
-void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cplx *Z, double tol_rel, int maxit);
 
 }  // namespace dcg

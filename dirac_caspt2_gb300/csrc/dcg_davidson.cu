@@ -1,8 +1,9 @@
 // Block Davidson eigensolver for the lowest roots of the CASCI Hamiltonian (Davidson,
 // J. Comput. Phys. 17, 87 (1975); block form of Liu, 1978), the large-ndet CASCI route that
 // replaces the dense ZHEEV of casci.F90:55-70 (diag.F90:66-128) when only a few roots are
-// wanted.  The dense Hamiltonian stays in HBM; every step is a device GEMM or a small kernel:
-//   W = H V                        (the sigma vectors)
+// wanted.  The Hamiltonian stays in HBM as CSR (the diagonal and the single and double
+// excitations of each determinant, dcg_ci.cu); every step is a device kernel:
+//   W = H V                        (the sigma vectors, one warp per row of H)
 //   G = V^H W                      (Rayleigh matrix, symmetrised)
 //   G Y = Y diag(theta)            (one-block cyclic Jacobi, below)
 //   R = W Y - V Y diag(theta)      (residuals of the block's Ritz pairs)
@@ -12,6 +13,7 @@
 // new directions back.  Converged when every wanted root has |r| <= tol.
 #include <algorithm>
 #include <cmath>
+#include <functional>
 #include <numeric>
 #include <vector>
 
@@ -172,12 +174,6 @@ __global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, cons
     if (tid == 0) *status = sweep >= kJacobiMaxSweeps ? 1 : 0;
 }
 
-// hd[i] = Re H(i, i)
-__global__ void hdiag_kernel(int n, const cplx *__restrict__ H, double *hd) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) hd[i] = H[i + (int64_t)n * i].x;
-}
-
 // Columns c of X (n x m) set to the unit vectors e_{idx[c]}.
 __global__ void unit_cols_kernel(int n, int m, const int *__restrict__ idx, cplx *X, int64_t ldx) {
     const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -261,38 +257,43 @@ __global__ void tall_small_kernel(int n, int m, int k, cplx alpha, const cplx *_
     C[r + ldc * c] = v;
 }
 
-// Partial products of H (n x n, column-major) with k vectors X (n x k): chunk q of the columns
-// of H (chunk columns each) contributes P[q][c][r] = sum_{j in chunk q} H[r, j] X[j, c]
-// (threads over rows r, so each column of H is read coalesced).
-__global__ void hx_partial_kernel(int n, int k, int chunk, const cplx *__restrict__ H, const cplx *__restrict__ X,
-                                  int64_t ldx, cplx *P) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const int q = blockIdx.y;
-    const int j0 = q * chunk, j1 = min(n, j0 + chunk);
-    if (r >= n) return;
-    cplx acc[8];
+// Y[:, c] = H X[:, c] for K vectors and a CSR H: one warp per row, the lanes striding the row's
+// entries in order and a fixed shuffle tree summing them (deterministic).
+template <int K>
+__global__ void __launch_bounds__(256) csr_hx_kernel(int n, int k, const int64_t *__restrict__ rowptr,
+                                                      const int *__restrict__ cols, const cplx *__restrict__ vals,
+                                                      const cplx *__restrict__ X, int64_t ldx, cplx *Y, int64_t ldy) {
+    const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (row >= n) return;
+    double re[K], im[K];
 #pragma unroll
-    for (int c = 0; c < 8; c++) acc[c] = mk(0.0, 0.0);
-    for (int j = j0; j < j1; j++) {
-        const cplx h = H[r + (int64_t)n * j];
+    for (int c = 0; c < K; c++) re[c] = im[c] = 0.0;
+    const int64_t e1 = rowptr[row + 1];
+    for (int64_t e = rowptr[row] + lane; e < e1; e += 32) {
+        const cplx h = vals[e];
+        const int j = cols[e];
 #pragma unroll
-        for (int c = 0; c < 8; c++)
-            if (c < k) acc[c] = cadd(acc[c], cmul(h, __ldg(X + j + ldx * c)));
+        for (int c = 0; c < K; c++) {
+            if (c < k) {
+                const cplx x = __ldg(X + j + ldx * c);
+                re[c] = fma(h.x, x.x, fma(-h.y, x.y, re[c]));
+                im[c] = fma(h.x, x.y, fma(h.y, x.x, im[c]));
+            }
+        }
     }
-    const int nq = gridDim.y;
 #pragma unroll
-    for (int c = 0; c < 8; c++)
-        if (c < k) P[((int64_t)c * nq + q) * n + r] = acc[c];
-}
-
-// Y[:, c] = sum over chunks of P (fixed order).
-__global__ void hx_reduce_kernel(int n, int k, int nq, const cplx *__restrict__ P, cplx *Y, int64_t ldy) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const int c = blockIdx.y;
-    if (r >= n) return;
-    cplx acc = mk(0.0, 0.0);
-    for (int q = 0; q < nq; q++) acc = cadd(acc, P[((int64_t)c * nq + q) * n + r]);
-    Y[r + ldy * c] = acc;
+    for (int c = 0; c < K; c++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            re[c] += __shfl_down_sync(0xffffffffu, re[c], o);
+            im[c] += __shfl_down_sync(0xffffffffu, im[c], o);
+        }
+    }
+    if (lane == 0) {
+#pragma unroll
+        for (int c = 0; c < K; c++)
+            if (c < k) Y[row + ldy * c] = mk(re[c], im[c]);
+    }
 }
 
 }  // namespace
@@ -312,17 +313,21 @@ static void tall_small(Context &c, int n, int m, int k, cplx alpha, const cplx *
     DCG_LAUNCHED(c);
 }
 
-// Y (n x k) = H X for up to 8 vectors at a time.  The columns of H are cut into at most 64
-// chunks (of at least 64 columns), so the partial sums stay a small multiple of Y.
-static void hx_many(Context &c, int n, const cplx *H, const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) {
-    const int chunk = std::max(64, (n + 63) / 64);
-    const int nq = (n + chunk - 1) / chunk;
-    cplx *P = wsget<cplx>(c, "dav.hxp", (size_t)8 * nq * n);
+// Y (n x k) = H X for the CSR H, up to 8 vectors a launch (one pass over H for each group).
+static void csr_hx(Context &c, const CsrMatrix &H, const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) {
+    const int n = H.n;
+    const int blocks = (int)(((int64_t)n * 32 + 255) / 256);
     for (int c0 = 0; c0 < k; c0 += 8) {
         const int kk = std::min(8, k - c0);
-        hx_partial_kernel<<<dim3(grid1d(n, 128), nq), 128, 0, c.stream>>>(n, kk, chunk, H, X + ldx * c0, ldx, P);
-        DCG_LAUNCHED(c);
-        hx_reduce_kernel<<<dim3(grid1d(n, 128), kk), 128, 0, c.stream>>>(n, kk, nq, P, Y + ldy * c0, ldy);
+        if (kk > 4)
+            csr_hx_kernel<8><<<blocks, 256, 0, c.stream>>>(n, kk, H.rowptr, H.cols, H.vals, X + ldx * c0, ldx,
+                                                            Y + ldy * c0, ldy);
+        else if (kk > 2)
+            csr_hx_kernel<4><<<blocks, 256, 0, c.stream>>>(n, kk, H.rowptr, H.cols, H.vals, X + ldx * c0, ldx,
+                                                            Y + ldy * c0, ldy);
+        else
+            csr_hx_kernel<2><<<blocks, 256, 0, c.stream>>>(n, kk, H.rowptr, H.cols, H.vals, X + ldx * c0, ldx,
+                                                            Y + ldy * c0, ldy);
         DCG_LAUNCHED(c);
     }
 }
@@ -338,10 +343,11 @@ void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, i
     DCG_LAUNCHED(c);
 }
 
-// Lowest nwant eigenpairs of the Hermitian H (n x n, column-major, full storage, left intact):
-// eigenvalues to w[0..nwant), eigenvectors to the columns of Z (n x nwant, ldz = n), each with
-// residual norm <= tol_rel * max(1, max_i |H_ii|).
-void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cplx *Z, double tol_rel, int maxit) {
+using HxFn = std::function<void(const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy)>;
+
+// Block Davidson on the operator hx (Y = H X) with diagonal hd (device, n).
+static void davidson_core(Context &c, int n, const HxFn &hx, const double *hd, int nwant, double *w, cplx *Z,
+                          double tol_rel, int maxit) {
     const int nb = std::min(n, nwant + 2);   // block: the wanted roots and a margin for near-degeneracy
     const int mmax = std::min(n, std::min(kJacobiMaxN, std::max(24, 8 * nb)));
     if (nwant < 1 || nb > mmax || n < 2) throw Error{DCG_E_ARG, "davidson: block does not fit the subspace"};
@@ -356,14 +362,11 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
     cplx *Y = wsget<cplx>(c, "dav.Y", (size_t)mmax * mmax);
     cplx *cf = wsget<cplx>(c, "dav.cf", (size_t)mmax);
     double *th = wsget<double>(c, "dav.th", mmax);
-    double *hd = wsget<double>(c, "dav.hd", n);
     double *nrm = wsget<double>(c, "dav.nrm", (size_t)3 * nb);
     int *idx = wsget<int>(c, "dav.idx", nb);
     int *jst = wsget<int>(c, "dav.jst", 1);
 
     // start: unit vectors on the nb lowest diagonal elements (ties by index)
-    hdiag_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, H, hd);
-    DCG_LAUNCHED(c);
     std::vector<double> hdh(n);
     DCG_CUDA(cudaMemcpyAsync(hdh.data(), hd, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
     DCG_CUDA(cudaStreamSynchronize(c.stream));
@@ -378,7 +381,7 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
     unit_cols_kernel<<<grid1d((int64_t)n * nb, 256), 256, 0, c.stream>>>(n, nb, idx, V, ld);
     DCG_LAUNCHED(c);
     int m = nb;
-    hx_many(c, n, H, V, ld, m, W, ld);
+    hx(V, ld, m, W, ld);
 
     std::vector<double> h2((size_t)nb);
     bool converged = false;
@@ -436,7 +439,7 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
             while (added < cand && nn[2 * added + 1] > 1e-20 * nn[2 * added] && nn[2 * added + 1] > 0.0) added++;
         }
         if (added == 0) break;   // stagnated: reported below
-        hx_many(c, n, H, V + ld * m, ld, added, W + ld * m, ld);
+        hx(V + ld * m, ld, added, W + ld * m, ld);
         m += added;
     }
     int jh = 0;
@@ -446,6 +449,15 @@ void davidson_lowest(Context &c, int n, const cplx *H, int nwant, double *w, cpl
         throw Error{DCG_E_NUMERIC, "CASCI Davidson did not converge to |r| <= " + std::to_string(tol)};
     DCG_CUDA(cudaMemcpyAsync(w, th, sizeof(double) * nwant, cudaMemcpyDeviceToDevice, c.stream));
     DCG_CUDA(cudaMemcpyAsync(Z, X, sizeof(cplx) * (size_t)n * nwant, cudaMemcpyDeviceToDevice, c.stream));
+}
+
+// Lowest nwant eigenpairs of the Hermitian CSR H (its diagonal kept beside it): eigenvalues to
+// w[0..nwant), eigenvectors to the columns of Z (n x nwant, ldz = n), each with residual norm
+// <= tol_rel * max(1, max_i |H_ii|).
+void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, cplx *Z, double tol_rel, int maxit) {
+    davidson_core(
+        c, H.n, [&](const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) { csr_hx(c, H, X, ldx, k, Y, ldy); },
+        H.diag, nwant, w, Z, tol_rel, maxit);
 }
 
 }  // namespace dcg
