@@ -93,6 +93,27 @@ class MdcintBuffers:
         self.realonly = bool(raw.realonly)
 
 
+class _ActiveInput(ctypes.Structure):
+    """dcg_active_input."""
+    _fields_ = [
+        ("ninact", ctypes.c_int32), ("nact", ctypes.c_int32), ("nsec", ctypes.c_int32), ("nelec", ctypes.c_int32),
+        ("diracver", ctypes.c_int32), ("scheme", ctypes.c_int32), ("nras1", ctypes.c_int32),
+        ("nras2", ctypes.c_int32), ("nras3", ctypes.c_int32), ("ras1", ctypes.c_void_p), ("ras2", ctypes.c_void_p),
+        ("ras3", ctypes.c_void_p),
+    ]
+
+
+class _Mrconee(ctypes.Structure):
+    """dcg_mrconee."""
+    _fields_ = [
+        ("nmo", ctypes.c_int32), ("nsymrpa", ctypes.c_int32), ("dirac_32bit", ctypes.c_int32),
+        ("ecore", ctypes.c_double), ("hf_energy", ctypes.c_double), ("multb", ctypes.POINTER(ctypes.c_int32)),
+        ("irpamo", ctypes.POINTER(ctypes.c_int32)), ("mo_energy", ctypes.POINTER(ctypes.c_double)),
+        ("dirac_to_cas", ctypes.POINTER(ctypes.c_int32)), ("cas_to_dirac", ctypes.POINTER(ctypes.c_int32)),
+        ("h_re", ctypes.POINTER(ctypes.c_double)), ("h_im", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
 class _RequestResult(ctypes.Structure):
     """dcg_request_result of the serving loop."""
     _fields_ = [
@@ -176,6 +197,14 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_server_device_bytes.argtypes = [ctypes.c_void_p]
     lib.dcg_server_device_bytes.restype = ctypes.c_int64
     lib.dcg_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.dcg_read_mrconee.argtypes = [ctypes.c_char_p, P(_ActiveInput), P(P(_Mrconee))]
+    lib.dcg_free_mrconee.argtypes = [P(_Mrconee)]
+    lib.dcg_free_mrconee.restype = None
+    lib.dcg_read_mdcint.argtypes = [ctypes.c_char_p, P(_Mrconee), P(_ActiveInput), ctypes.c_int32,
+                                    P(P(_MdcintRaw))]
+    lib.dcg_free_mdcint.argtypes = [P(_MdcintRaw)]
+    lib.dcg_free_mdcint.restype = None
+    lib.dcg_io_last_error.restype = ctypes.c_char_p
     _lib = lib
     return lib
 
@@ -188,7 +217,8 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_set_casci_solver", "dcg_casci_iterations", "dcg_set_metric_solver",
                     "dcg_gram_cholesky_blocks", "dcg_gram_deflated_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
-                    "dcg_server_device_bytes", "dcg_server_destroy"]
+                    "dcg_server_device_bytes", "dcg_server_destroy", "dcg_read_mrconee", "dcg_free_mrconee",
+                    "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
@@ -343,6 +373,111 @@ class Caspt2Result:
         return float(sum(self.sumc2.values()))
 
 
+class NativeFiles:
+    """MRCONEE and MDCINT of a DIRAC run directory read by the library's C++ readers
+    (dcg_read_mrconee / dcg_read_mdcint), without the Fortran driver or numpy parsing.
+
+    ``inp`` is a dirac_io.ActiveInput; ``pinned`` puts the MDCINT entry arrays in page-locked
+    memory.  ``mdcint`` can be passed to Caspt2Session.set_system_mdcint as is."""
+
+    def __init__(self, directory: str, inp, pinned: bool = False, mdcint: bool = True):
+        self.lib = load_library()
+        self._ras = [np.ascontiguousarray(x, np.int32) for x in (inp.ras1, inp.ras2, inp.ras3)]
+        a = _ActiveInput()
+        a.ninact, a.nact, a.nsec, a.nelec = inp.ninact, inp.nact, inp.nsec, inp.nelec
+        a.diracver = inp.diracver
+        a.scheme = int(inp.scheme or 0)
+        a.nras1, a.nras2, a.nras3 = (len(x) for x in self._ras)
+        a.ras1, a.ras2, a.ras3 = (x.ctypes.data if len(x) else None for x in self._ras)
+        self._inp = a
+        self.inp = inp
+        self._m = ctypes.POINTER(_Mrconee)()
+        self._r = ctypes.POINTER(_MdcintRaw)()
+        rc = self.lib.dcg_read_mrconee(os.path.join(directory, "MRCONEE").encode(), ctypes.byref(a),
+                                       ctypes.byref(self._m))
+        if rc != 0:
+            raise DcgError(rc, self.lib.dcg_io_last_error().decode())
+        self.realonly = None
+        if not mdcint:
+            return
+        rc = self.lib.dcg_read_mdcint(directory.encode(), self._m, ctypes.byref(a), int(bool(pinned)),
+                                      ctypes.byref(self._r))
+        if rc != 0:
+            self.close()
+            raise DcgError(rc, self.lib.dcg_io_last_error().decode())
+        self.realonly = bool(self._r.contents.realonly)
+
+    @property
+    def mdcint(self):
+        """The dcg_mdcint_raw the reader filled (its storage lives as long as this object)."""
+        return self._r.contents
+
+    def mrconee(self):
+        """The MRCONEE content as a dirac_io.MrconeeData (numpy copies)."""
+        from .dirac_io import MrconeeData
+        m = self._m.contents
+        n, n2 = m.nmo, 2 * m.nsymrpa
+        arr = lambda p, k: np.ctypeslib.as_array(p, shape=(k,)).copy()
+        h = arr(m.h_re, n * n).reshape(n, n).T + 1j * arr(m.h_im, n * n).reshape(n, n).T
+        return MrconeeData(nmo=n, ecore=m.ecore, nsymrpa=m.nsymrpa, repna=[],
+                           multb=arr(m.multb, n2 * n2).reshape(n2, n2).T.astype(np.int64),
+                           irpamo=arr(m.irpamo, n).astype(np.int64), mo_energy=arr(m.mo_energy, n),
+                           dirac_to_cas=arr(m.dirac_to_cas, n + 1).astype(np.int64),
+                           cas_to_dirac=arr(m.cas_to_dirac, n + 1).astype(np.int64), h=h,
+                           hf_energy=m.hf_energy, dirac_32bit=bool(m.dirac_32bit))
+
+    def raw(self):
+        """The MDCINT records as a dirac_io.MdcintRaw (numpy copies)."""
+        from .dirac_io import MdcintRaw
+        r = self._r.contents
+        def arr(addr, ct, k):
+            if k == 0:
+                return np.zeros(0, np.dtype(ct))
+            return np.ctypeslib.as_array(ctypes.cast(addr, ctypes.POINTER(ct)), shape=(k,)).copy()
+        ne = int(r.nent)
+        return MdcintRaw(rec_ikr=arr(r.ikr, ctypes.c_int32, r.nrec), rec_jkr=arr(r.jkr, ctypes.c_int32, r.nrec),
+                         rec_off=arr(r.rec_off, ctypes.c_int64, r.nrec + 1), indk=arr(r.indk, ctypes.c_int32, ne),
+                         indl=arr(r.indl, ctypes.c_int32, ne), re=arr(r.re, ctypes.c_double, ne),
+                         im=arr(r.im, ctypes.c_double, ne) if r.im else np.zeros(ne),
+                         kr=arr(r.kr, ctypes.c_int32, 2 * r.nkr).reshape(r.nkr, 2), nmo=int(r.nmo),
+                         dirac_to_cas=arr(r.dirac_to_cas, ctypes.c_int32, r.nmo + 1), scheme=int(r.scheme),
+                         realonly=bool(r.realonly))
+
+    def system_input(self, ciroot_index: int = 0) -> "SystemInput":
+        """The SystemInput of this run directory without records (pass ``mdcint`` to
+        Caspt2Session.set_system_mdcint, which builds them on the device)."""
+        inp = self.inp
+        m = self.mrconee()
+        ts, sr = inp.ciroots[ciroot_index] if inp.ciroots else (1, 1)
+        return SystemInput(ninact=inp.ninact, nact=inp.nact, nsec=inp.nsec, nelec=inp.nelec, nmo=m.nmo,
+                           nsymrpa=m.nsymrpa, multb=m.multb, irpamo=m.irpamo, h=m.h, ecore=m.ecore,
+                           rec_idx=np.zeros((0, 4), np.int32), rec_val=np.zeros(0, np.complex128),
+                           realonly=self.realonly, totsym=ts, selectroot=sr, eshift=inp.eshift,
+                           ras=(len(inp.ras1), len(inp.ras2), len(inp.ras3)), ras1_max_hole=inp.ras1_max_hole,
+                           ras3_max_elec=inp.ras3_max_elec, min_hole_ras1=inp.min_hole_ras1,
+                           min_elec_ras3=inp.min_elec_ras3)
+
+    def close(self) -> None:
+        if getattr(self, "_r", None):
+            self.lib.dcg_free_mdcint(self._r)
+            self._r = ctypes.POINTER(_MdcintRaw)()
+        if getattr(self, "_m", None):
+            self.lib.dcg_free_mrconee(self._m)
+            self._m = ctypes.POINTER(_Mrconee)()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Caspt2Session:
     def __init__(self, device: int = 0, precision: int = DCG_PREC_FP64):
         self.lib = load_library()
@@ -438,12 +573,19 @@ class Caspt2Session:
         return MdcintNew(idx=idx, val=re + 1j * im, realonly=mb.realonly)
 
     def set_system_mdcint(self, s: SystemInput, raw) -> None:
-        """dcg_set_system_mdcint: the system with its records built on the device from MDCINT."""
-        mb = raw if isinstance(raw, MdcintBuffers) else MdcintBuffers(raw)
+        """dcg_set_system_mdcint: the system with its records built on the device from MDCINT
+        (a dirac_io.MdcintRaw, MdcintBuffers, or the NativeFiles reader's ``mdcint``)."""
+        if isinstance(raw, NativeFiles):
+            raw = raw.mdcint
+        if isinstance(raw, _MdcintRaw):
+            mb, st = raw, raw
+        else:
+            mb = raw if isinstance(raw, MdcintBuffers) else MdcintBuffers(raw)
+            st = mb.struct
         self._bufs = HostBuffers(s)
         self.system = s
         self._mdcint = mb
-        self._check(self.lib.dcg_set_system_mdcint(self.h, ctypes.byref(self._bufs.struct), ctypes.byref(mb.struct)))
+        self._check(self.lib.dcg_set_system_mdcint(self.h, ctypes.byref(self._bufs.struct), ctypes.byref(st)))
 
     def set_casci_solver(self, solver: str) -> None:
         """CASCI eigensolver: "auto", "dense" or "davidson" (dcg_set_casci_solver)."""

@@ -38,6 +38,7 @@ extern "C" {
 #define DCG_E_NODET (-4)      /* no CASCI configuration for totsym (search_cas_configuration.F90:158-172) */
 #define DCG_E_NOMEM (-5)      /* device memory exhausted                                */
 #define DCG_E_NUMERIC (-6)    /* eigensolver or solver did not converge                 */
+#define DCG_E_IO (-7)         /* file missing, truncated or not in the expected format  */
 
 /* precision of the dense contractions (the transformation and S/B/V builds) */
 #define DCG_PREC_FP64 0       /* native FP64 everywhere                                  */
@@ -306,6 +307,47 @@ double dcg_server_clock(const dcg_server *srv);
 int64_t dcg_server_device_bytes(dcg_server *srv);
 /* Drop queued requests, finish the running ones, join the workers and free the contexts. */
 int dcg_server_destroy(dcg_server *srv);
+
+/* ------------------------------------------------------------------------ DIRAC files
+ * Host readers of DIRAC's MRCONEE and MDCINT files, so a process without the Fortran driver
+ * can fill dcg_system / dcg_mdcint_raw.  They need no GPU and no context; on failure they
+ * return DCG_E_IO or DCG_E_ARG with the reason in dcg_io_last_error() (per thread). */
+typedef struct dcg_active_input {
+    int32_t ninact, nact, nsec, nelec;   /* .ninact .nact .nsec .nelec                          */
+    int32_t diracver;                    /* .diracver: >= 21 flips the sign of Im h
+                                            (read_mrconee.F90:579-581)                           */
+    int32_t scheme;                      /* .scheme; 0 = the default of .diracver: 4 above 22,
+                                            else 6 (read_input_module.F90:986-1011)              */
+    int32_t nras1, nras2, nras3;         /* .ras1/.ras2/.ras3 list lengths (all 0: CAS)         */
+    const int32_t *ras1, *ras2, *ras3;   /* ascending energy-order spinor numbers, 1-based      */
+} dcg_active_input;
+
+/* MRCONEE (read_mrconee.F90:226-600): energy-order sort, optional RAS order
+ * (read_mrconee.F90:602-715), Kramers pairing by exactly equal orbital energies
+ * (read_mrconee.F90:515-530), one-electron integrals in CAS order. */
+typedef struct dcg_mrconee {
+    int32_t nmo, nsymrpa;
+    int32_t dirac_32bit;                 /* 1: 32-bit integers detected (read_mrconee.F90:1-222) */
+    double ecore, hf_energy;
+    int32_t *multb;                      /* MULTB(2n,2n) column-major, 1-based values            */
+    int32_t *irpamo;                     /* nmo, CAS order                                       */
+    double *mo_energy;                   /* nmo, CAS order (caspt2_mo_energy)                    */
+    int32_t *dirac_to_cas, *cas_to_dirac;   /* nmo + 1, 1-based, entry 0 unused                 */
+    double *h_re, *h_im;                 /* (nmo, nmo) column-major, CAS order                   */
+} dcg_mrconee;
+
+int dcg_read_mrconee(const char *path, const dcg_active_input *inp, dcg_mrconee **out);
+void dcg_free_mrconee(dcg_mrconee *m);
+
+/* MDCINT, MDCINXXXX1, MDCINXXXX2, ... of `directory` (get_filename.F90:1-41) as the flattened
+ * record stream of dcg_mdcint_raw (create_newmdcint.F90:3-171's reads; real-only detected from
+ * the record length as module_realonly.F90:29-77 does).  pinned = 1 places the entry arrays in
+ * page-locked memory (cudaHostAlloc), so dcg_set_system_mdcint copies them at link speed. */
+int dcg_read_mdcint(const char *directory, const dcg_mrconee *mrc, const dcg_active_input *inp, int32_t pinned,
+                    dcg_mdcint_raw **out);
+void dcg_free_mdcint(dcg_mdcint_raw *raw);
+
+const char *dcg_io_last_error(void);
 
 #ifdef __cplusplus
 }

@@ -55,3 +55,28 @@ def test_device_canonicalisation_synthetic(gpu_lib, tmp_path, realonly):
         e2, sc, e0, et = ses.caspt2()
     assert eig[0] == ref.casci_energies[0]
     assert et == ref.total_energy
+
+
+@pytest.mark.parametrize("pinned", [False, True])
+def test_native_files_to_device(gpu_lib, tmp_path, pinned):
+    """A run directory read by the library's C++ readers (MDCINT split over two files, entry
+    arrays optionally page-locked) and canonicalised on the device gives the energies of the
+    Python reader path exactly."""
+    from dirac_caspt2_gb300 import api, dirac_io, synth
+    S = synth.make_system(synth.SynthConfig(4, 6, 16, 3, seed=13))
+    d = str(tmp_path)
+    synth.write_case_files(S, d)
+    recs = dirac_io.read_fortran_records(str(tmp_path / "MDCINT"))
+    half = (len(recs) - 2) // 2
+    dirac_io.write_fortran_records(str(tmp_path / "MDCINT"), recs[:1 + half] + recs[-1:])
+    dirac_io.write_fortran_records(str(tmp_path / "MDCINXXXX1"), recs[:1] + recs[1 + half:])
+    s = api.SystemInput.from_files(d)
+    inp = dirac_io.read_active_inp(str(tmp_path / "active.inp"))
+    with api.Caspt2Session(0) as ses:
+        ref = ses.solve(s)
+        with api.NativeFiles(d, inp, pinned=pinned) as nf:
+            ses.set_system_mdcint(nf.system_input(), nf)
+            eig, _ = ses.casci(1)
+            e2, sc, e0, et = ses.caspt2()
+    assert eig[0] == ref.casci_energies[0]
+    assert et == ref.total_energy
