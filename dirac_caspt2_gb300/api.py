@@ -197,6 +197,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_server_device_bytes.argtypes = [ctypes.c_void_p]
     lib.dcg_server_device_bytes.restype = ctypes.c_int64
     lib.dcg_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.dcg_ivo.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
+                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_int32)]
     lib.dcg_read_mrconee.argtypes = [ctypes.c_char_p, P(_ActiveInput), P(P(_Mrconee))]
     lib.dcg_free_mrconee.argtypes = [P(_Mrconee)]
     lib.dcg_free_mrconee.restype = None
@@ -218,7 +220,7 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_gram_cholesky_blocks", "dcg_gram_deflated_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
                     "dcg_server_device_bytes", "dcg_server_destroy", "dcg_read_mrconee", "dcg_free_mrconee",
-                    "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error"]
+                    "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error", "dcg_ivo"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
@@ -586,6 +588,20 @@ class Caspt2Session:
         self.system = s
         self._mdcint = mb
         self._check(self.lib.dcg_set_system_mdcint(self.h, ctypes.byref(self._bufs.struct), ctypes.byref(st)))
+
+    def ivo(self, nfsym: int, mo_energy: np.ndarray, nhomo: int = 0):
+        """dcg_ivo: (eps (nsec,), U (nsec, nsec) complex, block_isym (nsec,), numh) of the
+        improved virtual orbitals of the resident system."""
+        ns = self.system.nsec
+        me = np.ascontiguousarray(mo_energy, np.float64)
+        eps = np.zeros(ns)
+        ure = np.zeros((ns, ns), order="F")
+        uim = np.zeros((ns, ns), order="F")
+        bs = np.zeros(ns, np.int32)
+        numh = ctypes.c_int32(0)
+        self._check(self.lib.dcg_ivo(self.h, int(nfsym), me.ctypes.data, int(nhomo), eps.ctypes.data, ure.ctypes.data,
+                                     uim.ctypes.data, bs.ctypes.data, ctypes.byref(numh)))
+        return eps, ure + 1j * uim, bs, numh.value
 
     def set_casci_solver(self, solver: str) -> None:
         """CASCI eigensolver: "auto", "dense" or "davidson" (dcg_set_casci_solver)."""

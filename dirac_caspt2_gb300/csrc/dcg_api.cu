@@ -91,20 +91,6 @@ static std::vector<uint64_t> enumerate_ci(const Context &c) {
     return out;
 }
 
-template <typename T>
-static T *upload(Context &c, const std::string &name, const std::vector<T> &v) {
-    T *p = wsget<T>(c, name, v.size() + 1);
-    if (!v.empty()) DCG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
-    return p;
-}
-
-template <typename T>
-static std::vector<T> download(Context &c, const T *p, size_t n) {
-    std::vector<T> v(n);
-    if (n) DCG_CUDA(cudaMemcpyAsync(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost, c.stream));
-    DCG_CUDA(cudaStreamSynchronize(c.stream));
-    return v;
-}
 
 // Stage names double as NVTX range names, so a profiler can select one stage's launches.
 static const char *const kStageName[ST_COUNT] = {"ints", "casci_matrix", "casci_eig", "fock", "ci_rotation",
@@ -250,6 +236,63 @@ static bool use_davidson(const Context &c, int ndet, int nvec) {
     const bool fits = nvec <= kDavidsonMaxRoots && ndet >= nvec + 5;
     if (c.casci_solver == DCG_CASCI_DAVIDSON) return fits;
     return fits && ndet >= kDavidsonMinDet;
+}
+
+// ------------------------------------------------------------------------- IVO
+// r4divo.F90:80-93 / fockivo.F90:44-215 on the resident integrals: the number of HOMO spinors
+// (fockivo.F90:49-53), the blocks of one abelian irrep of each Kramers pair per fermion-irrep
+// group, and their eigenpairs (dcg_ivo.cu).
+static void ivo(Context &c, int nfsym, const double *mo_energy, int nhomo, double *eps, double *u_re, double *u_im,
+                int32_t *block_isym, int32_t *numh_out) {
+    if (!c.have_system) throw Error{DCG_E_STATE, "dcg_ivo before dcg_set_system"};
+    if (nfsym != 1 && nfsym != 2) throw Error{DCG_E_ARG, "IVO: nfsym must be 1 or 2"};
+    if (!mo_energy || nhomo < 0) throw Error{DCG_E_ARG, "IVO: mo_energy missing or nhomo negative"};
+    const int ni = c.ni, na = c.na, ns = c.ns, act_end = ni + na;
+    int numh = nhomo;
+    if (numh == 0) {
+        if (c.ne + ni < 1) throw Error{DCG_E_ARG, "IVO: no occupied spinor"};
+        const double eh = mo_energy[c.ne + ni - 1];
+        for (int p = 0; p < act_end; p++)
+            if (std::fabs(mo_energy[p] - eh) < 1.0e-1) numh++;
+    }
+    if (numh < 1 || numh > na) throw Error{DCG_E_ARG, "IVO: the HOMO spinors must lie in the active space"};
+    std::vector<std::vector<int>> blocks;
+    std::vector<int> bsym;
+    for (int g = 0; g < nfsym; g++) {
+        const int s0 = g == 0 ? 1 : c.nsym / 2 + 1, s1 = g == 0 ? c.nsym / 2 : c.nsym;
+        for (int isym = s0; isym <= s1; isym += 2) {
+            std::vector<int> L;
+            for (int a = 0; a < ns; a++)
+                if (c.irpamo[act_end + a] == isym) L.push_back(a);
+            if (!L.empty()) {
+                blocks.push_back(L);
+                bsym.push_back(isym);
+            }
+        }
+    }
+    DevSystem &d = dev(c);
+    std::vector<std::vector<double>> w;
+    std::vector<std::vector<cplx>> v;
+    ivo_blocks_eig(c, d.cls[CL_F1A].p, d.cls[CL_F2A].p, mo_energy + act_end, na - numh, na, c.ne % 2, (double)numh,
+                   blocks, w, v);
+    if (eps) std::fill(eps, eps + ns, 0.0);
+    if (block_isym) std::fill(block_isym, block_isym + ns, 0);
+    if (u_re) std::fill(u_re, u_re + (size_t)ns * ns, 0.0);
+    if (u_im) std::fill(u_im, u_im + (size_t)ns * ns, 0.0);
+    for (size_t b = 0; b < blocks.size(); b++) {
+        const std::vector<int> &L = blocks[b];
+        const size_t n = L.size();
+        for (size_t i = 0; i < n; i++) {
+            if (eps) eps[L[i]] = w[b][i];
+            if (block_isym) block_isym[L[i]] = bsym[b];
+            for (size_t j = 0; j < n; j++) {
+                const cplx x = v[b][i + n * j];
+                if (u_re) u_re[L[i] + (size_t)ns * L[j]] = x.x;
+                if (u_im) u_im[L[i] + (size_t)ns * L[j]] = x.y;
+            }
+        }
+    }
+    if (numh_out) *numh_out = numh;
 }
 
 static int casci(Context &c, int nroot, double *eigen_out, double *ci_re, double *ci_im, int32_t *ndet_out) {
@@ -1540,6 +1583,14 @@ int dcg_set_system_mdcint(dcg_ctx *ctx, const dcg_system *sys, const dcg_mdcint_
     s2.realonly = ctx->c.mdc_realonly ? 1 : sys->realonly;
     s2.rec_on_device = 1;
     return dcg_set_system(ctx, &s2);
+}
+
+int dcg_ivo(dcg_ctx *ctx, int32_t nfsym, const double *mo_energy, int32_t nhomo, double *eps, double *u_re,
+            double *u_im, int32_t *block_isym, int32_t *numh_out) {
+    DCG_API_BODY(ctx, {
+        dcg::ivo(c_, nfsym, mo_energy, nhomo, eps, u_re, u_im, block_isym, numh_out);
+        return DCG_OK;
+    });
 }
 
 int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver) {

@@ -166,6 +166,23 @@ T *wsget(Context &c, const std::string &name, size_t count) {
     return reinterpret_cast<T *>(c.ws.get(name, count * sizeof(T) + 256));
 }
 
+// A host vector copied into the named workspace buffer (stream-ordered).
+template <typename T>
+T *upload(Context &c, const std::string &name, const std::vector<T> &v) {
+    T *p = wsget<T>(c, name, v.size() + 1);
+    if (!v.empty()) DCG_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c.stream));
+    return p;
+}
+
+// n elements of device memory read back (synchronises the context's stream).
+template <typename T>
+std::vector<T> download(Context &c, const T *p, size_t n) {
+    std::vector<T> v(n);
+    if (n) DCG_CUDA(cudaMemcpyAsync(v.data(), p, n * sizeof(T), cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaStreamSynchronize(c.stream));
+    return v;
+}
+
 // Records CUDA events around the launches of one kernel family when that family is
 // selected; elapsed times are collected by fam_collect() after the stream synchronises.
 struct FamScope {
@@ -287,6 +304,13 @@ void build_casmat_csr(Context &c, const uint64_t *dets, int ndet, const cplx *h,
 // Lowest nwant eigenpairs of the CSR Hamiltonian by block Davidson (dcg_davidson.cu):
 // eigenvalues to w (device), vectors to Z (n x nwant); |r| <= tol_rel max(1, max|H_ii|).
 void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, cplx *Z, double tol_rel, int maxit);
+
+// IVO (dcg_ivo.cu): the Fock matrix of the secondary spinors from (ab|kk) and (ak|kb) over the
+// active HOMO spinors [k0, k1), e_sec the secondary orbital energies (host), and the
+// eigenpairs of each block of secondary indices by the LAPACK ZHEEV algorithm.
+void ivo_blocks_eig(Context &c, const cplx *F1A, const cplx *F2A, const double *e_sec_host, int k0, int k1, int odd,
+                    double numh, const std::vector<std::vector<int>> &blocks, std::vector<std::vector<double>> &w_out,
+                    std::vector<std::vector<cplx>> &v_out);
 
 // Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
 void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);

@@ -27,7 +27,7 @@ import numpy as np
 __all__ = [
     "ActiveInput", "MrconeeData", "MdcintNew",
     "read_active_inp", "read_fortran_records", "write_fortran_records",
-    "read_mrconee", "read_mdcint_new", "mdcint_filenames",
+    "read_mrconee", "read_mdcint_new", "mdcint_filenames", "Dfpcmo", "read_dfpcmo", "write_dfpcmo",
 ]
 
 
@@ -101,6 +101,12 @@ class ActiveInput:
     min_hole_ras1: int = 0
     min_elec_ras3: int = 0
     subprograms: Tuple[str, ...] = ("CASCI", "CASPT2")
+    # IVO keywords (read_input_module.F90:150-201): .nhomo; .nocc/.nvcut without inversion
+    # symmetry, .noccg/.noccu/.nvcutg/.nvcutu with it
+    nhomo: int = 0
+    occ_mo_num: Tuple[int, int] = (0, 0)
+    vcut_mo_num: Tuple[int, int] = (0, 0)
+    inversion: bool = False
 
     @property
     def mdcint_scheme(self) -> int:
@@ -193,7 +199,14 @@ def read_active_inp(path_or_text: str) -> ActiveInput:
             kw[key] = _parse_int_list(lines[i])
             i += 1
         elif key in (".ninact", ".nact", ".nsec", ".nelec", ".diracver", ".scheme",
-                     ".minholeras1", ".minelecras3"):
+                     ".minholeras1", ".minelecras3", ".nhomo"):
+            kw[key] = int(lines[i])
+            i += 1
+        elif key in (".nocc", ".nvcut", ".noccg", ".noccu", ".nvcutg", ".nvcutu"):
+            inv = key in (".noccg", ".noccu", ".nvcutg", ".nvcutu")
+            if kw.get("inversion", inv) != inv:
+                raise ValueError("active.inp: .nocc/.nvcut and .noccg/.noccu/.nvcutg/.nvcutu exclude each other")
+            kw["inversion"] = inv
             kw[key] = int(lines[i])
             i += 1
         elif key == ".eshift":
@@ -213,7 +226,11 @@ def read_active_inp(path_or_text: str) -> ActiveInput:
         ras3=kw.get(".ras3", []), ras1_max_hole=kw.get(".ras1_max", 0),
         ras3_max_elec=kw.get(".ras3_max", 0), min_hole_ras1=kw.get(".minholeras1", 0),
         min_elec_ras3=kw.get(".minelecras3", 0),
-        subprograms=tuple(subprograms) if subprograms else ("CASCI", "CASPT2"))
+        subprograms=tuple(subprograms) if subprograms else ("CASCI", "CASPT2"),
+        nhomo=kw.get(".nhomo", 0),
+        occ_mo_num=(kw.get(".noccg", kw.get(".nocc", 0)), kw.get(".noccu", 0)),
+        vcut_mo_num=(kw.get(".nvcutg", kw.get(".nvcut", 0)), kw.get(".nvcutu", 0)),
+        inversion=bool(kw.get("inversion", False)))
 
 
 # --------------------------------------------------------------------------------------
@@ -568,3 +585,146 @@ def read_mdcint_new(directory: str, mrc: MrconeeData, inp: ActiveInput) -> Mdcin
     """Restatement of ``create_newmdcint`` (create_newmdcint.F90:3-321) returning the
     MDCINTNEW records in memory instead of on disk."""
     return canonicalize_mdcint(read_mdcint_raw(directory, mrc, inp))
+
+
+# --------------------------------------------------------------------------------------
+# DFPCMO (DIRAC's formatted MO coefficient file; read and rewritten by the IVO program)
+# --------------------------------------------------------------------------------------
+@dataclasses.dataclass
+class Dfpcmo:
+    """DFPCMO as fockivo.F90:87-160 reads it.  With DIRAC >= 21 the sections carry title
+    lines (INFO, COEFS, EVALS, SUPERSYM, KAPPA), kept verbatim; ``nfsym`` is the number of
+    fermion-irrep groups (2 with inversion symmetry), ``nfsym2`` the second integer of the
+    dimension line of the new format."""
+    titles: dict                 # "info", "coefs", "evals", "supersym", "kappa" -> line or None
+    name_line: str
+    energy_line: str
+    nfsym: int
+    nfsym2: Optional[int]
+    positronic: List[int]
+    electronic: List[int]
+    basis_ao: List[int]
+    coef: np.ndarray             # (total_ao,) float64, per group MO-major blocks
+    evals: np.ndarray            # (total_mo,)
+    supersym: np.ndarray         # (total_mo,) int
+    kappa: Optional[np.ndarray]  # (total_mo,) int or None
+    new_format: bool
+
+    @property
+    def total_mo(self) -> int:
+        return sum(self.positronic) + sum(self.electronic)
+
+    @property
+    def basis_all(self) -> List[int]:
+        return [(p + e) * b for p, e, b in zip(self.positronic, self.electronic, self.basis_ao)]
+
+
+def _tokens(lines: List[str], pos: int, n: int, conv):
+    out = []
+    while len(out) < n:
+        if pos >= len(lines):
+            raise ValueError("DFPCMO: unexpected end of file")
+        out.extend(conv(t.replace("D", "E").replace("d", "e")) for t in lines[pos].split())
+        pos += 1
+    if len(out) != n:
+        raise ValueError("DFPCMO: a list does not end on a line boundary")
+    return out, pos
+
+
+def read_dfpcmo(path: str, new_format: bool) -> Dfpcmo:
+    """fockivo.F90:87-160 (list-directed reads; the title lines only with ``new_format``,
+    i.e. DIRAC >= 21)."""
+    lines = open(path).read().split("\n")
+    if lines and lines[-1] == "":
+        lines.pop()
+    pos = 0
+    titles = {}
+
+    def title(key):
+        nonlocal pos
+        if new_format:
+            titles[key] = lines[pos]
+            pos += 1
+        else:
+            titles[key] = None
+
+    title("info")
+    name_line = lines[pos]
+    pos += 1
+    dims = [int(t) for t in lines[pos].split()]
+    pos += 1
+    nfsym = dims[0]
+    rest = dims[2:] if new_format else dims[1:]
+    nfsym2 = dims[1] if new_format else None
+    positronic = [rest[3 * g] for g in range(nfsym)]
+    electronic = [rest[3 * g + 1] for g in range(nfsym)]
+    basis_ao = [rest[3 * g + 2] for g in range(nfsym)]
+    energy_line = lines[pos]
+    pos += 1
+    title("coefs")
+    total_ao = sum((p + e) * b for p, e, b in zip(positronic, electronic, basis_ao))
+    total_mo = sum(positronic) + sum(electronic)
+    coef, pos = _tokens(lines, pos, total_ao, float)
+    title("evals")
+    evals, pos = _tokens(lines, pos, total_mo, float)
+    title("supersym")
+    sup, pos = _tokens(lines, pos, total_mo, int)
+    kappa = None
+    while pos < len(lines) and not lines[pos].strip():
+        pos += 1
+    if pos < len(lines):
+        title("kappa")
+        kappa, pos = _tokens(lines, pos, total_mo, int)
+        kappa = np.array(kappa, np.int64)
+    else:
+        titles["kappa"] = None
+    return Dfpcmo(titles=titles, name_line=name_line, energy_line=energy_line, nfsym=nfsym, nfsym2=nfsym2,
+                  positronic=positronic, electronic=electronic, basis_ao=basis_ao, coef=np.array(coef, np.float64),
+                  evals=np.array(evals, np.float64), supersym=np.array(sup, np.int64), kappa=kappa,
+                  new_format=new_format)
+
+
+def _fortran_e(x: float, w: int = 22, d: int = 12) -> str:
+    """Fortran Ew.d: 0.ddd...E+xx."""
+    if x == 0.0:
+        body = "0." + "0" * d + "E+00"
+    else:
+        m = f"{abs(x):.{d - 1}e}"
+        digits = m[0] + m[2:2 + d - 1]
+        ex = int(m.split("e")[1]) + 1
+        body = ("-" if x < 0 else "") + "0." + digits + (f"E{ex:+03d}" if abs(ex) < 100 else f"{ex:+04d}")
+    return body.rjust(w)
+
+
+def _rows(items: List[str], per: int) -> List[str]:
+    return ["".join(items[k:k + per]) for k in range(0, len(items), per)] or [""]
+
+
+def write_dfpcmo(path: str, d: Dfpcmo) -> None:
+    """fockivo.F90:296-346: the title lines as read (A150), the dimension line in I0 fields,
+    coefficients 6F22.16, energies 6E22.12, supersymmetry and kappa 66(X,I0)."""
+    out = []
+    a150 = lambda s: s[:150].ljust(150)
+    if d.new_format:
+        out.append(a150(d.titles["info"]))
+    out.append(a150(d.name_line))
+    dims = [d.nfsym] + ([d.nfsym2] if d.new_format else [])
+    for g in range(d.nfsym):
+        dims += [d.positronic[g], d.electronic[g], d.basis_ao[g]]
+    out.append("".join(f" {v}" for v in dims))
+    out.append(a150(d.energy_line))
+    if d.new_format:
+        out.append(a150(d.titles["coefs"]))
+    out += _rows([f"{x:22.16f}" for x in d.coef], 6)
+    if d.new_format:
+        out.append(a150(d.titles["evals"]))
+    out += _rows([_fortran_e(float(x)) for x in d.evals], 6)
+    if d.new_format:
+        out.append(a150(d.titles["supersym"]))
+    out += _rows([f" {int(v)}" for v in d.supersym], 66)
+    if d.kappa is not None:
+        if d.new_format:
+            out.append(a150(d.titles["kappa"]))
+        out += _rows([f" {int(v)}" for v in d.kappa], 66)
+    with open(path, "w") as f:
+        f.write("\n".join(out) + "\n")

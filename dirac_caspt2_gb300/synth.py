@@ -211,49 +211,68 @@ def make_system(cfg: SynthConfig, keep_factors: Optional[bool] = None) -> SynthS
 # --------------------------------------------------------------------------------------
 # DIRAC-format files for a synthetic system (small systems: exercises the readers)
 # --------------------------------------------------------------------------------------
-def write_case_files(sysm: SynthSystem, directory: str, diracver: int = 21) -> None:
-    """Write active.inp, MRCONEE and MDCINT (64-bit DIRAC layout, scheme 6) such that the
-    reference readers reproduce ``sysm`` exactly."""
-    import os
+def write_mrconee(path: str, nmo: int, ecore: float, h: np.ndarray, mo_energy: np.ndarray, diracver: int = 21,
+                  nsymrpa: int = 1, multb: Optional[np.ndarray] = None, irpamo: Optional[np.ndarray] = None) -> None:
+    """MRCONEE in the 64-bit DIRAC layout (read_mrconee.F90:226-600) with the spinors already
+    in energy (CAS) order: records NMO/ECORE, irreps, MULTB (2n x 2n, [i0-1, j0-1] =
+    MULTB(i0, j0)), (IRPMO, IRPAMO, energy) and the one-electron integrals."""
     import struct
-    from .dirac_io import ActiveInput, write_fortran_records
-    cfg = sysm.cfg
-    os.makedirs(directory, exist_ok=True)
-    nmo = sysm.nmo
-    inp = ActiveInput(ninact=cfg.ninact, nact=cfg.nact, nsec=cfg.nsec, nelec=cfg.nelec,
-                      ciroots=[(1, 1)], eshift=cfg.eshift, diracver=diracver, scheme=6)
-    open(os.path.join(directory, "active.inp"), "w").write(inp.to_text())
+    from .dirac_io import write_fortran_records
     i8 = lambda *xs: struct.pack("<" + "q" * len(xs), *xs)
-    r1 = i8(nmo, 0) + struct.pack("<d", sysm.ecore) + i8(1, 2, 0, nmo) + struct.pack("<d", 0.0)
-    r2 = i8(2) + b"   1A         " + b"   2A         "
-    r3 = i8(1) + b"   A" + b"   a"
-    r4 = i8(2, 1, 1, 2)
-    r5 = b"".join(i8(1, 1) + struct.pack("<d", float(e)) for e in sysm.mo_energy)
-    hh = sysm.h
-    onei = -hh.imag if diracver >= 21 else hh.imag
-    r6 = np.stack([hh.real, onei], axis=2).astype("<f8").tobytes()   # ((ONER(i,j),ONEI(i,j),j),i)
-    write_fortran_records(os.path.join(directory, "MRCONEE"), [r1, r2, r3, r4, r5, r6])
-    # MDCINT: header + records keyed by signed Kramers indices of the DIRAC-side quadruple
+    n2 = 2 * nsymrpa
+    mb = np.array([[2, 1], [1, 2]], np.int64) if multb is None else np.asarray(multb, np.int64)
+    irp = np.ones(nmo, np.int64) if irpamo is None else np.asarray(irpamo, np.int64)
+    r1 = i8(nmo, 0) + struct.pack("<d", ecore) + i8(1, 2, 0, nmo) + struct.pack("<d", 0.0)
+    r2 = i8(n2) + b"".join(f"{k + 1:>4d}A         ".encode()[:14] for k in range(n2))
+    r3 = i8(nsymrpa) + b"".join(f"{k + 1:>4d}"[-4:].encode() for k in range(n2))
+    r4 = i8(*[int(x) for x in mb.T.reshape(-1)])          # Fortran column-major
+    r5 = b"".join(i8(int(irp[k]), int(irp[k])) + struct.pack("<d", float(mo_energy[k])) for k in range(nmo))
+    onei = -h.imag if diracver >= 21 else h.imag
+    r6 = np.stack([h.real, onei], axis=2).astype("<f8").tobytes()   # ((ONER(i,j),ONEI(i,j),j),i)
+    write_fortran_records(path, [r1, r2, r3, r4, r5, r6])
+
+
+def write_mdcint(path: str, nmo: int, rec_idx: np.ndarray, rec_val: np.ndarray, realonly: bool) -> None:
+    """MDCINT (64-bit, scheme 6) holding the given MDCINTNEW records: header with the Kramers
+    table, one record per signed Kramers index pair of the DIRAC-side (i, j), values conjugated
+    as create_newmdcint undoes (create_newmdcint.F90:171-177), end record."""
+    import struct
+    from .dirac_io import write_fortran_records
+    i8 = lambda *xs: struct.pack("<" + "q" * len(xs), *xs)
     npair = nmo // 2
     hdr = b" 01Jan26  " + b"00:00:00" + i8(npair) + b"".join(i8(2 * m - 1, 2 * m) for m in range(1, npair + 1))
-    p = sysm.rec_idx.astype(np.int64) - 1
+    p = np.asarray(rec_idx).astype(np.int64) - 1
     dirac = (p ^ 1) + 1                                           # DIRAC-side 1-based spinors
     signed = np.where(dirac % 2 == 1, 1, -1) * ((dirac + 1) // 2)
-    w = np.conj(sysm.rec_val)
-    realonly = cfg.realonly
+    w = np.conj(np.asarray(rec_val))
     order = np.lexsort((signed[:, 1], signed[:, 0]))
     signed, w = signed[order], w[order]
     recs = [hdr]
     keys = signed[:, 0] * (npair + 1) * 4 + signed[:, 1]
-    starts = np.flatnonzero(np.r_[True, keys[1:] != keys[:-1]])
-    ends = np.r_[starts[1:], len(keys)]
-    for a, b in zip(starts, ends):
-        nz = b - a
-        kl = signed[a:b, 2:4].astype("<i8").tobytes()
-        if realonly:
-            vv = w[a:b].real.astype("<f8").tobytes()
-        else:
-            vv = np.stack([w[a:b].real, w[a:b].imag], axis=1).astype("<f8").tobytes()
-        recs.append(i8(int(signed[a, 0]), int(signed[a, 1]), int(nz)) + kl + vv)
+    if len(keys):
+        starts = np.flatnonzero(np.r_[True, keys[1:] != keys[:-1]])
+        ends = np.r_[starts[1:], len(keys)]
+        for a, b in zip(starts, ends):
+            nz = b - a
+            kl = signed[a:b, 2:4].astype("<i8").tobytes()
+            if realonly:
+                vv = w[a:b].real.astype("<f8").tobytes()
+            else:
+                vv = np.stack([w[a:b].real, w[a:b].imag], axis=1).astype("<f8").tobytes()
+            recs.append(i8(int(signed[a, 0]), int(signed[a, 1]), int(nz)) + kl + vv)
     recs.append(i8(0, 0, 0))
-    write_fortran_records(os.path.join(directory, "MDCINT"), recs)
+    write_fortran_records(path, recs)
+
+
+def write_case_files(sysm: SynthSystem, directory: str, diracver: int = 21) -> None:
+    """Write active.inp, MRCONEE and MDCINT (64-bit DIRAC layout, scheme 6) such that the
+    reference readers reproduce ``sysm`` exactly."""
+    import os
+    from .dirac_io import ActiveInput
+    cfg = sysm.cfg
+    os.makedirs(directory, exist_ok=True)
+    inp = ActiveInput(ninact=cfg.ninact, nact=cfg.nact, nsec=cfg.nsec, nelec=cfg.nelec,
+                      ciroots=[(1, 1)], eshift=cfg.eshift, diracver=diracver, scheme=6)
+    open(os.path.join(directory, "active.inp"), "w").write(inp.to_text())
+    write_mrconee(os.path.join(directory, "MRCONEE"), sysm.nmo, sysm.ecore, sysm.h, sysm.mo_energy, diracver)
+    write_mdcint(os.path.join(directory, "MDCINT"), sysm.nmo, sysm.rec_idx, sysm.rec_val, cfg.realonly)

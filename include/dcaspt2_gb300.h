@@ -308,6 +308,24 @@ int64_t dcg_server_device_bytes(dcg_server *srv);
 /* Drop queued requests, finish the running ones, join the workers and free the contexts. */
 int dcg_server_destroy(dcg_server *srv);
 
+/* ------------------------------------------------------------------------ IVO
+ * Improved virtual orbitals (r4divo.F90:80-93, fockivo.F90:44-215) on the system of the last
+ * dcg_set_system / dcg_set_system_mdcint (its ninact, nact, nsec, nelec as the IVO input
+ * gives them): the Fock matrix of the secondary spinors
+ *   f(a,b) = e_a delta_ab - sum_k w_k [(ab|kk) - (ak|kb)] / numh
+ * over the numh highest active spinors k (w_k = 1/2 for the two highest when nelec is odd;
+ * numh = nhomo, or for nhomo = 0 the spinors up to the last active one within 0.1 Eh of the
+ * HOMO energy), diagonalised per abelian irrep block by the LAPACK ZHEEV algorithm (its
+ * eigenvector signs included).  The blocks are, per fermion-irrep group (nfsym = 2 with
+ * inversion symmetry), every second irrep: 1, 3, .. nsymrpa/2 and nsymrpa/2+1, .. nsymrpa.
+ *   mo_energy : nmo orbital energies, CAS order (dcg_mrconee.mo_energy)
+ *   eps       : nsec, the eigenvalue at each block position (0 outside the blocks)
+ *   u_re/u_im : nsec x nsec column-major, U(a_i, a_j) = V(i, j) of the block of a_i and a_j
+ *   block_isym: nsec, the irrep of the block each secondary spinor belongs to, 0 if none
+ * Any output may be NULL. */
+int dcg_ivo(dcg_ctx *ctx, int32_t nfsym, const double *mo_energy, int32_t nhomo, double *eps, double *u_re,
+            double *u_im, int32_t *block_isym, int32_t *numh_out);
+
 /* ------------------------------------------------------------------------ DIRAC files
  * Host readers of DIRAC's MRCONEE and MDCINT files, so a process without the Fortran driver
  * can fill dcg_system / dcg_mdcint_raw.  They need no GPU and no context; on failure they

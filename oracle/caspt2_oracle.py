@@ -1073,3 +1073,374 @@ def e_subspace_envelope(s: System, trials: int = 6, seed: int = 0) -> Tuple[floa
 
 SOLVERS = {"A": solve_A, "B": solve_B, "C": solve_C, "D": solve_D,
            "E": solve_E, "F": solve_F, "G": solve_G, "H": solve_H}
+
+
+# ======================================================================================
+# IVO: improved virtual orbitals (r4divo.F90, fockivo.F90)
+# ======================================================================================
+def ivo_fock(s: System, ints: Integrals, mo_energy: np.ndarray, nhomo: int) -> Tuple[np.ndarray, int]:
+    """The Fock matrix of the secondary spinors for IVO (fockivo.F90:44-85):
+    f(i,j) = e_i delta_ij - sum_k w_k [(ij|kk) - (ik|kj)] / numh over the numh highest active
+    spinors k (w_k = 1/2 for the two highest when nelec is odd); numh = nhomo, or when 0 the
+    number of spinors up to the last active one whose energy lies within 0.1 Eh of the HOMO
+    e(ninact + nelec).  Only the upper triangle and the real diagonal are used downstream."""
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    act_end = ni + na   # 1-based global index of the last active spinor
+    if nhomo == 0:
+        numh = int(np.count_nonzero(np.abs(mo_energy[:act_end] - mo_energy[s.nelec + ni - 1]) < 1.0e-1))
+    else:
+        numh = nhomo
+    F1 = ints.block((3, 3, 2, 2))   # (ab|kl)
+    F2 = ints.block((3, 2, 2, 3))   # (ak|lb)
+    f = np.zeros((ns, ns), dtype=np.complex128)
+    for i in range(ns):
+        f[i, i] = mo_energy[act_end + i]
+    for k in range(act_end - numh + 1, act_end + 1):   # 1-based global
+        ka = k - 1 - ni
+        w = 0.5 if (k > act_end - 2 and s.nelec % 2 == 1) else 1.0
+        f += w * (-F1[:, :, ka, ka] + F2[:, ka, ka, :]) / numh
+    return np.triu(f), numh
+
+
+def ivo_blocks(s: System, nfsym: int) -> List[Tuple[int, np.ndarray]]:
+    """(isym, secondary indices) of the blocks fockivo diagonalises (fockivo.F90:180-215):
+    per fermion-irrep group, every second abelian irrep (one of each Kramers pair)."""
+    out = []
+    ni, na, ns = s.ninact, s.nact, s.nsec
+    irp = np.asarray(s.irpamo[ni + na:ni + na + ns])
+    for g in range(nfsym):
+        start, end = (1, s.nsymrpa // 2) if g == 0 else (s.nsymrpa // 2 + 1, s.nsymrpa)
+        for isym in range(start, end + 1, 2):
+            out.append((isym, np.flatnonzero(irp == isym)))
+    return out
+
+
+def ivo(s: System, ints: Integrals, mo_energy: np.ndarray, d, nhomo: int, occ_mo_num, vcut_mo_num,
+        lartg: str = "old"):
+    """IVO (r4divo.F90:80-93, fockivo.F90:44-270): the virtual-space Fock matrix, its
+    eigenvectors per abelian irrep block, and the DFPCMO coefficients of the virtual MOs
+    rotated by them.  Returns (new coefficient vector, {isym: eigenvalues}, numh)."""
+    fu, numh = ivo_fock(s, ints, mo_energy, nhomo)
+    coef = d.coef.copy()
+    mo = [p + e for p, e in zip(d.positronic, d.electronic)]
+    evals = {}
+    blocks = ivo_blocks(s, d.nfsym)
+    for g in range(d.nfsym):
+        nao = d.basis_ao[g]
+        base = (0 if g == 0 else d.basis_all[0]) + (d.positronic[g] + occ_mo_num[g]) * nao
+        nvirt = d.electronic[g] - occ_mo_num[g] - vcut_mo_num[g]
+        itrfmo = coef[base:base + nvirt * nao].reshape(nvirt, nao).T.astype(np.complex128)   # (ao, mo)
+        mo_off = (0 if g == 0 else mo[0]) + d.positronic[g] + occ_mo_num[g]
+        lo = mo_off + 1
+        hi = (0 if g == 0 else mo[0]) + d.positronic[g] + d.electronic[g] - vcut_mo_num[g]
+        for isym, sec in blocks:
+            if (g == 0) != (isym <= s.nsymrpa // 2):
+                continue
+            isym_sup = isym if g == 0 else isym - s.nsymrpa // 2
+            sup = d.supersym[lo - 1:hi]
+            if np.all(sup == 0):
+                dmosym = np.arange(lo, hi + 1)
+            else:
+                dmosym = np.arange(lo, hi + 1)[np.abs(sup) == isym_sup]
+            nv = len(sec)
+            fs = fu[np.ix_(sec, sec)]
+            A = np.triu(fs, 1)
+            A = A + A.conj().T + np.diag(fs.diagonal().real)
+            w, V = zheev_lapack(A, lartg)
+            evals[isym] = w
+            cols = dmosym - mo_off - 1
+            if len(cols) != nv:
+                raise ValueError("IVO: DFPCMO and input disagree on the virtual MOs of an irrep")
+            itrfmo[:, cols] = itrfmo[:, cols] @ V
+        coef[base:base + nvirt * nao] = itrfmo.real.T.reshape(-1)
+    return coef, evals, numh
+
+
+# ======================================================================================
+# LAPACK ZHEEV, restated step by step (the eigenvector signs of IVO's DFPCMONEW)
+# ======================================================================================
+# The IVO orbitals are ZHEEV's eigenvectors (diag.F90:66-128 cdiag, jobz 'V', uplo 'U'), and
+# the sign of each is whatever that algorithm leaves.  This restates the published LAPACK
+# 3.x reference algorithm (not in the reference project; a link-time dependency): ZHETD2
+# (Householder reduction, upper), ZUNGTR/ZUNG2L (accumulate Q), ZSTEQR (implicit QL/QR
+# with Wilkinson shifts, DLAEV2 for 2x2 blocks, selection sort).  Two generations of the
+# Givens generator DLARTG differ in the sign of the rotation when |f| <= |g|, f < 0 (LAPACK
+# <= 3.9 versus >= 3.10); ``lartg`` selects one.
+_EPS = np.finfo(np.float64).eps * 0.5        # dlamch('E')
+_SAFMIN = np.finfo(np.float64).tiny          # dlamch('S')
+
+
+def _dlapy2(x, y):
+    w, z = max(abs(x), abs(y)), min(abs(x), abs(y))
+    return w if z == 0.0 else w * math.sqrt(1.0 + (z / w) ** 2)
+
+
+def _dlartg(f, g, variant):
+    if variant == "new":   # LAPACK >= 3.10 (la_xlartg)
+        if g == 0.0:
+            return 1.0, 0.0, f
+        if f == 0.0:
+            return 0.0, math.copysign(1.0, g), abs(g)
+        d = math.sqrt(f * f + g * g)
+        r = math.copysign(d, f)
+        return abs(f) / d, g / r, r
+    if g == 0.0:           # LAPACK <= 3.9
+        return 1.0, 0.0, f
+    if f == 0.0:
+        return 0.0, 1.0, g
+    r = math.sqrt(f * f + g * g)
+    cs, sn = f / r, g / r
+    if abs(f) > abs(g) and cs < 0.0:
+        cs, sn, r = -cs, -sn, -r
+    return cs, sn, r
+
+
+def _dlaev2(a, b, c):
+    sm, df = a + c, a - c
+    adf, tb = abs(df), b + b
+    ab = abs(tb)
+    acmx, acmn = (a, c) if abs(a) > abs(c) else (c, a)
+    if adf > ab:
+        rt = adf * math.sqrt(1.0 + (ab / adf) ** 2)
+    elif adf < ab:
+        rt = ab * math.sqrt(1.0 + (adf / ab) ** 2)
+    else:
+        rt = ab * math.sqrt(2.0)
+    if sm < 0.0:
+        rt1, sgn1 = 0.5 * (sm - rt), -1
+        rt2 = (acmx / rt1) * acmn - (b / rt1) * b
+    elif sm > 0.0:
+        rt1, sgn1 = 0.5 * (sm + rt), 1
+        rt2 = (acmx / rt1) * acmn - (b / rt1) * b
+    else:
+        rt1, rt2, sgn1 = 0.5 * rt, -0.5 * rt, 1
+    if df >= 0.0:
+        cs, sgn2 = df + rt, 1
+    else:
+        cs, sgn2 = df - rt, -1
+    if abs(cs) > ab:
+        ct = -tb / cs
+        sn1 = 1.0 / math.sqrt(1.0 + ct * ct)
+        cs1 = ct * sn1
+    elif ab == 0.0:
+        cs1, sn1 = 1.0, 0.0
+    else:
+        tn = -cs / tb
+        cs1 = 1.0 / math.sqrt(1.0 + tn * tn)
+        sn1 = tn * cs1
+    if sgn1 == sgn2:
+        cs1, sn1 = -sn1, cs1
+    return rt1, rt2, cs1, sn1
+
+
+def _zlasr_rvb(Z, c, s, j0, mm, forward):
+    """ZLASR('R', 'V', 'B'/'F') on columns j0 .. j0+mm-1 of Z with rotations c, s."""
+    order = range(mm - 1) if forward else range(mm - 2, -1, -1)
+    for j in order:
+        ct, st = c[j], s[j]
+        if ct != 1.0 or st != 0.0:
+            t = Z[:, j0 + j + 1].copy()
+            Z[:, j0 + j + 1] = ct * t - st * Z[:, j0 + j]
+            Z[:, j0 + j] = st * t + ct * Z[:, j0 + j]
+
+
+def zheev_lapack(A: np.ndarray, lartg: str = "new"):
+    """ZHEEV(jobz='V', uplo='U') of the Hermitian A (upper triangle read): eigenvalues
+    ascending and the eigenvectors as the reference LAPACK computes them."""
+    n = A.shape[0]
+    a = np.triu(np.asarray(A, dtype=np.complex128)).copy()
+    if n == 0:
+        return np.zeros(0), np.zeros((0, 0), np.complex128)
+    if n == 1:
+        return np.array([a[0, 0].real]), np.ones((1, 1), np.complex128)
+    d = np.zeros(n)
+    e = np.zeros(n - 1)
+    tau = np.zeros(n - 1, np.complex128)
+    # ZHETD2, uplo 'U' (0-based: reflector i annihilates a[0:i-1, i+1])
+    a[n - 1, n - 1] = a[n - 1, n - 1].real
+
+    def herm(k):   # the Hermitian matrix held in the upper triangle of a[0:k, 0:k]
+        u = np.triu(a[:k, :k], 1)
+        return u + u.conj().T + np.diag(a[:k, :k].diagonal().real)
+
+    for i in range(n - 2, -1, -1):
+        alpha = a[i, i + 1]
+        x = a[:i, i + 1]
+        xnorm = float(np.linalg.norm(x)) if i > 0 else 0.0
+        alphr, alphi = alpha.real, alpha.imag
+        if xnorm == 0.0 and alphi == 0.0:
+            taui = 0.0 + 0.0j
+        else:
+            beta = -math.copysign(math.sqrt(alphr * alphr + alphi * alphi + xnorm * xnorm), alphr)
+            taui = complex((beta - alphr) / beta, -alphi / beta)
+            scal = 1.0 / (alpha - beta)
+            a[:i, i + 1] = x * scal
+            alpha = beta
+        e[i] = alpha.real
+        if taui != 0:
+            a[i, i + 1] = 1.0
+            v = a[:i + 1, i + 1].copy()
+            t = taui * (herm(i + 1) @ v)
+            al = -0.5 * taui * np.vdot(t, v)
+            t = t + al * v
+            upd = np.outer(v, t.conj()) + np.outer(t, v.conj())
+            a[:i + 1, :i + 1] -= np.triu(upd)
+            for q in range(i + 1):
+                a[q, q] = a[q, q].real
+        else:
+            a[i, i] = a[i, i].real
+        a[i, i + 1] = e[i]
+        d[i + 1] = a[i + 1, i + 1].real
+        tau[i] = taui
+    d[0] = a[0, 0].real
+    # ZUNGTR, uplo 'U': shift the reflector vectors one column left, then ZUNG2L
+    q = np.zeros((n, n), np.complex128)
+    for j in range(n - 1):
+        q[:j, j] = a[:j, j + 1]
+    q[n - 1, n - 1] = 1.0
+    m = n - 1
+    for i in range(m):        # ZUNG2L(m, m, m): ii = i
+        q[i, i] = 1.0
+        if i > 0:
+            v = q[:i + 1, i].copy()
+            C = q[:i + 1, :i]
+            w = C.conj().T @ v
+            q[:i + 1, :i] = C - tau[i] * np.outer(v, w.conj())
+            q[:i, i] = -tau[i] * q[:i, i]
+        q[i, i] = 1.0 - tau[i]
+        q[i + 1:m, i] = 0.0
+    Z = q
+    # ZSTEQR, compz 'V'
+    eps2 = _EPS * _EPS
+    nmaxit, jtot = 30 * n, 0
+    l1 = 0
+    while l1 < n:
+        if l1 > 0:
+            e[l1 - 1] = 0.0
+        msplit = n - 1
+        for mm_ in range(l1, n - 1):
+            tst = abs(e[mm_])
+            if tst == 0.0:
+                msplit = mm_
+                break
+            if tst <= math.sqrt(abs(d[mm_])) * math.sqrt(abs(d[mm_ + 1])) * _EPS:
+                e[mm_] = 0.0
+                msplit = mm_
+                break
+        l, lend = l1, msplit
+        lsv, lendsv = l, lend
+        l1 = msplit + 1
+        if lend == l:
+            continue
+        anorm = max(np.abs(d[l:lend + 1]).max(), np.abs(e[l:lend]).max() if lend > l else 0.0)
+        if anorm == 0.0:
+            continue
+        if abs(d[lend]) < abs(d[l]):
+            lend, l = lsv, lendsv
+        if lend > l:   # QL
+            while True:
+                mq = lend
+                for mm_ in range(l, lend):
+                    if abs(e[mm_]) ** 2 <= (eps2 * abs(d[mm_])) * abs(d[mm_ + 1]) + _SAFMIN:
+                        mq = mm_
+                        break
+                if mq < lend:
+                    e[mq] = 0.0
+                p = d[l]
+                if mq == l:
+                    d[l] = p
+                    l += 1
+                    if l <= lend:
+                        continue
+                    break
+                if mq == l + 1:
+                    rt1, rt2, c, s = _dlaev2(d[l], e[l], d[l + 1])
+                    _zlasr_rvb(Z, [c], [s], l, 2, forward=False)
+                    d[l], d[l + 1], e[l] = rt1, rt2, 0.0
+                    l += 2
+                    if l <= lend:
+                        continue
+                    break
+                if jtot == nmaxit:
+                    break
+                jtot += 1
+                g = (d[l + 1] - p) / (2.0 * e[l])
+                r = _dlapy2(g, 1.0)
+                g = d[mq] - p + (e[l] / (g + math.copysign(r, g)))
+                s, c, p = 1.0, 1.0, 0.0
+                cw, sw = np.zeros(mq - l), np.zeros(mq - l)
+                for i in range(mq - 1, l - 1, -1):
+                    f = s * e[i]
+                    b = c * e[i]
+                    c, s, r = _dlartg(g, f, lartg)
+                    if i != mq - 1:
+                        e[i + 1] = r
+                    g = d[i + 1] - p
+                    r = (d[i] - g) * s + 2.0 * c * b
+                    p = s * r
+                    d[i + 1] = g + p
+                    g = c * r - b
+                    cw[i - l], sw[i - l] = c, -s
+                _zlasr_rvb(Z, cw, sw, l, mq - l + 1, forward=False)
+                d[l] -= p
+                e[l] = g
+        else:          # QR
+            while True:
+                mq = lend
+                for mm_ in range(l, lend, -1):
+                    if abs(e[mm_ - 1]) ** 2 <= (eps2 * abs(d[mm_])) * abs(d[mm_ - 1]) + _SAFMIN:
+                        mq = mm_
+                        break
+                if mq > lend:
+                    e[mq - 1] = 0.0
+                p = d[l]
+                if mq == l:
+                    d[l] = p
+                    l -= 1
+                    if l >= lend:
+                        continue
+                    break
+                if mq == l - 1:
+                    rt1, rt2, c, s = _dlaev2(d[l - 1], e[l - 1], d[l])
+                    _zlasr_rvb(Z, [c], [s], l - 1, 2, forward=True)
+                    d[l - 1], d[l], e[l - 1] = rt1, rt2, 0.0
+                    l -= 2
+                    if l >= lend:
+                        continue
+                    break
+                if jtot == nmaxit:
+                    break
+                jtot += 1
+                g = (d[l - 1] - p) / (2.0 * e[l - 1])
+                r = _dlapy2(g, 1.0)
+                g = d[mq] - p + (e[l - 1] / (g + math.copysign(r, g)))
+                s, c, p = 1.0, 1.0, 0.0
+                cw, sw = np.zeros(l - mq), np.zeros(l - mq)
+                for i in range(mq, l):
+                    f = s * e[i]
+                    b = c * e[i]
+                    c, s, r = _dlartg(g, f, lartg)
+                    if i != mq:
+                        e[i - 1] = r
+                    g = d[i] - p
+                    r = (d[i + 1] - g) * s + 2.0 * c * b
+                    p = s * r
+                    d[i] = g + p
+                    g = c * r - b
+                    cw[i - mq], sw[i - mq] = c, s
+                _zlasr_rvb(Z, cw, sw, mq, l - mq + 1, forward=True)
+                d[l] -= p
+                e[l - 1] = g
+        if jtot >= nmaxit:
+            raise ValueError("ZSTEQR: no convergence")
+    # selection sort, swapping eigenvector columns
+    for ii in range(1, n):
+        i = ii - 1
+        k, p = i, d[i]
+        for j in range(ii, n):
+            if d[j] < p:
+                k, p = j, d[j]
+        if k != i:
+            d[k], d[i] = d[i], p
+            Z[:, [i, k]] = Z[:, [k, i]]
+    return d, Z

@@ -8,6 +8,11 @@ the CASCI total energy of the selected root, the per-subspace ``e2X`` and ``sumc
 the total CASPT2 energy.  For the cases with small MDCINT files it also stores the raw MDCINT
 records (``<case>_mdcint_raw.npz``), the input of the MDCINT canonicalisation.
 
+For the IVO cases (``ivo_*.npz``): the system read with ``active.ivo.inp``, the MDCINTNEW
+records IVO reads (two secondary and two active indices: the (ab|kk) and (ak|kb) classes of
+fockivo.F90:56-85), the orbital energies, the IVO keywords, the DFPCMO text and the
+coefficients of the reference's ``reference.DFPCMONEW``.
+
 Usage:  python tests/golden/make_golden_fixtures.py /path/to/reference/test/dev
 """
 import os
@@ -78,5 +83,35 @@ def main(devdir: str):
             print(case, "raw entries", len(raw.re))
 
 
+IVO_CASES = ["ivo_c32h_ar_with_kappa_dev", "ivo_c32h_n2_dev_dirac19", "ivo_c32h_n2_dev_dirac22"]
+
+
+def main_ivo(devdir: str):
+    for case in IVO_CASES:
+        d = os.path.join(devdir, case)
+        inp = dirac_io.read_active_inp(os.path.join(d, "active.ivo.inp"))
+        mrc = dirac_io.read_mrconee(os.path.join(d, "MRCONEE"), inp)
+        new = dirac_io.read_mdcint_new(d, mrc, inp)
+        ni, na, ns = inp.ninact, inp.nact, inp.nsec
+        g = new.idx.astype(np.int64) - 1
+        sp = np.where(g < ni, 1, np.where(g < ni + na, 2, np.where(g < ni + na + ns, 3, 4)))
+        keep = ((sp == 3).sum(axis=1) == 2) & ((sp == 2).sum(axis=1) == 2)
+        ref = dirac_io.read_dfpcmo(os.path.join(d, "reference.DFPCMONEW"), inp.diracver >= 21)
+        out = dict(ninact=ni, nact=na, nsec=ns, nelec=inp.nelec, nmo=mrc.nmo, nsymrpa=mrc.nsymrpa,
+                   multb=mrc.multb.astype(np.int32), irpamo=mrc.irpamo.astype(np.int32), h_re=mrc.h.real,
+                   h_im=mrc.h.imag, ecore=mrc.ecore, mo_energy=mrc.mo_energy, realonly=new.realonly,
+                   rec_idx=new.idx[keep].astype(np.int16), rec_re=new.val.real[keep], diracver=inp.diracver,
+                   nhomo=inp.nhomo, occ_mo_num=np.array(inp.occ_mo_num, np.int32),
+                   vcut_mo_num=np.array(inp.vcut_mo_num, np.int32), inversion=inp.inversion,
+                   dfpcmo_text=np.frombuffer(open(os.path.join(d, "DFPCMO"), "rb").read(), np.uint8),
+                   ref_coef=ref.coef)
+        if not new.realonly:
+            out["rec_im"] = new.val.imag[keep]
+        np.savez_compressed(os.path.join(HERE, f"{case}.npz"), **out)
+        print(case, "records", int(keep.sum()), "of", len(new))
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test/dev")
+    top = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/test/dev"
+    main(top)
+    main_ivo(top)
