@@ -42,3 +42,25 @@ def test_ras_casci_dense_davidson_oracle(gpu_lib, dims, ras, ndet, realonly):
         ref = O.run(oracle_system(s), subspaces="")
         assert ref.ndet == ndet
         assert np.abs(out["davidson"] - ref.casci_energies[:3]).max() <= 1e-10
+
+
+@pytest.mark.parametrize("realonly", [False, True])
+def test_ras_caspt2_matches_oracle(gpu_lib, realonly):
+    """RASPT2 through the whole path (RAS CI space, the CI rotation by the linear solve of the
+    restricted determinant list, densities, A-H) against the oracle: every e2 within 1e-9 Eh,
+    the total within 1e-10 Eh."""
+    from dirac_caspt2_gb300 import api, synth
+    from oracle import caspt2_oracle as O
+    from conftest import oracle_system
+    S = synth.make_system(synth.SynthConfig(4, 8, 10, 4, seed=43, realonly=realonly))
+    s = api.SystemInput.from_synth(S)
+    s.ras = (2, 4, 2)
+    s.ras1_max_hole = 1
+    s.ras3_max_elec = 1
+    with api.Caspt2Session(0) as ses:
+        r = ses.solve(s)
+    ref = O.run(oracle_system(s))
+    assert r.ndet == ref.ndet and r.ndet < 70    # restricted below the 70 of the full space
+    for k in "ABCDEFGH":
+        assert abs(r.e2[k] - ref.e2[k]) <= 1e-9, k
+    assert abs(r.total_energy - ref.total_energy) <= 1e-10
