@@ -114,6 +114,13 @@ class _Mrconee(ctypes.Structure):
     ]
 
 
+class _TuneEntry(ctypes.Structure):
+    """dcg_tune_entry."""
+    _fields_ = [("kind", ctypes.c_int32), ("ops", ctypes.c_int32), ("m", ctypes.c_int32), ("n", ctypes.c_int32),
+                ("k", ctypes.c_int32), ("flags", ctypes.c_int32), ("choice", ctypes.c_int32),
+                ("ncand", ctypes.c_int32), ("best_ms", ctypes.c_float), ("heuristic_ms", ctypes.c_float)]
+
+
 class _RequestResult(ctypes.Structure):
     """dcg_request_result of the serving loop."""
     _fields_ = [
@@ -197,6 +204,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_server_device_bytes.argtypes = [ctypes.c_void_p]
     lib.dcg_server_device_bytes.restype = ctypes.c_int64
     lib.dcg_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.dcg_autotune_mode.argtypes = [ctypes.c_int32]
+    lib.dcg_autotune_entries.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.dcg_autotune_entries.restype = ctypes.c_int32
     lib.dcg_ivo.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
                             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, P(ctypes.c_int32)]
     lib.dcg_read_mrconee.argtypes = [ctypes.c_char_p, P(_ActiveInput), P(P(_Mrconee))]
@@ -220,9 +230,30 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_gram_cholesky_blocks", "dcg_gram_deflated_blocks", "dcg_device_bytes", "dcg_trim", "dcg_footprint_estimate", "dcg_server_create",
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
                     "dcg_server_device_bytes", "dcg_server_destroy", "dcg_read_mrconee", "dcg_free_mrconee",
-                    "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error", "dcg_ivo"]
+                    "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error", "dcg_ivo",
+                    "dcg_autotune_mode", "dcg_autotune_entries"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
+
+
+TUNE_KINDS = {1: "fp64_gemm_ksplit", 2: "split_gemm_kchunk"}
+
+
+def autotune_mode(mode: int = -1) -> int:
+    """dcg_autotune_mode: 1 tune on first use, 0 heuristics, 2 clear the table; -1 query.
+    Returns the previous mode."""
+    return int(load_library().dcg_autotune_mode(int(mode)))
+
+
+def autotune_entries() -> List[dict]:
+    """The process-wide table of tuned choices (dcg_autotune_entries)."""
+    lib = load_library()
+    n = int(lib.dcg_autotune_entries(None, 0))
+    buf = (_TuneEntry * max(n, 1))()
+    n = int(lib.dcg_autotune_entries(ctypes.cast(buf, ctypes.c_void_p), n))
+    return [dict(kind=TUNE_KINDS.get(e.kind, e.kind), ops=e.ops, m=e.m, n=e.n, k=e.k, flags=e.flags,
+                 choice=e.choice, ncand=e.ncand, best_ms=round(e.best_ms, 4), heuristic_ms=round(e.heuristic_ms, 4))
+            for e in buf[:n]]
 
 
 def _ptr(a: Optional[np.ndarray], ct):

@@ -185,18 +185,61 @@ __global__ void casmat_kernel(int ni, int na, int ne, const uint64_t *__restrict
 // ------------------------------------------------------------------------- sparse CASCI matrix
 // The same Slater-Condon elements (casmat.F90:3-222), as a CSR matrix for the Davidson route:
 // row i holds its diagonal and every single and double excitation of det i that lies in the
-// CI space (RAS restrictions included), each element computed from row i's determinant.
-// Candidates of a row: q < ne nv singles, then the ne(ne-1)/2 x nv(nv-1)/2 doubles.
+// CI space (RAS restrictions included).  Candidates of a row: q < ne nv singles, then the
+// ne(ne-1)/2 x nv(nv-1)/2 doubles.  An element H(i, j) with j > i is computed from det i as
+// the dense kernel does; one with j < i is conj(H(j, i)) computed from det j by the same
+// arithmetic in the same order, so the matrix is Hermitian to the bit (the dense kernel
+// mirrors its upper triangle the same way).
 struct CsrRow {
     int occ[64], vir[64];
 };
 
-__device__ bool casmat_candidate(int ni, int na, int ne, const uint64_t *__restrict__ dets, int ndet,
-                                 const cplx *__restrict__ h, int nmo, const cplx *__restrict__ g, uint64_t I,
-                                 const CsrRow &rw, int64_t q, int64_t &jout, cplx &vout) {
-    const int nmoc = ni + na, nv = na - ne, nocc = ni + ne;
+// <single excitation av <- ro of the source determinant S> (S holds ro, not av): h plus the
+// sum over S's occupied spinors (inactive, then active in increasing order), signed by the
+// excitation's phase.
+__device__ cplx single_elem(int ni, int na, const cplx *__restrict__ h, int nmo, const cplx *__restrict__ g,
+                            uint64_t S, int ro, int av) {
+    const int nmoc = ni + na;
 #define GIDX(p, q_, r, s) ((int64_t)(p) + (int64_t)nmoc * ((q_) + (int64_t)nmoc * ((r) + (int64_t)nmoc * (s))))
-#define OCCG(x) ((x) < ni ? (x) : ni + rw.occ[(x) - ni])
+    uint64_t J;
+    int ph;
+    exct(S, av, ro, na, J, ph);
+    const int ir = ni + ro, ia = ni + av;
+    cplx v = h[ir + (int64_t)nmo * ia];
+    for (int k = 0; k < ni; k++) {
+        v = cadd(v, g[GIDX(ir, ia, k, k)]);
+        v = csub(v, g[GIDX(ir, k, k, ia)]);
+    }
+    for (uint64_t B = S; B; B &= B - 1) {
+        const int s2 = ni + __ffsll((long long)B) - 1;
+        v = cadd(v, g[GIDX(ir, ia, s2, s2)]);
+        v = csub(v, g[GIDX(ir, s2, s2, ia)]);
+    }
+    if (ph & 1) v = mk(-v.x, -v.y);
+    return v;
+}
+
+// <double excitation a <- r, b <- s of S> (r < s occupied, a < b empty).
+__device__ cplx double_elem(int ni, int na, const cplx *__restrict__ g, uint64_t S, int r_, int s_, int a_, int b_) {
+    const int nmoc = ni + na;
+    uint64_t J1, J2;
+    int p1, p2;
+    exct(S, a_, r_, na, J1, p1);
+    exct(J1, b_, s_, na, J2, p2);
+    const int ir = ni + r_, is = ni + s_, ia = ni + a_, ib = ni + b_;
+    cplx v = csub(g[GIDX(ir, ia, is, ib)], g[GIDX(ir, ib, is, ia)]);
+    if ((p1 + p2) & 1) v = mk(-v.x, -v.y);
+    return v;
+#undef GIDX
+}
+
+// Candidate q of row i (determinant I): false when the excitation vanishes or leaves the CI
+// space; else its column and (WANT_VAL) its element.
+template <bool WANT_VAL>
+__device__ bool casmat_candidate(int ni, int na, int ne, const uint64_t *__restrict__ dets, int ndet,
+                                 const cplx *__restrict__ h, int nmo, const cplx *__restrict__ g, int64_t i,
+                                 uint64_t I, const CsrRow &rw, int64_t q, int64_t &jout, cplx &vout) {
+    const int nv = na - ne;
     const int64_t nsing = (int64_t)ne * nv;
     if (q < nsing) {
         const int ro = rw.occ[q / nv], av = rw.vir[q % nv];
@@ -205,16 +248,8 @@ __device__ bool casmat_candidate(int ni, int na, int ne, const uint64_t *__restr
         if (!exct(I, av, ro, na, J, ph)) return false;
         const int64_t j = find_sorted(dets, ndet, J);
         if (j < 0) return false;
-        const int ir = ni + ro, ia = ni + av;
-        cplx v = h[ir + (int64_t)nmo * ia];
-        for (int x = 0; x < nocc; x++) {
-            const int s2 = OCCG(x);
-            v = cadd(v, g[GIDX(ir, ia, s2, s2)]);
-            v = csub(v, g[GIDX(ir, s2, s2, ia)]);
-        }
-        if (ph & 1) v = mk(-v.x, -v.y);
         jout = j;
-        vout = v;
+        if (WANT_VAL) vout = j > i ? single_elem(ni, na, h, nmo, g, I, ro, av) : cconj(single_elem(ni, na, h, nmo, g, J, av, ro));
         return true;
     }
     q -= nsing;
@@ -250,14 +285,10 @@ __device__ bool casmat_candidate(int ni, int na, int ne, const uint64_t *__restr
     if (!exct(J1, b_, s_, na, J2, p2)) return false;
     const int64_t j = find_sorted(dets, ndet, J2);
     if (j < 0) return false;
-    const int ir = ni + r_, is = ni + s_, ia = ni + a_, ib = ni + b_;
-    cplx v = csub(g[GIDX(ir, ia, is, ib)], g[GIDX(ir, ib, is, ia)]);
-    if ((p1 + p2) & 1) v = mk(-v.x, -v.y);
     jout = j;
-    vout = v;
+    // from det j the occupied pair is (a, b) and the empty pair (r, s), both increasing
+    if (WANT_VAL) vout = j > i ? double_elem(ni, na, g, I, r_, s_, a_, b_) : cconj(double_elem(ni, na, g, J2, a_, b_, r_, s_));
     return true;
-#undef OCCG
-#undef GIDX
 }
 
 __device__ void casmat_row_setup(int na, uint64_t I, CsrRow &rw) {
@@ -315,7 +346,7 @@ __global__ void __launch_bounds__(256) casmat_csr_count_kernel(int ni, int na, i
     for (int64_t q = threadIdx.x; q < ncand; q += blockDim.x) {
         int64_t j;
         cplx v;
-        cnt += casmat_candidate(ni, na, ne, dets, ndet, h, nmo, g, I, rw, q, j, v) ? 1 : 0;
+        cnt += casmat_candidate<false>(ni, na, ne, dets, ndet, h, nmo, g, i, I, rw, q, j, v) ? 1 : 0;
     }
     for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = cnt;
@@ -353,7 +384,7 @@ __global__ void __launch_bounds__(256) casmat_csr_fill_kernel(int ni, int na, in
         const int64_t q = q0 + threadIdx.x;
         int64_t j = 0;
         cplx v = mk(0.0, 0.0);
-        const bool kept = q < ncand && casmat_candidate(ni, na, ne, dets, ndet, h, nmo, g, I, rw, q, j, v);
+        const bool kept = q < ncand && casmat_candidate<true>(ni, na, ne, dets, ndet, h, nmo, g, i, I, rw, q, j, v);
         const unsigned bal = __ballot_sync(0xffffffffu, kept);
         if (lane == 0) wsum[warp] = __popc(bal);
         __syncthreads();

@@ -6,6 +6,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <cstdio>
+#include <cstdlib>
 #include <map>
 #include <string>
 #include <vector>
@@ -56,6 +58,8 @@ struct Context;
 class Workspace {
   public:
     void *get(const std::string &name, size_t bytes);
+    // page-locked host buffer (small per-step readbacks), kept like the device buffers
+    void *host(const std::string &name, size_t bytes);
     void release_all();
     size_t bytes_in_use() const { return total_; }
     ~Workspace() { release_all(); }
@@ -65,7 +69,7 @@ class Workspace {
         void *p = nullptr;
         size_t bytes = 0;
     };
-    std::map<std::string, Buf> bufs_;
+    std::map<std::string, Buf> bufs_, host_;
     size_t total_ = 0;
 };
 
@@ -182,6 +186,64 @@ std::vector<T> download(Context &c, const T *p, size_t n) {
     DCG_CUDA(cudaStreamSynchronize(c.stream));
     return v;
 }
+
+// ---------------------------------------------------------------- autotuner
+// A process-wide table of tuned choices, keyed by the decision and the problem shape.  The
+// first call of a key with trial_ok runs every candidate once (untimed, so workspaces grow
+// outside the timing), then times each on the caller's stream with CUDA events (best of two)
+// and keeps the fastest; later calls of the key, in any context, reuse it.  Candidate 0 is the
+// built-in heuristic, used while tuning is off (dcg_autotune_mode) and for keys first met
+// without trial_ok.  The trial runs must leave the same result as the final run.
+enum TuneKind { TUNE_ZGEMM_SPLITK = 1, TUNE_SPLIT_KCHUNK = 2 };
+struct TuneKey {
+    int kind, ops, m, n, k, flags;
+    bool operator<(const TuneKey &o) const {
+        if (kind != o.kind) return kind < o.kind;
+        if (ops != o.ops) return ops < o.ops;
+        if (m != o.m) return m < o.m;
+        if (n != o.n) return n < o.n;
+        if (k != o.k) return k < o.k;
+        return flags < o.flags;
+    }
+};
+int autotune_run(Context &c, const TuneKey &key, int ncand, bool trial_ok, void (*fn)(void *, int), void *arg);
+template <typename F>
+int autotune(Context &c, const TuneKey &key, int ncand, bool trial_ok, F &&run) {
+    return autotune_run(c, key, ncand, trial_ok, [](void *p, int q) { (*static_cast<F *>(p))(q); }, &run);
+}
+
+// Diagnostic: with DCG_GEMM_TRACE=1 in the environment, each GEMM call is timed by CUDA events
+// (synchronising the stream) and printed to stderr as "gemm <kind> m n k batch <ms>".
+struct GemmTrace {
+    Context &c;
+    const char *kind;
+    int m, n, k, batch;
+    cudaEvent_t a = nullptr, b = nullptr;
+    static bool enabled() {
+        static const bool on = [] {
+            const char *e = getenv("DCG_GEMM_TRACE");
+            return e && e[0] == '1';
+        }();
+        return on;
+    }
+    GemmTrace(Context &c_, const char *kind_, int m_, int n_, int k_, int batch_)
+        : c(c_), kind(kind_), m(m_), n(n_), k(k_), batch(batch_) {
+        if (!enabled()) return;
+        cudaEventCreate(&a);
+        cudaEventCreate(&b);
+        cudaEventRecord(a, c.stream);
+    }
+    ~GemmTrace() {
+        if (!a) return;
+        cudaEventRecord(b, c.stream);
+        cudaEventSynchronize(b);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, a, b);
+        fprintf(stderr, "gemm %s %d %d %d %d %.4f\n", kind, m, n, k, batch, ms);
+        cudaEventDestroy(a);
+        cudaEventDestroy(b);
+    }
+};
 
 // Records CUDA events around the launches of one kernel family when that family is
 // selected; elapsed times are collected by fam_collect() after the stream synchronises.

@@ -63,9 +63,11 @@ __device__ __forceinline__ int rr_player(int pos, int s, int np) {
 // J_pp = J_qq = c, J_pq = s e^{i phi}, J_qp = -s e^{-i phi}.  Sweeps stop when the squared
 // off-diagonal Frobenius norm is below 1e-30 of the whole (status 1 after 40 sweeps).
 // Output: ascending eigenvalues w[n], eigenvectors Y (n x n, ldy).  One block.
-__global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, const cplx *__restrict__ G, int ldg,
+__global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, const int *__restrict__ n_dev,
+                                                                       const cplx *__restrict__ G, int ldg,
                                                                        double *w, cplx *Y, int ldy, int *status) {
     extern __shared__ double2 jsm[];
+    if (n_dev) n = *n_dev;   // dimension read on the device (graph replays of a Davidson step)
     const int np = n + (n & 1);   // padded to even: the dummy player pairs with nobody
     cplx *A = jsm;                // np x np
     cplx *V = A + np * np;        // np x np
@@ -171,7 +173,7 @@ __global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, cons
         const int i = e % n, j = e / n;
         Y[i + (int64_t)ldy * rank_sh[j]] = V[i + np * j];
     }
-    if (tid == 0) *status = sweep >= kJacobiMaxSweeps ? 1 : 0;
+    if (tid == 0 && sweep >= kJacobiMaxSweeps) *status = 1;
 }
 
 // Columns c of X (n x m) set to the unit vectors e_{idx[c]}.
@@ -201,60 +203,6 @@ __global__ void residual_kernel(int n, const cplx *__restrict__ HX, const cplx *
     }
     acc = block_sum_d(acc, sh);
     if (threadIdx.x == 0) out2[c] = acc;
-}
-
-// out2[0] = |x|^2 (one block, fixed reduction order)
-__global__ void norm2_kernel(int n, const cplx *__restrict__ x, double *out2) {
-    __shared__ double sh[32];
-    double acc = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += x[i].x * x[i].x + x[i].y * x[i].y;
-    acc = block_sum_d(acc, sh);
-    if (threadIdx.x == 0) out2[0] = acc;
-}
-
-// x <- x / sqrt(*n2)
-__global__ void normalize_kernel(int n, cplx *x, const double *__restrict__ n2) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const double s = 1.0 / sqrt(*n2);
-    x[i] = mk(x[i].x * s, x[i].y * s);
-}
-
-// C[i + ldc j] (op)= sum_k conj(A[k + lda i]) B[k + ldb j] for a small i x j output and a long
-// k: one block per output element, fixed-order reduction.  beta: 0 overwrite, 1 accumulate
-// with alpha.
-__global__ void dotc_small_kernel(int n, const cplx *__restrict__ A, int64_t lda, const cplx *__restrict__ B,
-                                  int64_t ldb, cplx *C, int ldc, double alpha, int accumulate) {
-    __shared__ double sh[32];
-    const int i = blockIdx.x, j = blockIdx.y;
-    const cplx *a = A + lda * i, *b = B + ldb * j;
-    double re = 0.0, im = 0.0;
-    for (int k = threadIdx.x; k < n; k += blockDim.x) {
-        const cplx x = a[k], y = b[k];
-        re += x.x * y.x + x.y * y.y;
-        im += x.x * y.y - x.y * y.x;
-    }
-    re = block_sum_d(re, sh);
-    im = block_sum_d(im, sh);
-    if (threadIdx.x == 0) {
-        cplx v = mk(alpha * re, alpha * im);
-        if (accumulate) v = cadd(v, C[i + (int64_t)ldc * j]);
-        C[i + (int64_t)ldc * j] = v;
-    }
-}
-
-// C (n x k) = alpha A (n x m) B (m x k) + beta C, m and k small: one thread per row (coalesced
-// over rows), the m x k factor read through the read-only cache.
-__global__ void tall_small_kernel(int n, int m, int k, cplx alpha, const cplx *__restrict__ A, int64_t lda,
-                                  const cplx *__restrict__ B, int ldb, cplx beta, cplx *C, int64_t ldc) {
-    const int r = blockIdx.x * blockDim.x + threadIdx.x;
-    const int c = blockIdx.y;
-    if (r >= n) return;
-    cplx acc = mk(0.0, 0.0);
-    for (int q = 0; q < m; q++) acc = cadd(acc, cmul(A[r + lda * q], __ldg(B + q + (int64_t)ldb * c)));
-    cplx v = cmul(alpha, acc);
-    if (beta.x != 0.0 || beta.y != 0.0) v = cadd(v, cmul(beta, C[r + ldc * c]));
-    C[r + ldc * c] = v;
 }
 
 // Y[:, c] = H X[:, c] for K vectors and a CSR H: one warp per row, the lanes striding the row's
@@ -296,22 +244,193 @@ __global__ void __launch_bounds__(256) csr_hx_kernel(int n, int k, const int64_t
     }
 }
 
+// ---- the Davidson step with its sizes on the device ------------------------------------
+// A step's launches read the subspace size m and the running counts from DavState, so one
+// captured sequence (a CUDA graph) serves every step.
+struct DavState {
+    int m;        // vectors in V (and W = H V)
+    int cand;     // new directions accepted in this step
+    int stop;     // a direction was rejected: none after it this step
+    int act;      // the direction being built is live
+    int jac;      // a Jacobi solve ran out of sweeps (sticky)
+    int pad[3];
+    double worst;  // largest residual norm of the wanted roots
+    double n0;     // |direction|^2 before the Gram-Schmidt passes
+};
+
+// G[i + ldg j] = V[:, i]^H W[:, j] for i, j < m (one block per element, fixed order).
+__global__ void rr_kernel(int n, const cplx *__restrict__ V, const cplx *__restrict__ W, int64_t ld, cplx *G,
+                          int ldg, const DavState *__restrict__ st) {
+    __shared__ double sh[32];
+    const int i = blockIdx.x, j = blockIdx.y, m = st->m;
+    if (i >= m || j >= m) return;
+    const cplx *a = V + ld * i, *b = W + ld * j;
+    double re = 0.0, im = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const cplx x = a[k], y = b[k];
+        re += x.x * y.x + x.y * y.y;
+        im += x.x * y.y - x.y * y.x;
+    }
+    re = block_sum_d(re, sh);
+    im = block_sum_d(im, sh);
+    if (threadIdx.x == 0) G[i + (int64_t)ldg * j] = mk(re, im);
+}
+
+// X = V Y[:, :nb] (z = 0) and HX = W Y[:, :nb] (z = 1) over the m columns of V and W.
+__global__ void ritz_kernel(int n, const cplx *__restrict__ V, const cplx *__restrict__ W, int64_t ld,
+                            const cplx *__restrict__ Y, int ldy, cplx *X, cplx *HX, const DavState *__restrict__ st) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x, c = blockIdx.y;
+    if (r >= n) return;
+    const cplx *A = blockIdx.z ? W : V;
+    const int m = st->m;
+    cplx acc = mk(0.0, 0.0);
+    for (int q = 0; q < m; q++) acc = cadd(acc, cmul(A[r + ld * q], __ldg(Y + q + (int64_t)ldy * c)));
+    (blockIdx.z ? HX : X)[r + ld * c] = acc;
+}
+
+// The residual norms of the wanted roots; the step's direction counters reset.
+__global__ void step_begin_kernel(int nwant, const double *__restrict__ h2, DavState *st) {
+    if (threadIdx.x != 0) return;
+    double w = 0.0;
+    for (int q = 0; q < nwant; q++) w = fmax(w, sqrt(h2[q]));
+    st->worst = w;
+    st->cand = 0;
+    st->stop = 0;
+}
+
+// Restart on the block's Ritz vectors when the next block would not fit: V, W <- X, HX.
+__global__ void restart_copy_kernel(int n, int nb, int mmax, const cplx *__restrict__ X, const cplx *__restrict__ HX,
+                                    cplx *V, cplx *W, int64_t ld, const DavState *__restrict__ st) {
+    if (st->m + nb <= mmax) return;
+    const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= (int64_t)n * nb) return;
+    const int i = (int)(e % n), c = (int)(e / n);
+    V[i + ld * c] = X[i + ld * c];
+    W[i + ld * c] = HX[i + ld * c];
+}
+
+__global__ void restart_set_kernel(int nb, int mmax, DavState *st) {
+    if (threadIdx.x == 0 && st->m + nb > mmax) st->m = nb;
+}
+
+// Direction q: live when its residual is above tol, the block has not stopped and V has room;
+// then T[:, q] goes to column m + cand of V and its squared norm to n0 (one block).
+__global__ void cand_begin_kernel(int n, int q, int mmax, double tol, const double *__restrict__ h2,
+                                  const cplx *__restrict__ T, cplx *V, int64_t ld, DavState *st) {
+    __shared__ double sh[32];
+    __shared__ int live;
+    if (threadIdx.x == 0) {
+        live = !st->stop && sqrt(h2[q]) > tol && st->m + st->cand < mmax;
+        st->act = live;
+    }
+    __syncthreads();
+    if (!live) return;
+    cplx *dst = V + ld * (st->m + st->cand);
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const cplx x = T[i + ld * q];
+        dst[i] = x;
+        acc += x.x * x.x + x.y * x.y;
+    }
+    acc = block_sum_d(acc, sh);
+    if (threadIdx.x == 0) st->n0 = acc;
+}
+
+// Classical Gram-Schmidt pass of the live direction against the vectors before it.
+__global__ void cgs_dot_kernel(int n, const cplx *__restrict__ V, int64_t ld, cplx *cf, const DavState *__restrict__ st) {
+    __shared__ double sh[32];
+    const int i = blockIdx.x, mm = st->m + st->cand;
+    if (!st->act || i >= mm) return;
+    const cplx *a = V + ld * i, *b = V + ld * mm;
+    double re = 0.0, im = 0.0;
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const cplx x = a[k], y = b[k];
+        re += x.x * y.x + x.y * y.y;
+        im += x.x * y.y - x.y * y.x;
+    }
+    re = block_sum_d(re, sh);
+    im = block_sum_d(im, sh);
+    if (threadIdx.x == 0) cf[i] = mk(re, im);
+}
+
+__global__ void cgs_axpy_kernel(int n, cplx *V, int64_t ld, const cplx *__restrict__ cf, const DavState *__restrict__ st) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    const int mm = st->m + st->cand;
+    if (!st->act || r >= n) return;
+    cplx acc = mk(0.0, 0.0);
+    for (int q = 0; q < mm; q++) acc = cadd(acc, cmul(V[r + ld * q], cf[q]));
+    cplx &d = V[r + ld * mm];
+    d = csub(d, acc);
+}
+
+// Accept the live direction when it kept more than 1e-10 of its length (normalised, counted),
+// else stop the block's directions here.
+__global__ void cand_end_kernel(int n, cplx *V, int64_t ld, DavState *st) {
+    __shared__ double sh[32];
+    if (!st->act) return;
+    cplx *dst = V + ld * (st->m + st->cand);
+    double acc = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) acc += dst[i].x * dst[i].x + dst[i].y * dst[i].y;
+    acc = block_sum_d(acc, sh);
+    const bool ok = acc > 1e-20 * st->n0 && acc > 0.0;
+    if (ok) {
+        const double s = 1.0 / sqrt(acc);
+        for (int i = threadIdx.x; i < n; i += blockDim.x) dst[i] = mk(dst[i].x * s, dst[i].y * s);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (ok) st->cand++;
+        else st->stop = 1;
+    }
+}
+
+// W[:, m + c] = H V[:, m + c] for the cand accepted directions (CSR, one warp per row).
+template <int K>
+__global__ void __launch_bounds__(256) csr_hx_step_kernel(int n, const int64_t *__restrict__ rowptr,
+                                                           const int *__restrict__ cols, const cplx *__restrict__ vals,
+                                                           const cplx *__restrict__ V, cplx *W, int64_t ld,
+                                                           const DavState *__restrict__ st) {
+    const int row = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    const int k = st->cand;
+    if (row >= n || k == 0) return;
+    const cplx *X = V + ld * st->m;
+    double re[K], im[K];
+#pragma unroll
+    for (int c = 0; c < K; c++) re[c] = im[c] = 0.0;
+    const int64_t e1 = rowptr[row + 1];
+    for (int64_t e = rowptr[row] + lane; e < e1; e += 32) {
+        const cplx h = vals[e];
+        const int j = cols[e];
+#pragma unroll
+        for (int c = 0; c < K; c++) {
+            if (c < k) {
+                const cplx x = __ldg(X + j + ld * c);
+                re[c] = fma(h.x, x.x, fma(-h.y, x.y, re[c]));
+                im[c] = fma(h.x, x.y, fma(h.y, x.x, im[c]));
+            }
+        }
+    }
+#pragma unroll
+    for (int c = 0; c < K; c++) {
+        for (int o = 16; o > 0; o >>= 1) {
+            re[c] += __shfl_down_sync(0xffffffffu, re[c], o);
+            im[c] += __shfl_down_sync(0xffffffffu, im[c], o);
+        }
+    }
+    if (lane == 0) {
+        cplx *Y = W + ld * st->m;
+#pragma unroll
+        for (int c = 0; c < K; c++)
+            if (c < k) Y[row + ld * c] = mk(re[c], im[c]);
+    }
+}
+
+__global__ void step_end_kernel(DavState *st) {
+    if (threadIdx.x == 0) st->m += st->cand;
+}
+
 }  // namespace
-
-// C (mi x mj, ldc) = A^H B over n rows (Davidson inner products).
-static void dotc_small(Context &c, int n, int mi, int mj, const cplx *A, int64_t lda, const cplx *B, int64_t ldb,
-                       cplx *C, int ldc, double alpha = 1.0, bool accumulate = false) {
-    if (mi <= 0 || mj <= 0) return;
-    dotc_small_kernel<<<dim3(mi, mj), 256, 0, c.stream>>>(n, A, lda, B, ldb, C, ldc, alpha, accumulate ? 1 : 0);
-    DCG_LAUNCHED(c);
-}
-
-static void tall_small(Context &c, int n, int m, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B, int ldb,
-                       cplx beta, cplx *C, int64_t ldc) {
-    if (n <= 0 || k <= 0) return;
-    tall_small_kernel<<<dim3(grid1d(n, 128), k), 128, 0, c.stream>>>(n, m, k, alpha, A, lda, B, ldb, beta, C, ldc);
-    DCG_LAUNCHED(c);
-}
 
 // Y (n x k) = H X for the CSR H, up to 8 vectors a launch (one pass over H for each group).
 static void csr_hx(Context &c, const CsrMatrix &H, const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) {
@@ -338,20 +457,29 @@ void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, i
     const size_t smem = 2 * sizeof(cplx) * (size_t)np * np;
     DCG_CUDA(cudaFuncSetAttribute(jacobi_heev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     int *st = wsget<int>(c, "dav.jst", 1);
+    DCG_CUDA(cudaMemsetAsync(st, 0, sizeof(int), c.stream));
     // two warps: the rounds are short (n/2 rotations), so barrier latency, not work, sets the pace
-    jacobi_heev_kernel<<<1, 64, smem, c.stream>>>(n, G, ldg, w, Y, ldy, st);
+    jacobi_heev_kernel<<<1, 64, smem, c.stream>>>(n, nullptr, G, ldg, w, Y, ldy, st);
     DCG_LAUNCHED(c);
 }
 
-using HxFn = std::function<void(const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy)>;
-
-// Block Davidson on the operator hx (Y = H X) with diagonal hd (device, n).
-static void davidson_core(Context &c, int n, const HxFn &hx, const double *hd, int nwant, double *w, cplx *Z,
-                          double tol_rel, int maxit) {
+// Lowest nwant eigenpairs of the Hermitian CSR H (its diagonal kept beside it): eigenvalues to
+// w[0..nwant), eigenvectors to the columns of Z (n x nwant, ldz = n), each with residual norm
+// <= tol_rel * max(1, max_i |H_ii|).
+//
+// One step: the Rayleigh matrix G = V^H W and its eigenpairs (Jacobi), the block's Ritz
+// vectors X = V Y and images HX = W Y, their residuals and preconditioned corrections T, a
+// restart V, W <- X, HX when the next block would not fit, then each unconverged correction
+// orthonormalised against V (classical Gram-Schmidt twice) and appended, and W extended by
+// H times the new directions.  Every size the step needs lives on the device (DavState), so
+// the step is one fixed launch sequence: captured once as a CUDA graph and replayed, with
+// one read of the state per step (the environment variable DCG_DAVIDSON_GRAPH=0 launches
+// the sequence directly instead).
+void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, cplx *Z, double tol_rel, int maxit) {
+    const int n = H.n;
     const int nb = std::min(n, nwant + 2);   // block: the wanted roots and a margin for near-degeneracy
     const int mmax = std::min(n, std::min(kJacobiMaxN, std::max(24, 8 * nb)));
     if (nwant < 1 || nb > mmax || n < 2) throw Error{DCG_E_ARG, "davidson: block does not fit the subspace"};
-    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     const int64_t ld = n;
     cplx *V = wsget<cplx>(c, "dav.V", (size_t)n * mmax);
     cplx *W = wsget<cplx>(c, "dav.W", (size_t)n * mmax);
@@ -362,13 +490,14 @@ static void davidson_core(Context &c, int n, const HxFn &hx, const double *hd, i
     cplx *Y = wsget<cplx>(c, "dav.Y", (size_t)mmax * mmax);
     cplx *cf = wsget<cplx>(c, "dav.cf", (size_t)mmax);
     double *th = wsget<double>(c, "dav.th", mmax);
-    double *nrm = wsget<double>(c, "dav.nrm", (size_t)3 * nb);
+    double *h2 = wsget<double>(c, "dav.h2", (size_t)nb);
     int *idx = wsget<int>(c, "dav.idx", nb);
-    int *jst = wsget<int>(c, "dav.jst", 1);
+    DavState *st = wsget<DavState>(c, "dav.st", 1);
+    DavState *hst = reinterpret_cast<DavState *>(c.ws.host("dav.hst", sizeof(DavState)));
 
     // start: unit vectors on the nb lowest diagonal elements (ties by index)
     std::vector<double> hdh(n);
-    DCG_CUDA(cudaMemcpyAsync(hdh.data(), hd, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
+    DCG_CUDA(cudaMemcpyAsync(hdh.data(), H.diag, sizeof(double) * n, cudaMemcpyDeviceToHost, c.stream));
     DCG_CUDA(cudaStreamSynchronize(c.stream));
     double hscale = 1.0;
     for (double x : hdh) hscale = std::max(hscale, std::fabs(x));
@@ -380,84 +509,86 @@ static void davidson_core(Context &c, int n, const HxFn &hx, const double *hd, i
     DCG_CUDA(cudaMemcpyAsync(idx, order.data(), sizeof(int) * nb, cudaMemcpyHostToDevice, c.stream));
     unit_cols_kernel<<<grid1d((int64_t)n * nb, 256), 256, 0, c.stream>>>(n, nb, idx, V, ld);
     DCG_LAUNCHED(c);
-    int m = nb;
-    hx(V, ld, m, W, ld);
+    csr_hx(c, H, V, ld, nb, W, ld);
+    DavState s0{};
+    s0.m = nb;
+    DCG_CUDA(cudaMemcpyAsync(st, &s0, sizeof(DavState), cudaMemcpyHostToDevice, c.stream));
 
-    std::vector<double> h2((size_t)nb);
+    const int np = mmax + (mmax & 1);
+    const size_t jsmem = 2 * sizeof(cplx) * (size_t)np * np;
+    DCG_CUDA(cudaFuncSetAttribute(jacobi_heev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
+    const int hx_blocks = (int)(((int64_t)n * 32 + 255) / 256);
+    auto enqueue_step = [&]() {
+        rr_kernel<<<dim3(mmax, mmax), 256, 0, c.stream>>>(n, V, W, ld, G, mmax, st);
+        jacobi_heev_kernel<<<1, 64, jsmem, c.stream>>>(mmax, &st->m, G, mmax, th, Y, mmax, &st->jac);
+        ritz_kernel<<<dim3(grid1d(n, 128), nb, 2), 128, 0, c.stream>>>(n, V, W, ld, Y, mmax, X, HX, st);
+        residual_kernel<<<nb, 256, 0, c.stream>>>(n, HX, X, ld, th, H.diag, T, h2);
+        step_begin_kernel<<<1, 32, 0, c.stream>>>(nwant, h2, st);
+        restart_copy_kernel<<<grid1d((int64_t)n * nb, 256), 256, 0, c.stream>>>(n, nb, mmax, X, HX, V, W, ld, st);
+        restart_set_kernel<<<1, 32, 0, c.stream>>>(nb, mmax, st);
+        for (int q = 0; q < nb; q++) {
+            cand_begin_kernel<<<1, 256, 0, c.stream>>>(n, q, mmax, tol, h2, T, V, ld, st);
+            for (int pass = 0; pass < 2; pass++) {
+                cgs_dot_kernel<<<mmax, 256, 0, c.stream>>>(n, V, ld, cf, st);
+                cgs_axpy_kernel<<<grid1d(n, 128), 128, 0, c.stream>>>(n, V, ld, cf, st);
+            }
+            cand_end_kernel<<<1, 256, 0, c.stream>>>(n, V, ld, st);
+        }
+        if (nb > 4)
+            csr_hx_step_kernel<8><<<hx_blocks, 256, 0, c.stream>>>(n, H.rowptr, H.cols, H.vals, V, W, ld, st);
+        else if (nb > 2)
+            csr_hx_step_kernel<4><<<hx_blocks, 256, 0, c.stream>>>(n, H.rowptr, H.cols, H.vals, V, W, ld, st);
+        else
+            csr_hx_step_kernel<2><<<hx_blocks, 256, 0, c.stream>>>(n, H.rowptr, H.cols, H.vals, V, W, ld, st);
+        step_end_kernel<<<1, 32, 0, c.stream>>>(st);
+        DCG_CUDA(cudaMemcpyAsync(hst, st, sizeof(DavState), cudaMemcpyDeviceToHost, c.stream));
+    };
+    const int step_kernels = 8 + 6 * nb;   // kernels per step
+    if (nb > 8) throw Error{DCG_E_ARG, "davidson: more than 8 directions per step"};
+
+    static const bool use_graph = [] {
+        const char *e = getenv("DCG_DAVIDSON_GRAPH");
+        return !(e && e[0] == '0');
+    }();
+    cudaGraphExec_t exec = nullptr;
+    if (use_graph) {
+        cudaGraph_t graph = nullptr;
+        DCG_CUDA(cudaStreamBeginCapture(c.stream, cudaStreamCaptureModeThreadLocal));
+        enqueue_step();
+        DCG_CUDA(cudaStreamEndCapture(c.stream, &graph));
+        const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (e != cudaSuccess) throw Error{DCG_E_CUDA, std::string("davidson graph: ") + cudaGetErrorString(e)};
+    }
+    struct ExecGuard {
+        cudaGraphExec_t g;
+        ~ExecGuard() {
+            if (g) cudaGraphExecDestroy(g);
+        }
+    } guard{exec};
+
     bool converged = false;
     c.casci_iters = 0;
     for (int it = 0; it < maxit; it++) {
-        dotc_small(c, n, m, m, V, ld, W, ld, G, mmax);
-        small_heev(c, m, G, mmax, th, Y, mmax);
-        // Ritz vectors of the block and their images
-        tall_small(c, n, m, nb, one, V, ld, Y, mmax, zero, X, ld);
-        tall_small(c, n, m, nb, one, W, ld, Y, mmax, zero, HX, ld);
-        residual_kernel<<<nb, 256, 0, c.stream>>>(n, HX, X, ld, th, hd, T, nrm);
-        DCG_LAUNCHED(c);
-        DCG_CUDA(cudaMemcpyAsync(h2.data(), nrm, sizeof(double) * nb, cudaMemcpyDeviceToHost, c.stream));
+        if (exec) {
+            DCG_CUDA(cudaGraphLaunch(exec, c.stream));
+            c.launches += step_kernels;
+        } else {
+            enqueue_step();
+            c.launches += step_kernels;
+        }
         DCG_CUDA(cudaStreamSynchronize(c.stream));
         c.casci_iters = it + 1;
-        double worst = 0.0;
-        for (int q = 0; q < nwant; q++) worst = std::max(worst, std::sqrt(h2[q]));
-        if (worst <= tol) {
+        if (hst->worst <= tol) {
             converged = true;
             break;
         }
-        if (m + nb > mmax) {   // restart on the block's Ritz vectors (orthonormal)
-            DCG_CUDA(cudaMemcpyAsync(V, X, sizeof(cplx) * (size_t)n * nb, cudaMemcpyDeviceToDevice, c.stream));
-            DCG_CUDA(cudaMemcpyAsync(W, HX, sizeof(cplx) * (size_t)n * nb, cudaMemcpyDeviceToDevice, c.stream));
-            m = nb;
-        }
-        // new directions: preconditioned residuals of the unconverged Ritz pairs, made
-        // orthonormal to V and to each other (classical Gram-Schmidt, twice) on the device; the
-        // norms before and after come back in one read, and a direction that has lost all but
-        // 1e-10 of its length ends the block there
-        int cand = 0;
-        for (int q = 0; q < nb && m + cand < mmax; q++) {
-            if (std::sqrt(h2[q]) <= tol) continue;
-            cplx *dst = V + ld * (m + cand);
-            DCG_CUDA(cudaMemcpyAsync(dst, T + ld * q, sizeof(cplx) * n, cudaMemcpyDeviceToDevice, c.stream));
-            norm2_kernel<<<1, 256, 0, c.stream>>>(n, dst, nrm + nb + 2 * cand);
-            DCG_LAUNCHED(c);
-            const int mm = m + cand;
-            for (int pass = 0; pass < 2; pass++) {
-                dotc_small(c, n, mm, 1, V, ld, dst, ld, cf, mmax);
-                tall_small(c, n, mm, 1, mone, V, ld, cf, mmax, one, dst, ld);
-            }
-            norm2_kernel<<<1, 256, 0, c.stream>>>(n, dst, nrm + nb + 2 * cand + 1);
-            DCG_LAUNCHED(c);
-            normalize_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, dst, nrm + nb + 2 * cand + 1);
-            DCG_LAUNCHED(c);
-            cand++;
-        }
-        int added = 0;
-        if (cand > 0) {
-            std::vector<double> nn((size_t)2 * cand);
-            DCG_CUDA(cudaMemcpyAsync(nn.data(), nrm + nb, sizeof(double) * 2 * cand, cudaMemcpyDeviceToHost,
-                                     c.stream));
-            DCG_CUDA(cudaStreamSynchronize(c.stream));
-            while (added < cand && nn[2 * added + 1] > 1e-20 * nn[2 * added] && nn[2 * added + 1] > 0.0) added++;
-        }
-        if (added == 0) break;   // stagnated: reported below
-        hx(V + ld * m, ld, added, W + ld * m, ld);
-        m += added;
+        if (hst->cand == 0) break;   // stagnated: reported below
     }
-    int jh = 0;
-    DCG_CUDA(cudaMemcpyAsync(&jh, jst, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-    DCG_CUDA(cudaStreamSynchronize(c.stream));
-    if (!converged || jh != 0)
+    if (!converged || hst->jac != 0)
         throw Error{DCG_E_NUMERIC, "CASCI Davidson did not converge to |r| <= " + std::to_string(tol)};
     DCG_CUDA(cudaMemcpyAsync(w, th, sizeof(double) * nwant, cudaMemcpyDeviceToDevice, c.stream));
     DCG_CUDA(cudaMemcpyAsync(Z, X, sizeof(cplx) * (size_t)n * nwant, cudaMemcpyDeviceToDevice, c.stream));
-}
-
-// Lowest nwant eigenpairs of the Hermitian CSR H (its diagonal kept beside it): eigenvalues to
-// w[0..nwant), eigenvectors to the columns of Z (n x nwant, ldz = n), each with residual norm
-// <= tol_rel * max(1, max_i |H_ii|).
-void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, cplx *Z, double tol_rel, int maxit) {
-    davidson_core(
-        c, H.n, [&](const cplx *X, int64_t ldx, int k, cplx *Y, int64_t ldy) { csr_hx(c, H, X, ldx, k, Y, ldy); },
-        H.diag, nwant, w, Z, tol_rel, maxit);
 }
 
 }  // namespace dcg

@@ -32,10 +32,32 @@ void *Workspace::get(const std::string &name, size_t bytes) {
     return b.p;
 }
 
+void *Workspace::host(const std::string &name, size_t bytes) {
+    Buf &b = host_[name];
+    if (b.bytes >= bytes && b.p) return b.p;
+    if (b.p) {
+        cudaFreeHost(b.p);
+        b.p = nullptr;
+        b.bytes = 0;
+    }
+    const size_t alloc = bytes < 256 ? 256 : bytes;
+    const cudaError_t e = cudaHostAlloc(&b.p, alloc, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        b.p = nullptr;
+        cudaGetLastError();
+        throw Error{DCG_E_NOMEM, "page-locked allocation for " + name + " failed: " + cudaGetErrorString(e)};
+    }
+    b.bytes = alloc;
+    return b.p;
+}
+
 void Workspace::release_all() {
     for (auto &kv : bufs_)
         if (kv.second.p) cudaFree(kv.second.p);
     bufs_.clear();
+    for (auto &kv : host_)
+        if (kv.second.p) cudaFreeHost(kv.second.p);
+    host_.clear();
     total_ = 0;
 }
 
@@ -307,21 +329,11 @@ static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx
                          const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
                          int batch, int upper);
 
-// Split-K for a single GEMM whose output has too few 64x64 tiles to occupy every SM (a GB300
-// SM retires only about two FP64 FMAs per clock, so a GEMM on a handful of SMs runs at a
-// small fraction of the GPU): K is cut into equal chunks (at least 64 long) computed as one
-// batched GEMM into partial products, then reduced in a fixed order.  Returns false when
-// the shape does not qualify.
+// One split-K product with a given number of K chunks (>= 2): the chunks are computed as one
+// batched GEMM into partial products, then reduced in a fixed order.
 template <int OPA, int OPB>
-static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B,
-                         int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper = 0) {
-    const int64_t tm = (m + 63) / 64, tn = (n + 63) / 64;
-    // tiles on or above the diagonal only, for a Hermitian product's upper half
-    const int64_t tiles = upper ? (tn * (tn + 1)) / 2 : tm * tn;
-    const int sms = std::max(1, c.num_sms);
-    if (tiles >= sms || k < 128) return false;
-    int nsplit = (int)std::min<int64_t>((2 * sms + tiles - 1) / tiles, k / 64);
-    if (nsplit < 2) return false;
+static void zgemm_splitk_run(Context &c, int m, int n, int k, int nsplit, cplx alpha, const cplx *A, int64_t lda,
+                             const cplx *B, int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper) {
     const int kc = (k + nsplit - 1) / nsplit;
     nsplit = (k + kc - 1) / kc;
     const int nfull = k / kc;             // chunks of exactly kc
@@ -338,12 +350,44 @@ static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx
                                m, 0, 1, upper);
     splitk_reduce_kernel<<<grid1d(mn, 256), 256, 0, c.stream>>>(m, n, nsplit, P, alpha, beta, C, ldc, upper);
     DCG_LAUNCHED(c);
+}
+
+// Split-K for a single GEMM whose output has too few 64x64 tiles to occupy every SM (a GB300
+// SM retires only about two FP64 FMAs per clock, so a GEMM on a handful of SMs runs at a
+// small fraction of the GPU): K is cut into equal chunks of at least 64.  The number of
+// chunks is the autotuner's choice for the shape (candidates: no split, the occupancy
+// heuristic min(2 SMs / tiles, k / 64), and powers of two up to k / 64), or the heuristic
+// when tuning is off or the call accumulates into C (beta != 0, which the timed trial runs
+// would disturb).  Returns false when the product runs unsplit.
+template <int OPA, int OPB>
+static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B,
+                         int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper = 0) {
+    const int64_t tm = (m + 63) / 64, tn = (n + 63) / 64;
+    // tiles on or above the diagonal only, for a Hermitian product's upper half
+    const int64_t tiles = upper ? (tn * (tn + 1)) / 2 : tm * tn;
+    const int sms = std::max(1, c.num_sms);
+    if (tiles >= sms || k < 128) return false;
+    const int heur = (int)std::min<int64_t>((2 * sms + tiles - 1) / tiles, k / 64);
+    std::vector<int> cand{heur < 2 ? 1 : heur, 1};
+    for (int p = 2; p <= k / 64 && p <= 64; p *= 2) cand.push_back(p);
+    std::sort(cand.begin() + 1, cand.end());
+    cand.erase(std::unique(cand.begin() + 1, cand.end()), cand.end());
+    const TuneKey key{TUNE_ZGEMM_SPLITK, OPA * 8 + OPB, m, n, k, upper};
+    const bool trial_ok = beta.x == 0.0 && beta.y == 0.0;
+    const int pick = autotune(c, key, (int)cand.size(), trial_ok, [&](int q) {
+        if (cand[q] < 2) zgemm_launch<OPA, OPB>(c, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, upper);
+        else zgemm_splitk_run<OPA, OPB>(c, m, n, k, cand[q], alpha, A, lda, B, ldb, beta, C, ldc, upper);
+    });
+    const int nsplit = cand[pick];
+    if (nsplit < 2) return false;
+    zgemm_splitk_run<OPA, OPB>(c, m, n, k, nsplit, alpha, A, lda, B, ldb, beta, C, ldc, upper);
     return true;
 }
 
 void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
            const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc, int batch) {
     if (m <= 0 || n <= 0 || batch <= 0) return;
+    GemmTrace trace(c, "fp64", m, n, k, batch);
     if (zgemm_small(c, opa, opb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch)) return;
 #define DCG_ZG(a, b)                                                                                   \
     if (opa == a && opb == b) {                                                                        \
@@ -365,6 +409,7 @@ void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cp
 // Hermitian fill from the upper triangle completes it.
 void zherk_upper(Context &c, int n, int k, const cplx *A, int64_t lda, cplx *C, int64_t ldc) {
     if (n <= 0) return;
+    GemmTrace trace(c, "herk", n, n, k, 1);
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
     if (zgemm_splitk<OP_N, OP_C>(c, n, n, k, one, A, lda, A, lda, zero, C, ldc, 1)) return;
     zgemm_launch<OP_N, OP_C>(c, n, n, k, one, A, lda, 0, A, lda, 0, zero, C, ldc, 0, 1, 1);

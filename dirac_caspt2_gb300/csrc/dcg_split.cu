@@ -480,6 +480,7 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
         }
         return;
     }
+    GemmTrace trace(c, "split", M, N, K, batch);
     const int nks = (2 * K + SP_TK - 1) / SP_TK;
     const int nrb = (M + SP_TM - 1) / SP_TM;
     const int nnb = (2 * N + SP_TN - 1) / SP_TN;

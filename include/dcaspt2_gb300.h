@@ -308,6 +308,26 @@ int64_t dcg_server_device_bytes(dcg_server *srv);
 /* Drop queued requests, finish the running ones, join the workers and free the contexts. */
 int dcg_server_destroy(dcg_server *srv);
 
+/* ------------------------------------------------------------------------ autotuner
+ * Shape-dependent launch choices (today: the K-split of the FP64 GEMMs whose output tiles do
+ * not fill the GPU, and the K-chunking of the split-precision GEMMs) are tuned on first use:
+ * every candidate is timed with CUDA events on the calling context's stream and the fastest
+ * is kept in a process-wide table that every context then uses.  Different choices change
+ * only the summation order of the products.
+ * mode: 1 tune (default; environment DCG_AUTOTUNE=0 starts with 0), 0 use the built-in
+ * heuristics for keys not yet tuned, 2 clear the table (mode unchanged), other values only
+ * query.  Returns the mode before the call. */
+typedef struct dcg_tune_entry {
+    int32_t kind;                 /* 1: FP64 GEMM K-split, 2: split-precision GEMM K-chunks */
+    int32_t ops, m, n, k, flags;  /* the decision's key (ops: op codes, flags: e.g. upper)   */
+    int32_t choice, ncand;        /* chosen candidate (0 = the heuristic) of ncand           */
+    float best_ms, heuristic_ms;  /* measured time of the choice and of the heuristic        */
+} dcg_tune_entry;
+
+int dcg_autotune_mode(int32_t mode);
+/* Entries of the table (at most max_entries written to out); returns their total number. */
+int32_t dcg_autotune_entries(dcg_tune_entry *out, int32_t max_entries);
+
 /* ------------------------------------------------------------------------ IVO
  * Improved virtual orbitals (r4divo.F90:80-93, fockivo.F90:44-215) on the system of the last
  * dcg_set_system / dcg_set_system_mdcint (its ninact, nact, nsec, nelec as the IVO input
