@@ -288,6 +288,13 @@ def run_ours(args, cfg_name):
             "clocks": clocks_v, "roofline": roof,
             "stage_ms_last_step": {k: round(v, 3) for k, v in stage.items()},
             "total_energy": e_tot, "energy_spread": float(max(energies) - min(energies))}
+    tuned = api.autotune_entries()
+    line["autotune"] = {"mode": api.autotune_mode(-1), "keys": len(tuned),
+                        "changed_from_heuristic": sum(1 for t in tuned if t["choice"] != 0),
+                        "heuristic_ms_sum": round(sum(t["heuristic_ms"] for t in tuned), 3),
+                        "tuned_ms_sum": round(sum(t["best_ms"] for t in tuned), 3),
+                        "decisions": sorted({t["kind"] for t in tuned})}
+    line["cuda_graphs"] = "CASCI Davidson step (device-resident sizes) captured once per eigensolve and replayed"
     if fp64 is not None:
         line["fp64_gpu"] = fp64
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

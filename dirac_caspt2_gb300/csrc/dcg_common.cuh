@@ -194,7 +194,7 @@ std::vector<T> download(Context &c, const T *p, size_t n) {
 // and keeps the fastest; later calls of the key, in any context, reuse it.  Candidate 0 is the
 // built-in heuristic, used while tuning is off (dcg_autotune_mode) and for keys first met
 // without trial_ok.  The trial runs must leave the same result as the final run.
-enum TuneKind { TUNE_ZGEMM_SPLITK = 1, TUNE_SPLIT_KCHUNK = 2 };
+enum TuneKind { TUNE_ZGEMM = 1, TUNE_SPLIT_ORDER = 2 };
 struct TuneKey {
     int kind, ops, m, n, k, flags;
     bool operator<(const TuneKey &o) const {

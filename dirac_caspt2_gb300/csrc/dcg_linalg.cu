@@ -85,12 +85,19 @@ __device__ double block_sum(double v, double *sh) {
 }
 
 // ===================================================================== ZGEMM
-template <int OPA, int OPB>
+// 256 threads as TYN x (256 / TYN), each owning a 4 x 4 block of outputs spaced TYN rows and
+// 256/TYN columns apart: tiles of 64 x 64 (TYN 16), 32 x 128 (TYN 8) or 128 x 32 (TYN 32).
+// A GB300 SM retires about two FP64 FMAs per clock, so the useful fraction of a tile is the
+// fraction of the GPU's FP64 rate a skinny product gets: the autotuner picks the tile.
+constexpr int kZgTiles = 3;
+constexpr int kZgTyn[kZgTiles] = {16, 8, 32};
+
+template <int OPA, int OPB, int TYN>
 __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx alpha, const cplx *__restrict__ A,
                                                     int64_t lda, int64_t sa, const cplx *__restrict__ B,
                                                     int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc,
                                                     int64_t sc, int zoff, int upper) {
-    constexpr int BM = 64, BN = 64, BK = 16;
+    constexpr int TXN = 256 / TYN, BM = 4 * TYN, BN = 4 * TXN, BK = 16;
     __shared__ cplx As[BK][BM + 1];
     __shared__ cplx Bs[BK][BN + 1];
     const int64_t bz = (int64_t)blockIdx.z + zoff;
@@ -99,7 +106,7 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx al
     C += bz * sc;
     const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
     if (upper && m0 >= n0 + BN) return;   // tile strictly below the diagonal (Hermitian product, upper half)
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int tx = threadIdx.x % TXN, ty = threadIdx.x / TXN;
     cplx acc[4][4];
 #pragma unroll
     for (int a = 0; a < 4; a++)
@@ -146,8 +153,8 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx al
             cplx a[4], b[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                a[q] = As[kk][ty + 16 * q];
-                b[q] = Bs[kk][tx + 16 * q];
+                a[q] = As[kk][ty + TYN * q];
+                b[q] = Bs[kk][tx + TXN * q];
             }
 #pragma unroll
             for (int p = 0; p < 4; p++)
@@ -159,11 +166,11 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int m, int n, int k, cplx al
     const bool use_beta = (beta.x != 0.0 || beta.y != 0.0);
 #pragma unroll
     for (int p = 0; p < 4; p++) {
-        int gi = m0 + ty + 16 * p;
+        int gi = m0 + ty + TYN * p;
         if (gi >= m) continue;
 #pragma unroll
         for (int q = 0; q < 4; q++) {
-            int gj = n0 + tx + 16 * q;
+            int gj = n0 + tx + TXN * q;
             if (gj >= n) continue;
             cplx r = cmul(alpha, acc[p][q]);
             int64_t o = gi + (int64_t)gj * ldc;
@@ -298,14 +305,32 @@ static bool zgemm_small(Context &c, Op opa, Op opb, int m, int n, int k, cplx al
 template <int OPA, int OPB>
 static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
                          const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
-                         int batch, int upper) {
+                         int batch, int upper, int tile) {
+    const int bm = 4 * kZgTyn[tile], bn = 1024 / kZgTyn[tile];
     for (int z0 = 0; z0 < batch; z0 += 65535) {
         int nz = batch - z0 < 65535 ? batch - z0 : 65535;
-        dim3 grid(grid1d(m, 64), grid1d(n, 64), nz);
-        zgemm_kernel<OPA, OPB><<<grid, 256, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc,
-                                                           sc, z0, upper);
+        dim3 grid(grid1d(m, bm), grid1d(n, bn), nz);
+        if (tile == 1)
+            zgemm_kernel<OPA, OPB, 8><<<grid, 256, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc,
+                                                                  sc, z0, upper);
+        else if (tile == 2)
+            zgemm_kernel<OPA, OPB, 32><<<grid, 256, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C,
+                                                                   ldc, sc, z0, upper);
+        else
+            zgemm_kernel<OPA, OPB, 16><<<grid, 256, 0, c.stream>>>(m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C,
+                                                                   ldc, sc, z0, upper);
         DCG_LAUNCHED(c);
     }
+}
+
+// Output tiles of a tile shape (for a Hermitian product's upper half, those touching it).
+static int64_t zg_tiles(int m, int n, int tile, int upper) {
+    const int bm = 4 * kZgTyn[tile], bn = 1024 / kZgTyn[tile];
+    const int64_t tm = (m + bm - 1) / bm, tn = (n + bn - 1) / bn;
+    if (!upper) return tm * tn;
+    int64_t t = 0;
+    for (int64_t j = 0; j < tn; j++) t += std::min<int64_t>(tm, ((j + 1) * bn + bm - 1) / bm);
+    return t;
 }
 
 // C = alpha * sum_s P_s + beta * C over nsplit partial products (fixed summation order).
@@ -327,13 +352,14 @@ __global__ void splitk_reduce_kernel(int m, int n, int nsplit, const cplx *__res
 template <int OPA, int OPB>
 static void zgemm_launch(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
                          const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc,
-                         int batch, int upper);
+                         int batch, int upper, int tile);
+static int64_t zg_tiles(int m, int n, int tile, int upper);
 
 // One split-K product with a given number of K chunks (>= 2): the chunks are computed as one
 // batched GEMM into partial products, then reduced in a fixed order.
 template <int OPA, int OPB>
 static void zgemm_splitk_run(Context &c, int m, int n, int k, int nsplit, cplx alpha, const cplx *A, int64_t lda,
-                             const cplx *B, int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper) {
+                             const cplx *B, int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper, int tile) {
     const int kc = (k + nsplit - 1) / nsplit;
     nsplit = (k + kc - 1) / kc;
     const int nfull = k / kc;             // chunks of exactly kc
@@ -344,44 +370,66 @@ static void zgemm_splitk_run(Context &c, int m, int n, int k, int nsplit, cplx a
     // K-chunk strides: A is m x k (OP_N/OP_R, chunk = columns) or k x m (OP_T/OP_C, chunk = rows)
     const int64_t sa = (OPA == OP_N || OPA == OP_R) ? (int64_t)kc * lda : kc;
     const int64_t sb = (OPB == OP_N || OPB == OP_R) ? kc : (int64_t)kc * ldb;
-    zgemm_launch<OPA, OPB>(c, m, n, kc, one, A, lda, sa, B, ldb, sb, zero, P, m, mn, nfull, upper);
+    zgemm_launch<OPA, OPB>(c, m, n, kc, one, A, lda, sa, B, ldb, sb, zero, P, m, mn, nfull, upper, tile);
     if (rem > 0)
         zgemm_launch<OPA, OPB>(c, m, n, rem, one, A + nfull * sa, lda, 0, B + nfull * sb, ldb, 0, zero, P + nfull * mn,
-                               m, 0, 1, upper);
+                               m, 0, 1, upper, tile);
     splitk_reduce_kernel<<<grid1d(mn, 256), 256, 0, c.stream>>>(m, n, nsplit, P, alpha, beta, C, ldc, upper);
     DCG_LAUNCHED(c);
 }
 
-// Split-K for a single GEMM whose output has too few 64x64 tiles to occupy every SM (a GB300
-// SM retires only about two FP64 FMAs per clock, so a GEMM on a handful of SMs runs at a
-// small fraction of the GPU): K is cut into equal chunks of at least 64.  The number of
-// chunks is the autotuner's choice for the shape (candidates: no split, the occupancy
-// heuristic min(2 SMs / tiles, k / 64), and powers of two up to k / 64), or the heuristic
-// when tuning is off or the call accumulates into C (beta != 0, which the timed trial runs
-// would disturb).  Returns false when the product runs unsplit.
-template <int OPA, int OPB>
-static bool zgemm_splitk(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, const cplx *B,
-                         int64_t ldb, cplx beta, cplx *C, int64_t ldc, int upper = 0) {
-    const int64_t tm = (m + 63) / 64, tn = (n + 63) / 64;
-    // tiles on or above the diagonal only, for a Hermitian product's upper half
-    const int64_t tiles = upper ? (tn * (tn + 1)) / 2 : tm * tn;
+// The tile shape and K split of one FP64 product.  A GEMM whose output tiles do not fill the
+// GPU is split along K into equal chunks of at least 64, computed as one batched GEMM into
+// partial products and reduced in a fixed order.  The autotuner times, per shape, every tile
+// with no split, with the occupancy heuristic min(2 SMs / tiles, k / 64) and with powers of
+// two up to k / 64 (batched products: the tiles alone); candidate 0 (64 x 64 tiles, the
+// heuristic split) is used while tuning is off and for calls that accumulate into C (beta
+// != 0, which the timed trial runs would disturb).
+constexpr double kTuneMinFp64Flops = 1.0e9;
+
+struct ZgPlan {
+    int tile, nsplit;
+};
+
+static std::vector<ZgPlan> zg_candidates(Context &c, int m, int n, int k, int upper, int batch) {
     const int sms = std::max(1, c.num_sms);
-    if (tiles >= sms || k < 128) return false;
-    const int heur = (int)std::min<int64_t>((2 * sms + tiles - 1) / tiles, k / 64);
-    std::vector<int> cand{heur < 2 ? 1 : heur, 1};
-    for (int p = 2; p <= k / 64 && p <= 64; p *= 2) cand.push_back(p);
-    std::sort(cand.begin() + 1, cand.end());
-    cand.erase(std::unique(cand.begin() + 1, cand.end()), cand.end());
-    const TuneKey key{TUNE_ZGEMM_SPLITK, OPA * 8 + OPB, m, n, k, upper};
-    const bool trial_ok = beta.x == 0.0 && beta.y == 0.0;
+    std::vector<ZgPlan> out;
+    for (int t = 0; t < kZgTiles; t++) {
+        const int64_t tiles = zg_tiles(m, n, t, upper);
+        std::vector<int> ns{1};
+        if (batch == 1 && tiles < sms && k >= 128) {
+            const int heur = (int)std::min<int64_t>((2 * sms + tiles - 1) / tiles, k / 64);
+            if (heur >= 2) ns.insert(ns.begin(), heur);
+            for (int p = 2; p <= k / 64 && p <= 64; p *= 2)
+                if (std::find(ns.begin(), ns.end(), p) == ns.end()) ns.push_back(p);
+        }
+        for (int x : ns) out.push_back({t, x});
+    }
+    return out;
+}
+
+template <int OPA, int OPB>
+static void zgemm_plan_run(Context &c, const ZgPlan &p, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda,
+                           int64_t sa, const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc,
+                           int64_t sc, int batch, int upper) {
+    if (p.nsplit >= 2) zgemm_splitk_run<OPA, OPB>(c, m, n, k, p.nsplit, alpha, A, lda, B, ldb, beta, C, ldc, upper, p.tile);
+    else zgemm_launch<OPA, OPB>(c, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, upper, p.tile);
+}
+
+template <int OPA, int OPB>
+static void zgemm_tuned(Context &c, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
+                        const cplx *B, int64_t ldb, int64_t sb, cplx beta, cplx *C, int64_t ldc, int64_t sc, int batch,
+                        int upper) {
+    const std::vector<ZgPlan> cand = zg_candidates(c, m, n, k, upper, batch);
+    const TuneKey key{TUNE_ZGEMM, OPA * 8 + OPB, m, n, k, upper + 2 * std::min(batch, 1 << 20)};
+    // products under ~1 ms of FP64 work keep the heuristic: their trials would cost more than
+    // tuning can return (and a served stream meets many shapes once)
+    const double work = 8.0 * m * n * (double)k * batch;
+    const bool trial_ok = beta.x == 0.0 && beta.y == 0.0 && work >= kTuneMinFp64Flops;
     const int pick = autotune(c, key, (int)cand.size(), trial_ok, [&](int q) {
-        if (cand[q] < 2) zgemm_launch<OPA, OPB>(c, m, n, k, alpha, A, lda, 0, B, ldb, 0, beta, C, ldc, 0, 1, upper);
-        else zgemm_splitk_run<OPA, OPB>(c, m, n, k, cand[q], alpha, A, lda, B, ldb, beta, C, ldc, upper);
+        zgemm_plan_run<OPA, OPB>(c, cand[q], m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, upper);
     });
-    const int nsplit = cand[pick];
-    if (nsplit < 2) return false;
-    zgemm_splitk_run<OPA, OPB>(c, m, n, k, nsplit, alpha, A, lda, B, ldb, beta, C, ldc, upper);
-    return true;
+    zgemm_plan_run<OPA, OPB>(c, cand[pick], m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, upper);
 }
 
 void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cplx *A, int64_t lda, int64_t sa,
@@ -389,11 +437,10 @@ void zgemm(Context &c, Op opa, Op opb, int m, int n, int k, cplx alpha, const cp
     if (m <= 0 || n <= 0 || batch <= 0) return;
     GemmTrace trace(c, "fp64", m, n, k, batch);
     if (zgemm_small(c, opa, opb, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch)) return;
-#define DCG_ZG(a, b)                                                                                   \
-    if (opa == a && opb == b) {                                                                        \
-        if (batch == 1 && zgemm_splitk<a, b>(c, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)) return;  \
-        zgemm_launch<a, b>(c, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, 0);     \
-        return;                                                                                        \
+#define DCG_ZG(a, b)                                                                                  \
+    if (opa == a && opb == b) {                                                                       \
+        zgemm_tuned<a, b>(c, m, n, k, alpha, A, lda, sa, B, ldb, sb, beta, C, ldc, sc, batch, 0);     \
+        return;                                                                                       \
     }
     DCG_ZG(OP_N, OP_N) DCG_ZG(OP_N, OP_T) DCG_ZG(OP_N, OP_C) DCG_ZG(OP_N, OP_R)
     DCG_ZG(OP_T, OP_N) DCG_ZG(OP_T, OP_T) DCG_ZG(OP_T, OP_C) DCG_ZG(OP_T, OP_R)
@@ -411,8 +458,7 @@ void zherk_upper(Context &c, int n, int k, const cplx *A, int64_t lda, cplx *C, 
     if (n <= 0) return;
     GemmTrace trace(c, "herk", n, n, k, 1);
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
-    if (zgemm_splitk<OP_N, OP_C>(c, n, n, k, one, A, lda, A, lda, zero, C, ldc, 1)) return;
-    zgemm_launch<OP_N, OP_C>(c, n, n, k, one, A, lda, 0, A, lda, 0, zero, C, ldc, 0, 1, 1);
+    zgemm_tuned<OP_N, OP_C>(c, n, n, k, one, A, lda, 0, A, lda, 0, zero, C, ldc, 0, 1, 1);
 }
 
 // ===================================================================== Hermitian fill

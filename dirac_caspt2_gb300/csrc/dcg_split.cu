@@ -299,6 +299,7 @@ struct SplitArgs {
     int M, N, nz, nrb, nnb, nks;
     int lbo, sbo;     // descriptor leading / stride byte offsets
     int accumulate;   // C += result
+    int order;        // CTA raster: 0 column blocks of a row block adjacent, 1 row blocks of a column block
     int *err;
 };
 
@@ -327,9 +328,12 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
     __shared__ uint32_t s_tmem;
     unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~(uintptr_t)1023);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    // linear (row block, column block) index with the column blocks of a row block adjacent,
-    // so the CTAs that share an A tile run together and find it in L2
-    const int rb = (int)(blockIdx.x / (unsigned)a.nnb), nb = (int)(blockIdx.x % (unsigned)a.nnb), z = blockIdx.z;
+    // linear (row block, column block) index: order 0 keeps the column blocks of a row block
+    // adjacent (the CTAs sharing an A tile run together and find it in L2), order 1 the row
+    // blocks of a column block (sharing a B tile); the autotuner picks per shape
+    const int rb = a.order ? (int)(blockIdx.x % (unsigned)a.nrb) : (int)(blockIdx.x / (unsigned)a.nnb);
+    const int nb = a.order ? (int)(blockIdx.x / (unsigned)a.nrb) : (int)(blockIdx.x % (unsigned)a.nnb);
+    const int z = blockIdx.z;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < SP_STAGES; s++) {
@@ -529,11 +533,25 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     sa.lbo = lbo;
     sa.sbo = sbo;
     sa.accumulate = accumulate ? 1 : 0;
+    sa.order = 0;
     sa.err = err;
     dim3 grid((unsigned)((int64_t)nrb * nnb), 1, batch);
+    // CTA raster tuned per shape when both orders have more than one block to order; trial
+    // launches overwrite C, so only non-accumulating products are timed
+    const double tensor_work = 15.0 * 8.0 * (double)M * N * K * batch;
+    if (nrb > 1 && nnb > 1) {
+        const TuneKey key{TUNE_SPLIT_ORDER, batch, M, N, K, 0};
+        // products under ~0.1 ms of tensor work keep the default raster
+        sa.order = autotune(c, key, 2, !accumulate && tensor_work >= 1.0e11, [&](int q) {
+            SplitArgs t = sa;
+            t.order = q;
+            sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(t);
+            DCG_LAUNCHED(c);
+        });
+    }
     {
         // tensor work: 15 slice products, each a real GEMM of M x 2N x 2K
-        FamScope fs(c, DCG_FAM_SPLIT_MMA, 15.0 * 8.0 * (double)M * N * K * batch);
+        FamScope fs(c, DCG_FAM_SPLIT_MMA, tensor_work);
         sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(sa);
         DCG_LAUNCHED(c);
     }

@@ -309,8 +309,10 @@ int64_t dcg_server_device_bytes(dcg_server *srv);
 int dcg_server_destroy(dcg_server *srv);
 
 /* ------------------------------------------------------------------------ autotuner
- * Shape-dependent launch choices (today: the K-split of the FP64 GEMMs whose output tiles do
- * not fill the GPU, and the K-chunking of the split-precision GEMMs) are tuned on first use:
+ * Shape-dependent launch choices (today: the tile shape, 64x64, 32x128 or 128x32, and the
+ * K-split of the FP64 GEMMs, and the CTA raster of the split-precision tensor-core GEMMs,
+ * row-block or column-block major, which decides which operand tiles meet in L2) are tuned
+ * on first use, for products of at least ~1 ms of work:
  * every candidate is timed with CUDA events on the calling context's stream and the fastest
  * is kept in a process-wide table that every context then uses.  Different choices change
  * only the summation order of the products.
@@ -318,8 +320,9 @@ int dcg_server_destroy(dcg_server *srv);
  * heuristics for keys not yet tuned, 2 clear the table (mode unchanged), other values only
  * query.  Returns the mode before the call. */
 typedef struct dcg_tune_entry {
-    int32_t kind;                 /* 1: FP64 GEMM K-split, 2: split-precision GEMM K-chunks */
-    int32_t ops, m, n, k, flags;  /* the decision's key (ops: op codes, flags: e.g. upper)   */
+    int32_t kind;                 /* 1: FP64 GEMM tile and K-split, 2: split GEMM CTA raster */
+    int32_t ops, m, n, k, flags;  /* the decision's key (ops: op codes or batch; flags:
+                                     upper + 2 batch for the FP64 GEMM)                    */
     int32_t choice, ncand;        /* chosen candidate (0 = the heuristic) of ncand           */
     float best_ms, heuristic_ms;  /* measured time of the choice and of the heuristic        */
 } dcg_tune_entry;
