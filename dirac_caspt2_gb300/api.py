@@ -205,6 +205,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_server_device_bytes.restype = ctypes.c_int64
     lib.dcg_server_destroy.argtypes = [ctypes.c_void_p]
     lib.dcg_autotune_mode.argtypes = [ctypes.c_int32]
+    lib.dcg_set_autotune_trials.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_autotune_entries.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_autotune_entries.restype = ctypes.c_int32
     lib.dcg_ivo.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
@@ -231,7 +232,7 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
                     "dcg_server_device_bytes", "dcg_server_destroy", "dcg_read_mrconee", "dcg_free_mrconee",
                     "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error", "dcg_ivo",
-                    "dcg_autotune_mode", "dcg_autotune_entries"]
+                    "dcg_autotune_mode", "dcg_autotune_entries", "dcg_set_autotune_trials"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 

@@ -1593,6 +1593,12 @@ int dcg_ivo(dcg_ctx *ctx, int32_t nfsym, const double *mo_energy, int32_t nhomo,
     });
 }
 
+int dcg_set_autotune_trials(dcg_ctx *ctx, int32_t on) {
+    if (!ctx) return DCG_E_ARG;
+    ctx->c.tune_trials = on != 0;
+    return DCG_OK;
+}
+
 int dcg_set_casci_solver(dcg_ctx *ctx, int32_t solver) {
     if (!ctx || solver < DCG_CASCI_AUTO || solver > DCG_CASCI_DAVIDSON) return DCG_E_ARG;
     ctx->c.casci_solver = solver;

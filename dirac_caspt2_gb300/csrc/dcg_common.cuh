@@ -87,6 +87,7 @@ struct Context {
     std::string err;
     int64_t launches = 0;
     int num_sms = 0;
+    bool tune_trials = true;     // may run autotuner trials (off for serving slots)
     void *dev_state = nullptr;   // device-side system state (owned, see dcg_api.cu)
 
     // ---- per-family kernel timing (dcg_time_family)

@@ -205,6 +205,9 @@ int dcg_server_create(int device, int precision, int32_t slots, int64_t hbm_budg
             delete sv;
             return st;
         }
+        // a served stream meets most shapes once: its slots use tuned entries and heuristics
+        // and run no tuning trials of their own (they would sit in the requests' latency)
+        dcg_set_autotune_trials(c, 0);
         sv->ctx.push_back(c);
         sv->held.push_back(dcg_device_bytes(c));
     }

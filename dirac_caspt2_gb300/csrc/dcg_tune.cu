@@ -33,7 +33,7 @@ int autotune_run(Context &c, const TuneKey &key, int ncand, bool trial_ok, void 
         std::lock_guard<std::mutex> lk(g_mu);
         auto it = g_table.find(key);
         if (it != g_table.end()) return it->second.choice;
-        if (mode_locked() == 0 || ncand < 2 || !trial_ok) return 0;
+        if (mode_locked() == 0 || ncand < 2 || !trial_ok || !c.tune_trials) return 0;
     }
     // untimed pass: every candidate once (workspace growth, first-launch costs)
     for (int q = 0; q < ncand; q++) fn(arg, q);

@@ -328,6 +328,9 @@ typedef struct dcg_tune_entry {
 } dcg_tune_entry;
 
 int dcg_autotune_mode(int32_t mode);
+/* Per context: on = 0 makes the context use tuned entries and heuristics only, never running
+ * trials itself (the serving loop's slots are created so). */
+int dcg_set_autotune_trials(dcg_ctx *ctx, int32_t on);
 /* Entries of the table (at most max_entries written to out); returns their total number. */
 int32_t dcg_autotune_entries(dcg_tune_entry *out, int32_t max_entries);
 

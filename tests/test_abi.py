@@ -40,3 +40,14 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
 def test_version_string_without_gpu():
     from dirac_caspt2_gb300 import api
     assert b"sm_103a" in api.load_library().dcg_version()
+
+
+def test_autotune_table_without_gpu():
+    """The tuner's mode and table are host state: readable without a device."""
+    from dirac_caspt2_gb300 import api
+    prev = api.autotune_mode(-1)
+    assert prev in (0, 1)
+    assert api.autotune_mode(0) == prev
+    assert api.autotune_mode(-1) == 0
+    api.autotune_mode(prev)
+    assert isinstance(api.autotune_entries(), list)
