@@ -9,7 +9,7 @@ pytestmark = pytest.mark.gpu
 
 def test_tuned_solve_matches_heuristic(gpu_lib):
     from dirac_caspt2_gb300 import api, synth
-    s = api.SystemInput.from_synth(synth.make_system(synth.SynthConfig(8, 8, 120, 4, seed=21)))
+    s = api.SystemInput.from_synth(synth.make_system(synth.SynthConfig(16, 8, 240, 4, seed=21)))
     prev = api.autotune_mode(0)
     try:
         api.autotune_mode(2)
