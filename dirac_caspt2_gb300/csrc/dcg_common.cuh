@@ -10,6 +10,7 @@
 #include <cstdlib>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "../../include/dcaspt2_gb300.h"
@@ -195,7 +196,7 @@ std::vector<T> download(Context &c, const T *p, size_t n) {
 // and keeps the fastest; later calls of the key, in any context, reuse it.  Candidate 0 is the
 // built-in heuristic, used while tuning is off (dcg_autotune_mode) and for keys first met
 // without trial_ok.  The trial runs must leave the same result as the final run.
-enum TuneKind { TUNE_ZGEMM = 1, TUNE_SPLIT_ORDER = 2 };
+enum TuneKind { TUNE_ZGEMM = 1, TUNE_SPLIT_KERNEL = 2 };
 struct TuneKey {
     int kind, ops, m, n, k, flags;
     bool operator<(const TuneKey &o) const {
@@ -210,7 +211,9 @@ struct TuneKey {
 int autotune_run(Context &c, const TuneKey &key, int ncand, bool trial_ok, void (*fn)(void *, int), void *arg);
 template <typename F>
 int autotune(Context &c, const TuneKey &key, int ncand, bool trial_ok, F &&run) {
-    return autotune_run(c, key, ncand, trial_ok, [](void *p, int q) { (*static_cast<F *>(p))(q); }, &run);
+    using Fn = typename std::remove_reference<F>::type;
+    return autotune_run(c, key, ncand, trial_ok, [](void *p, int q) { (*static_cast<Fn *>(p))(q); },
+                        const_cast<void *>(static_cast<const void *>(&run)));
 }
 
 // Diagnostic: with DCG_GEMM_TRACE=1 in the environment, each GEMM call is timed by CUDA events

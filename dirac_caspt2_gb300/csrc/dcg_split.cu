@@ -276,6 +276,28 @@ __device__ __forceinline__ void umma_f16(uint32_t dtmem, uint64_t adesc, uint64_
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
         "l"(adesc), "l"(bdesc), "r"(SP_IDESC), "r"(acc));
 }
+// instruction descriptor of the persistent kernel's 128 x 64 products
+constexpr int SPP_TN = 64;
+constexpr uint32_t SPP_IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(SPP_TN >> 3) << 17) |
+                               ((uint32_t)(SP_TM >> 4) << 24);
+
+__device__ __forceinline__ void umma_f16_n64(uint32_t dtmem, uint64_t adesc, uint64_t bdesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(dtmem),
+        "l"(adesc), "l"(bdesc), "r"(SPP_IDESC), "r"(acc));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+// wait used while shutting down after an error: bounded by time only
+__device__ __forceinline__ void mbar_drain(uint64_t *bar, uint32_t parity) {
+    const uint64_t t0 = sp_now();
+    while (!mbar_try_wait(bar, parity)) {
+        if (sp_now() - t0 > SP_WAIT_NS) return;
+        __nanosleep(64);
+    }
+}
 __device__ __forceinline__ void umma_commit(uint64_t *bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
                  : "memory");
@@ -458,6 +480,190 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
     }
 }
 
+// Persistent form of the same product.  Work items are 128 x 64 output tiles (half of a
+// 128-column B tile); each CTA takes items grid-stride.  Two accumulator sets of four groups
+// x 64 columns fill the 512 TMEM columns, so the MMAs of one item run while the epilogue
+// warps recombine the previous one: the epilogue, bound by the FP64 pipe, overlaps the
+// tensor work instead of following it.  Roles and stage pipeline as in sp_gemm_kernel, with
+// the stage and item counters running across items.
+constexpr int SPP_STAGES = 5;
+constexpr int SPP_STAGE_BYTES = SPLIT_S * SP_TILE_BYTES + SPLIT_S * (SP_TILE_BYTES / 2);   // 30 KB
+constexpr int SPP_SMEM = SPP_STAGES * SPP_STAGE_BYTES + 1024;
+
+__global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArgs a) {
+    extern __shared__ __align__(1024) unsigned char sp_raw[];
+    __shared__ __align__(8) uint64_t bar_full[SPP_STAGES], bar_empty[SPP_STAGES], acc_full[2], acc_empty[2], bar_drain;
+    __shared__ uint32_t s_tmem;
+    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nnh = (2 * a.N + SPP_TN - 1) / SPP_TN;        // 64-column halves holding output columns
+    const int64_t items = (int64_t)a.nz * a.nrb * nnh;
+    const int nks = a.nks;
+    auto item_coords = [&](int64_t t, int &z, int &rb, int &nh) {
+        z = (int)(t / ((int64_t)a.nrb * nnh));
+        const int64_t r = t % ((int64_t)a.nrb * nnh);
+        if (a.order) {
+            rb = (int)(r % a.nrb);
+            nh = (int)(r / a.nrb);
+        } else {
+            rb = (int)(r / nnh);
+            nh = (int)(r % nnh);
+        }
+    };
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < SPP_STAGES; q++) {
+            mbar_init(&bar_full[q], 1);
+            mbar_init(&bar_empty[q], 1);
+        }
+        for (int q = 0; q < 2; q++) {
+            mbar_init(&acc_full[q], 1);
+            mbar_init(&acc_empty[q], 4);   // one arrival per epilogue warp
+        }
+        mbar_init(&bar_drain, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {   // 2 sets x 4 groups x 64 columns = 512 TMEM columns
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = s_tmem;
+
+    if (warp == 4) {
+        if (lane == 0) {   // producer
+            int64_t it = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x) {
+                int z, rb, nh;
+                item_coords(t, z, rb, nh);
+                const int nb = nh >> 1, half = nh & 1;
+                for (int ks = 0; ks < nks; ks++, it++) {
+                    const int s = (int)(it % SPP_STAGES);
+                    if (it >= SPP_STAGES && !mbar_wait(&bar_empty[s], (uint32_t)(((it / SPP_STAGES) - 1) & 1), a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    unsigned char *st = smem + s * SPP_STAGE_BYTES;
+                    mbar_expect_tx(&bar_full[s], SPP_STAGE_BYTES);
+                    for (int p = 0; p < SPLIT_S; p++) {
+                        const int64_t ta = (((int64_t)p * a.nz + z) * a.nrb + rb) * nks + ks;
+                        bulk_g2s(st + p * SP_TILE_BYTES, reinterpret_cast<const char *>(a.As) + ta * SP_TILE_BYTES,
+                                 SP_TILE_BYTES, &bar_full[s]);
+                        const int64_t tb = ((int64_t)p * a.nnb + nb) * nks + ks;
+                        bulk_g2s(st + SPLIT_S * SP_TILE_BYTES + p * (SP_TILE_BYTES / 2),
+                                 reinterpret_cast<const char *>(a.Bs) + tb * SP_TILE_BYTES + half * (SP_TILE_BYTES / 2),
+                                 SP_TILE_BYTES / 2, &bar_full[s]);
+                    }
+                }
+            }
+            if (!ok)   // copies still in flight land before the CTA leaves
+                for (int64_t j = it - 1; j >= 0 && j >= it - SPP_STAGES; j--)
+                    mbar_drain(&bar_full[j % SPP_STAGES], (uint32_t)((j / SPP_STAGES) & 1));
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {   // MMA issuer
+            int64_t it = 0, tl = 0;
+            bool ok = true;
+            for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x, tl++) {
+                const int b = (int)(tl & 1);
+                if (tl >= 2 && !mbar_wait(&acc_empty[b], (uint32_t)(((tl >> 1) - 1) & 1), a.err)) {
+                    ok = false;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const uint32_t acc = tmem + (uint32_t)(b * 4 * SPP_TN);
+                for (int ks = 0; ks < nks; ks++, it++) {
+                    const int s = (int)(it % SPP_STAGES);
+                    if (!mbar_wait(&bar_full[s], (uint32_t)((it / SPP_STAGES) & 1), a.err)) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;");
+                    const unsigned char *st = smem + s * SPP_STAGE_BYTES;
+                    uint64_t da[SPLIT_S], db[SPLIT_S];
+#pragma unroll
+                    for (int p = 0; p < SPLIT_S; p++) {
+                        da[p] = sp_desc(st + p * SP_TILE_BYTES, a.lbo, a.sbo);
+                        db[p] = sp_desc(st + SPLIT_S * SP_TILE_BYTES + p * (SP_TILE_BYTES / 2), a.lbo, a.sbo);
+                    }
+                    const uint32_t first = ks > 0 ? 1u : 0u;
+                    umma_f16_n64(acc + 0 * SPP_TN, da[0], db[0], first);
+                    umma_f16_n64(acc + 1 * SPP_TN, da[0], db[1], first);
+                    umma_f16_n64(acc + 1 * SPP_TN, da[1], db[0], 1u);
+                    umma_f16_n64(acc + 2 * SPP_TN, da[0], db[2], first);
+                    umma_f16_n64(acc + 2 * SPP_TN, da[1], db[1], 1u);
+                    umma_f16_n64(acc + 2 * SPP_TN, da[2], db[0], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[0], db[3], first);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[1], db[2], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[2], db[1], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[3], db[0], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[0], db[4], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[1], db[3], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[2], db[2], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[3], db[1], 1u);
+                    umma_f16_n64(acc + 3 * SPP_TN, da[4], db[0], 1u);
+                    umma_commit(&bar_empty[s]);
+                }
+                if (ok) umma_commit(&acc_full[b]);
+            }
+            umma_commit(&bar_drain);   // arrives once every MMA issued above has completed
+            mbar_drain(&bar_drain, 0);
+        }
+    } else {
+        // epilogue warps 0-3: warp w owns TMEM lanes 32w..32w+31 = tile rows
+        int64_t tl = 0;
+        for (int64_t t = blockIdx.x; t < items; t += gridDim.x, tl++) {
+            const int b = (int)(tl & 1);
+            if (!mbar_wait(&acc_full[b], (uint32_t)((tl >> 1) & 1), a.err)) break;
+            asm volatile("tcgen05.fence::after_thread_sync;");
+            int z, rb, nh;
+            item_coords(t, z, rb, nh);
+            const int r = warp * 32 + lane;
+            const int64_t i = (int64_t)rb * SP_TM + r;
+            const bool row_ok = i < a.M;
+            const int e = row_ok ? a.eexp[(int64_t)z * a.M + i] : 0;
+            const uint32_t base = tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(b * 4 * SPP_TN);
+            for (int c0 = 0; c0 < SPP_TN; c0 += 32) {
+                uint32_t g0[32], g1[32], g2[32], g3[32];
+                SP_LD32(base + 0 * SPP_TN + c0, g0);
+                SP_LD32(base + 1 * SPP_TN + c0, g1);
+                SP_LD32(base + 2 * SPP_TN + c0, g2);
+                SP_LD32(base + 3 * SPP_TN + c0, g3);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (c0 + 32 >= SPP_TN) {   // the accumulator set is read: hand it back to the MMAs
+                    asm volatile("tcgen05.fence::before_thread_sync;");
+                    __syncwarp();
+                    if (lane == 0) mbar_arrive(&acc_empty[b]);
+                }
+                if (!row_ok) continue;
+#pragma unroll
+                for (int q = 0; q < 32; q += 2) {
+                    const int jr = nh * SPP_TN + c0 + q;   // real column (even: Re)
+                    const int j = jr >> 1;
+                    if (j >= a.N) break;
+                    const int sc = e + a.fexp[j] - 2 * SPLIT_BITS;
+                    const double re = scale_pow2(recombine(g0[q], g1[q], g2[q], g3[q]), sc);
+                    const double im = scale_pow2(recombine(g0[q + 1], g1[q + 1], g2[q + 1], g3[q + 1]), sc);
+                    cplx v = mk(re, im);
+                    cplx *dst = a.C + (int64_t)z * a.c_sb + i * a.c_si + (int64_t)j * a.c_sj;
+                    if (a.accumulate) v = cadd(v, *dst);
+                    *dst = v;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    }
+}
+
 // ------------------------------------------------------------------------- host driver
 // C = A * op(B) (+ C when accumulate), complex FP64 in and out, through the split path.
 // Large operand: element (i, k) of batch z at A[z*a_sb + i*a_si + k*a_sk], i < M, k < K.
@@ -539,21 +745,27 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     // CTA raster tuned per shape when both orders have more than one block to order; trial
     // launches overwrite C, so only non-accumulating products are timed
     const double tensor_work = 15.0 * 8.0 * (double)M * N * K * batch;
-    if (nrb > 1 && nnb > 1) {
-        const TuneKey key{TUNE_SPLIT_ORDER, batch, M, N, K, 0};
-        // products under ~0.1 ms of tensor work keep the default raster
-        sa.order = autotune(c, key, 2, !accumulate && tensor_work >= 1.0e11, [&](int q) {
-            SplitArgs t = sa;
-            t.order = q;
-            sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(t);
-            DCG_LAUNCHED(c);
-        });
-    }
+    // kernel and CTA raster, tuned per shape: candidate q = raster (q & 1), persistent (q & 2);
+    // products under ~0.1 ms of tensor work keep candidate 0
+    DCG_CUDA(cudaFuncSetAttribute(sp_gemm_persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPP_SMEM));
+    const int64_t pitems = (int64_t)batch * nrb * ((2 * N + SPP_TN - 1) / SPP_TN);
+    const unsigned pgrid = (unsigned)std::min<int64_t>(pitems, std::max(1, c.num_sms));
+    auto launch = [&](int q) {
+        SplitArgs t = sa;
+        t.order = q & 1;
+        if (q & 2) sp_gemm_persist_kernel<<<pgrid, SP_THREADS, SPP_SMEM, c.stream>>>(t);
+        else sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(t);
+        DCG_LAUNCHED(c);
+    };
+    const TuneKey key{TUNE_SPLIT_KERNEL, batch, M, N, K, 0};
+    int pick;
+    const char *force = getenv("DCG_SPLIT_KERNEL");   // diagnostic: a fixed candidate 0-3
+    if (force && force[0] >= '0' && force[0] <= '3' && force[1] == 0) pick = force[0] - '0';
+    else pick = autotune(c, key, 4, !accumulate && tensor_work >= 1.0e11, launch);
     {
         // tensor work: 15 slice products, each a real GEMM of M x 2N x 2K
         FamScope fs(c, DCG_FAM_SPLIT_MMA, tensor_work);
-        sp_gemm_kernel<<<grid, SP_THREADS, SP_SMEM, c.stream>>>(sa);
-        DCG_LAUNCHED(c);
+        launch(pick);
     }
 }
 

@@ -106,3 +106,28 @@ def test_split_gemm_accumulate(session):
     torch.cuda.synchronize()
     Cref = (C0 + A @ B).cuda()
     _check(C.T, Cref, A.abs().amax(dim=1).cuda(), B.abs().amax(dim=0).cuda(), K)
+
+
+@pytest.mark.parametrize("M,N,K,batch", [(1000, 300, 300, 2), (257, 7, 600, 1), (130, 33, 40, 3), (64, 129, 129, 1)])
+def test_split_gemm_kernel_variants_agree(session, monkeypatch, M, N, K, batch):
+    """The four tuned variants (row- or column-block raster, one tile per CTA or persistent
+    CTAs with double-buffered accumulators) give the same bits, and those pass the bound."""
+    gen = torch.Generator().manual_seed(3 * M + N + K)
+    A = _rand((batch, K, M), gen).transpose(1, 2)
+    B = _rand((N, K), gen).T
+    A_cm = torch.empty((batch, K, M), dtype=torch.complex128, device="cuda")
+    A_cm.copy_(A.transpose(1, 2))
+    B_cm = torch.empty((N, K), dtype=torch.complex128, device="cuda")
+    B_cm.copy_(B.T)
+    out = []
+    for q in "0123":
+        monkeypatch.setenv("DCG_SPLIT_KERNEL", q)
+        C = torch.zeros((batch, N, M), dtype=torch.complex128, device="cuda")
+        session.zgemm(SPLIT, M, N, K, batch, A_cm.data_ptr(), 1, M, M * K, B_cm.data_ptr(), K, False,
+                      C.data_ptr(), 1, M, M * N)
+        torch.cuda.synchronize()
+        out.append(C.clone())
+    for C in out[1:]:
+        assert torch.equal(C, out[0])
+    Cref = torch.matmul(A.cuda(), B.cuda())
+    _check(out[2].transpose(1, 2), Cref, A.abs().amax(dim=(0, 2)).cuda(), B.abs().amax(dim=0).cuda(), K)
