@@ -237,7 +237,7 @@ FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "ei
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
 
-TUNE_KINDS = {1: "fp64_gemm_tile_ksplit", 2: "split_gemm_raster"}
+TUNE_KINDS = {1: "fp64_gemm_tile_ksplit", 2: "split_gemm_kernel_raster"}
 
 
 def autotune_mode(mode: int = -1) -> int:

@@ -310,9 +310,10 @@ int dcg_server_destroy(dcg_server *srv);
 
 /* ------------------------------------------------------------------------ autotuner
  * Shape-dependent launch choices (today: the tile shape, 64x64, 32x128 or 128x32, and the
- * K-split of the FP64 GEMMs, and the CTA raster of the split-precision tensor-core GEMMs,
- * row-block or column-block major, which decides which operand tiles meet in L2) are tuned
- * on first use, for products of at least ~1 ms of work:
+ * K-split of the FP64 GEMMs; for the split-precision tensor-core GEMMs the kernel, one tile
+ * per CTA or persistent CTAs whose epilogue overlaps the next tile's MMAs, and the CTA
+ * raster, row-block or column-block major, which decides which operand tiles meet in L2) are
+ * tuned on first use, for products of at least ~1 ms of work:
  * every candidate is timed with CUDA events on the calling context's stream and the fastest
  * is kept in a process-wide table that every context then uses.  Different choices change
  * only the summation order of the products.
@@ -320,7 +321,7 @@ int dcg_server_destroy(dcg_server *srv);
  * heuristics for keys not yet tuned, 2 clear the table (mode unchanged), other values only
  * query.  Returns the mode before the call. */
 typedef struct dcg_tune_entry {
-    int32_t kind;                 /* 1: FP64 GEMM tile and K-split, 2: split GEMM CTA raster */
+    int32_t kind;                 /* 1: FP64 GEMM tile and K-split, 2: split GEMM kernel/raster */
     int32_t ops, m, n, k, flags;  /* the decision's key (ops: op codes or batch; flags:
                                      upper + 2 batch for the FP64 GEMM)                    */
     int32_t choice, ncand;        /* chosen candidate (0 = the heuristic) of ncand           */

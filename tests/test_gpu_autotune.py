@@ -27,7 +27,7 @@ def test_tuned_solve_matches_heuristic(gpu_lib):
             r2 = ses.solve(s)
         tuned = api.autotune_entries()
         assert tuned, "no product was large enough to tune"
-        assert {t["kind"] for t in tuned} <= {"fp64_gemm_tile_ksplit", "split_gemm_raster"}
+        assert {t["kind"] for t in tuned} <= {"fp64_gemm_tile_ksplit", "split_gemm_kernel_raster"}
         for t in tuned:
             assert 0 <= t["choice"] < t["ncand"] and t["best_ms"] <= t["heuristic_ms"] + 1e-6
         assert r1.total_energy == r2.total_energy     # tuned choices are reused
