@@ -1,5 +1,6 @@
 // The autotuner's table (see dcg_common.cuh): tuned choices per decision and problem shape,
 // shared by every context of the process, and its C ABI.
+#include <cstdio>
 #include <mutex>
 #include <vector>
 
@@ -17,6 +18,7 @@ struct TuneEntry {
 std::mutex g_mu;
 std::map<TuneKey, TuneEntry> g_table;
 int g_mode = -1;   // -1: not read yet
+bool g_loaded = false;
 
 int mode_locked() {
     if (g_mode < 0) {
@@ -26,13 +28,45 @@ int mode_locked() {
     return g_mode;
 }
 
+// With DCG_TUNE_FILE set, the table persists in that text file, one entry per line
+// ("kind ops m n k flags choice ncand best_ms heuristic_ms"): entries are read at the first
+// lookup and every new entry is appended, so another process (a profiler's run of the same
+// workload, a service restart) reuses the choices without trials.
+const char *tune_file() { return getenv("DCG_TUNE_FILE"); }
+
+void load_locked() {
+    if (g_loaded) return;
+    g_loaded = true;
+    const char *f = tune_file();
+    if (!f || !f[0]) return;
+    FILE *fp = fopen(f, "r");
+    if (!fp) return;
+    TuneKey k;
+    TuneEntry e;
+    while (fscanf(fp, "%d %d %d %d %d %d %d %d %f %f", &k.kind, &k.ops, &k.m, &k.n, &k.k, &k.flags, &e.choice,
+                  &e.ncand, &e.best_ms, &e.heuristic_ms) == 10)
+        if (e.choice >= 0 && e.choice < e.ncand) g_table.emplace(k, e);
+    fclose(fp);
+}
+
+void save_locked(const TuneKey &k, const TuneEntry &e) {
+    const char *f = tune_file();
+    if (!f || !f[0]) return;
+    FILE *fp = fopen(f, "a");
+    if (!fp) return;
+    fprintf(fp, "%d %d %d %d %d %d %d %d %.6f %.6f\n", k.kind, k.ops, k.m, k.n, k.k, k.flags, e.choice, e.ncand,
+            e.best_ms, e.heuristic_ms);
+    fclose(fp);
+}
+
 }  // namespace
 
 int autotune_run(Context &c, const TuneKey &key, int ncand, bool trial_ok, void (*fn)(void *, int), void *arg) {
     {
         std::lock_guard<std::mutex> lk(g_mu);
+        load_locked();
         auto it = g_table.find(key);
-        if (it != g_table.end()) return it->second.choice;
+        if (it != g_table.end()) return it->second.choice < ncand ? it->second.choice : 0;
         if (mode_locked() == 0 || ncand < 2 || !trial_ok || !c.tune_trials) return 0;
     }
     // untimed pass: every candidate once (workspace growth, first-launch costs)
@@ -58,6 +92,7 @@ int autotune_run(Context &c, const TuneKey &key, int ncand, bool trial_ok, void 
         if (best[q] < best[pick]) pick = q;
     std::lock_guard<std::mutex> lk(g_mu);
     auto ins = g_table.emplace(key, TuneEntry{pick, ncand, best[pick], best[0]});
+    if (ins.second) save_locked(key, ins.first->second);
     return ins.first->second.choice;   // a concurrent tuner of the same key may have won
 }
 
@@ -75,6 +110,7 @@ int dcg_autotune_mode(int32_t mode) {
 
 int32_t dcg_autotune_entries(dcg_tune_entry *out, int32_t max_entries) {
     std::lock_guard<std::mutex> lk(dcg::g_mu);
+    dcg::load_locked();
     int32_t n = 0;
     for (const auto &kv : dcg::g_table) {
         if (out && n < max_entries) {

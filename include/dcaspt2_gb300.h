@@ -317,6 +317,8 @@ int dcg_server_destroy(dcg_server *srv);
  * every candidate is timed with CUDA events on the calling context's stream and the fastest
  * is kept in a process-wide table that every context then uses.  Different choices change
  * only the summation order of the products.
+ * With the environment variable DCG_TUNE_FILE naming a text file, the table is read from it
+ * at first use and each new entry appended to it, so later processes reuse the choices.
  * mode: 1 tune (default; environment DCG_AUTOTUNE=0 starts with 0), 0 use the built-in
  * heuristics for keys not yet tuned, 2 clear the table (mode unchanged), other values only
  * query.  Returns the mode before the call. */

@@ -51,3 +51,17 @@ def test_autotune_table_without_gpu():
     assert api.autotune_mode(-1) == 0
     api.autotune_mode(prev)
     assert isinstance(api.autotune_entries(), list)
+
+
+def test_autotune_table_file_is_read(tmp_path, monkeypatch):
+    """DCG_TUNE_FILE entries are loaded at the first lookup (in a fresh process)."""
+    import subprocess
+    import sys
+    f = tmp_path / "tune.txt"
+    f.write_text("1 0 792 300 1728 2 5 18 3.19 4.36\n2 1 43200 300 300 0 3 4 0.52 0.58\n")
+    code = ("from dirac_caspt2_gb300 import api; e = api.autotune_entries(); "
+            "print(len(e), sorted((x['kind'], x['m'], x['choice']) for x in e))")
+    env = dict(os.environ, DCG_TUNE_FILE=str(f), PYTHONPATH=ROOT)
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, env=env, cwd=ROOT)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == "2 [('fp64_gemm_tile_ksplit', 792, 5), ('split_gemm_kernel_raster', 43200, 3)]"
