@@ -158,6 +158,19 @@ def run_reference(args, cfg_name):
     return 0
 
 
+def _traffic(family, cfg_name):
+    """DRAM bytes per launch of the family, from the ncu capture summarised under profiles/
+    (dram__bytes_read.sum + dram__bytes_write.sum, mean over one solve's launches)."""
+    import re
+    if family != "split_mma":
+        return None
+    p = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"launch_list_{cfg_name}_split.md")
+    if not os.path.exists(p):
+        return None
+    m = re.search(r"^traffic_bytes_per_launch = (\d+)", open(p).read(), re.M)
+    return int(m.group(1)) if m else None
+
+
 def run_ours(args, cfg_name):
     import torch
     rank, world, local = _dist()
@@ -264,7 +277,7 @@ def run_ours(args, cfg_name):
         achieved = fam_work / (fam_ms * 1e-3) / 1e12
         roof = {"bound": "fp64", "achieved": achieved, "peak": None, "unit": "TFLOP/s", "frac": None,
                 "work": "FP64 FLOPs; GB300 has no FP64 tensor rate to compare against"}
-    roof.update({"traffic": None, "kernel_family": family, "launches_timed": fam_launch,
+    roof.update({"traffic": _traffic(family, cfg_name), "kernel_family": family, "launches_timed": fam_launch,
                  "mean_launch_ms": fam_ms / max(1, fam_launch),
                  "peak_source": f"{src} MEASURED_PEAKS.json ({'sustained' if roof['unit'] == 'TFLOP/s' else 'burst'})"})
     e_casci, e2_last, e_tot = res_v[-1]

@@ -378,7 +378,5 @@ void ivo_blocks_eig(Context &c, const cplx *F1A, const cplx *F2A, const double *
                     double numh, const std::vector<std::vector<int>> &blocks, std::vector<std::vector<double>> &w_out,
                     std::vector<std::vector<cplx>> &v_out);
 
-// Small Hermitian eigenproblem (n <= 64) in one block by cyclic Jacobi (dcg_davidson.cu).
-void small_heev(Context &c, int n, const cplx *G, int ldg, double *w, cplx *Y, int ldy);
 
 }  // namespace dcg
