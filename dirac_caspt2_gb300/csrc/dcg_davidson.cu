@@ -5,7 +5,7 @@
 // excitations of each determinant, dcg_ci.cu); every step is a device kernel:
 //   W = H V                        (the sigma vectors, one warp per row of H)
 //   G = V^H W                      (Rayleigh matrix, symmetrised)
-//   G Y = Y diag(theta)            (one-CTA ZHEEV algorithm, dcg_zheev.cuh)
+//   G Y = Y diag(theta)            (one-block cyclic Jacobi, below)
 //   R = W Y - V Y diag(theta)      (residuals of the block's Ritz pairs)
 //   T = R / (theta - diag(H))      (diagonal preconditioner)
 //   T orthonormalised against V    (classical Gram-Schmidt applied twice), appended to V.
@@ -19,13 +19,14 @@
 
 #include "dcg_common.cuh"
 #include "dcg_kernels.cuh"
-#include "dcg_zheev.cuh"
 
 namespace dcg {
 
 namespace {
 
-constexpr int kDavMaxM = 64;   // largest subspace
+constexpr int kJacobiMaxN = 64;
+constexpr int kJacobiThreads = 256;
+constexpr int kJacobiMaxSweeps = 40;
 
 __device__ __forceinline__ double warp_sum_d(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -46,6 +47,133 @@ __device__ double block_sum_d(double v, double *sh) {
     const double r = sh[0];
     __syncthreads();
     return r;
+}
+
+// Player at position `pos` of round `s` of a round-robin tournament of np players (np even):
+// position 0 stays, the others rotate.  Round s pairs positions k and np-1-k.
+__device__ __forceinline__ int rr_player(int pos, int s, int np) {
+    return pos == 0 ? 0 : 1 + (pos - 1 + s) % (np - 1);
+}
+
+// All eigenpairs of a small Hermitian matrix G (n <= 64, column-major, ldg; the matrix used is
+// (G + G^H)/2) by cyclic Jacobi with the parallel round-robin ordering (Golub & Van Loan,
+// Matrix Computations, 4th ed., 8.5.5): each round rotates n/2 disjoint pairs at once,
+// A <- J^H A J, V <- V J.  The 2x2 Hermitian block [[a, |b| e^{i phi}], [., d]] is made real
+// by the phase e^{i phi} and rotated by the symmetric Schur step (ibid. 8.5.2), so
+// J_pp = J_qq = c, J_pq = s e^{i phi}, J_qp = -s e^{-i phi}.  Sweeps stop when the squared
+// off-diagonal Frobenius norm is below 1e-30 of the whole (status 1 after 40 sweeps).
+// Output: ascending eigenvalues w[n], eigenvectors Y (n x n, ldy).  One block.
+__global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, const int *__restrict__ n_dev,
+                                                                       const cplx *__restrict__ G, int ldg,
+                                                                       double *w, cplx *Y, int ldy, int *status) {
+    extern __shared__ double2 jsm[];
+    if (n_dev) n = *n_dev;   // dimension read on the device (graph replays of a Davidson step)
+    const int np = n + (n & 1);   // padded to even: the dummy player pairs with nobody
+    cplx *A = jsm;                // np x np
+    cplx *V = A + np * np;        // np x np
+    __shared__ double cs_c[kJacobiMaxN / 2], cs_s[kJacobiMaxN / 2], cs_pr[kJacobiMaxN / 2], cs_pi[kJacobiMaxN / 2];
+    __shared__ int cs_p[kJacobiMaxN / 2], cs_q[kJacobiMaxN / 2];
+    __shared__ double red[32];
+    __shared__ int rank_sh[kJacobiMaxN];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int e = tid; e < np * np; e += nt) {
+        const int i = e % np, j = e / np;
+        cplx a = mk(0.0, 0.0);
+        if (i < n && j < n) {
+            const cplx x = G[i + (int64_t)ldg * j], y = G[j + (int64_t)ldg * i];
+            a = mk(0.5 * (x.x + y.x), 0.5 * (x.y - y.y));
+            if (i == j) a.y = 0.0;
+        }
+        A[e] = a;
+        V[e] = mk(i == j ? 1.0 : 0.0, 0.0);
+    }
+    __syncthreads();
+    double fro = 0.0;
+    for (int e = tid; e < np * np; e += nt) fro += A[e].x * A[e].x + A[e].y * A[e].y;
+    fro = block_sum_d(fro, red);
+    const int npair = np / 2;
+    int sweep = 0;
+    for (; sweep < kJacobiMaxSweeps; sweep++) {
+        double off = 0.0;
+        for (int e = tid; e < np * np; e += nt)
+            if (e % np != e / np) off += A[e].x * A[e].x + A[e].y * A[e].y;
+        off = block_sum_d(off, red);
+        if (off <= 1e-30 * fro || fro == 0.0) break;
+        for (int s = 0; s < np - 1; s++) {
+            // rotation parameters of each pair from the current A
+            for (int k = tid; k < npair; k += nt) {
+                int p = rr_player(k, s, np), q = rr_player(np - 1 - k, s, np);
+                if (p > q) {
+                    const int t = p;
+                    p = q;
+                    q = t;
+                }
+                cs_p[k] = p;
+                cs_q[k] = q;
+                double c = 1.0, sn = 0.0, pr = 1.0, pi = 0.0;
+                const cplx b = A[p + np * q];
+                const double ab = sqrt(b.x * b.x + b.y * b.y);
+                if (q < n && ab > 0.0) {
+                    const double app = A[p + np * p].x, aqq = A[q + np * q].x;
+                    const double zeta = (aqq - app) / (2.0 * ab);
+                    const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    sn = t * c;
+                    pr = b.x / ab;
+                    pi = b.y / ab;
+                }
+                cs_c[k] = c;
+                cs_s[k] = sn;
+                cs_pr[k] = pr;
+                cs_pi[k] = pi;
+            }
+            __syncthreads();
+            // columns: A <- A J, V <- V J
+            for (int e = tid; e < np * npair; e += nt) {
+                const int i = e % np, k = e / np;
+                const int p = cs_p[k], q = cs_q[k];
+                const double c = cs_c[k], sn = cs_s[k];
+                const cplx sp = mk(sn * cs_pr[k], sn * cs_pi[k]);    // s e^{i phi}
+                const cplx sm = mk(sn * cs_pr[k], -sn * cs_pi[k]);   // s e^{-i phi}
+                const cplx ap = A[i + np * p], aq = A[i + np * q];
+                A[i + np * p] = csub(mk(c * ap.x, c * ap.y), cmul(sm, aq));
+                A[i + np * q] = cadd(cmul(sp, ap), mk(c * aq.x, c * aq.y));
+                const cplx vp = V[i + np * p], vq = V[i + np * q];
+                V[i + np * p] = csub(mk(c * vp.x, c * vp.y), cmul(sm, vq));
+                V[i + np * q] = cadd(cmul(sp, vp), mk(c * vq.x, c * vq.y));
+            }
+            __syncthreads();
+            // rows: A <- J^H A
+            for (int e = tid; e < np * npair; e += nt) {
+                const int j = e % np, k = e / np;
+                const int p = cs_p[k], q = cs_q[k];
+                const double c = cs_c[k], sn = cs_s[k];
+                const cplx sp = mk(sn * cs_pr[k], sn * cs_pi[k]);
+                const cplx sm = mk(sn * cs_pr[k], -sn * cs_pi[k]);
+                const cplx ap = A[p + np * j], aq = A[q + np * j];
+                A[p + np * j] = csub(mk(c * ap.x, c * ap.y), cmul(sp, aq));
+                A[q + np * j] = cadd(cmul(sm, ap), mk(c * aq.x, c * aq.y));
+            }
+            __syncthreads();
+        }
+    }
+    // ascending order (ties by index), then the outputs
+    for (int i = tid; i < n; i += nt) {
+        const double di = A[i + np * i].x;
+        int r = 0;
+        for (int j = 0; j < n; j++) {
+            const double dj = A[j + np * j].x;
+            r += (dj < di) || (dj == di && j < i);
+        }
+        rank_sh[i] = r;
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt) w[rank_sh[i]] = A[i + np * i].x;
+    for (int e = tid; e < n * n; e += nt) {
+        const int i = e % n, j = e / n;
+        Y[i + (int64_t)ldy * rank_sh[j]] = V[i + np * j];
+    }
+    if (tid == 0 && sweep >= kJacobiMaxSweeps) *status = 1;
 }
 
 // Columns c of X (n x m) set to the unit vectors e_{idx[c]}.
@@ -116,30 +244,6 @@ __global__ void __launch_bounds__(256) csr_hx_kernel(int n, int k, const int64_t
     }
 }
 
-// Eigenpairs of the m x m Rayleigh matrix, (G + G^H) / 2, by the CTA ZHEEV: ascending w[0..m)
-// and the vectors in the columns of Y (ldy); *status set on failure (sticky).
-__global__ void __launch_bounds__(zheev_detail::kZheevThreads) rayleigh_eig_kernel(const int *__restrict__ m_dev,
-                                                                                 const cplx *__restrict__ G, int ldg,
-                                                                                 double *w, cplx *Y, int ldy,
-                                                                                 zheev_detail::ZheevJob J, int *status) {
-    const int n = *m_dev;
-    J.n = n;
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) {
-        const int i = e % n, j = e / n;
-        cplx a = mk(0.0, 0.0);
-        if (i <= j) {
-            const cplx x = G[i + (int64_t)ldg * j], y = G[j + (int64_t)ldg * i];
-            a = mk(0.5 * (x.x + y.x), i == j ? 0.0 : 0.5 * (x.y - y.y));
-        }
-        J.a[e] = a;
-    }
-    __syncthreads();
-    const int st = zheev_detail::zheev_cta(J);
-    for (int e = threadIdx.x; e < n * n; e += blockDim.x) Y[e % n + (int64_t)ldy * (e / n)] = J.z[e];
-    for (int k = threadIdx.x; k < n; k += blockDim.x) w[k] = J.w[k];
-    if (threadIdx.x == 0 && st != 0) *status = 1;
-}
-
 // ---- the Davidson step with its sizes on the device ------------------------------------
 // A step's launches read the subspace size m and the running counts from DavState, so one
 // captured sequence (a CUDA graph) serves every step.
@@ -148,7 +252,7 @@ struct DavState {
     int cand;     // new directions accepted in this step
     int stop;     // a direction was rejected: none after it this step
     int act;      // the direction being built is live
-    int jac;      // a Rayleigh eigensolve failed (sticky)
+    int jac;      // a Jacobi solve ran out of sweeps (sticky)
     int pad[3];
     double worst;  // largest residual norm of the wanted roots
     double n0;     // |direction|^2 before the Gram-Schmidt passes
@@ -351,7 +455,7 @@ static void csr_hx(Context &c, const CsrMatrix &H, const cplx *X, int64_t ldx, i
 // w[0..nwant), eigenvectors to the columns of Z (n x nwant, ldz = n), each with residual norm
 // <= tol_rel * max(1, max_i |H_ii|).
 //
-// One step: the Rayleigh matrix G = V^H W and its eigenpairs (one-CTA ZHEEV), the block's Ritz
+// One step: the Rayleigh matrix G = V^H W and its eigenpairs (Jacobi), the block's Ritz
 // vectors X = V Y and images HX = W Y, their residuals and preconditioned corrections T, a
 // restart V, W <- X, HX when the next block would not fit, then each unconverged correction
 // orthonormalised against V (classical Gram-Schmidt twice) and appended, and W extended by
@@ -362,7 +466,7 @@ static void csr_hx(Context &c, const CsrMatrix &H, const cplx *X, int64_t ldx, i
 void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, cplx *Z, double tol_rel, int maxit) {
     const int n = H.n;
     const int nb = std::min(n, nwant + 2);   // block: the wanted roots and a margin for near-degeneracy
-    const int mmax = std::min(n, std::min(kDavMaxM, std::max(24, 8 * nb)));
+    const int mmax = std::min(n, std::min(kJacobiMaxN, std::max(24, 8 * nb)));
     if (nwant < 1 || nb > mmax || n < 2) throw Error{DCG_E_ARG, "davidson: block does not fit the subspace"};
     const int64_t ld = n;
     cplx *V = wsget<cplx>(c, "dav.V", (size_t)n * mmax);
@@ -398,24 +502,13 @@ void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, c
     s0.m = nb;
     DCG_CUDA(cudaMemcpyAsync(st, &s0, sizeof(DavState), cudaMemcpyHostToDevice, c.stream));
 
-    zheev_detail::ZheevJob ej{};
-    ej.a = wsget<cplx>(c, "dav.ea", (size_t)mmax * mmax);
-    ej.z = wsget<cplx>(c, "dav.ez", (size_t)mmax * mmax);
-    ej.t = wsget<cplx>(c, "dav.et", (size_t)mmax);
-    ej.tau = wsget<cplx>(c, "dav.etau", (size_t)mmax);
-    ej.w = wsget<double>(c, "dav.ew", (size_t)mmax);
-    ej.d = wsget<double>(c, "dav.ed", (size_t)mmax);
-    ej.e = wsget<double>(c, "dav.ee", (size_t)mmax);
-    ej.cap_rot = 30LL * mmax * mmax + mmax + 16;
-    ej.cap_hdr = 31 * mmax + 16;
-    ej.rc = wsget<double>(c, "dav.erc", (size_t)ej.cap_rot);
-    ej.rs = wsget<double>(c, "dav.ers", (size_t)ej.cap_rot);
-    ej.hdr = wsget<int4>(c, "dav.ehdr", (size_t)ej.cap_hdr);
-    ej.swp = wsget<int2>(c, "dav.eswp", (size_t)mmax);
+    const int np = mmax + (mmax & 1);
+    const size_t jsmem = 2 * sizeof(cplx) * (size_t)np * np;
+    DCG_CUDA(cudaFuncSetAttribute(jacobi_heev_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)jsmem));
     const int hx_blocks = (int)(((int64_t)n * 32 + 255) / 256);
     auto enqueue_step = [&]() {
         rr_kernel<<<dim3(mmax, mmax), 256, 0, c.stream>>>(n, V, W, ld, G, mmax, st);
-        rayleigh_eig_kernel<<<1, zheev_detail::kZheevThreads, 0, c.stream>>>(&st->m, G, mmax, th, Y, mmax, ej, &st->jac);
+        jacobi_heev_kernel<<<1, 64, jsmem, c.stream>>>(mmax, &st->m, G, mmax, th, Y, mmax, &st->jac);
         ritz_kernel<<<dim3(grid1d(n, 128), nb, 2), 128, 0, c.stream>>>(n, V, W, ld, Y, mmax, X, HX, st);
         residual_kernel<<<nb, 256, 0, c.stream>>>(n, HX, X, ld, th, H.diag, T, h2);
         step_begin_kernel<<<1, 32, 0, c.stream>>>(nwant, h2, st);
