@@ -241,6 +241,37 @@ def run_ours(args, cfg_name):
     tot_v = sum(per_v) / 1e3
     tot_e = sum(per_e) / 1e3
 
+    # end to end through the serving loop: the same host-buffer requests on two slots, so one
+    # request's host-to-device copy and set-up overlap the other's solve (each request still
+    # copies its records from pinned host memory and reads its energies back)
+    def e2e_served(steps, slots=2):
+        srv = api.Caspt2Server(local, prec, slots=slots)
+        try:
+            for k in range(slots):   # slot workspaces
+                srv.submit(k, hb_host)
+            for _ in range(slots):
+                r = srv.poll(600000)
+                if r is None or r.status != 0:
+                    raise RuntimeError(f"served e2e warm-up failed: {None if r is None else r.error}")
+            replicas.barrier()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for k in range(steps):
+                srv.submit(100 + k, hb_host)
+            got = []
+            while len(got) < steps:
+                r = srv.poll(600000)
+                if r is None:
+                    raise RuntimeError("served e2e: no result within 600 s")
+                if r.status != 0:
+                    raise RuntimeError(f"served e2e request failed: {r.error}")
+                got.append(r)
+            return time.perf_counter() - t0, got
+        finally:
+            srv.close()
+
+    tot_s, res_s = e2e_served(args.steps)
+
     # plain FP64 GPU path on the same system: the comparison the metric names
     fp64 = None
     if prec == api.DCG_PREC_SPLIT and not args.no_fp64_compare:
@@ -260,8 +291,8 @@ def run_ours(args, cfg_name):
                 "dE2_by_subspace": {k: e2_s[k] - e2_d[k] for k in e2_s}}
 
     # replicas: every rank solves its own copy; the slowest rank bounds the job
-    tot_v, tot_e = replicas.max_over_ranks([tot_v, tot_e])
-    value, e2e = world * args.steps / tot_v, world * args.steps / tot_e
+    tot_v, tot_e, tot_s = replicas.max_over_ranks([tot_v, tot_e, tot_s])
+    value, e2e, e2e_s = world * args.steps / tot_v, world * args.steps / tot_e, world * args.steps / tot_s
     peaks, src = _peaks()
     fam_ms, fam_launch, fam_work = fam
     if family in ("hstream", "scatter"):
@@ -294,9 +325,17 @@ def run_ours(args, cfg_name):
                        "precision": args.precision, "parallelism": f"replicas x{world}",
                        "l2": "inputs larger than L2 (1 GB of records, 0.6 GB H class per step)"},
             "p50_ms": float(np.percentile(per_v, 50)), "p99_ms": float(np.percentile(per_v, 99)),
-            "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": hb_host.h2d_bytes,
-                    "d2h_bytes_per_step": 8 * (1 + 8 + 8 + 2), "p50_ms": float(np.percentile(per_e, 50)),
-                    "p99_ms": float(np.percentile(per_e, 99))},
+            "e2e": {"value": e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hb_host.h2d_bytes,
+                    "d2h_bytes_per_step": 8 * (1 + 8 + 8 + 2),
+                    "path": "dcg_server with 2 slots (public serving API): each step one request from "
+                            "pinned host buffers, host wall clock from the first submit to the last result",
+                    "p50_ms": float(np.percentile([(r.t_end - r.t_submit) * 1e3 for r in res_s], 50)),
+                    "p99_ms": float(np.percentile([(r.t_end - r.t_submit) * 1e3 for r in res_s], 99)),
+                    "max_abs_dE_vs_device_resident": max(abs(r.total_energy - res_v[-1][2]) for r in res_s),
+                    "single_context": {"value": e2e, "unit": "solves/s",
+                                       "p50_ms": float(np.percentile(per_e, 50)),
+                                       "p99_ms": float(np.percentile(per_e, 99)),
+                                       "timing": "CUDA events on the context's stream"}},
             "gpu_launches": int(launches_v),
             "clocks": clocks_v, "roofline": roof,
             "stage_ms_last_step": {k: round(v, 3) for k, v in stage.items()},
