@@ -274,7 +274,7 @@ def run_ours(args, cfg_name):
 
     # the FP64 eigensolver families, timed live on two more steps: Householder reduction
     # (work (16/3) n^3 per matrix), tridiagonal eigenvalues, back-transformation (8 n^2 m)
-    fp64_nominal = 152 * 4 * 2.070   # TF/s: 152 SMs x 2 FP64 FMA per clock x 2.07 GHz
+    fp64_nominal = 152 * 4 * 2.070e-3   # TF/s: 152 SMs x 2 FP64 FMA per clock x 2.07 GHz
     fam_live = {}
     for fname in ("eig_tri", "eig_val", "eig_back"):
         _, _, _, _, st = timed(ses, hb_dev, 2, fname)
