@@ -1467,30 +1467,33 @@ void heev_values_batched(Context &c, const std::vector<EigJob> &jobs) {
 // y <- Q^H y for the columns of Y0 (written to Y), Q = H_0 H_1 ... H_{n-2} the reflectors of a
 // tridiagonal reduction (H_k = I - tau_k v_k v_k^H, v_k in column k of A below the diagonal):
 // H_0^H first.  One warp per column, the column in registers (R = ceil(n / 32)).
-template <int R>
+template <int R, int WPC>
 __global__ void __launch_bounds__(64) apply_qh_kernel(int n, const cplx *__restrict__ A, int64_t lda,
                                                      const cplx *__restrict__ tau, const cplx *__restrict__ Y0,
                                                      int64_t ldy0, int ncol, cplx *Y, int64_t ldy) {
+    __shared__ double part[2][2][2];   // [parity][warp][re, im]
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int col = blockIdx.x * 2 + warp;
-    if (col >= ncol) return;   // whole warp
+    const int wsub = warp % WPC;                              // warp within its column
+    const int col = blockIdx.x * (2 / WPC) + warp / WPC;      // 64 threads: 2 / WPC columns
+    const bool have = col < ncol;
+    if (WPC == 1 && !have) return;   // whole warp; with two warps per column both stay for the barriers
     cplx z[R];
 #pragma unroll
     for (int i = 0; i < R; i++) {
-        const int r = lane + 32 * i;
-        z[i] = r < n ? Y0[r + (int64_t)col * ldy0] : mk(0.0, 0.0);
+        const int r = lane + 32 * (WPC * i + wsub);
+        z[i] = (have && r < n) ? Y0[r + (int64_t)col * ldy0] : mk(0.0, 0.0);
     }
     for (int k = 0; k + 1 < n; k++) {
         const cplx t = __ldg(tau + k);
-        if (t.x == 0.0 && t.y == 0.0) continue;
-        const int i0 = (k + 1) >> 5;
+        if (t.x == 0.0 && t.y == 0.0) continue;   // uniform over the block
+        const int i0 = (k + 1) / (32 * WPC);      // row chunks below k+1 hold v = 0 in every lane
         const cplx *vk = A + (int64_t)k * lda;
         double sr = 0.0, si = 0.0;
 #pragma unroll
         for (int i = 0; i < R; i++) {
             if (i < i0) continue;
-            const int r = lane + 32 * i;
-            const cplx vv = (r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
+            const int r = lane + 32 * (WPC * i + wsub);
+            const cplx vv = (have && r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
             sr = fma(vv.x, z[i].x, fma(vv.y, z[i].y, sr));    // conj(v) z
             si = fma(vv.x, z[i].y, fma(-vv.y, z[i].x, si));
         }
@@ -1498,19 +1501,29 @@ __global__ void __launch_bounds__(64) apply_qh_kernel(int n, const cplx *__restr
             sr += __shfl_xor_sync(0xffffffffu, sr, o);
             si += __shfl_xor_sync(0xffffffffu, si, o);
         }
+        if (WPC == 2) {   // the two warps' partial dots, summed in a fixed order
+            if (lane == 0) {
+                part[k & 1][wsub][0] = sr;
+                part[k & 1][wsub][1] = si;
+            }
+            __syncthreads();
+            sr = part[k & 1][0][0] + part[k & 1][1][0];
+            si = part[k & 1][0][1] + part[k & 1][1][1];
+        }
         const double fr = t.x * sr + t.y * si, fi = t.x * si - t.y * sr;   // f = conj(tau) (v^H z)
 #pragma unroll
         for (int i = 0; i < R; i++) {
             if (i < i0) continue;
-            const int r = lane + 32 * i;
-            const cplx vv = (r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
+            const int r = lane + 32 * (WPC * i + wsub);
+            const cplx vv = (have && r > k && r < n) ? __ldg(vk + r) : mk(0.0, 0.0);
             z[i].x = fma(-vv.x, fr, fma(vv.y, fi, z[i].x));   // z -= v f
             z[i].y = fma(-vv.x, fi, fma(-vv.y, fr, z[i].y));
         }
     }
+    if (!have) return;
 #pragma unroll
     for (int i = 0; i < R; i++) {
-        const int r = lane + 32 * i;
+        const int r = lane + 32 * (WPC * i + wsub);
         if (r < n) Y[r + (int64_t)col * ldy] = z[i];
     }
 }
@@ -1587,10 +1600,17 @@ void tridiag_e2(Context &c, int slot, int n, const cplx *A, int64_t lda, const c
     HeevWork h = heev_work(c, n, slot);
     cplx *Y = wsget<cplx>(c, slot_name("te2.Y", slot), (size_t)n * nouter);
     FamScope fs(c, DCG_FAM_EIG, 8.0 * (double)n * n * nouter);
-    const unsigned g = grid1d(nouter, 2);
-    if (n <= 256) apply_qh_kernel<8><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
-    else if (n <= 512) apply_qh_kernel<16><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
-    else apply_qh_kernel<32><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+    // one warp per vector up to 256 rows; above, two warps per vector (twice the warps to hide
+    // the per-reflector reduction latency) and the register chunks sized to the rows
+    if (n <= 256) {
+        apply_qh_kernel<8, 1><<<grid1d(nouter, 2), 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+    } else {
+        const unsigned g = (unsigned)nouter;
+        if (n <= 512) apply_qh_kernel<8, 2><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+        else if (n <= 768) apply_qh_kernel<12, 2><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+        else if (n <= 896) apply_qh_kernel<14, 2><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+        else apply_qh_kernel<16, 2><<<g, 64, 0, c.stream>>>(n, A, lda, h.tau, VC, ldvc, nouter, Y, n);
+    }
     DCG_LAUNCHED(c);
     const size_t sz = (size_t)n * nouter;
     double *D = wsget<double>(c, slot_name("te2.D", slot), sz);
@@ -1622,11 +1642,18 @@ void heev_vectors_slot(Context &c, int slot, int n, cplx *A, int64_t lda, int vl
             if (many) launch_bt_reg<8, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
             else launch_bt_reg<8, 1, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
         } else if (n <= 512) {
-            if (many) launch_bt_reg<16, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            if (many) launch_bt_reg<8, 2, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
             else launch_bt_reg<16, 1, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
         } else {
-            if (many) launch_bt_reg<32, 1, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
-            else launch_bt_reg<16, 2, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            // many columns: two warps per column, register chunks sized to the rows (a 792-row
+            // column in 14 chunks instead of 32 one-warp chunks of which 7 are empty)
+            if (many) {
+                if (n <= 768) launch_bt_reg<12, 2, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+                else if (n <= 896) launch_bt_reg<14, 2, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+                else launch_bt_reg<16, 2, false>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            } else {
+                launch_bt_reg<16, 2, true>(c, n, A, lda, h.tau, Qt, vlo, nvec, Z, ldz);
+            }
         }
         return;
     }
