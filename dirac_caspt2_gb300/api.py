@@ -204,6 +204,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_server_device_bytes.argtypes = [ctypes.c_void_p]
     lib.dcg_server_device_bytes.restype = ctypes.c_int64
     lib.dcg_server_destroy.argtypes = [ctypes.c_void_p]
+    lib.dcg_casci_energy_check.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_autotune_mode.argtypes = [ctypes.c_int32]
     lib.dcg_set_autotune_trials.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_autotune_entries.argtypes = [ctypes.c_void_p, ctypes.c_int32]
@@ -232,7 +233,8 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_server_submit", "dcg_server_poll", "dcg_server_pending", "dcg_server_clock",
                     "dcg_server_device_bytes", "dcg_server_destroy", "dcg_read_mrconee", "dcg_free_mrconee",
                     "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error", "dcg_ivo",
-                    "dcg_autotune_mode", "dcg_autotune_entries", "dcg_set_autotune_trials"]
+                    "dcg_autotune_mode", "dcg_autotune_entries", "dcg_set_autotune_trials",
+                    "dcg_casci_energy_check"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
 
@@ -621,6 +623,13 @@ class Caspt2Session:
         self._mdcint = mb
         self._check(self.lib.dcg_set_system_mdcint(self.h, ctypes.byref(self._bufs.struct), ctypes.byref(st)))
 
+    def casci_energy_check(self) -> Dict[str, float]:
+        """dcg_casci_energy_check: the e0test terms of the selected root after casci()."""
+        out = np.zeros(8)
+        self._check(self.lib.dcg_casci_energy_check(self.h, out.ctypes.data))
+        keys = ("energyHF1", "energyHF2", "energy1", "energy2", "energy3", "energy4", "t_energy", "error")
+        return {k: float(v) for k, v in zip(keys, out)}
+
     def ivo(self, nfsym: int, mo_energy: np.ndarray, nhomo: int = 0):
         """dcg_ivo: (eps (nsec,), U (nsec, nsec) complex, block_isym (nsec,), numh) of the
         improved virtual orbitals of the resident system."""
@@ -904,8 +913,21 @@ def run_case(directory: str, device: int = 0, precision: int = DCG_PREC_FP64, ve
     with Caspt2Session(device, precision) as ses:
         for k in range(len(inp.ciroots)):
             s = SystemInput.from_files(directory, k)
-            r = ses.solve(s, nroot=s.selectroot)
+            ses.set_system(s)
+            eig, ndet = ses.casci(s.selectroot)
+            chk = ses.casci_energy_check()   # r4dcasci's e0test (r4dcasci.F90:89)
+            e2, sc2, e0, et = ses.caspt2()
+            r = Caspt2Result(casci_energies=eig, ndet=ndet, e2=e2, sumc2=sc2, e0=e0, total_energy=et,
+                             stage_ms=ses.stage_ms(), kernel_launches=ses.kernel_launches())
             if verbose:
+                print("\n".join(format_e0test_lines(chk, s.selectroot)))
                 print("\n".join(format_reference_lines(r, s)))
             results.append(r)
     return results
+
+
+def format_e0test_lines(chk: Dict[str, float], selectroot: int) -> List[str]:
+    """e0test's energy lines (e0test.F90:92-96, 262-268), real parts."""
+    return [f" energyHF(1) {chk['energyHF1']:30.17f}", f" energyHF(2) {chk['energyHF2']:30.17f}",
+            f"selectroot {selectroot}"] + [f" energy {q} = {chk[f'energy{q}']:30.17f}" for q in range(1, 5)] + \
+           [f" t-energy(1-4) {chk['t_energy']:30.17f}", f" C the error {chk['error']:30.17e}"]

@@ -529,6 +529,86 @@ static RdmBufs rdm_build(Context &c, const uint64_t *full, int64_t M, const cplx
     return r;
 }
 
+// ------------------------------------------------------------------------- e0test
+// e0test (e0test.F90:4-272), which r4dcasci runs after the CASCI (r4dcasci.F90:89): the
+// HF-like energy of the lowest ninact + nelec spinors and the selected root's energy from its
+// 1- and 2-RDM in four parts, against eigen - ecore.  The RDMs come from the device (the
+// density GEMMs in FP64 whatever the context's precision); the na^4 and nmoc^2 sums run on
+// the host.  out: energyHF(1), energyHF(2), energy 1..4, their sum, and eigen - ecore - sum.
+static void e0test(Context &c, double *out) {
+    if (!c.have_casci) throw Error{DCG_E_STATE, "dcg_casci_energy_check before dcg_casci"};
+    DevSystem &d = dev(c);
+    const int ni = c.ni, na = c.na, nmoc = ni + na, nmo = c.nmo;
+    const std::vector<uint64_t> full = gosper_all(na, c.ne);
+    const int64_t M = (int64_t)full.size();
+    std::vector<int64_t> pos(d.ndet);
+    for (int i = 0; i < d.ndet; i++) pos[i] = std::lower_bound(full.begin(), full.end(), c.dets[i]) - full.begin();
+    uint64_t *d_full = upload(c, "e0.full", full);
+    int64_t *d_pos = upload(c, "e0.pos", pos);
+    cplx *psi = wsget<cplx>(c, "e0.psi", (size_t)M);
+    launch_embed(c, d.ndet, d_pos, d.c0, psi, M);
+    const int prec = c.precision;
+    c.precision = DCG_PREC_FP64;
+    RdmBufs r;
+    try {
+        r = rdm_build(c, d_full, M, psi, nullptr, false);
+    } catch (...) {
+        c.precision = prec;
+        throw;
+    }
+    c.precision = prec;
+    const size_t na2 = (size_t)na * na;
+    const std::vector<cplx> g1 = download(c, r.g1, na2);                 // <E_pq> at p + na q
+    const std::vector<cplx> gall = download(c, r.gall, na2 * na2);       // <E_qp E_rs> at (p + na q) + na^2 (r + na s)
+    const std::vector<cplx> h = download(c, d.h, (size_t)nmo * nmo);
+    const std::vector<cplx> g = download(c, d.inttw, (size_t)nmoc * nmoc * nmoc * nmoc);
+    auto G = [&](int p, int q, int rr, int ss) {
+        return g[p + (size_t)nmoc * (q + (size_t)nmoc * (rr + (size_t)nmoc * ss))];
+    };
+    auto D1 = [&](int i, int j) { return g1[i + (size_t)na * j]; };
+    auto D2 = [&](int i, int j, int k, int l) { return gall[(j + (size_t)na * i) + na2 * (k + (size_t)na * l)]; };
+    auto cs = [](cplx a, cplx b) { return cadd(a, b); };
+    cplx hf1 = mk(0.0, 0.0), hf2 = mk(0.0, 0.0), e1 = mk(0.0, 0.0), e2 = mk(0.0, 0.0), e3 = mk(0.0, 0.0),
+         e4 = mk(0.0, 0.0);
+    const int nocc = ni + c.ne;
+    for (int i = 0; i < nocc; i++) hf1 = cs(hf1, h[i + (size_t)nmo * i]);
+    for (int i = 0; i < nocc; i++)
+        for (int j = i; j < nocc; j++) hf2 = cs(hf2, csub(G(i, i, j, j), G(i, j, j, i)));
+    hf2 = cscale(hf2, 0.5);
+    hf2 = cadd(hf2, cconj(hf2));
+    for (int i = 0; i < ni; i++) e1 = cs(e1, h[i + (size_t)nmo * i]);
+    for (int i = 0; i < ni; i++)
+        for (int j = i; j < ni; j++) e2 = cs(e2, csub(G(i, i, j, j), G(i, j, j, i)));
+    e2 = cscale(e2, 0.5);
+    e2 = cadd(e2, cconj(e2));
+    for (int i = ni; i < nmoc; i++)
+        for (int j = i; j < nmoc; j++) {
+            cplx one = h[i + (size_t)nmo * j];
+            for (int k = 0; k < ni; k++) one = cadd(one, csub(G(i, j, k, k), G(i, k, k, j)));
+            if (i == j) one = cscale(one, 0.5);
+            e3 = cadd(e3, cmul(one, D1(i - ni, j - ni)));
+        }
+    e3 = cadd(e3, cconj(e3));
+    for (int i = 0; i < na; i++)
+        for (int j = 0; j < na; j++)
+            for (int k = 0; k < na; k++)
+                for (int l = 0; l < na; l++) {
+                    const cplx x = G(ni + i, ni + j, ni + k, ni + l);
+                    e4 = cadd(e4, cmul(D2(i, j, k, l), x));
+                    if (j == k) e4 = csub(e4, cmul(D1(i, l), x));
+                }
+    e4 = cscale(e4, 0.5);
+    const double t = e1.x + e2.x + e3.x + e4.x;
+    out[0] = hf1.x;
+    out[1] = hf2.x;
+    out[2] = e1.x;
+    out[3] = e2.x;
+    out[4] = e3.x;
+    out[5] = e4.x;
+    out[6] = t;
+    out[7] = (c.ecas[c.selectroot - 1] - c.ecore) - t;
+}
+
 // ------------------------------------------------------------------------- subspace drivers
 struct SubCtx {
     Context *c;
@@ -1589,6 +1669,14 @@ int dcg_ivo(dcg_ctx *ctx, int32_t nfsym, const double *mo_energy, int32_t nhomo,
             double *u_im, int32_t *block_isym, int32_t *numh_out) {
     DCG_API_BODY(ctx, {
         dcg::ivo(c_, nfsym, mo_energy, nhomo, eps, u_re, u_im, block_isym, numh_out);
+        return DCG_OK;
+    });
+}
+
+int dcg_casci_energy_check(dcg_ctx *ctx, double out[8]) {
+    if (!out) return DCG_E_ARG;
+    DCG_API_BODY(ctx, {
+        dcg::e0test(c_, out);
         return DCG_OK;
     });
 }

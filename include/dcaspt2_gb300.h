@@ -308,6 +308,13 @@ int64_t dcg_server_device_bytes(dcg_server *srv);
 /* Drop queued requests, finish the running ones, join the workers and free the contexts. */
 int dcg_server_destroy(dcg_server *srv);
 
+/* The CASCI check of e0test (e0test.F90:4-272, called by r4dcasci.F90:89) for the selected
+ * root of the last dcg_casci: out[0..1] energyHF(1), energyHF(2) of the lowest
+ * ninact + nelec spinors; out[2..5] energy 1..4 (inactive one- and two-electron, active
+ * one-electron with the inactive mean field, active two-electron); out[6] their sum;
+ * out[7] eigen - ecore - out[6] (the printed "error"). */
+int dcg_casci_energy_check(dcg_ctx *ctx, double out[8]);
+
 /* ------------------------------------------------------------------------ autotuner
  * Shape-dependent launch choices (today: the tile shape, 64x64, 32x128 or 128x32, and the
  * K-split of the FP64 GEMMs; for the split-precision tensor-core GEMMs the kernel, one tile

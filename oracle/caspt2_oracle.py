@@ -1444,3 +1444,55 @@ def zheev_lapack(A: np.ndarray, lartg: str = "new"):
             d[k], d[i] = d[i], p
             Z[:, [i, k]] = Z[:, [k, i]]
     return d, Z
+
+
+# ======================================================================================
+# e0test: the CASCI energy of the selected root from its 1- and 2-RDM
+# ======================================================================================
+def e0test(s: System) -> Dict[str, complex]:
+    """e0test (e0test.F90:4-272), run by r4dcasci after the CASCI (r4dcasci.F90:89): the
+    HF-like energy of the lowest ninact + nelec spinors and the selected root's energy split
+    into inactive one-electron (1), inactive two-electron (2), active one-electron with the
+    inactive mean field (3) and active two-electron (4) parts, against eigen - ecore."""
+    ni, na = s.ninact, s.nact
+    ints = Integrals(s)
+    g = ints.occ_block()                       # (pq|rs), nmoc^4
+    dets = enumerate_dets(s)
+    H = casmat(s, dets, g)
+    w, v = heev_upper(H)
+    iroot = s.selectroot - 1
+    c = v[:, iroot]
+    rd = RDM(FullSpace(s, dets), c, order=2)
+    h = s.h
+    out: Dict[str, complex] = {}
+    nocc = ni + s.nelec
+    out["energyHF1"] = complex(np.sum(np.diag(h)[:nocc]))
+    e = 0.0 + 0.0j
+    for i in range(nocc):
+        for j in range(i, nocc):
+            e += g[i, i, j, j] - g[i, j, j, i]
+    e *= 0.5
+    out["energyHF2"] = e + np.conj(e)
+    out["energy1"] = complex(np.sum(np.diag(h)[:ni]))
+    e = 0.0 + 0.0j
+    for i in range(ni):
+        for j in range(i, ni):
+            e += g[i, i, j, j] - g[i, j, j, i]
+    e *= 0.5
+    out["energy2"] = e + np.conj(e)
+    e = 0.0 + 0.0j
+    for i in range(ni, ni + na):
+        for j in range(i, ni + na):
+            one = h[i, j] + sum(g[i, j, k, k] - g[i, k, k, j] for k in range(ni))
+            if i == j:
+                one *= 0.5
+            e += one * rd.D1[i - ni, j - ni]
+    out["energy3"] = e + np.conj(e)
+    ga = g[ni:ni + na, ni:ni + na, ni:ni + na, ni:ni + na]
+    e4 = np.einsum("ijkl,ijkl->", ga, rd.D2)
+    e4 -= np.einsum("ijjl,il->", ga, rd.D1)
+    out["energy4"] = 0.5 * e4
+    out["t_energy"] = out["energy1"] + out["energy2"] + out["energy3"] + out["energy4"]
+    out["eigen_minus_ecore"] = complex(w[iroot])
+    out["error"] = out["eigen_minus_ecore"] - out["t_energy"]
+    return out

@@ -4,8 +4,8 @@ For each case directory of the reference's ``test/dev`` tree that ships its MDCI
 this reads ``active.inp``, ``MRCONEE`` and ``MDCINT*`` with the package's readers
 (restatements of read_mrconee / create_newmdcint) and stores the resulting system in
 ``<case>.npz`` together with the energies printed in ``reference.<case>.out``:
-the CASCI total energy of the selected root, the per-subspace ``e2X`` and ``sumc2,X`` and
-the total CASPT2 energy.  For the cases with small MDCINT files it also stores the raw MDCINT
+the CASCI total energy of the selected root, the per-subspace ``e2X`` and ``sumc2,X``, the
+total CASPT2 energy and the e0test terms (energyHF(1..2), energy 1..4).  For the cases with small MDCINT files it also stores the raw MDCINT
 records (``<case>_mdcint_raw.npz``), the input of the MDCINT canonicalisation.
 
 For the IVO cases (``ivo_*.npz``): the system read with ``active.ivo.inp``, the MDCINTNEW
@@ -28,6 +28,19 @@ from dirac_caspt2_gb300 import dirac_io  # noqa: E402
 
 CASES = ["c2_h2o_dev", "check_minelecras3_dev", "ninact_0_h2_dev", "mdcint_scheme_6_dirac23_c32h_n2_dev"]
 RAW_CASES = ["check_minelecras3_dev", "ninact_0_h2_dev"]   # MDCINT small enough to keep (28 / 48 KB)
+
+
+def parse_e0test(path: str):
+    """The e0test block (e0test.F90:85-270): energyHF(1), energyHF(2), energy 1..4 (real parts
+    of the printed complex numbers), NaN where absent."""
+    keys = [r"energyHF\(1\)", r"energyHF\(2\)", "energy 1 =", "energy 2 =", "energy 3 =", "energy 4 ="]
+    out = [np.nan] * len(keys)
+    for ln in open(path, errors="replace").read().splitlines():
+        for q, k in enumerate(keys):
+            m = re.match(r"^\s*" + k + r"\s*\(\s*([-+0-9.Ee]+)\s*,", ln)
+            if m and np.isnan(out[q]):
+                out[q] = float(m.group(1))
+    return np.array(out)
 
 
 def parse_output(path: str, selectroot: int):
@@ -69,7 +82,8 @@ def main(devdir: str):
                    min_hole_ras1=inp.min_hole_ras1, min_elec_ras3=inp.min_elec_ras3,
                    ref_casci=casci, ref_total=total,
                    ref_e2=np.array([e2.get(k, np.nan) for k in "ABCDEFGH"]),
-                   ref_sumc2=np.array([sc2.get(k, np.nan) for k in "ABCDEFGH"]))
+                   ref_sumc2=np.array([sc2.get(k, np.nan) for k in "ABCDEFGH"]),
+                   ref_e0test=parse_e0test(os.path.join(d, f"reference.{case}.out")))
         if not new.realonly:
             out["rec_im"] = new.val.imag
         np.savez_compressed(os.path.join(HERE, f"{case}.npz"), **out)

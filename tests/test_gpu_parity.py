@@ -132,3 +132,21 @@ def test_gpu_errors_are_status_codes(session):
         session.casci(1)
     ok = session.solve(s)
     assert np.isfinite(ok.total_energy)
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_gpu_e0test_matches_reference(gpu_lib, case):
+    """dcg_casci_energy_check reproduces the reference's e0test lines within 1e-10 Eh."""
+    import os
+    import numpy as np
+    from conftest import GOLDEN_DIR
+    from dirac_caspt2_gb300 import api
+    s = api.SystemInput.from_npz(os.path.join(GOLDEN_DIR, f"{case}.npz"))
+    z = np.load(os.path.join(GOLDEN_DIR, f"{case}.npz"))
+    with api.Caspt2Session(0) as ses:
+        ses.set_system(s)
+        ses.casci(max(1, s.selectroot))
+        r = ses.casci_energy_check()
+    got = np.array([r[k] for k in ("energyHF1", "energyHF2", "energy1", "energy2", "energy3", "energy4")])
+    assert np.abs(got - z["ref_e0test"]).max() <= 1e-10
+    assert abs(r["error"]) <= 1e-10

@@ -27,3 +27,19 @@ def test_oracle_matches_reference_golden(case):
         assert abs(r.e2[k] - ref) < TOL, (k, r.e2[k], ref)
         assert abs(r.sumc2[k] - z["ref_sumc2"][i]) < TOL, (k, r.sumc2[k], z["ref_sumc2"][i])
     assert abs(r.total_energy - float(z["ref_total"])) < TOL
+
+
+E0TEST_KEYS = ("energyHF1", "energyHF2", "energy1", "energy2", "energy3", "energy4")
+
+
+@pytest.mark.parametrize("case", [c for c in GOLDEN_CASES if "c32h_n2" not in c])
+def test_oracle_e0test_matches_reference(case):
+    """e0test's printed terms (energyHF(1..2), energy 1..4) and its error line."""
+    from dirac_caspt2_gb300 import api
+    from oracle import caspt2_oracle as O
+    s = api.SystemInput.from_npz(os.path.join(GOLDEN_DIR, f"{case}.npz"))
+    z = np.load(os.path.join(GOLDEN_DIR, f"{case}.npz"))
+    r = O.e0test(oracle_system(s))
+    got = np.array([r[k].real for k in E0TEST_KEYS])
+    assert np.abs(got - z["ref_e0test"]).max() <= 1e-10
+    assert abs(r["error"]) <= 1e-10
