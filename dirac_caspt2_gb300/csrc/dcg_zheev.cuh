@@ -419,12 +419,27 @@ __device__ __noinline__ int zheev_cta(const ZheevJob &J) {
         for (int r = i + 1 + tid; r < m; r += nt) q[(size_t)i * n + r] = mk(0.0, 0.0);
         __syncthreads();
     }
-    // ---- ZSTEQR: the recurrence in one thread, then its rotations on the rows of Q
+    // ---- ZSTEQR: the recurrence in one thread, then its rotations on the rows of Q.  The
+    // recurrence is a serial chain through d and e: up to kSteqrSmem entries they sit in
+    // shared memory for it (the same arithmetic, a shorter load latency).
+    constexpr int kSteqrSmem = 512;
+    __shared__ double sd[kSteqrSmem], se[kSteqrSmem];
+    const bool in_smem = n <= kSteqrSmem;
+    if (in_smem) {
+        for (int k = tid; k < n; k += nt) {
+            sd[k] = J.d[k];
+            se[k] = k + 1 < n ? J.e[k] : 0.0;
+        }
+        __syncthreads();
+    }
     if (tid == 0) {
         int nh = 0;
-        s_st = steqr_scalar(n, J.d, J.e, J, nh);
+        s_st = in_smem ? steqr_scalar(n, sd, se, J, nh) : steqr_scalar(n, J.d, J.e, J, nh);
         s_nh = nh;
     }
+    __syncthreads();
+    if (in_smem)
+        for (int k = tid; k < n; k += nt) J.d[k] = sd[k];
     __syncthreads();
     const int nh = s_nh;
     for (int r = tid; r < n; r += nt) {
