@@ -460,11 +460,23 @@ static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *
     zgemm(c, OP_N, OP_N, dimn, dimm, dimn, one, B, dimn, 0, X, dimn, 0, zero, BX, dimn, 0, 1);
     zgemm(c, OP_C, OP_N, dimm, dimm, dimn, one, X, dimn, 0, BX, dimn, 0, zero, Bp, dimm, 0, 1);
     herm_from_upper(c, dimm, Bp, dimm);
-    cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
-    zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, X, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
     double *e2o = wsget<double>(c, "blk.e2o", nouter);
     double *sco = wsget<double>(c, "blk.sco", nouter);
-    e2_from_bprime(c, dimm, Bp, VC0, nouter, alpha, e2o, sco);
+    cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
+    if (tridiag_e2_pays(dimm, nouter)) {
+        zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, X, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
+        e2_from_bprime(c, dimm, Bp, VC0, nouter, alpha, e2o, sco);
+    } else {
+        // B' = W w W^H, then the outer-index vectors in the combined basis (X W)^H Vsel: one
+        // product over the long outer index instead of X^H Vsel followed by W^H (X^H Vsel)
+        double *wb = wsget<double>(c, "blk.wb", dimm);
+        cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
+        heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
+        cplx *XW = wsget<cplx>(c, "blk.XW", (size_t)dimn * dimm);
+        zgemm(c, OP_N, OP_N, dimn, dimm, dimm, one, X, dimn, 0, W, dimm, 0, zero, XW, dimn, 0, 1);
+        zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, XW, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
+        launch_e2(c, VC0, dimm, nouter, alpha, wb, e2o, sco);
+    }
     double *red = wsget<double>(c, "blk.red", 2);
     dsum(c, e2o, nouter, red);
     dsum(c, sco, nouter, red + 1);
