@@ -30,7 +30,7 @@ CASCI_SOLVERS = {"auto": 0, "dense": 1, "davidson": 2}
 METRIC_SOLVERS = {"auto": 0, "eigen": 1}
 SUBSPACES = "ABCDEFGH"
 STAGES = ["ints", "casci_matrix", "casci_eig", "fock", "ci_rotation", "rdm", "transformation",
-          "A", "B", "C", "D", "E", "F", "G", "H", "AC"]
+          "A", "B", "C", "D", "E", "F", "G", "H", "AC", "BDEFG"]
 
 
 class DcgError(RuntimeError):

@@ -95,7 +95,7 @@ static std::vector<uint64_t> enumerate_ci(const Context &c) {
 // Stage names double as NVTX range names, so a profiler can select one stage's launches.
 static const char *const kStageName[ST_COUNT] = {"ints", "casci_matrix", "casci_eig", "fock", "ci_rotation",
                                                  "rdm", "transformation", "A", "B", "C", "D", "E", "F", "G", "H",
-                                                 "AC"};
+                                                 "AC", "BDEFG"};
 static void stage_begin(Context &c, int st) {
     nvtxRangePushA(kStageName[st]);
     DCG_CUDA(cudaEventRecord(c.ev[st], c.stream));
@@ -486,6 +486,107 @@ static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *
     return r;
 }
 
+// A block of B, D, E, F or G queued for the joint solve: its S, B and outer-index vectors
+// in buffers of its own (named per job), so the blocks of every subspace can be reduced
+// together once all are built.
+struct BlockJob {
+    int sub;          // subspace index, 0 A .. 7 H
+    int dimn, nouter;
+    cplx *S, *B, *Vsel;
+    double *alpha;
+};
+
+// solve_block for many blocks at once: their S matrices reduced in shared batched launches
+// (at most kEigSlots at a time), the cutoff and B' per block, then their B' matrices reduced
+// together the same way; the per-block E2 as solve_block forms it.  The tridiagonal loops of
+// independent blocks overlap instead of adding.
+static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_sub[8], double sc2_sub[8]) {
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    auto nm = [](const char *b, size_t j) { return std::string(b) + "#" + std::to_string(j); };
+    for (size_t p0 = 0; p0 < all.size(); p0 += kEigSlots) {
+        const size_t np = std::min<size_t>(kEigSlots, all.size() - p0);
+        std::vector<double *> ws(np), wb(np, nullptr), red(np);
+        std::vector<cplx *> X(np, nullptr), Bp(np, nullptr);
+        std::vector<int> dimm(np, 0);
+        // S: eigenvalues together, then each block's cutoff, kept vectors and B'
+        std::vector<EigJob> es;
+        for (size_t j = 0; j < np; j++) {
+            BlockJob &b = all[p0 + j];
+            ws[j] = wsget<double>(c, nm("bj.ws", j), b.dimn);
+            EigJob e;
+            e.n = b.dimn;
+            e.A = b.S;
+            e.lda = b.dimn;
+            e.w = ws[j];
+            e.slot = (int)j;
+            es.push_back(e);
+        }
+        heev_values_batched(c, es);
+        std::vector<EigJob> eb;
+        for (size_t j = 0; j < np; j++) {
+            BlockJob &b = all[p0 + j];
+            const std::vector<double> wsh = download(c, ws[j], b.dimn);
+            int vlo = b.dimn;
+            for (int q = 0; q < b.dimn; q++)
+                if (wsh[q] >= 1.0e-8) {   // cutoff.F90:37-70 (ascending eigenvalues)
+                    vlo = q;
+                    break;
+                }
+            dimm[j] = b.dimn - vlo;
+            if (dimm[j] == 0 || b.nouter == 0) continue;
+            X[j] = wsget<cplx>(c, nm("bj.X", j), (size_t)b.dimn * dimm[j]);
+            heev_vectors_slot(c, (int)j, b.dimn, b.S, b.dimn, vlo, b.dimn, X[j], b.dimn);
+            launch_scale_cols(c, X[j], b.dimn, b.dimn, dimm[j], ws[j], vlo);   // X = U lambda^-1/2
+            cplx *BX = wsget<cplx>(c, "bj.BX", (size_t)b.dimn * dimm[j]);
+            Bp[j] = wsget<cplx>(c, nm("bj.Bp", j), (size_t)dimm[j] * dimm[j]);
+            zgemm(c, OP_N, OP_N, b.dimn, dimm[j], b.dimn, one, b.B, b.dimn, 0, X[j], b.dimn, 0, zero, BX, b.dimn, 0, 1);
+            zgemm(c, OP_C, OP_N, dimm[j], dimm[j], b.dimn, one, X[j], b.dimn, 0, BX, b.dimn, 0, zero, Bp[j], dimm[j], 0,
+                  1);
+            herm_from_upper(c, dimm[j], Bp[j], dimm[j]);
+            wb[j] = wsget<double>(c, nm("bj.wb", j), dimm[j]);
+            EigJob e;
+            e.n = dimm[j];
+            e.A = Bp[j];
+            e.lda = dimm[j];
+            e.w = wb[j];
+            e.slot = (int)j;
+            e.tridiag_only = tridiag_e2_pays(dimm[j], b.nouter);
+            eb.push_back(e);
+        }
+        // B': reductions together, then E2 per block (tridiagonal form, or eigenvectors and
+        // one product over the outer index in the combined basis X W)
+        heev_values_batched(c, eb);
+        for (size_t j = 0; j < np; j++) {
+            BlockJob &b = all[p0 + j];
+            if (!Bp[j]) continue;
+            const int m = dimm[j];
+            double *e2o = wsget<double>(c, nm("bj.e2o", j), b.nouter);
+            double *sco = wsget<double>(c, nm("bj.sco", j), b.nouter);
+            cplx *VC = wsget<cplx>(c, "bj.VC", (size_t)m * b.nouter);
+            if (tridiag_e2_pays(m, b.nouter)) {
+                zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, X[j], b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
+                tridiag_e2(c, (int)j, m, Bp[j], m, VC, m, b.nouter, b.alpha, e2o, sco);
+            } else {
+                cplx *W = wsget<cplx>(c, "bj.W", (size_t)m * m);
+                heev_vectors_slot(c, (int)j, m, Bp[j], m, 0, m, W, m);
+                cplx *XW = wsget<cplx>(c, "bj.XW", (size_t)b.dimn * m);
+                zgemm(c, OP_N, OP_N, b.dimn, m, m, one, X[j], b.dimn, 0, W, m, 0, zero, XW, b.dimn, 0, 1);
+                zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, XW, b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
+                launch_e2(c, VC, m, b.nouter, b.alpha, wb[j], e2o, sco);
+            }
+            red[j] = wsget<double>(c, nm("bj.red", j), 2);
+            dsum(c, e2o, b.nouter, red[j]);
+            dsum(c, sco, b.nouter, red[j] + 1);
+        }
+        for (size_t j = 0; j < np; j++) {
+            if (!Bp[j]) continue;
+            const std::vector<double> hr = download(c, red[j], 2);
+            e2_sub[all[p0 + j].sub] += hr[0];
+            sc2_sub[all[p0 + j].sub] += hr[1];
+        }
+    }
+}
+
 }  // namespace dcg
 
 namespace dcg {
@@ -632,6 +733,7 @@ struct SubCtx {
     int64_t M = 0;
     struct GramJob *defer = nullptr;   // when set, Gram-route blocks are queued here (see GramJob)
     std::vector<struct GramJob> *jobs = nullptr;
+    std::vector<BlockJob> *bjobs = nullptr;   // when set, S/B-route blocks are queued here
 };
 
 struct BlockSpec {
@@ -993,6 +1095,25 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
             sc2 += o.sc2;
             continue;
         }
+        if (sc.bjobs) {   // queue for the joint solve of the S/B-route blocks
+            if (nouter == 0) continue;
+            const std::string jn = std::string(1, sub) + std::to_string(bi);
+            int *ind = upload(c, "bq.ind" + jn, b.ind);
+            BlockJob j;
+            j.sub = sub - 'A';
+            j.dimn = b.dimn;
+            j.nouter = nouter;
+            j.S = wsget<cplx>(c, "bq.S" + jn, (size_t)b.dimn * b.dimn);
+            j.B = wsget<cplx>(c, "bq.B" + jn, (size_t)b.dimn * b.dimn);
+            launch_SB(c, sub, sc.rv, ind, b.dimn, sc.eps_act_d, sc.e0, j.S, j.B);
+            int64_t *oo = upload(c, "bq.oo" + jn, b.outer_off);
+            int64_t *io = upload(c, "bq.io" + jn, b.inner_off);
+            j.alpha = upload(c, "bq.alpha" + jn, b.alpha);
+            j.Vsel = wsget<cplx>(c, "bq.Vsel" + jn, (size_t)b.dimn * nouter);
+            launch_gather_v(c, V, oo, nouter, io, b.dimn, j.Vsel);
+            sc.bjobs->push_back(j);
+            continue;
+        }
         int *ind = upload(c, "blk.ind", b.ind);
         cplx *S = wsget<cplx>(c, "blk.S", (size_t)b.dimn * b.dimn);
         cplx *B = wsget<cplx>(c, "blk.B", (size_t)b.dimn * b.dimn);
@@ -1292,6 +1413,10 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         run_blocks(sc, 'A', V, blocks, e2_sub[0], sc2_sub[0]);
     });
 
+    // the S/B-route blocks of B .. G are queued and solved together after G
+    std::vector<BlockJob> bjobs;
+    sc.bjobs = &bjobs;
+
     // ================= B: E_ti E_uj|0>, t>u, i>j  (solve_B_subspace.F90:27-591)
     if (ni > 0 && !(skip & 2u)) timed(ST_B, [&] {
         stage_begin(c, ST_TRANS);
@@ -1491,6 +1616,9 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         }
         run_blocks(sc, 'G', V, blocks, e2_sub[6], sc2_sub[6]);
     });
+
+    if (!bjobs.empty()) timed(ST_BDEFG, [&] { solve_block_jobs(c, bjobs, e2_sub, sc2_sub); });
+    sc.bjobs = nullptr;
 
     // ================= H: streaming (solve_H_subspace.F90:23-191)
     if (ni > 0 && ns > 0 && !(skip & 128u)) timed(ST_H, [&] {

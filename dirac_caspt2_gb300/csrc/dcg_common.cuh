@@ -77,7 +77,7 @@ class Workspace {
 // Stage indices of dcg_stage_times
 enum Stage {
     ST_INTS = 0, ST_CASMAT, ST_CASEIG, ST_FOCK, ST_CIROT, ST_RDM, ST_TRANS,
-    ST_A, ST_B, ST_C, ST_D, ST_E, ST_F, ST_G, ST_H, ST_AC, ST_COUNT
+    ST_A, ST_B, ST_C, ST_D, ST_E, ST_F, ST_G, ST_H, ST_AC, ST_BDEFG, ST_COUNT
 };
 
 struct Context {

@@ -164,8 +164,9 @@ int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n);
 /* Per-stage device times of the last dcg_casci/dcg_caspt2 (ms), in the order:
  * 0 integral expansion, 1 CASCI matrix, 2 CASCI eigensolve, 3 Fock build+diag,
  * 4 CI rotation, 5 RDMs, 6 transformation, 7..14 subspaces A..H (their builds and own
- * solves), 15 the joint eigensolves of the A and C blocks that go through the Gram factor.
- * Returns the count. */
+ * solves), 15 the joint eigensolves of the A and C blocks that go through the Gram factor,
+ * 16 the joint S and B' eigensolves and E2 of the B, D, E, F and G blocks.  Returns the
+ * count. */
 int dcg_stage_times(const dcg_ctx *ctx, double *ms_out, int32_t n);
 
 /* Device kernel launches issued by the last dcg_set_system+dcg_casci+dcg_caspt2. */
