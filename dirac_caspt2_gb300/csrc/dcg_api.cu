@@ -1690,6 +1690,12 @@ int dcg_create(int device, int precision, dcg_ctx **out) {
         DCG_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
         for (int k = 0; k <= dcg::ST_COUNT; k++) DCG_CUDA(cudaEventCreate(&c.ev[k]));
         c.ev_init = true;
+        DCG_CUDA(cudaEventCreateWithFlags(&c.aux_fork, cudaEventDisableTiming));
+        for (int k = 0; k < Context::kAux; k++) {
+            DCG_CUDA(cudaStreamCreateWithFlags(&c.aux[k], cudaStreamNonBlocking));
+            DCG_CUDA(cudaEventCreateWithFlags(&c.aux_join[k], cudaEventDisableTiming));
+        }
+        if (const char *es = getenv("DCG_EIG_STREAMS")) c.eig_streams = std::max(1, std::min(Context::kAux, atoi(es)));
         DCG_CUDA(cudaDeviceGetAttribute(&c.num_sms, cudaDevAttrMultiProcessorCount, device));
         if (const char *ds = getenv("DCG_SPLIT_DESC_STRIDES")) {   // diagnostic: "lbo,sbo"
             int l = 0, s = 0;
@@ -1720,6 +1726,14 @@ int dcg_destroy(dcg_ctx *ctx) {
     c.dev_state = nullptr;
     if (c.ev_init)
         for (int k = 0; k <= dcg::ST_COUNT; k++) cudaEventDestroy(c.ev[k]);
+    for (int k = 0; k < Context::kAux; k++) {
+        if (c.aux[k]) {
+            cudaStreamSynchronize(c.aux[k]);
+            cudaStreamDestroy(c.aux[k]);
+        }
+        if (c.aux_join[k]) cudaEventDestroy(c.aux_join[k]);
+    }
+    if (c.aux_fork) cudaEventDestroy(c.aux_fork);
     if (c.stream) cudaStreamDestroy(c.stream);
     delete ctx;
     return DCG_OK;

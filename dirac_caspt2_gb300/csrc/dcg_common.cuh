@@ -84,6 +84,12 @@ struct Context {
     int device = 0;
     int precision = DCG_PREC_FP64;
     cudaStream_t stream = nullptr;
+    // auxiliary streams for independent eigensolver jobs, forked from and joined back to
+    // `stream` (DCG_EIG_STREAMS: how many are used, 1 = none)
+    static constexpr int kAux = 4;
+    cudaStream_t aux[kAux] = {};
+    cudaEvent_t aux_fork = nullptr, aux_join[kAux] = {};
+    int eig_streams = kAux;
     Workspace ws;
     std::string err;
     int64_t launches = 0;

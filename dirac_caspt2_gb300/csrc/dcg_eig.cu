@@ -1398,6 +1398,38 @@ static void tridiag_single(Context &c, int n, cplx *A, int64_t lda, HeevWork &h)
     DCG_LAUNCHED(c);
 }
 
+// Runs f(k) for k in [0, njob), job k's launches on auxiliary stream k mod (streams used):
+// the streams first wait for the context stream, and the context stream waits for all of them
+// after, so the jobs overlap each other and nothing else.  The jobs must share no buffers.
+template <class F>
+static void on_aux_streams(Context &c, int njob, F &&f) {
+    const int used = std::min({c.eig_streams, (int)Context::kAux, njob});
+    if (used <= 1) {
+        for (int k = 0; k < njob; k++) f(k);
+        return;
+    }
+    cudaStream_t main = c.stream;
+    DCG_CUDA(cudaEventRecord(c.aux_fork, main));
+    for (int s = 0; s < used; s++) DCG_CUDA(cudaStreamWaitEvent(c.aux[s], c.aux_fork, 0));
+    auto join = [&]() {
+        c.stream = main;
+        for (int s = 0; s < used; s++) {
+            cudaEventRecord(c.aux_join[s], c.aux[s]);
+            cudaStreamWaitEvent(main, c.aux_join[s], 0);
+        }
+    };
+    try {
+        for (int k = 0; k < njob; k++) {
+            c.stream = c.aux[k % used];
+            f(k);
+        }
+    } catch (...) {
+        join();
+        throw;
+    }
+    join();
+}
+
 static void check_dc_status(Context &c, int slot) {
     if (!c.eig_status[slot]) return;
     int st = 0;
@@ -1456,9 +1488,14 @@ void heev_values_batched(Context &c, const std::vector<EigJob> &jobs) {
     }
     {
         FamScope f2(c, DCG_FAM_EIG_VAL, work / 4.0);
+        std::vector<size_t> dq;   // largest first, so the long chains start first
         for (size_t q = 0; q < jobs.size(); q++)
-            if (jobs[q].n > 0 && !jobs[q].tridiag_only)
-                tridiag_dc(c, jobs[q].n, hw[q].d, hw[q].e, jobs[q].w, jobs[q].slot);
+            if (jobs[q].n > 0 && !jobs[q].tridiag_only) dq.push_back(q);
+        std::stable_sort(dq.begin(), dq.end(), [&](size_t x, size_t y) { return jobs[x].n > jobs[y].n; });
+        on_aux_streams(c, (int)dq.size(), [&](int k) {
+            const size_t q = dq[k];
+            tridiag_dc(c, jobs[q].n, hw[q].d, hw[q].e, jobs[q].w, jobs[q].slot);
+        });
     }
     for (const EigJob &j : jobs)
         if (j.n > 0 && !j.tridiag_only) check_dc_status(c, j.slot);
