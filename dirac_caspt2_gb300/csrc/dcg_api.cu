@@ -522,21 +522,41 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
             es.push_back(e);
         }
         heev_values_batched(c, es);
+        std::vector<std::vector<double>> wsh(np);
+        for (size_t j = 0; j < np; j++) {
+            wsh[j].resize(all[p0 + j].dimn);
+            DCG_CUDA(cudaMemcpyAsync(wsh[j].data(), ws[j], sizeof(double) * wsh[j].size(), cudaMemcpyDeviceToHost,
+                                     c.stream));
+        }
+        DCG_CUDA(cudaStreamSynchronize(c.stream));
+        std::vector<int> vlo(np, 0);
+        std::vector<VecJob> xv;
+        for (size_t j = 0; j < np; j++) {
+            BlockJob &b = all[p0 + j];
+            vlo[j] = b.dimn;
+            for (int q = 0; q < b.dimn; q++)
+                if (wsh[j][q] >= 1.0e-8) {   // cutoff.F90:37-70 (ascending eigenvalues)
+                    vlo[j] = q;
+                    break;
+                }
+            dimm[j] = b.dimn - vlo[j];
+            if (dimm[j] == 0 || b.nouter == 0) continue;
+            X[j] = wsget<cplx>(c, nm("bj.X", j), (size_t)b.dimn * dimm[j]);
+            VecJob v;
+            v.slot = (int)j;
+            v.n = v.lda = v.ldz = b.dimn;
+            v.A = b.S;
+            v.vlo = vlo[j];
+            v.vhi = b.dimn;
+            v.Z = X[j];
+            xv.push_back(v);
+        }
+        eig_slot_jobs(c, xv, {});   // the kept S eigenvectors of every block, overlapped
         std::vector<EigJob> eb;
         for (size_t j = 0; j < np; j++) {
             BlockJob &b = all[p0 + j];
-            const std::vector<double> wsh = download(c, ws[j], b.dimn);
-            int vlo = b.dimn;
-            for (int q = 0; q < b.dimn; q++)
-                if (wsh[q] >= 1.0e-8) {   // cutoff.F90:37-70 (ascending eigenvalues)
-                    vlo = q;
-                    break;
-                }
-            dimm[j] = b.dimn - vlo;
-            if (dimm[j] == 0 || b.nouter == 0) continue;
-            X[j] = wsget<cplx>(c, nm("bj.X", j), (size_t)b.dimn * dimm[j]);
-            heev_vectors_slot(c, (int)j, b.dimn, b.S, b.dimn, vlo, b.dimn, X[j], b.dimn);
-            launch_scale_cols(c, X[j], b.dimn, b.dimn, dimm[j], ws[j], vlo);   // X = U lambda^-1/2
+            if (!X[j]) continue;
+            launch_scale_cols(c, X[j], b.dimn, b.dimn, dimm[j], ws[j], vlo[j]);   // X = U lambda^-1/2
             cplx *BX = wsget<cplx>(c, "bj.BX", (size_t)b.dimn * dimm[j]);
             Bp[j] = wsget<cplx>(c, nm("bj.Bp", j), (size_t)dimm[j] * dimm[j]);
             zgemm(c, OP_N, OP_N, b.dimn, dimm[j], b.dimn, one, b.B, b.dimn, 0, X[j], b.dimn, 0, zero, BX, b.dimn, 0, 1);
@@ -556,27 +576,57 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
         // B': reductions together, then E2 per block (tridiagonal form, or eigenvectors and
         // one product over the outer index in the combined basis X W)
         heev_values_batched(c, eb);
+        std::vector<VecJob> wv;
+        std::vector<TE2Job> tv;
+        std::vector<cplx *> W(np, nullptr);
+        std::vector<double *> e2o(np, nullptr), sco(np, nullptr);
         for (size_t j = 0; j < np; j++) {
             BlockJob &b = all[p0 + j];
             if (!Bp[j]) continue;
             const int m = dimm[j];
-            double *e2o = wsget<double>(c, nm("bj.e2o", j), b.nouter);
-            double *sco = wsget<double>(c, nm("bj.sco", j), b.nouter);
-            cplx *VC = wsget<cplx>(c, "bj.VC", (size_t)m * b.nouter);
+            e2o[j] = wsget<double>(c, nm("bj.e2o", j), b.nouter);
+            sco[j] = wsget<double>(c, nm("bj.sco", j), b.nouter);
             if (tridiag_e2_pays(m, b.nouter)) {
+                cplx *VC = wsget<cplx>(c, nm("bj.VC", j), (size_t)m * b.nouter);
                 zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, X[j], b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
-                tridiag_e2(c, (int)j, m, Bp[j], m, VC, m, b.nouter, b.alpha, e2o, sco);
+                TE2Job t;
+                t.slot = (int)j;
+                t.n = m;
+                t.A = Bp[j];
+                t.lda = t.ldvc = m;
+                t.VC = VC;
+                t.nouter = b.nouter;
+                t.alpha = b.alpha;
+                t.e2o = e2o[j];
+                t.sco = sco[j];
+                tv.push_back(t);
             } else {
-                cplx *W = wsget<cplx>(c, "bj.W", (size_t)m * m);
-                heev_vectors_slot(c, (int)j, m, Bp[j], m, 0, m, W, m);
+                W[j] = wsget<cplx>(c, nm("bj.W", j), (size_t)m * m);
+                VecJob v;
+                v.slot = (int)j;
+                v.n = v.lda = v.ldz = m;
+                v.A = Bp[j];
+                v.vlo = 0;
+                v.vhi = m;
+                v.Z = W[j];
+                wv.push_back(v);
+            }
+        }
+        eig_slot_jobs(c, wv, tv);   // B' of every block, overlapped
+        for (size_t j = 0; j < np; j++) {
+            BlockJob &b = all[p0 + j];
+            if (!Bp[j]) continue;
+            const int m = dimm[j];
+            if (W[j]) {
+                cplx *VC = wsget<cplx>(c, "bj.VCw", (size_t)m * b.nouter);
                 cplx *XW = wsget<cplx>(c, "bj.XW", (size_t)b.dimn * m);
-                zgemm(c, OP_N, OP_N, b.dimn, m, m, one, X[j], b.dimn, 0, W, m, 0, zero, XW, b.dimn, 0, 1);
+                zgemm(c, OP_N, OP_N, b.dimn, m, m, one, X[j], b.dimn, 0, W[j], m, 0, zero, XW, b.dimn, 0, 1);
                 zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, XW, b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
-                launch_e2(c, VC, m, b.nouter, b.alpha, wb[j], e2o, sco);
+                launch_e2(c, VC, m, b.nouter, b.alpha, wb[j], e2o[j], sco[j]);
             }
             red[j] = wsget<double>(c, nm("bj.red", j), 2);
-            dsum(c, e2o, b.nouter, red[j]);
-            dsum(c, sco, b.nouter, red[j] + 1);
+            dsum(c, e2o[j], b.nouter, red[j]);
+            dsum(c, sco[j], b.nouter, red[j] + 1);
         }
         for (size_t j = 0; j < np; j++) {
             if (!Bp[j]) continue;
@@ -952,6 +1002,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         }
         DCG_CUDA(cudaStreamSynchronize(c.stream));
         std::vector<EigJob> eb;
+        std::vector<VecJob> pv;
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
             vlo[j] = g.Mp;
@@ -975,9 +1026,21 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
                 dsum(c, sco, g.nouter, red[j] + 1);
                 continue;
             }
+            P[j] = wsget<cplx>(c, nm("gj.P", j), (size_t)g.Mp * dimm[j]);
+            VecJob v;
+            v.slot = (int)j;
+            v.n = v.lda = v.ldz = g.Mp;
+            v.A = K[j];
+            v.vlo = vlo[j];
+            v.vhi = g.Mp;
+            v.Z = P[j];
+            pv.push_back(v);
+        }
+        eig_slot_jobs(c, pv, {});   // the kept metric eigenvectors of every block, overlapped
+        for (size_t j = 0; j < np; j++) {
+            if (!P[j]) continue;
+            GramJob &g = all[p0 + j];
             const int dm = dimm[j], Mp = g.Mp;
-            P[j] = wsget<cplx>(c, nm("gj.P", j), (size_t)Mp * dm);
-            heev_vectors_slot(c, (int)j, Mp, K[j], Mp, vlo[j], Mp, P[j], Mp);
             cplx *GV = wsget<cplx>(c, nm("gj.GV", j), (size_t)Mp * g.nouter);
             zgemm(c, OP_N, OP_N, Mp, g.nouter, g.dimn, one, g.G, Mp, 0, g.Vsel, g.dimn, 0, zero, GV, Mp, 0, 1);
             VC0[j] = wsget<cplx>(c, nm("gj.VC0", j), (size_t)dm * g.nouter);
@@ -1000,25 +1063,54 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             eb.push_back(e);
         }
         heev_values_batched(c, eb);
+        // B' of every block: E2 from the tridiagonal form, or its eigenvectors, overlapped
+        std::vector<VecJob> wv;
+        std::vector<TE2Job> tv;
+        std::vector<cplx *> W(np, nullptr);
+        std::vector<double *> e2o(np, nullptr), sco(np, nullptr);
         for (size_t j = 0; j < np; j++) {
             GramJob &g = all[p0 + j];
-            if (chol[j]) continue;
-            if (dimm[j] == 0 || g.nouter == 0) continue;
+            if (chol[j] || !Bp[j]) continue;
             const int dm = dimm[j];
-            double *e2o = wsget<double>(c, nm("gj.e2o", j), g.nouter);
-            double *sco = wsget<double>(c, nm("gj.sco", j), g.nouter);
+            e2o[j] = wsget<double>(c, nm("gj.e2o", j), g.nouter);
+            sco[j] = wsget<double>(c, nm("gj.sco", j), g.nouter);
             if (tridiag_e2_pays(dm, g.nouter)) {
-                tridiag_e2(c, (int)(16 + j), dm, Bp[j], dm, VC0[j], dm, g.nouter, g.alpha, e2o, sco);
+                TE2Job t;
+                t.slot = (int)(16 + j);
+                t.n = dm;
+                t.A = Bp[j];
+                t.lda = t.ldvc = dm;
+                t.VC = VC0[j];
+                t.nouter = g.nouter;
+                t.alpha = g.alpha;
+                t.e2o = e2o[j];
+                t.sco = sco[j];
+                tv.push_back(t);
             } else {
-                cplx *W = wsget<cplx>(c, nm("gj.W", j), (size_t)dm * dm);
-                heev_vectors_slot(c, (int)(16 + j), dm, Bp[j], dm, 0, dm, W, dm);
+                W[j] = wsget<cplx>(c, nm("gj.W", j), (size_t)dm * dm);
+                VecJob v;
+                v.slot = (int)(16 + j);
+                v.n = v.lda = v.ldz = dm;
+                v.A = Bp[j];
+                v.vlo = 0;
+                v.vhi = dm;
+                v.Z = W[j];
+                wv.push_back(v);
+            }
+        }
+        eig_slot_jobs(c, wv, tv);
+        for (size_t j = 0; j < np; j++) {
+            GramJob &g = all[p0 + j];
+            if (chol[j] || !Bp[j]) continue;
+            const int dm = dimm[j];
+            if (W[j]) {
                 cplx *VC1 = wsget<cplx>(c, nm("gj.VC1", j), (size_t)dm * g.nouter);
-                zgemm(c, OP_C, OP_N, dm, g.nouter, dm, one, W, dm, 0, VC0[j], dm, 0, zero, VC1, dm, 0, 1);
-                launch_e2(c, VC1, dm, g.nouter, g.alpha, wb[j], e2o, sco);
+                zgemm(c, OP_C, OP_N, dm, g.nouter, dm, one, W[j], dm, 0, VC0[j], dm, 0, zero, VC1, dm, 0, 1);
+                launch_e2(c, VC1, dm, g.nouter, g.alpha, wb[j], e2o[j], sco[j]);
             }
             red[j] = wsget<double>(c, nm("gj.red", j), 2);
-            dsum(c, e2o, g.nouter, red[j]);
-            dsum(c, sco, g.nouter, red[j] + 1);
+            dsum(c, e2o[j], g.nouter, red[j]);
+            dsum(c, sco[j], g.nouter, red[j] + 1);
         }
         std::vector<double> hr(2 * np, 0.0);
         for (size_t j = 0; j < np; j++)
@@ -1256,10 +1348,20 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
             jobs.push_back(e);
         }
         heev_values_batched(c, jobs);
+        std::vector<VecJob> vj;
+        for (size_t q = 0; q < nbat; q++) {
+            FockBlk &b = fb[b0 + q];
+            VecJob v;
+            v.slot = (int)q;
+            v.n = v.lda = v.ldz = v.vhi = (int)b.ind.size();
+            v.A = b.blk;
+            v.Z = b.vec;
+            vj.push_back(v);
+        }
+        eig_slot_jobs(c, vj, {});
         for (size_t q = 0; q < nbat; q++) {
             FockBlk &b = fb[b0 + q];
             const int nb = (int)b.ind.size();
-            heev_vectors_slot(c, (int)q, nb, b.blk, nb, 0, nb, b.vec, nb);
             std::vector<double> wh = download(c, b.w, nb);
             if (b.sp == 1) {   // active space: canonical vectors inside degenerate pairs
                 std::vector<cplx> vh = download(c, b.vec, (size_t)nb * nb);

@@ -278,6 +278,38 @@ struct FamScope {
 };
 void fam_collect(Context &c);
 
+// Runs f(k) for k in [0, njob), job k's launches on auxiliary stream k mod (streams used):
+// the streams first wait for the context stream, and the context stream waits for all of them
+// after, so the jobs overlap each other and nothing else.  The jobs must share no buffers.
+template <class F>
+void on_aux_streams(Context &c, int njob, F &&f) {
+    const int used = std::min(std::min(c.eig_streams, (int)Context::kAux), njob);
+    if (used <= 1) {
+        for (int k = 0; k < njob; k++) f(k);
+        return;
+    }
+    cudaStream_t main = c.stream;
+    DCG_CUDA(cudaEventRecord(c.aux_fork, main));
+    for (int s = 0; s < used; s++) DCG_CUDA(cudaStreamWaitEvent(c.aux[s], c.aux_fork, 0));
+    auto join = [&]() {
+        c.stream = main;
+        for (int s = 0; s < used; s++) {
+            cudaEventRecord(c.aux_join[s], c.aux[s]);
+            cudaStreamWaitEvent(main, c.aux_join[s], 0);
+        }
+    };
+    try {
+        for (int k = 0; k < njob; k++) {
+            c.stream = c.aux[k % used];
+            f(k);
+        }
+    } catch (...) {
+        join();
+        throw;
+    }
+    join();
+}
+
 // ---------------------------------------------------------------- linear algebra (dcg_linalg.cu)
 enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };   // R = conjugate without transpose
 
@@ -332,6 +364,29 @@ constexpr int kTridiagE2MaxN = 1024;
 // (alpha + w_m)^2 over the eigenpairs (w_m, W) of B'.  n <= kTridiagE2MaxN.
 void tridiag_e2(Context &c, int slot, int n, const cplx *A, int64_t lda, const cplx *VC, int64_t ldvc, int nouter,
                 const double *alpha, double *e2o, double *sco);
+
+// heev_vectors_slot and tridiag_e2 calls of distinct slots, overlapped on the auxiliary
+// streams (vector jobs above 1024 rows share the blocked back-transformation's workspace and
+// run first, on the context stream).  The family timers see the overlapped group once.
+struct VecJob {
+    int slot = 0, n = 0;
+    cplx *A = nullptr;
+    int64_t lda = 0;
+    int vlo = 0, vhi = 0;
+    cplx *Z = nullptr;
+    int64_t ldz = 0;
+};
+struct TE2Job {
+    int slot = 0, n = 0;
+    const cplx *A = nullptr;
+    int64_t lda = 0;
+    const cplx *VC = nullptr;
+    int64_t ldvc = 0;
+    int nouter = 0;
+    const double *alpha = nullptr;
+    double *e2o = nullptr, *sco = nullptr;
+};
+void eig_slot_jobs(Context &c, const std::vector<VecJob> &vj, const std::vector<TE2Job> &tj);
 
 // Solve A x = b (n x n, LU with partial pivoting), b overwritten.  Returns info.
 int zgesv(Context &c, int n, cplx *A, int64_t lda, cplx *b);

@@ -1398,38 +1398,6 @@ static void tridiag_single(Context &c, int n, cplx *A, int64_t lda, HeevWork &h)
     DCG_LAUNCHED(c);
 }
 
-// Runs f(k) for k in [0, njob), job k's launches on auxiliary stream k mod (streams used):
-// the streams first wait for the context stream, and the context stream waits for all of them
-// after, so the jobs overlap each other and nothing else.  The jobs must share no buffers.
-template <class F>
-static void on_aux_streams(Context &c, int njob, F &&f) {
-    const int used = std::min({c.eig_streams, (int)Context::kAux, njob});
-    if (used <= 1) {
-        for (int k = 0; k < njob; k++) f(k);
-        return;
-    }
-    cudaStream_t main = c.stream;
-    DCG_CUDA(cudaEventRecord(c.aux_fork, main));
-    for (int s = 0; s < used; s++) DCG_CUDA(cudaStreamWaitEvent(c.aux[s], c.aux_fork, 0));
-    auto join = [&]() {
-        c.stream = main;
-        for (int s = 0; s < used; s++) {
-            cudaEventRecord(c.aux_join[s], c.aux[s]);
-            cudaStreamWaitEvent(main, c.aux_join[s], 0);
-        }
-    };
-    try {
-        for (int k = 0; k < njob; k++) {
-            c.stream = c.aux[k % used];
-            f(k);
-        }
-    } catch (...) {
-        join();
-        throw;
-    }
-    join();
-}
-
 static void check_dc_status(Context &c, int slot) {
     if (!c.eig_status[slot]) return;
     int st = 0;
@@ -1720,6 +1688,50 @@ void heev_vectors_slot(Context &c, int slot, int n, cplx *A, int64_t lda, int vl
         zgemm(c, OP_N, OP_N, nbp, nvec, nbp, one, T, WY_NB, 0, W1, nbp, 0, zero, W2, nbp, 0, 1);
         zgemm(c, OP_N, OP_N, m0, nvec, nbp, mone, Vp, m0, 0, W2, nbp, 0, one, Zs, ldz, 0, 1);
     }
+}
+
+void eig_slot_jobs(Context &c, const std::vector<VecJob> &vj, const std::vector<TE2Job> &tj) {
+    struct Item {
+        const VecJob *v;
+        const TE2Job *t;
+        double work;
+    };
+    std::vector<Item> items;
+    double wv = 0.0, wt = 0.0;
+    for (const VecJob &v : vj) {
+        if (v.n <= 0 || v.vhi <= v.vlo || v.Z == nullptr) continue;
+        if (v.n > 1024) {
+            heev_vectors_slot(c, v.slot, v.n, v.A, v.lda, v.vlo, v.vhi, v.Z, v.ldz);
+            continue;
+        }
+        const double w = 8.0 * (double)v.n * v.n * (v.vhi - v.vlo);
+        items.push_back({&v, nullptr, w});
+        wv += w;
+    }
+    for (const TE2Job &t : tj) {
+        if (t.n <= 0 || t.nouter <= 0) continue;
+        const double w = 8.0 * (double)t.n * t.n * t.nouter;
+        items.push_back({nullptr, &t, w});
+        wt += w;
+    }
+    if (items.empty()) return;
+    std::stable_sort(items.begin(), items.end(), [](const Item &x, const Item &y) { return x.work > y.work; });
+    FamScope fs(c, DCG_FAM_EIG, wv + wt);
+    FamScope fb(c, DCG_FAM_EIG_BACK, wv);
+    const int fam = c.fam;
+    c.fam = 0;   // the two scopes above time the overlapped group once, on the context stream
+    try {
+        on_aux_streams(c, (int)items.size(), [&](int k) {
+            const Item &it = items[k];
+            if (it.v) heev_vectors_slot(c, it.v->slot, it.v->n, it.v->A, it.v->lda, it.v->vlo, it.v->vhi, it.v->Z, it.v->ldz);
+            else tridiag_e2(c, it.t->slot, it.t->n, it.t->A, it.t->lda, it.t->VC, it.t->ldvc, it.t->nouter, it.t->alpha,
+                            it.t->e2o, it.t->sco);
+        });
+    } catch (...) {
+        c.fam = fam;
+        throw;
+    }
+    c.fam = fam;
 }
 
 void heev(Context &c, int n, cplx *A, int64_t lda, double *w, int vlo, int vhi, cplx *Z, int64_t ldz) {
