@@ -1811,7 +1811,7 @@ int dcg_create(int device, int precision, dcg_ctx **out) {
         DCG_CUDA(cudaStreamSynchronize(c.stream));
     } catch (const Error &e) {
         int code = e.code;
-        delete x;
+        dcg_destroy(x);   // releases the streams and events created so far
         return code;
     }
     *out = x;
