@@ -155,6 +155,9 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_caspt2.argtypes = [ctypes.c_void_p, ctypes.c_uint32, P(ctypes.c_double), P(ctypes.c_double),
                                P(ctypes.c_double), P(ctypes.c_double)]
     lib.dcg_get_eps.argtypes = [ctypes.c_void_p, P(ctypes.c_double), ctypes.c_int32]
+    lib.dcg_caspt2_irreps.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_void_p]
+    lib.dcg_casci_determinants.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_stage_times.argtypes = [ctypes.c_void_p, P(ctypes.c_double), ctypes.c_int32]
     lib.dcg_kernel_launches.argtypes = [ctypes.c_void_p]
     lib.dcg_kernel_launches.restype = ctypes.c_int64
@@ -165,6 +168,7 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_stream.argtypes = [ctypes.c_void_p]
     lib.dcg_stream.restype = ctypes.c_void_p
     lib.dcg_time_family.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.dcg_set_wait_limit.argtypes = [ctypes.c_void_p, ctypes.c_double]
     lib.dcg_family_stats.argtypes = [ctypes.c_void_p, P(ctypes.c_double), P(ctypes.c_int64), P(ctypes.c_double)]
     lib.dcg_zgemm.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int32, ctypes.c_int32, ctypes.c_int32,
                               ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64,
@@ -224,8 +228,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
 
 
 EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_system", "dcg_casci",
-                    "dcg_caspt2", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
-                    "dcg_stream", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
+                    "dcg_caspt2", "dcg_caspt2_irreps", "dcg_casci_determinants", "dcg_get_eps", "dcg_stage_times", "dcg_kernel_launches", "dcg_version",
+                    "dcg_stream", "dcg_set_wait_limit", "dcg_time_family", "dcg_family_stats", "dcg_solve_h",
                     "dcg_solve_h_noalloc", "dcg_heev", "dcg_heev_range", "dcg_heev_batch", "dcg_stedc", "dcg_zgemm",
                     "dcg_mdcint_canonicalize", "dcg_mdcint_records", "dcg_set_system_mdcint",
                     "dcg_set_casci_solver", "dcg_casci_iterations", "dcg_set_metric_solver",
@@ -399,6 +403,8 @@ class Caspt2Result:
     total_energy: float
     stage_ms: Dict[str, float]
     kernel_launches: int
+    # e2X(isym) of the symmetry blocks solve_X_subspace prints (subspaces A..G), by isym
+    e2_sym: Dict[str, Dict[int, float]] = dataclasses.field(default_factory=dict)
 
     @property
     def e2_total(self) -> float:
@@ -581,6 +587,23 @@ class Caspt2Session:
         return ({k: float(e2[i]) for i, k in enumerate(SUBSPACES)},
                 {k: float(sc[i]) for i, k in enumerate(SUBSPACES)}, e0.value, et.value)
 
+    def caspt2_irreps(self) -> Tuple[Dict[str, Dict[int, float]], np.ndarray, np.ndarray, np.ndarray]:
+        """Per-irrep results of the last caspt2 (dcg_caspt2_irreps): the printed e2X(isym)
+        values as {subspace: {isym: e2}}, and the raw (8, nsym) arrays e2, sumc2, printed."""
+        ns = int(self.system.nsymrpa)
+        e2 = np.zeros((8, ns))
+        sc = np.zeros((8, ns))
+        pr = np.zeros((8, ns), np.int32)
+        self._check(self.lib.dcg_caspt2_irreps(self.h, ns, e2.ctypes.data, sc.ctypes.data, pr.ctypes.data))
+        out = {k: {q + 1: float(e2[i, q]) for q in range(ns) if pr[i, q]} for i, k in enumerate(SUBSPACES)}
+        return {k: v for k, v in out.items() if v}, e2, sc, pr
+
+    def casci_determinants(self, ndet: int) -> np.ndarray:
+        """Bit strings of the CASCI determinants in the reference's dict order."""
+        out = np.zeros(max(1, ndet), np.int64)
+        self._check(self.lib.dcg_casci_determinants(self.h, out.ctypes.data, len(out)))
+        return out[:ndet]
+
     def eps(self) -> np.ndarray:
         n = self.system.nmo
         out = np.zeros(n)
@@ -750,6 +773,10 @@ class Caspt2Session:
     def stream_ptr(self) -> int:
         return int(self.lib.dcg_stream(self.h) or 0)
 
+    def set_wait_limit(self, seconds: float) -> None:
+        """dcg_set_wait_limit: time limit of the device-side waits that can give up (0: defaults)."""
+        self._check(self.lib.dcg_set_wait_limit(self.h, float(seconds)))
+
     def time_family(self, family: str) -> None:
         self._check(self.lib.dcg_time_family(self.h, FAMILIES[family]))
 
@@ -767,7 +794,8 @@ class Caspt2Session:
         eig, ndet = self.casci(max(nroot, s.selectroot))
         e2, sc2, e0, et = self.caspt2(skip_mask)
         return Caspt2Result(casci_energies=eig, ndet=ndet, e2=e2, sumc2=sc2, e0=e0, total_energy=et,
-                            stage_ms=self.stage_ms(), kernel_launches=self.kernel_launches())
+                            stage_ms=self.stage_ms(), kernel_launches=self.kernel_launches(),
+                            e2_sym=self.caspt2_irreps()[0])
 
 
 def footprint_estimate(bufs: "HostBuffers") -> int:
@@ -883,6 +911,13 @@ def format_reference_lines(r: Caspt2Result, s: SystemInput) -> List[str]:
     r4dcaspt2_tra.F90:437-442)."""
     out = [f"CASCI Total Energy ROOT{k + 1}{e:30.20f} a.u." for k, e in enumerate(r.casci_energies)]
     for k in SUBSPACES:
+        if k != "H" and k in r.e2:
+            # solve_X_subspace: the header and one line per printed symmetry block
+            # (solve_A_subspace.F90:89,262/908: the real variant of A has two spaces before '=')
+            out.append(f" e2{k.lower()}(isym)")
+            gap = "  " if k == "B" or (k == "A" and s.realonly) else " "
+            for q, v in sorted(r.e2_sym.get(k, {}).items()):
+                out.append(f" e2{k.lower()}({q:3d}){gap}= {_e25(v)} a.u.")
         if k in r.e2:
             out.append(f" e2{k.lower()}      = {_e25(r.e2[k])} a.u.")
             out.append(f" sumc2,{k.lower()}  = {_e25(r.sumc2[k])}")
@@ -918,7 +953,8 @@ def run_case(directory: str, device: int = 0, precision: int = DCG_PREC_FP64, ve
             chk = ses.casci_energy_check()   # r4dcasci's e0test (r4dcasci.F90:89)
             e2, sc2, e0, et = ses.caspt2()
             r = Caspt2Result(casci_energies=eig, ndet=ndet, e2=e2, sumc2=sc2, e0=e0, total_energy=et,
-                             stage_ms=ses.stage_ms(), kernel_launches=ses.kernel_launches())
+                             stage_ms=ses.stage_ms(), kernel_launches=ses.kernel_launches(),
+                             e2_sym=ses.caspt2_irreps()[0])
             if verbose:
                 print("\n".join(format_e0test_lines(chk, s.selectroot)))
                 print("\n".join(format_reference_lines(r, s)))

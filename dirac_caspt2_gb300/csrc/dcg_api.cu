@@ -396,6 +396,28 @@ static void transform4(Context &c, const cplx *in, cplx *out, cplx *tmp, const i
 }
 
 // ------------------------------------------------------------------------- subspace block solve
+// One symmetry block's share of the per-irrep results: solve_X_subspace prints e2X(isym) for a
+// block whose S keeps dimm > 0 vectors above the cutoff (solve_A_subspace.F90:158-164,262).
+static void sym_record(Context &c, int sub, int isym, double e2, double sc2, int dimm) {
+    if (dimm <= 0) return;
+    const size_t k = (size_t)sub * c.nsym + (size_t)(isym - 1);
+    c.sym_e2[k] += e2;
+    c.sym_sc2[k] += sc2;
+    c.sym_printed[k] = 1;
+}
+
+// Vectors S keeps above the 1e-8 cutoff (cutoff.F90:37-70); S (dimn x dimn, upper triangle
+// read) is destroyed.  Only for blocks without an outer index, where the count alone decides
+// whether the reference prints a zero e2X(isym).
+static int kept_count(Context &c, int dimn, cplx *S, int64_t lds) {
+    double *w = wsget<double>(c, "blk.wcount", dimn);
+    heev(c, dimn, S, lds, w, dimn, dimn, nullptr, dimn);   // values only
+    const std::vector<double> wh = download(c, w, dimn);
+    int kept = 0;
+    for (double x : wh) kept += x >= 1.0e-8 ? 1 : 0;
+    return kept;
+}
+
 struct BlockOut {
     double e2 = 0.0, sc2 = 0.0;
     int dimm = 0;
@@ -491,6 +513,7 @@ static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *
 // together once all are built.
 struct BlockJob {
     int sub;          // subspace index, 0 A .. 7 H
+    int isym;         // symmetry block
     int dimn, nouter;
     cplx *S, *B, *Vsel;
     double *alpha;
@@ -633,6 +656,7 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
             const std::vector<double> hr = download(c, red[j], 2);
             e2_sub[all[p0 + j].sub] += hr[0];
             sc2_sub[all[p0 + j].sub] += hr[1];
+            sym_record(c, all[p0 + j].sub, all[p0 + j].isym, hr[0], hr[1], dimm[j]);
         }
     }
 }
@@ -789,6 +813,7 @@ struct SubCtx {
 struct BlockSpec {
     std::vector<int> ind;             // flattened tuples
     int dimn = 0;
+    int isym = 1;                     // the symmetry block's isym (solve_X_subspace's loop index)
     std::vector<int64_t> outer_off;   // into V
     std::vector<int64_t> inner_off;   // into V
     std::vector<double> alpha;
@@ -955,6 +980,7 @@ struct GramJob {
     const double *Dd = nullptr;
     double *alpha = nullptr;
     int sub = 0;   // index into e2_sub / sc2_sub (0 = A, 2 = C)
+    int isym = 1;  // symmetry block
 };
 
 // Solve queued Gram blocks (same algebra as solve_gram_block), at most 16 per pass so that the
@@ -1119,6 +1145,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         for (size_t j = 0; j < np; j++) {
             e2_sub[all[p0 + j].sub] += hr[2 * j];
             sc2_sub[all[p0 + j].sub] += hr[2 * j + 1];
+            sym_record(c, all[p0 + j].sub, all[p0 + j].isym, hr[2 * j], hr[2 * j + 1], dimm[j]);
         }
     }
 }
@@ -1143,7 +1170,7 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
         if (b.dimn == 0) continue;
         const int nouter = (int)b.outer_off.size();
         if (gram_kind && b.dimn > Mp) {
-            if (Mp == 0 || nouter == 0) continue;   // S = 0 (or no outer index): no contribution
+            if (Mp == 0) continue;   // S = 0: no kept vector, nothing printed
             if (!d_dets_p) {
                 std::vector<double> Dp(Mp);
                 for (int r = 0; r < Mp; r++) {
@@ -1154,6 +1181,15 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
                 }
                 d_dets_p = upload(c, "gram.dets" + sfx, dets_p);
                 d_Dp = upload(c, "gram.D" + sfx, Dp);
+            }
+            if (nouter == 0) {   // no contribution; the kept count of K = G G^H decides the print
+                int *ind = upload(c, "blk.ind", b.ind);
+                cplx *G = wsget<cplx>(c, "gram.G", (size_t)Mp * b.dimn);
+                launch_gram(c, c.na, Mp, d_dets_p, sc.M, sc.Y, ind, b.dimn, sub == 'A' ? 1 : 0, G);
+                cplx *K = wsget<cplx>(c, "gram.Kcount", (size_t)Mp * Mp);
+                zherk_upper(c, Mp, b.dimn, G, Mp, K, Mp);
+                sym_record(c, sub - 'A', b.isym, 0.0, 0.0, kept_count(c, Mp, K, Mp));
+                continue;
             }
             if (sc.jobs) {   // queue for the joint A/C solve: buffers named per job
                 const std::string jn = sfx + std::to_string(bi);
@@ -1171,6 +1207,7 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
                 launch_gather_v(c, V, oo, nouter, io, b.dimn, g.Vsel);
                 g.Dd = d_Dp;
                 g.sub = sub == 'A' ? 0 : 2;
+                g.isym = b.isym;
                 sc.jobs->push_back(g);
                 continue;
             }
@@ -1185,14 +1222,23 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
             BlockOut o = solve_gram_block(c, Mp, b.dimn, G, d_Dp, Vsel, nouter, al);
             e2 += o.e2;
             sc2 += o.sc2;
+            sym_record(c, sub - 'A', b.isym, o.e2, o.sc2, o.dimm);
+            continue;
+        }
+        if (nouter == 0) {   // no contribution; the kept count of S decides the print
+            int *ind = upload(c, "blk.ind", b.ind);
+            cplx *S = wsget<cplx>(c, "blk.S", (size_t)b.dimn * b.dimn);
+            cplx *B = wsget<cplx>(c, "blk.B", (size_t)b.dimn * b.dimn);
+            launch_SB(c, sub, sc.rv, ind, b.dimn, sc.eps_act_d, sc.e0, S, B);
+            sym_record(c, sub - 'A', b.isym, 0.0, 0.0, kept_count(c, b.dimn, S, b.dimn));
             continue;
         }
         if (sc.bjobs) {   // queue for the joint solve of the S/B-route blocks
-            if (nouter == 0) continue;
             const std::string jn = std::string(1, sub) + std::to_string(bi);
             int *ind = upload(c, "bq.ind" + jn, b.ind);
             BlockJob j;
             j.sub = sub - 'A';
+            j.isym = b.isym;
             j.dimn = b.dimn;
             j.nouter = nouter;
             j.S = wsget<cplx>(c, "bq.S" + jn, (size_t)b.dimn * b.dimn);
@@ -1210,7 +1256,6 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
         cplx *S = wsget<cplx>(c, "blk.S", (size_t)b.dimn * b.dimn);
         cplx *B = wsget<cplx>(c, "blk.B", (size_t)b.dimn * b.dimn);
         launch_SB(c, sub, sc.rv, ind, b.dimn, sc.eps_act_d, sc.e0, S, B);
-        if (nouter == 0) continue;
         int64_t *oo = upload(c, "blk.oo", b.outer_off);
         int64_t *io = upload(c, "blk.io", b.inner_off);
         double *al = upload(c, "blk.alpha", b.alpha);
@@ -1219,6 +1264,7 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
         BlockOut o = solve_block(c, b.dimn, S, B, Vsel, nouter, al);
         e2 += o.e2;
         sc2 += o.sc2;
+        sym_record(c, sub - 'A', b.isym, o.e2, o.sc2, o.dimm);
     }
 }
 
@@ -1285,6 +1331,9 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
     const int ni = c.ni, na = c.na, ns = c.ns, nmoc = ni + na;
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0), mone = mk(-1.0, 0.0);
     for (int k = 0; k < 8; k++) { e2_sub[k] = 0.0; sc2_sub[k] = 0.0; }
+    c.sym_e2.assign((size_t)8 * c.nsym, 0.0);
+    c.sym_sc2.assign((size_t)8 * c.nsym, 0.0);
+    c.sym_printed.assign((size_t)8 * c.nsym, 0);
     if (ni == 0 && ns == 0) throw Error{DCG_E_ARG, "CASPT2 energy undefined for ninact = 0 and nsec = 0"};
     if (c.precision == DCG_PREC_SPLIT) split_reset(c);
 
@@ -1497,6 +1546,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int x = 0; x < na; x++)
                 for (int y = 0; y < na; y++)
                     for (int z = 0; z < na; z++)
@@ -1532,6 +1582,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int t = 0; t < na; t++)
                 for (int u = 0; u < t; u++)
                     if (c1sym || c.md(irp(ni + t), kp(irp(ni + u))) == isym) {
@@ -1571,6 +1622,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int x = 0; x < na; x++)
                 for (int y = 0; y < na; y++)
                     for (int z = 0; z < na; z++)
@@ -1604,6 +1656,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int t = 0; t < na; t++)
                 for (int u = 0; u < na; u++)
                     if (c1sym || c.md(irp(ni + t), irp(ni + u)) == isym) {
@@ -1634,6 +1687,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int t = 0; t < na; t++)
                 if (irp(ni + t) == isym) {
                     b.ind.push_back(t);
@@ -1671,6 +1725,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int t = 0; t < na; t++)
                 for (int u = 0; u < t; u++)
                     if (c1sym || c.md(kp(irp(ni + u)), irp(ni + t)) == isym) {
@@ -1701,6 +1756,7 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         std::vector<BlockSpec> blocks;
         for (int isym = 1; isym <= c.nsym; isym++) {
             BlockSpec b;
+            b.isym = isym;
             for (int t = 0; t < na; t++)
                 if (irp(ni + t) == isym) {
                     b.ind.push_back(t);
@@ -1727,13 +1783,15 @@ static int caspt2(Context &c, uint32_t skip, double e2_sub[8], double sc2_sub[8]
         stage_begin(c, ST_TRANS);
         cplx *Hc = tr_id("H", CL_H);
         stage_end(c, ST_TRANS);
-        const int nblk = std::max(1, c.num_sms) * 8;
+        const int nblk = h_stream_blocks(ni, ns);
         double *part = wsget<double>(c, "h.part", 2 * (size_t)nblk);
         double *red = wsget<double>(c, "h.red", 2);
         {
-            FamScope fs(c, DCG_FAM_HSTREAM, (double)d.cls[CL_H].size * sizeof(cplx));
+            // bytes the kernel must read: both operands of every a > b, i > j pair, the a > b
+            // half of the class
+            FamScope fs(c, DCG_FAM_HSTREAM, 0.5 * ns * (ns - 1.0) * ni * (ni - 1.0) * sizeof(cplx));
             launch_h_stream2(c, Hc, ni, ns, d.eps, d.eps + nmoc, d.irp, d.irp + nmoc, d.md, d.msy, c.nsym, es, part,
-                             part + nblk, nblk);
+                             part + nblk);
         }
         dsum(c, part, nblk, red);
         dsum(c, part + nblk, nblk, red + 1);
@@ -1860,6 +1918,27 @@ int dcg_caspt2(dcg_ctx *ctx, uint32_t skip_mask, double e2_sub[8], double sumc2_
                double *etotal_out) {
     if (!e2_sub || !sumc2_sub) return DCG_E_ARG;
     DCG_API_BODY(ctx, { return dcg::caspt2(c_, skip_mask, e2_sub, sumc2_sub, e0_out, etotal_out); });
+}
+
+int dcg_caspt2_irreps(const dcg_ctx *ctx, int32_t nsym, double *e2_sym, double *sumc2_sym, int32_t *printed) {
+    if (!ctx) return DCG_E_ARG;
+    const Context &c = ctx->c;
+    if (c.sym_printed.empty()) return DCG_E_STATE;
+    if (nsym != c.nsym) return DCG_E_ARG;
+    const size_t n = (size_t)8 * c.nsym;
+    if (e2_sym) std::copy(c.sym_e2.begin(), c.sym_e2.begin() + n, e2_sym);
+    if (sumc2_sym) std::copy(c.sym_sc2.begin(), c.sym_sc2.begin() + n, sumc2_sym);
+    if (printed) std::copy(c.sym_printed.begin(), c.sym_printed.begin() + n, printed);
+    return DCG_OK;
+}
+
+int dcg_casci_determinants(const dcg_ctx *ctx, int64_t *dets_out, int32_t n) {
+    if (!ctx || !dets_out) return DCG_E_ARG;
+    const Context &c = ctx->c;
+    if (!c.have_casci) return DCG_E_STATE;
+    if (n < (int32_t)c.dets.size()) return DCG_E_ARG;
+    for (size_t i = 0; i < c.dets.size(); i++) dets_out[i] = (int64_t)c.dets[i];
+    return DCG_OK;
 }
 
 int dcg_get_eps(const dcg_ctx *ctx, double *eps_out, int32_t n) {
@@ -2143,17 +2222,24 @@ int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, 
     DCG_API_BODY(ctx, {
         out[0] = out[1] = 0.0;
         if ((int64_t)ninact * nsec == 0) return DCG_OK;
-        const int nblk = std::max(1, c_.num_sms) * 8;
+        const int nblk = dcg::h_stream_blocks(ninact, nsec);
         double *part = dcg::wsget<double>(c_, "hsolve.part", 2 * (size_t)nblk);
         double *red = dcg::wsget<double>(c_, "hsolve.red", 2);
         dcg::launch_h_stream2(c_, static_cast<const dcg::cplx *>(hclass), ninact, nsec, eps_i, eps_s, irp_i, irp_s,
-                              multb_d, multb_s, nsymrpa, eshift, part, part + nblk, nblk);
+                              multb_d, multb_s, nsymrpa, eshift, part, part + nblk);
         dcg::dsum(c_, part, nblk, red);
         dcg::dsum(c_, part + nblk, nblk, red + 1);
         DCG_CUDA(cudaMemcpyAsync(out, red, 2 * sizeof(double), cudaMemcpyDeviceToHost, c_.stream));
         DCG_CUDA(cudaStreamSynchronize(c_.stream));
         return DCG_OK;
     });
+}
+
+int dcg_set_wait_limit(dcg_ctx *ctx, double seconds) {
+    if (!ctx || !(seconds >= 0.0) || seconds > 60.0) return DCG_E_ARG;
+    // 0 restores the defaults; any positive limit is at least 1 ns
+    ctx->c.wait_limit_ns = seconds == 0.0 ? 0 : std::max<uint64_t>(1, (uint64_t)(seconds * 1.0e9));
+    return DCG_OK;
 }
 
 int dcg_time_family(dcg_ctx *ctx, int32_t family) {

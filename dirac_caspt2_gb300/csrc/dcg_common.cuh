@@ -94,6 +94,9 @@ struct Context {
     std::string err;
     int64_t launches = 0;
     int num_sms = 0;
+    // limit of the device-side waits that can give up (grid barriers of the tridiagonalisation,
+    // pipeline waits of the tensor-core GEMM), ns; 0 = each kernel's default (dcg_set_wait_limit)
+    uint64_t wait_limit_ns = 0;
     bool tune_trials = true;     // may run autotuner trials (off for serving slots)
     void *dev_state = nullptr;   // device-side system state (owned, see dcg_api.cu)
 
@@ -118,6 +121,11 @@ struct Context {
     int metric_solver = 0;
     int gram_cholesky_blocks = 0;   // Gram blocks of the last dcg_caspt2 solved by Cholesky
     int gram_woodbury_blocks = 0;   // ... of them with metric eigenvalues under the cutoff deflated
+    // per-irrep results of the last dcg_caspt2, [sub * nsym + isym - 1] for subspaces A..H:
+    // e2X(isym), its c^2 share, and whether solve_X_subspace prints the e2X(isym) line
+    // (a symmetry block with dimn > 0 whose S keeps dimm > 0 vectors above the cutoff)
+    std::vector<double> sym_e2, sym_sc2;
+    std::vector<int32_t> sym_printed;
     // last MDCINT canonicalisation (device, in the workspace)
     int64_t mdc_n = -1;
     int32_t *mdc_ijkl = nullptr;

@@ -195,6 +195,7 @@ struct GridBar {
     unsigned gen;
     int err;       // 1: a barrier wait exceeded its time limit
     unsigned pub;  // reflectors published so far (shared-memory tridiagonalisation)
+    unsigned long long limit_ns;   // time limit of one wait (set by the host before the launch)
 };
 
 __device__ __forceinline__ uint64_t globaltimer_ns() {
@@ -205,7 +206,8 @@ __device__ __forceinline__ uint64_t globaltimer_ns() {
 
 // Grid-wide barrier for a cooperative launch: one monotonically increasing arrival counter
 // (count), so a barrier costs one fence, one atomic and an acquire poll.  Each wait is bounded
-// (5 s); a block that gives up sets gb->err and every waiting block then leaves the kernel.
+// (gb->limit_ns, 5 s by default, the clock read every 16 polls); a block that gives up sets
+// gb->err and every waiting block then leaves the kernel.
 constexpr uint64_t kBarrierLimitNs = 5000000000ull;
 __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned nblocks) {
     __shared__ int s_ok;
@@ -223,12 +225,12 @@ __device__ __forceinline__ bool grid_barrier(GridBar *gb, unsigned nblocks) {
             while (true) {
                 asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->count) : "memory");
                 if ((int)(cur - target) >= 0) break;
-                if ((++spins & 255u) == 0) {
+                if ((++spins & 15u) == 0) {
                     if (*(volatile int *)&gb->err) {
                         ok = 0;
                         break;
                     }
-                    if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+                    if (globaltimer_ns() - t0 > gb->limit_ns) {
                         atomicExch(&gb->err, 1);
                         ok = 0;
                         break;
@@ -257,12 +259,12 @@ __device__ __forceinline__ bool wait_published(GridBar *gb, unsigned want) {
             while (true) {
                 asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cur) : "l"(&gb->pub) : "memory");
                 if (cur >= want) break;
-                if ((++spins & 255u) == 0) {
+                if ((++spins & 15u) == 0) {
                     if (*(volatile int *)&gb->err) {
                         ok = 0;
                         break;
                     }
-                    if (globaltimer_ns() - t0 > kBarrierLimitNs) {
+                    if (globaltimer_ns() - t0 > gb->limit_ns) {
                         atomicExch(&gb->err, 1);
                         ok = 0;
                         break;
@@ -1280,6 +1282,14 @@ static HeevWork heev_work(Context &c, int n, int slot) {
 // kernels must never wait for each other's SMs.
 static std::mutex g_coop_mutex;
 
+// A fresh barrier (counters and error flag zero) with the context's wait limit, written in
+// stream order (a copy from pageable host memory is staged before the call returns).
+static void gridbar_reset(Context &c, GridBar *gb) {
+    GridBar x{};
+    x.limit_ns = c.wait_limit_ns ? c.wait_limit_ns : kBarrierLimitNs;
+    DCG_CUDA(cudaMemcpyAsync(gb, &x, sizeof(GridBar), cudaMemcpyHostToDevice, c.stream));
+}
+
 static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork &h) {
     std::lock_guard<std::mutex> coop(g_coop_mutex);
     const size_t smem = 2 * sizeof(cplx) * (size_t)std::max(n - 1, 1);
@@ -1293,7 +1303,7 @@ static void tridiag_persistent(Context &c, int n, cplx *A, int64_t lda, HeevWork
     cplx *pbuf = wsget<cplx>(c, "trd.p", (size_t)n + 1);
     double2 *part = wsget<double2>(c, "trd.part", (size_t)nblocks + 1);
     GridBar *gb = wsget<GridBar>(c, "trd.bar", 1);
-    DCG_CUDA(cudaMemsetAsync(gb, 0, sizeof(GridBar), c.stream));
+    gridbar_reset(c, gb);
     void *args[] = {&n, &A, &lda, &h.d, &h.e, &h.tau, &pbuf, &part, &gb};
     DCG_CUDA(cudaLaunchCooperativeKernel((const void *)tridiag_persistent_kernel, dim3(nblocks), dim3(TRD_THREADS),
                                          args, smem, c.stream));
@@ -1357,7 +1367,7 @@ static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
     int per_sm = 0;
     DCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_smem_batched_kernel, TRD_THREADS, smem));
     if (per_sm < 1 || total > per_sm * sms) return false;
-    for (size_t q = 0; q < jobs.size(); q++) DCG_CUDA(cudaMemsetAsync(jobs[q].gb, 0, sizeof(GridBar), c.stream));
+    for (size_t q = 0; q < jobs.size(); q++) gridbar_reset(c, jobs[q].gb);
     TrdJob *dj = wsget<TrdJob>(c, "trd.jobs", jobs.size());
     DCG_CUDA(cudaMemcpyAsync(dj, jobs.data(), jobs.size() * sizeof(TrdJob), cudaMemcpyHostToDevice, c.stream));
     int nj = (int)jobs.size();

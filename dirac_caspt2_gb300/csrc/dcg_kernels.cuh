@@ -75,8 +75,10 @@ void launch_perm_F(Context &c, const RDMView &r, cplx *P2, cplx *unused);
 void launch_permute_A1(Context &c, const cplx *A1, int na, int ni, cplx *A1p);
 void launch_v_A_rest(Context &c, const RDMView &r, const cplx *A1, const cplx *effh, int ni, cplx *V);
 void launch_F_pack(Context &c, const cplx *Fc, int ns, int na, cplx *Fp);
+// partial sums launch_h_stream2 writes (h_stream_blocks(ni, ns) of each)
+int h_stream_blocks(int ni, int ns);
 void launch_h_stream2(Context &c, const cplx *Hc, int ni, int ns, const double *eps_i, const double *eps_s,
                       const int *irp_i, const int *irp_s, const int *md, const int *msy, int nsym, double eshift,
-                      double *e2part, double *sc2part, int nblk);
+                      double *e2part, double *sc2part);
 
 }  // namespace dcg

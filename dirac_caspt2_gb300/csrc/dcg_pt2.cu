@@ -439,31 +439,56 @@ void launch_F_pack(Context &c, const cplx *Fc, int ns, int na, cplx *Fp) {
 // e2h = -sum |V|^2/e, sumc2 = sum |V/e|^2 over a > b, i > j with
 // V = (ai|bj) - (aj|bi), e = eps_a + eps_b - eps_i - eps_j + eshift and the symmetry
 // condition MULTB_S(MULTB_D(irp a, irp i), MULTB_D(irp b, irp j)) == 1
-// (solve_H_subspace.F90:119-175).  Hc: (ns, ni, ns, ni); thread index runs over the
-// class in storage order so both reads are coalesced.
-__global__ void h_stream_kernel(const cplx *__restrict__ Hc, int ni, int ns, const double *__restrict__ eps_i,
-                                const double *__restrict__ eps_s, const int *__restrict__ irp_i,
-                                const int *__restrict__ irp_s, const int *__restrict__ md, const int *__restrict__ msy,
-                                int nsym, double eshift, double *e2part, double *sc2part) {
-    __shared__ double sh[2][32];
+// (solve_H_subspace.F90:119-175).  Hc: (ns, ni, ns, ni), (a i|b j) at a + ns (i + ni (b + ns j)).
+//
+// One block per (b, i), i >= 1: its threads run over the (j < i, a > b) pairs with a fastest, so
+// both operands, (a i|b j) and (a j|b i), are contiguous runs over a and every element of the
+// a > b half of the class is read exactly once (streaming loads); the a < b half is never read.
+// The FP64 pipe, not HBM, bounds this kernel on GB300 (about two FP64 operations per clock per
+// SM): per element two subtractions and |V|^2, the denominator, a reciprocal and the two
+// accumulations.  The reciprocal is the FP32 one widened and refined by one Newton-Raphson step
+// for 1/e, r = r0 + r0 (1 - e r0), whose relative error is the square of the FP32 error
+// (<= 2^-48) plus rounding; a denominator outside the FP32 normal range takes 1.0 / e.
+__device__ __forceinline__ double h_recip(double e) {
+    const float ef = __double2float_rn(e);
+    const float af = fabsf(ef);
+    if (!(af >= 1.1754944e-38f && af <= 3.0e38f)) return 1.0 / e;
+    const double r0 = (double)__frcp_rn(ef);
+    return fma(r0, fma(-e, r0, 1.0), r0);
+}
+
+__global__ void __launch_bounds__(256) h_stream_kernel(const cplx *__restrict__ Hc, int ni, int ns,
+                                                       const double *__restrict__ eps_i,
+                                                       const double *__restrict__ eps_s,
+                                                       const int *__restrict__ irp_i, const int *__restrict__ irp_s,
+                                                       const int *__restrict__ md, const int *__restrict__ msy,
+                                                       int nsym, double eshift, double *e2part, double *sc2part) {
+    __shared__ double sh[2][8];
+    const int b = blockIdx.x, i = blockIdx.y + 1;
     const int64_t S = ns, I = ni;
-    const int64_t tot = S * I * S * I;
+    const int nab = ns - 1 - b;    // a = b + 1 .. ns - 1
+    const int tot = i * nab;       // (j, a) pairs of this block
+    const double cbi = eps_s[b] - eps_i[i] + eshift;
+    const int irb = irp_s[b], iri = irp_i[i];
+    const cplx *row1 = Hc + (b + 1) + S * (i + I * (int64_t)b);   // (a i|b j) = row1[a' + S I S j]
+    const cplx *row2 = Hc + (b + 1) + S * I * (b + S * (int64_t)i);   // (a j|b i) = row2[a' + S j]
     double e2 = 0.0, sc2 = 0.0;
-    for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
-        int64_t x = q;
-        const int a = (int)(x % S); x /= S;
-        const int i = (int)(x % I); x /= I;
-        const int b = (int)(x % S); x /= S;
-        const int j = (int)x;
-        if (a <= b || i <= j) continue;
-        const int s1 = md[(irp_s[a] - 1) * nsym + irp_i[i] - 1];
-        const int s2 = md[(irp_s[b] - 1) * nsym + irp_i[j] - 1];
-        if (msy[(s1 - 1) * nsym + s2 - 1] != 1) continue;
-        const cplx v = csub(Hc[q], Hc[a + S * (j + I * (b + S * (int64_t)i))]);
-        const double e = eps_s[a] + eps_s[b] - eps_i[i] - eps_i[j] + eshift;
-        const double a2 = cabs2(v);
-        e2 -= a2 / e;
-        sc2 += a2 / (e * e);
+    for (int q = threadIdx.x; q < tot; q += blockDim.x) {
+        const int j = q / nab, a1 = q - j * nab, a = b + 1 + a1;
+        if (nsym > 1) {
+            const int s1 = md[(irp_s[a] - 1) * nsym + iri - 1];
+            const int s2 = md[(irb - 1) * nsym + irp_i[j] - 1];
+            if (msy[(s1 - 1) * nsym + s2 - 1] != 1) continue;
+        }
+        const cplx x1 = __ldcs(row1 + a1 + S * I * S * (int64_t)j);
+        const cplx x2 = __ldcs(row2 + a1 + S * (int64_t)j);
+        const double vr = x1.x - x2.x, vi = x1.y - x2.y;
+        const double a2 = fma(vr, vr, vi * vi);
+        const double e = __ldg(eps_s + a) + (cbi - __ldg(eps_i + j));
+        const double r = h_recip(e);
+        const double t = a2 * r;
+        e2 -= t;
+        sc2 = fma(t, r, sc2);
     }
     // deterministic block reduction
     for (int o = 16; o > 0; o >>= 1) {
@@ -474,18 +499,30 @@ __global__ void h_stream_kernel(const cplx *__restrict__ Hc, int ni, int ns, con
     if (lane == 0) { sh[0][wid] = e2; sh[1][wid] = sc2; }
     __syncthreads();
     if (threadIdx.x == 0) {
-        double a = 0.0, b = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { a += sh[0][w]; b += sh[1][w]; }
-        e2part[blockIdx.x] = a;
-        sc2part[blockIdx.x] = b;
+        double x = 0.0, y = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) { x += sh[0][w]; y += sh[1][w]; }
+        const int64_t blk = (int64_t)blockIdx.y * gridDim.x + blockIdx.x;
+        e2part[blk] = x;
+        sc2part[blk] = y;
     }
 }
 
+__global__ void zero2_kernel(double *a, double *b) {
+    a[0] = 0.0;
+    b[0] = 0.0;
+}
+
+int h_stream_blocks(int ni, int ns) { return (ni >= 2 && ns >= 2) ? (ns - 1) * (ni - 1) : 1; }
+
 void launch_h_stream2(Context &c, const cplx *Hc, int ni, int ns, const double *eps_i, const double *eps_s,
                       const int *irp_i, const int *irp_s, const int *md, const int *msy, int nsym, double eshift,
-                      double *e2part, double *sc2part, int nblk) {
-    h_stream_kernel<<<nblk, 256, 0, c.stream>>>(Hc, ni, ns, eps_i, eps_s, irp_i, irp_s, md, msy, nsym, eshift, e2part,
-                                                sc2part);
+                      double *e2part, double *sc2part) {
+    if (ni < 2 || ns < 2) {   // no pair a > b, i > j
+        zero2_kernel<<<1, 1, 0, c.stream>>>(e2part, sc2part);
+    } else {
+        h_stream_kernel<<<dim3((unsigned)(ns - 1), (unsigned)(ni - 1)), 256, 0, c.stream>>>(
+            Hc, ni, ns, eps_i, eps_s, irp_i, irp_s, md, msy, nsym, eshift, e2part, sc2part);
+    }
     DCG_LAUNCHED(c);
 }
 
@@ -498,8 +535,6 @@ void launch_h_stream2(Context &c, const cplx *Hc, int ni, int ns, const double *
 // held in a file-scope device array instead of the context workspace.  The array is
 // sized for at most DCG_H_NOALLOC_MAX_NINACT inactive spinors (8128 pairs, 127 KiB) and
 // stays resident on every device that loads the library until the process exits.
-#include <mutex>
-
 namespace dcg {
 
 constexpr int H_NOALLOC_MAX_NINACT = 128;
@@ -558,9 +593,6 @@ __global__ void h_pair_final_kernel(double *scratch, int npair) {
     scratch[2 * H_NOALLOC_MAX_PAIRS + 1] = y;
 }
 
-static std::mutex g_noalloc_mu;
-static double *g_noalloc_ptr[128] = {};
-
 }  // namespace dcg
 
 extern "C" int dcg_solve_h_noalloc(const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
@@ -573,21 +605,14 @@ extern "C" int dcg_solve_h_noalloc(const void *hclass, int32_t ninact, int32_t n
     out[0] = out[1] = 0.0;
     if (ninact < 2 || nsec < 2) return DCG_OK;              // no pair i > j or a > b
     if (!hclass || !eps_i || !eps_s || !irp_i || !irp_s || !multb_d || !multb_s) return DCG_E_ARG;
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return DCG_E_CUDA;
+    // An error the caller left pending is not this call's: report it without clearing it, so
+    // that the launch check below sees only these launches.
+    if (cudaPeekAtLastError() != cudaSuccess) return DCG_E_CUDA;
+    // The device address of the array in the context current now (the caller's device and
+    // context; a context of its own, or one created again after cudaDeviceReset, has its own
+    // copy of the array), looked up on every call.
     double *scratch = nullptr;
-    {
-        // once per device, with that device current: the device address of the array
-        std::lock_guard<std::mutex> lk(g_noalloc_mu);
-        if (!g_noalloc_ptr[dev]) {
-            cudaError_t e = cudaGetSymbolAddress((void **)&g_noalloc_ptr[dev], g_h_noalloc_scratch);
-            if (e != cudaSuccess) {
-                g_noalloc_ptr[dev] = nullptr;
-                return DCG_E_CUDA;
-            }
-        }
-        scratch = g_noalloc_ptr[dev];
-    }
+    if (cudaGetSymbolAddress((void **)&scratch, g_h_noalloc_scratch) != cudaSuccess || !scratch) return DCG_E_CUDA;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     const int npair = ninact * (ninact - 1) / 2;
     h_pair_kernel<<<npair, 256, 0, st>>>(static_cast<const cplx *>(hclass), ninact, nsec, eps_i, eps_s, irp_i, irp_s,

@@ -241,13 +241,13 @@ __device__ __forceinline__ uint64_t sp_now() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// bounded wait; false (and *err set) when the limit runs out
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err) {
+// bounded wait; false (and *err set) when limit_ns runs out
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int *err, uint64_t limit_ns) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = sp_now();
     while (!mbar_try_wait(bar, parity)) {
         if (*(volatile int *)err) return false;
-        if (sp_now() - t0 > SP_WAIT_NS) {
+        if (sp_now() - t0 > limit_ns) {
             atomicExch(err, 1);
             return false;
         }
@@ -323,6 +323,7 @@ struct SplitArgs {
     int accumulate;   // C += result
     int order;        // CTA raster: 0 column blocks of a row block adjacent, 1 row blocks of a column block
     int *err;
+    uint64_t wait_ns;   // limit of the pipeline waits (SP_WAIT_NS unless a test shortens it)
 };
 
 // g0 + g1 + g2 + g3 (FP32 bit patterns) as a double: TwoSum (Knuth) keeps g0 + g1 exact as
@@ -375,12 +376,14 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = s_tmem;
     const int nks = a.nks;
+    int issued = 0;   // producer: stages whose copies were issued
 
     if (warp == 4) {
         if (lane == 0) {   // producer: 2 x SPLIT_S bulk copies of 4 KB per stage
             for (int ks = 0; ks < nks; ks++) {
                 const int s = ks % SP_STAGES;
-                if (ks >= SP_STAGES && !mbar_wait(&bar_empty[s], ((ks / SP_STAGES) - 1) & 1, a.err)) break;
+                if (ks >= SP_STAGES && !mbar_wait(&bar_empty[s], ((ks / SP_STAGES) - 1) & 1, a.err, a.wait_ns)) break;
+                issued = ks + 1;
                 unsigned char *st = smem + s * SP_STAGE_BYTES;
                 mbar_expect_tx(&bar_full[s], SP_STAGE_BYTES);
                 for (int p = 0; p < SPLIT_S; p++) {
@@ -398,7 +401,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
             bool ok = true;
             for (int ks = 0; ks < nks && ok; ks++) {
                 const int s = ks % SP_STAGES;
-                if (!mbar_wait(&bar_full[s], (ks / SP_STAGES) & 1, a.err)) {
+                if (!mbar_wait(&bar_full[s], (ks / SP_STAGES) & 1, a.err, a.wait_ns)) {
                     ok = false;
                     break;
                 }
@@ -436,7 +439,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
         }
     } else {
         // epilogue: warp w reads TMEM lanes 32w..32w+31 = tile rows
-        const bool ok = mbar_wait(&bar_done, 0, a.err);
+        const bool ok = mbar_wait(&bar_done, 0, a.err, a.wait_ns);
         asm volatile("tcgen05.fence::after_thread_sync;");
         if (ok) {
             const int r = warp * 32 + lane;
@@ -473,6 +476,14 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_kernel(SplitArgs a) {
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    // After a wait gave up, copies may still be in flight and MMAs still running: the last
+    // round of each stage lands and every issued MMA completes before the CTA frees its TMEM
+    // and leaves (waits bounded by SP_WAIT_NS; without an error they return at once).
+    if (warp == 4 && lane == 0)
+        for (int ks = issued - 1; ks >= 0 && ks >= issued - SP_STAGES; ks--)
+            mbar_drain(&bar_full[ks % SP_STAGES], (uint32_t)((ks / SP_STAGES) & 1));
+    if (warp == 5 && lane == 0) mbar_drain(&bar_done, 0);
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;");
@@ -533,6 +544,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
     asm volatile("tcgen05.fence::after_thread_sync;");
     const uint32_t tmem = s_tmem;
 
+    int64_t issued = 0;   // producer: stage rounds whose copies were issued
     if (warp == 4) {
         if (lane == 0) {   // producer
             int64_t it = 0;
@@ -543,7 +555,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
                 const int nb = nh >> 1, half = nh & 1;
                 for (int ks = 0; ks < nks; ks++, it++) {
                     const int s = (int)(it % SPP_STAGES);
-                    if (it >= SPP_STAGES && !mbar_wait(&bar_empty[s], (uint32_t)(((it / SPP_STAGES) - 1) & 1), a.err)) {
+                    if (it >= SPP_STAGES && !mbar_wait(&bar_empty[s], (uint32_t)(((it / SPP_STAGES) - 1) & 1), a.err, a.wait_ns)) {
                         ok = false;
                         break;
                     }
@@ -560,9 +572,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
                     }
                 }
             }
-            if (!ok)   // copies still in flight land before the CTA leaves
-                for (int64_t j = it - 1; j >= 0 && j >= it - SPP_STAGES; j--)
-                    mbar_drain(&bar_full[j % SPP_STAGES], (uint32_t)((j / SPP_STAGES) & 1));
+            issued = it;
         }
     } else if (warp == 5) {
         if (lane == 0) {   // MMA issuer
@@ -570,7 +580,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
             bool ok = true;
             for (int64_t t = blockIdx.x; t < items && ok; t += gridDim.x, tl++) {
                 const int b = (int)(tl & 1);
-                if (tl >= 2 && !mbar_wait(&acc_empty[b], (uint32_t)(((tl >> 1) - 1) & 1), a.err)) {
+                if (tl >= 2 && !mbar_wait(&acc_empty[b], (uint32_t)(((tl >> 1) - 1) & 1), a.err, a.wait_ns)) {
                     ok = false;
                     break;
                 }
@@ -578,7 +588,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
                 const uint32_t acc = tmem + (uint32_t)(b * 4 * SPP_TN);
                 for (int ks = 0; ks < nks; ks++, it++) {
                     const int s = (int)(it % SPP_STAGES);
-                    if (!mbar_wait(&bar_full[s], (uint32_t)((it / SPP_STAGES) & 1), a.err)) {
+                    if (!mbar_wait(&bar_full[s], (uint32_t)((it / SPP_STAGES) & 1), a.err, a.wait_ns)) {
                         ok = false;
                         break;
                     }
@@ -618,7 +628,7 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
         int64_t tl = 0;
         for (int64_t t = blockIdx.x; t < items; t += gridDim.x, tl++) {
             const int b = (int)(tl & 1);
-            if (!mbar_wait(&acc_full[b], (uint32_t)((tl >> 1) & 1), a.err)) break;
+            if (!mbar_wait(&acc_full[b], (uint32_t)((tl >> 1) & 1), a.err, a.wait_ns)) break;
             asm volatile("tcgen05.fence::after_thread_sync;");
             int z, rb, nh;
             item_coords(t, z, rb, nh);
@@ -657,6 +667,12 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
         }
     }
     asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    // copies still in flight after any role gave up land before the CTA leaves (the MMA issuer
+    // has already waited for its MMAs through bar_drain); without an error this returns at once
+    if (warp == 4 && lane == 0)
+        for (int64_t j = issued - 1; j >= 0 && j >= issued - SPP_STAGES; j--)
+            mbar_drain(&bar_full[j % SPP_STAGES], (uint32_t)((j / SPP_STAGES) & 1));
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;");
@@ -741,6 +757,7 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     sa.accumulate = accumulate ? 1 : 0;
     sa.order = 0;
     sa.err = err;
+    sa.wait_ns = c.wait_limit_ns ? c.wait_limit_ns : SP_WAIT_NS;
     dim3 grid((unsigned)((int64_t)nrb * nnb), 1, batch);
     // CTA raster tuned per shape when both orders have more than one block to order; trial
     // launches overwrite C, so only non-accumulating products are timed

@@ -494,6 +494,31 @@ def read_mdcint_raw(directory: str, mrc: MrconeeData, inp: ActiveInput) -> Mdcin
                      realonly=bool(realonly))
 
 
+def write_mdcint_raw(path: str, raw: MdcintRaw, is32: bool, realonly: Optional[bool] = None,
+                     header_stamp: bytes = b" 01Jan26  00:00:00") -> None:
+    """Write ``raw`` back as one DIRAC MDCINT file (the layout create_newmdcint.F90:210-265 and
+    module_realonly.F90:29-77 read): header ``datex, timex, nkr, (kr(i), kr(-i))``, one record
+    ``ikr, jkr, nz, (indk, indl) * nz, values`` per raw record, and the ``ikr = 0`` end record.
+    The values are ``re`` alone (real-only layout) or interleaved ``(re, im)`` pairs (complex
+    layout); ``realonly`` defaults to ``raw.realonly``, and a real-only ``raw`` written in the
+    complex layout gets zero imaginary parts, which makes check_realonly report complex."""
+    it = "<i4" if is32 else "<i8"
+    ro = raw.realonly if realonly is None else bool(realonly)
+    ints = lambda *xs: np.array(xs, it).tobytes()
+    hdr = header_stamp[:18].ljust(18) + ints(len(raw.kr)) + np.asarray(raw.kr, it).reshape(-1).tobytes()
+    recs = [hdr]
+    for r in range(len(raw.rec_ikr)):
+        a, b = int(raw.rec_off[r]), int(raw.rec_off[r + 1])
+        kl = np.stack([raw.indk[a:b], raw.indl[a:b]], axis=1).astype(it).tobytes()
+        if ro:
+            vv = np.asarray(raw.re[a:b], "<f8").tobytes()
+        else:
+            vv = np.stack([raw.re[a:b], raw.im[a:b]], axis=1).astype("<f8").tobytes()
+        recs.append(ints(int(raw.rec_ikr[r]), int(raw.rec_jkr[r]), b - a) + kl + vv)
+    recs.append(ints(0, 0, 0))
+    write_fortran_records(path, recs)
+
+
 def canonicalize_mdcint(raw: MdcintRaw) -> MdcintNew:
     """Restatement of create_newmdcint's canonicalisation (create_newmdcint.F90:171-321) on
     the raw records: both Kramers partners of every record, the bra/ket-exchanged copies of

@@ -7,7 +7,7 @@ The library marks each stage with an NVTX range (``ints``, ``casci_eig``, ``A`` 
 ``transformation``) and each transformed integral class with ``tr_<class>``, so a profiler
 can select the launches of one stage, e.g.
 
-    ncu --nvtx --nvtx-include "tr_H/" -k regex:zgemm -c 3 ... \\
+    ncu --clock-control none --nvtx --nvtx-include "tr_H/" -k regex:zgemm -c 3 ... \\
         python -m dirac_caspt2_gb300.profile_solve --ninact 16 --nact 8 --nsec 240 --nelec 4
 
 Prints the total energy and per-stage device times of the last solve.  With ``--heev N`` it

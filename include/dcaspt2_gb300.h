@@ -130,6 +130,26 @@ int dcg_casci(dcg_ctx *ctx, int32_t nroot, double *eigen_out, double *ci_re, dou
 int dcg_caspt2(dcg_ctx *ctx, uint32_t skip_mask, double e2_sub[8], double sumc2_sub[8],
                double *e0_out, double *etotal_out);
 
+/* Per-irrep energies of the last dcg_caspt2: the e2X(isym) lines that solve_A..G_subspace
+ * print before their totals (solve_A_subspace.F90:262, solve_B_subspace.F90:268,
+ * solve_C_subspace.F90:263, solve_D_subspace.F90:285, solve_E_subspace.F90:259,
+ * solve_F_subspace.F90:284, solve_G_subspace.F90:273; the e2(isym) of e.g.
+ * solve_A_subspace.F90:256).  All three arrays are e2_sym[8][nsym] in C order, index
+ * k * nsym + isym - 1 for subspace k = 0 (A) .. 7 (H); Fortran reads them as (nsym, 8).
+ * printed is 1 where the reference prints the line: a symmetry block with dimn > 0 whose S
+ * keeps dimm > 0 vectors above the linear-dependence cutoff (solve_A_subspace.F90:118,158-164);
+ * H prints no per-irrep lines, so its row stays 0.  sumc2_sym holds each block's share of
+ * sumc2,X (not printed by the reference).  Any output may be NULL; nsym must equal the
+ * system's nsymrpa.  DCG_E_STATE before the first dcg_caspt2. */
+int dcg_caspt2_irreps(const dcg_ctx *ctx, int32_t nsym, double *e2_sym, double *sumc2_sym, int32_t *printed);
+
+/* The CASCI determinants of the last dcg_casci as the bit strings the reference keeps in
+ * dict_cas_idx (search_cas_configuration.F90:33-56, module_dict.F90:246-260): bit t-1 set when
+ * active spinor t is occupied, in the reference's index order (ascending bit strings through
+ * Gosper's hack, RAS and totsym filtered), which is also the row order of the CI coefficients
+ * dcg_casci returns and of the dict records of CIDATA_sym<n> (casci.F90:118-160).  n >= ndet. */
+int dcg_casci_determinants(const dcg_ctx *ctx, int64_t *dets_out, int32_t n);
+
 /* H subspace on a caller-supplied, device-resident transformed H class (replaces
  * solve_H_subspace, src/solve_H_subspace.F90:23-191): with V = (ai|bj) - (aj|bi),
  * e = eps_a + eps_b - eps_i - eps_j + eshift, over a > b, i > j whose symmetry product
@@ -150,9 +170,13 @@ int dcg_solve_h(dcg_ctx *ctx, const void *hclass, int32_t ninact, int32_t nsec, 
  * NULL = default stream) of the current device, without a context.  Its partial sums live
  * in a file-scope device array of the library sized for ninact <= 128 (8128 inactive
  * pairs, 127 KiB), which every device that loads the library keeps until the process
- * exits; ninact > 128 returns DCG_E_ARG.  The first call on a device looks up that array's
- * device address (make that first call before any stream capture).  All calls share the
- * array: calls that overlap on the GPU race on it and must be serialised by the caller. */
+ * exits; ninact > 128 returns DCG_E_ARG.  Every call looks up the array's device address in
+ * the CUDA context current at the call, so it works in the device's primary context, in a
+ * context of the caller's own and after cudaDeviceReset.  The call is synchronous (it reads
+ * the result back into `out` and waits for `stream`): do not make it while `stream`, or in
+ * global capture mode any stream, is being captured.  An error the caller left pending
+ * returns DCG_E_CUDA without being cleared.  All calls share the array: calls that overlap
+ * on the GPU race on it and must be serialised by the caller. */
 int dcg_solve_h_noalloc(const void *hclass, int32_t ninact, int32_t nsec, const double *eps_i,
                         const double *eps_s, const int32_t *irp_i, const int32_t *irp_s,
                         const int32_t *multb_d, const int32_t *multb_s, int32_t nsymrpa, double eshift,
@@ -218,7 +242,8 @@ int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int3
 /* Kernel families whose launches can be timed with CUDA events on the context stream. */
 #define DCG_FAM_NONE 0
 #define DCG_FAM_TRANSFORM 1   /* 4-index transformation GEMMs; work = FLOPs (complex MAC = 8)  */
-#define DCG_FAM_HSTREAM 2     /* H-subspace streaming reduction; work = bytes of the H class    */
+#define DCG_FAM_HSTREAM 2     /* H-subspace streaming reduction; work = bytes it must read: the a > b
+                                 half of the H class, C(ns,2) ni (ni-1) complex values          */
 #define DCG_FAM_RDM 3         /* density GEMMs; work = FLOPs                                     */
 #define DCG_FAM_SCATTER 4     /* record expansion; work = record bytes read                      */
 #define DCG_FAM_EIG 5         /* Hermitian eigensolver launches; work = nominal FLOPs 16/3 n^3   */
@@ -227,6 +252,17 @@ int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int3
 #define DCG_FAM_EIG_VEC 8     /*   reserved (no launches)                                          */
 #define DCG_FAM_EIG_BACK 9    /*   back-transformation (FLOPs 8 n^2 m)                            */
 #define DCG_FAM_SPLIT_MMA 10  /* tcgen05 split-precision GEMM kernel; work = BF16 tensor FLOPs      */
+
+/* Time limit of the context's device-side waits that can give up: the grid barriers and the
+ * published-reflector waits of the Householder tridiagonalisation (default 5 s) and the
+ * pipeline waits of the tensor-core GEMM kernels (default 2 s).  A wait that runs out sets an
+ * error flag; the kernel's other blocks leave at their next wait, copies still in flight land
+ * and issued tensor-core operations complete (waits bounded by the default limits) before a
+ * block frees its tensor memory and returns, and the call returns DCG_E_NUMERIC with the
+ * reason in dcg_last_error.  The context stays usable.  seconds = 0 restores the defaults;
+ * values in (0, 60] set the limit.  A diagnostic and fault-test hook: a short limit makes
+ * ordinary waits run out. */
+int dcg_set_wait_limit(dcg_ctx *ctx, double seconds);
 
 /* Select the family timed during subsequent calls (DCG_FAM_NONE disables; resets stats). */
 int dcg_time_family(dcg_ctx *ctx, int32_t family);

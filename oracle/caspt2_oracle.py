@@ -626,6 +626,11 @@ def solve_block(S: np.ndarray, B: np.ndarray, Vcols: np.ndarray, alphas: np.ndar
     return e2, sc2, dimm
 
 
+def _kept(S: np.ndarray) -> int:
+    """dimm of cdiag(S, ..., smat_lin_dep_threshold): eigenvalues at or above the cutoff."""
+    return int(np.count_nonzero(heev_upper(S)[0] >= SMAT_LIN_DEP_THRESHOLD))
+
+
 def herm_from_upper(A: np.ndarray) -> np.ndarray:
     u = np.triu(A)
     return u + np.conj(np.triu(u, 1)).T
@@ -777,13 +782,16 @@ def solve_A(s, rd, cls, hU, eps, e0):
         Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
         outer = [i for i in range(ni) if s.nsymrpa == 1 or s.irpamo[i] == isym]
         if not outer:
-            # the reference still diagonalises; no outer index contributes
-            per[isym] = 0.0
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = V[np.array(outer)][:, x, y, z].T
         alphas = np.array([-eps[i] - e0 + s.eshift for i in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per
@@ -823,11 +831,16 @@ def solve_B(s, rd, cls, hU, eps, e0):
         outer = [(i, j) for (i, j) in pairs
                  if s.nsymrpa == 1 or _ms(s, _md(s, _kp(s.irpamo[i]), s.irpamo[j]), isym) == 1]
         if not outer:
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = np.stack([V[i, j][x, y] for (i, j) in outer], axis=1)
         alphas = np.array([-eps[i] - eps[j] - e0 + s.eshift for (i, j) in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per
@@ -868,11 +881,16 @@ def solve_C(s, rd, cls, hU, eps, e0):
         Sm, Bm = herm_from_upper(Sm), herm_from_upper(Bm)
         outer = [a for a in range(ns) if s.nsymrpa == 1 or s.irpamo[nmoc + a] == isym]
         if not outer:
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = V[np.array(outer)][:, x, y, z].T
         alphas = np.array([eps[nmoc + a] - e0 + s.eshift for a in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per
@@ -912,11 +930,16 @@ def solve_D(s, rd, cls, hU, eps, e0):
         outer = [(a, i) for a in range(ns) for i in range(ni)
                  if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[nmoc + a], s.irpamo[i]), isym) == 1]
         if not outer:
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = np.stack([V[a, i][x, y] for (a, i) in outer], axis=1)
         alphas = np.array([eps[nmoc + a] - eps[i] - e0 + s.eshift for (a, i) in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per
@@ -946,11 +969,16 @@ def solve_E(s, rd, cls, hU, eps, e0):
         outer = [(i, j, a) for (i, j, a) in trip
                  if s.nsymrpa == 1 or _ms(s, _md(s, isym, s.irpamo[i]), _md(s, s.irpamo[nmoc + a], s.irpamo[j])) == 1]
         if not outer:
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = np.stack([V[a, i, j][ind] for (i, j, a) in outer], axis=1)
         alphas = np.array([eps[nmoc + a] - eps[i] - eps[j] - e0 + s.eshift for (i, j, a) in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per
@@ -985,11 +1013,16 @@ def solve_F(s, rd, cls, hU, eps, e0):
         outer = [(a, b) for (a, b) in pairs
                  if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[nmoc + a], _kp(s.irpamo[nmoc + b])), isym) == 1]
         if not outer:
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = np.stack([V[a, b][vv, xx] for (a, b) in outer], axis=1)
         alphas = np.array([eps[nmoc + a] + eps[nmoc + b] - e0 + s.eshift for (a, b) in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per
@@ -1018,11 +1051,16 @@ def solve_G(s, rd, cls, hU, eps, e0):
         outer = [(a, b, i) for (a, b, i) in trip
                  if s.nsymrpa == 1 or _ms(s, _md(s, s.irpamo[nmoc + b], isym), _md(s, s.irpamo[nmoc + a], s.irpamo[i])) == 1]
         if not outer:
+            # the reference still diagonalises S and prints a zero e2X(isym) when it keeps
+            # vectors (solve_A_subspace.F90:155-164,262)
+            if _kept(Sm):
+                per[isym] = 0.0
             continue
         Vc = np.stack([V[a, b, i][ind] for (a, b, i) in outer], axis=1)
         alphas = np.array([-eps[i] + eps[nmoc + a] + eps[nmoc + b] - e0 + s.eshift for (a, b, i) in outer])
-        e2, sc2, _ = solve_block(Sm, Bm, Vc, alphas)
-        per[isym] = e2
+        e2, sc2, dimm = solve_block(Sm, Bm, Vc, alphas)
+        if dimm:   # printed only for a kept dimension (solve_A_subspace.F90:158-164)
+            per[isym] = e2
         e2_tot += e2
         sc2_tot += sc2
     return e2_tot, sc2_tot, per

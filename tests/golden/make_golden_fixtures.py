@@ -5,8 +5,12 @@ this reads ``active.inp``, ``MRCONEE`` and ``MDCINT*`` with the package's reader
 (restatements of read_mrconee / create_newmdcint) and stores the resulting system in
 ``<case>.npz`` together with the energies printed in ``reference.<case>.out``:
 the CASCI total energy of the selected root, the per-subspace ``e2X`` and ``sumc2,X``, the
-total CASPT2 energy and the e0test terms (energyHF(1..2), energy 1..4).  For the cases with small MDCINT files it also stores the raw MDCINT
-records (``<case>_mdcint_raw.npz``), the input of the MDCINT canonicalisation.
+per-irrep ``e2X(isym)`` lines (``ref_e2_sym``, (8, nsymrpa), NaN where the reference prints
+none), the total CASPT2 energy and the e0test terms (energyHF(1..2), energy 1..4).  For every
+case it also stores the raw MDCINT records (``<case>_mdcint_raw.npz``), the input of the MDCINT
+canonicalisation, together with the case's MRCONEE bytes and active.inp text, so that a test
+can rewrite the run directory (for instance with MDCINT in the complex record format) and read
+it back through the library's own readers.
 
 For the IVO cases (``ivo_*.npz``): the system read with ``active.ivo.inp``, the MDCINTNEW
 records IVO reads (two secondary and two active indices: the (ab|kk) and (ak|kb) classes of
@@ -27,7 +31,7 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 from dirac_caspt2_gb300 import dirac_io  # noqa: E402
 
 CASES = ["c2_h2o_dev", "check_minelecras3_dev", "ninact_0_h2_dev", "mdcint_scheme_6_dirac23_c32h_n2_dev"]
-RAW_CASES = ["check_minelecras3_dev", "ninact_0_h2_dev"]   # MDCINT small enough to keep (28 / 48 KB)
+RAW_CASES = CASES
 
 
 def parse_e0test(path: str):
@@ -41,6 +45,17 @@ def parse_e0test(path: str):
             if m and np.isnan(out[q]):
                 out[q] = float(m.group(1))
     return np.array(out)
+
+
+def parse_e2_sym(path: str, nsym: int):
+    """The e2X(isym) lines of solve_A..G_subspace (e.g. solve_A_subspace.F90:262) as an
+    (8, nsym) array, NaN where nothing is printed."""
+    out = np.full((8, nsym), np.nan)
+    for ln in open(path, errors="replace").read().splitlines():
+        m = re.match(r"^\s*e2([a-h])\(\s*(\d+)\)\s*=\s*([-+0-9.Ee]+)\s*a\.u\.", ln)
+        if m:
+            out["abcdefgh".index(m.group(1)), int(m.group(2)) - 1] = float(m.group(3))
+    return out
 
 
 def parse_output(path: str, selectroot: int):
@@ -83,6 +98,7 @@ def main(devdir: str):
                    ref_casci=casci, ref_total=total,
                    ref_e2=np.array([e2.get(k, np.nan) for k in "ABCDEFGH"]),
                    ref_sumc2=np.array([sc2.get(k, np.nan) for k in "ABCDEFGH"]),
+                   ref_e2_sym=parse_e2_sym(os.path.join(d, f"reference.{case}.out"), mrc.nsymrpa),
                    ref_e0test=parse_e0test(os.path.join(d, f"reference.{case}.out")))
         if not new.realonly:
             out["rec_im"] = new.val.imag
@@ -93,7 +109,10 @@ def main(devdir: str):
             np.savez_compressed(os.path.join(HERE, f"{case}_mdcint_raw.npz"), rec_ikr=raw.rec_ikr,
                                 rec_jkr=raw.rec_jkr, rec_off=raw.rec_off, indk=raw.indk, indl=raw.indl, re=raw.re,
                                 im=raw.im, kr=raw.kr, nmo=raw.nmo, dirac_to_cas=raw.dirac_to_cas,
-                                scheme=raw.scheme, realonly=raw.realonly)
+                                scheme=raw.scheme, realonly=raw.realonly,
+                                mrconee=np.frombuffer(open(os.path.join(d, "MRCONEE"), "rb").read(), np.uint8),
+                                active_inp=open(os.path.join(d, "active.inp")).read(),
+                                dirac_32bit=mrc.dirac_32bit)
             print(case, "raw entries", len(raw.re))
 
 

@@ -23,6 +23,19 @@ def load_raw(case):
                               dirac_to_cas=z["dirac_to_cas"], scheme=int(z["scheme"]), realonly=bool(z["realonly"]))
 
 
+def write_case_dir(case, directory, complex_layout):
+    """The case's run directory rebuilt from its fixture: MRCONEE and active.inp as the reference
+    ships them, MDCINT rewritten as one file in the real-only or the complex record layout."""
+    from dirac_caspt2_gb300 import dirac_io
+    z = np.load(os.path.join(GOLDEN_DIR, f"{case}_mdcint_raw.npz"))
+    os.makedirs(directory, exist_ok=True)
+    open(os.path.join(directory, "MRCONEE"), "wb").write(z["mrconee"].tobytes())
+    open(os.path.join(directory, "active.inp"), "w").write(str(z["active_inp"]))
+    dirac_io.write_mdcint_raw(os.path.join(directory, "MDCINT"), load_raw(case), bool(z["dirac_32bit"]),
+                              realonly=not complex_layout)
+    return dirac_io.read_active_inp(os.path.join(directory, "active.inp"))
+
+
 @pytest.mark.parametrize("case", RAW_CASES)
 def test_host_canonicalisation_reproduces_golden_stream(case):
     from dirac_caspt2_gb300 import dirac_io

@@ -43,3 +43,26 @@ def test_oracle_e0test_matches_reference(case):
     got = np.array([r[k].real for k in E0TEST_KEYS])
     assert np.abs(got - z["ref_e0test"]).max() <= 1e-10
     assert abs(r["error"]) <= 1e-10
+
+
+def check_e2_sym(e2_sym, ref, tol=TOL):
+    """e2_sym {subspace: {isym: e2}} against the golden (8, nsym) e2X(isym) array: the same set of
+    printed lines (solve_X_subspace prints a block with a kept dimension) and their values."""
+    for i, k in enumerate("ABCDEFG"):
+        want = {q + 1: float(v) for q, v in enumerate(ref[i]) if not np.isnan(v)}
+        got = e2_sym.get(k, {})
+        assert sorted(got) == sorted(want), (k, sorted(got), sorted(want))
+        for q, v in want.items():
+            assert abs(got[q] - v) < tol, (k, q, got[q], v)
+    assert not e2_sym.get("H")
+
+
+@pytest.mark.parametrize("case", GOLDEN_CASES)
+def test_oracle_per_irrep_energies_match_reference(case):
+    """The e2X(isym) lines every solve_A..G_subspace prints (e.g. solve_A_subspace.F90:262)."""
+    from dirac_caspt2_gb300 import api
+    from oracle import caspt2_oracle as O
+    path = os.path.join(GOLDEN_DIR, f"{case}.npz")
+    s = api.SystemInput.from_npz(path)
+    r = O.run(oracle_system(s))
+    check_e2_sym(r.e2_sym, np.load(path)["ref_e2_sym"])

@@ -1,7 +1,8 @@
 """dcg_solve_h_noalloc: the H-subspace sum for callers that cannot allocate device memory
 (their device memory comes from their own pool or another runtime's allocator), checked
 through the C ABI against the allocating entry point dcg_solve_h on the same device data,
-on two calls in a row (the static scratch keeps the previous call's contents)."""
+on two calls in a row (the static scratch keeps the previous call's contents), up to the
+largest size the scratch holds (ninact = 128: all 8128 inactive pairs)."""
 import ctypes
 
 import numpy as np
@@ -37,7 +38,7 @@ def _noalloc(lib, t, ni, ns, nsym, eshift, stream):
     return rc, (out[0], out[1])
 
 
-@pytest.mark.parametrize("nsym,ni,ns", [(1, 6, 10), (2, 8, 12), (1, 20, 40)])
+@pytest.mark.parametrize("nsym,ni,ns", [(1, 6, 10), (2, 8, 12), (1, 20, 40), (2, 128, 4)])
 def test_noalloc_matches_allocating_entry(gpu_lib, nsym, ni, ns):
     torch = pytest.importorskip("torch")
     from dirac_caspt2_gb300 import api
