@@ -274,17 +274,44 @@ def run_ours(args, cfg_name):
     e2e_steps = max(args.steps, 16)
     tot_s, res_s = e2e_served(e2e_steps)
 
-    # the FP64 eigensolver families, timed live on two more steps: Householder reduction
-    # (work (16/3) n^3 per matrix), tridiagonal eigenvalues, back-transformation (8 n^2 m)
-    fp64_nominal = 152 * 4 * 2.070e-3   # TF/s: 152 SMs x 2 FP64 FMA per clock x 2.07 GHz
+    # every kernel family timed live on two more steps each, against the roofline that bounds it:
+    # the BF16 tensor pipe (measured sustained peak), HBM (measured copy bandwidth) or the FP64
+    # pipe (nominal 152 SMs x 2 FMA per clock x 2.07 GHz: MEASURED_PEAKS.json holds no FP64 figure)
+    fp64_nominal = 152 * 4 * 2.070e-3   # TF/s
+    peaks0, src0 = _peaks()
+    fam_spec = {   # family: (bound, work unit, what the work counts)
+        "split_mma": ("tensor", "flop", "BF16 tensor FLOPs of the 15 slice products"),
+        "transform": ("fp64", "flop", "FP64-equivalent FLOPs of the 4-index transformation (complex MAC = 8)"),
+        "rdm": ("fp64", "flop", "FP64-equivalent FLOPs of the density GEMMs"),
+        "hstream": ("hbm", "byte", "bytes the H-subspace sum must read (the a > b half of the H class)"),
+        "scatter": ("hbm", "byte", "record bytes the integral expansion reads"),
+        "eig_tri": ("fp64", "flop", "Householder reduction, (16/3) n^3 per matrix (tridiagonal or band form)"),
+        "eig_val": ("fp64", "flop", "tridiagonal divide and conquer, (4/3) n^3 per matrix"),
+        "eig_back": ("fp64", "flop", "eigenvector back-transformation, 8 n^2 m"),
+    }
     fam_live = {}
-    for fname in ("eig_tri", "eig_val", "eig_back"):
+    for fname, (bound, unit, what) in fam_spec.items():
+        if fname == "split_mma" and prec != api.DCG_PREC_SPLIT:
+            continue
         _, _, _, _, st = timed(ses, hb_dev, 2, fname)
         f_ms, f_launch, f_work = st
-        if f_launch:
+        if not f_launch or f_ms <= 0:
+            continue
+        ent = {"bound": bound, "ms_per_step": f_ms / 2, "launches_per_step": f_launch / 2, "work": what}
+        if unit == "byte":
+            ach = f_work / (f_ms * 1e-3) / 1e9
+            ent.update({"achieved": ach, "unit": "GB/s", "peak": peaks0["hbm_gbs"],
+                        "frac": ach / peaks0["hbm_gbs"], "peak_source": f"{src0} (copy bandwidth)"})
+        elif bound == "tensor":
             ach = f_work / (f_ms * 1e-3) / 1e12
-            fam_live[fname] = {"ms_per_step": f_ms / 2, "launches_per_step": f_launch / 2,
-                               "achieved_tflops_fp64": ach, "frac_of_fp64_nominal": ach / fp64_nominal}
+            pk = peaks0["bf16_tflops_sustained"]
+            ent.update({"achieved": ach, "unit": "TFLOP/s", "peak": pk, "frac": ach / pk,
+                        "peak_source": f"{src0} (bf16 sustained)"})
+        else:
+            ach = f_work / (f_ms * 1e-3) / 1e12
+            ent.update({"achieved": ach, "unit": "TFLOP/s", "peak": fp64_nominal, "frac": ach / fp64_nominal,
+                        "peak_source": "nominal FP64 pipe"})
+        fam_live[fname] = ent
 
     # plain FP64 GPU path on the same system: the comparison the metric names
     fp64 = None
@@ -342,7 +369,10 @@ def run_ours(args, cfg_name):
             "e2e": {"value": e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hb_host.h2d_bytes,
                     "d2h_bytes_per_step": 8 * (1 + 8 + 8 + 2),
                     "path": "dcg_server with 4 slots (public serving API): each step one request from "
-                            "pinned host buffers, host wall clock from the first submit to the last result",
+                            "pinned host buffers, host wall clock from the first submit to the last result; "
+                            "up to 4 requests in flight overlap their copies and latency-bound phases. "
+                            "single_context below is the same requests one after another on one context "
+                            "(dcg_set_system / dcg_casci / dcg_caspt2 from pinned host buffers)",
                     "requests": e2e_steps,
                     "p50_ms": float(np.percentile([(r.t_end - r.t_submit) * 1e3 for r in res_s], 50)),
                     "p99_ms": float(np.percentile([(r.t_end - r.t_submit) * 1e3 for r in res_s], 99)),
@@ -355,9 +385,12 @@ def run_ours(args, cfg_name):
             "clocks": clocks_v, "roofline": roof,
             "stage_ms_last_step": {k: round(v, 3) for k, v in stage.items()},
             "total_energy": e_tot, "energy_spread": float(max(energies) - min(energies))}
-    line["fp64_families"] = {"peak_tflops_nominal": fp64_nominal,
-                             "note": "FP64 pipe, no measured peak: 152 SMs x 2 FMA/clock x 2.07 GHz",
-                             **fam_live}
+    line["families"] = fam_live   # every kernel family against its own roofline
+    if fam_live:
+        dom = max(fam_live, key=lambda k: fam_live[k]["ms_per_step"])
+        line["dominant_family"] = {"family": dom, "ms_per_step": fam_live[dom]["ms_per_step"],
+                                   "share_of_step": fam_live[dom]["ms_per_step"] / (tot_v / args.steps * 1e3),
+                                   "frac": fam_live[dom]["frac"], "bound": fam_live[dom]["bound"]}
     tuned = api.autotune_entries()
     line["autotune"] = {"mode": api.autotune_mode(-1), "keys": len(tuned),
                         "changed_from_heuristic": sum(1 for t in tuned if t["choice"] != 0),
@@ -410,7 +443,9 @@ def serve_leg(args, local, world):
             while srv.poll(1000) is None:
                 pass
         replicas.barrier()
+        m0 = api.merged_reduction_stats(local)
         rep = serve.run_stream(srv, list(enumerate(bufs)), arrivals)
+        m1 = api.merged_reduction_stats(local)
         worst = 0.0
         nchk = min(8, len(bufs))
         for k in range(nchk):
@@ -431,6 +466,11 @@ def serve_leg(args, local, world):
            "resident_record_gb": round(sum(s.record_bytes for s in systems) / 1e9, 2),
            "server_workspace_gb": round(dev_gb, 2),
            "alone_vs_mix_max_abs_dE": worst, "alone_checked": nchk,
+           "merged_reductions": {"launches": m1["launches"] - m0["launches"],
+                                 "joint_launches": m1["joint_launches"] - m0["joint_launches"],
+                                 "submissions": m1["submissions"] - m0["submissions"],
+                                 "what": "cooperative Householder-reduction launches of the slots during the "
+                                         "stream; joint = carrying the reductions of more than one request"},
            "sizes": "nact in {4,6,8,10,12} (nelec = nact/2), ninact 4-24, nsec 60-400 (even), per-request seeds"}
     del bufs, systems
     torch.cuda.empty_cache()

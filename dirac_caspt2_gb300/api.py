@@ -211,6 +211,8 @@ def load_library(path: str = LIB_PATH) -> ctypes.CDLL:
     lib.dcg_casci_energy_check.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
     lib.dcg_autotune_mode.argtypes = [ctypes.c_int32]
     lib.dcg_set_autotune_trials.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.dcg_set_merge_reductions.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    lib.dcg_merged_reduction_stats.argtypes = [ctypes.c_int, ctypes.c_void_p]
     lib.dcg_autotune_entries.argtypes = [ctypes.c_void_p, ctypes.c_int32]
     lib.dcg_autotune_entries.restype = ctypes.c_int32
     lib.dcg_ivo.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p,
@@ -238,6 +240,7 @@ EXPORTED_SYMBOLS = ["dcg_create", "dcg_destroy", "dcg_last_error", "dcg_set_syst
                     "dcg_server_device_bytes", "dcg_server_destroy", "dcg_read_mrconee", "dcg_free_mrconee",
                     "dcg_read_mdcint", "dcg_free_mdcint", "dcg_io_last_error", "dcg_ivo",
                     "dcg_autotune_mode", "dcg_autotune_entries", "dcg_set_autotune_trials",
+                    "dcg_set_merge_reductions", "dcg_merged_reduction_stats",
                     "dcg_casci_energy_check"]
 FAMILIES = {"none": 0, "transform": 1, "hstream": 2, "rdm": 3, "scatter": 4, "eig": 5, "eig_tri": 6,
             "eig_val": 7, "eig_vec": 8, "eig_back": 9, "split_mma": 10}
@@ -796,6 +799,15 @@ class Caspt2Session:
         return Caspt2Result(casci_energies=eig, ndet=ndet, e2=e2, sumc2=sc2, e0=e0, total_energy=et,
                             stage_ms=self.stage_ms(), kernel_launches=self.kernel_launches(),
                             e2_sym=self.caspt2_irreps()[0])
+
+
+def merged_reduction_stats(device: int = 0) -> Dict[str, int]:
+    """dcg_merged_reduction_stats: joint cooperative launches of the serving slots' reductions."""
+    out = np.zeros(3, np.int64)
+    rc = load_library().dcg_merged_reduction_stats(device, out.ctypes.data)
+    if rc != 0:
+        raise DcgError(rc, "dcg_merged_reduction_stats")
+    return {"launches": int(out[0]), "joint_launches": int(out[1]), "submissions": int(out[2])}
 
 
 def footprint_estimate(bufs: "HostBuffers") -> int:

@@ -16,7 +16,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libdcaspt2_gb300.so")
 SOURCES = ["dcg_linalg.cu", "dcg_eig.cu", "dcg_split.cu", "dcg_ci.cu", "dcg_ints.cu", "dcg_pt2.cu", "dcg_api.cu",
            "dcg_serve.cu", "dcg_davidson.cu",
-           "dcg_chol.cu", "dcg_mdcint.cu", "dcg_ivo.cu", "dcg_tune.cu", "dcg_files.cpp"]
+           "dcg_chol.cu", "dcg_band.cu", "dcg_mdcint.cu", "dcg_ivo.cu", "dcg_tune.cu", "dcg_files.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
          "--expt-relaxed-constexpr", "-Xptxas", "-O3"]

@@ -434,6 +434,10 @@ static bool tridiag_e2_pays(int dimm, int nouter) { return dimm <= kTridiagE2Max
 // VC: dimm x nouter), as the reference's solve_X_subspace evaluates them.
 static void e2_from_bprime(Context &c, int dimm, cplx *Bp, const cplx *VC, int nouter, const double *alpha,
                            double *e2o, double *sco) {
+    if (tridiag_e2_pays(dimm, nouter) && band_e2_pays(dimm, nouter)) {   // band form, banded solves
+        band_e2(c, 0, dimm, Bp, dimm, VC, dimm, nouter, alpha, e2o, sco);
+        return;
+    }
     if (tridiag_e2_pays(dimm, nouter)) {
         EigJob e;
         e.n = dimm;
@@ -531,6 +535,7 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
         std::vector<double *> ws(np), wb(np, nullptr), red(np);
         std::vector<cplx *> X(np, nullptr), Bp(np, nullptr);
         std::vector<int> dimm(np, 0);
+        std::vector<bool> band(np, false);
         // S: eigenvalues together, then each block's cutoff, kept vectors and B'
         std::vector<EigJob> es;
         for (size_t j = 0; j < np; j++) {
@@ -587,6 +592,10 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
                   1);
             herm_from_upper(c, dimm[j], Bp[j], dimm[j]);
             wb[j] = wsget<double>(c, nm("bj.wb", j), dimm[j]);
+            if (tridiag_e2_pays(dimm[j], b.nouter) && band_e2_pays(dimm[j], b.nouter)) {
+                band[j] = true;   // E2 from its band form below, no tridiagonal reduction
+                continue;
+            }
             EigJob e;
             e.n = dimm[j];
             e.A = Bp[j];
@@ -609,7 +618,11 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
             const int m = dimm[j];
             e2o[j] = wsget<double>(c, nm("bj.e2o", j), b.nouter);
             sco[j] = wsget<double>(c, nm("bj.sco", j), b.nouter);
-            if (tridiag_e2_pays(m, b.nouter)) {
+            if (band[j]) {
+                cplx *VC = wsget<cplx>(c, nm("bj.VC", j), (size_t)m * b.nouter);
+                zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, X[j], b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
+                band_e2(c, (int)j, m, Bp[j], m, VC, m, b.nouter, b.alpha, e2o[j], sco[j]);
+            } else if (tridiag_e2_pays(m, b.nouter)) {
                 cplx *VC = wsget<cplx>(c, nm("bj.VC", j), (size_t)m * b.nouter);
                 zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, X[j], b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
                 TE2Job t;
@@ -994,7 +1007,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         std::vector<double *> wk(np), wb(np, nullptr), red(np);
         std::vector<int> vlo(np, 0), dimm(np, 0);
         std::vector<EigJob> ek;
-        std::vector<bool> chol(np, false);
+        std::vector<bool> chol(np, false), band(np, false);
         std::vector<cplx *> Kc(np, nullptr);
         for (size_t j = 0; j < np; j++) {   // metrics, and (AUTO) their definiteness above the cutoff
             GramJob &g = all[p0 + j];
@@ -1079,6 +1092,10 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             bprime_product(c, Mp, dm, P[j], PD, Bp[j]);   // P^H D P
             herm_from_upper(c, dm, Bp[j], dm);
             wb[j] = wsget<double>(c, nm("gj.wb", j), dm);
+            if (tridiag_e2_pays(dm, g.nouter) && band_e2_pays(dm, g.nouter)) {
+                band[j] = true;   // E2 from its band form below, no tridiagonal reduction
+                continue;
+            }
             EigJob e;
             e.n = dm;
             e.A = Bp[j];
@@ -1100,7 +1117,9 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             const int dm = dimm[j];
             e2o[j] = wsget<double>(c, nm("gj.e2o", j), g.nouter);
             sco[j] = wsget<double>(c, nm("gj.sco", j), g.nouter);
-            if (tridiag_e2_pays(dm, g.nouter)) {
+            if (band[j]) {
+                band_e2(c, (int)(16 + j), dm, Bp[j], dm, VC0[j], dm, g.nouter, g.alpha, e2o[j], sco[j]);
+            } else if (tridiag_e2_pays(dm, g.nouter)) {
                 TE2Job t;
                 t.slot = (int)(16 + j);
                 t.n = dm;
@@ -2014,6 +2033,18 @@ int dcg_casci_energy_check(dcg_ctx *ctx, double out[8]) {
         dcg::e0test(c_, out);
         return DCG_OK;
     });
+}
+
+int dcg_set_merge_reductions(dcg_ctx *ctx, int32_t on) {
+    if (!ctx) return DCG_E_ARG;
+    ctx->c.merge_reductions = on != 0;
+    return DCG_OK;
+}
+
+int dcg_merged_reduction_stats(int device, int64_t out[3]) {
+    if (!out) return DCG_E_ARG;
+    dcg::coop_merge_stats(device, out);
+    return DCG_OK;
 }
 
 int dcg_set_autotune_trials(dcg_ctx *ctx, int32_t on) {

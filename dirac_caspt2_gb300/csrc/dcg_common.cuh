@@ -98,6 +98,9 @@ struct Context {
     // pipeline waits of the tensor-core GEMM), ns; 0 = each kernel's default (dcg_set_wait_limit)
     uint64_t wait_limit_ns = 0;
     bool tune_trials = true;     // may run autotuner trials (off for serving slots)
+    // hand batched tridiagonal reductions to the device's batcher, which merges those of all
+    // contexts that set it into joint cooperative launches (on for serving slots)
+    bool merge_reductions = false;
     void *dev_state = nullptr;   // device-side system state (owned, see dcg_api.cu)
 
     // ---- per-family kernel timing (dcg_time_family)
@@ -373,6 +376,18 @@ constexpr int kTridiagE2MaxN = 1024;
 void tridiag_e2(Context &c, int slot, int n, const cplx *A, int64_t lda, const cplx *VC, int64_t ldvc, int nouter,
                 const double *alpha, double *e2o, double *sco);
 
+// The same E2 terms from a band form: B' (n x n, both triangles, destroyed) reduced to a Hermitian
+// matrix of lower bandwidth kBandNB by blocked Householder panels (FP64 GEMM trailing updates),
+// y_o = Q^H VC[:, o], then one banded solve with partial pivoting per outer index (dcg_band.cu).
+// band_e2_pays: whether B' of dimension n with nouter outer indices takes it: only when the
+// environment variable DCG_BPRIME_ROUTE = band asks for it (measured slower than the
+// tridiagonal form on GB300, see dcg_band.cu; kBandMinN is the size it was measured from).
+constexpr int kBandNB = 16;
+constexpr int kBandMinN = 256;
+bool band_e2_pays(int n, int nouter);
+void band_e2(Context &c, int slot, int n, cplx *A, int64_t lda, const cplx *VC, int64_t ldvc, int nouter,
+             const double *alpha, double *e2o, double *sco);
+
 // heev_vectors_slot and tridiag_e2 calls of distinct slots, overlapped on the auxiliary
 // streams (vector jobs above 1024 rows share the blocked back-transformation's workspace and
 // run first, on the context stream).  The family timers see the overlapped group once.
@@ -405,6 +420,10 @@ void zherk_upper(Context &c, int n, int k, const cplx *A, int64_t lda, cplx *C, 
 // Hermitian fill from the upper triangle (ZHEEV uplo='U' semantics): A(j,i) = conj(A(i,j))
 // for i < j, Im A(i,i) = 0.
 void herm_from_upper(Context &c, int n, cplx *A, int64_t lda);
+
+// Joint-launch counters of the merged tridiagonal reductions on a device (dcg_eig.cu): launches,
+// launches that carried more than one context's submission, submissions carried.
+void coop_merge_stats(int device, int64_t out[3]);
 
 // deterministic sum of n doubles on the device into *out (device)
 void dsum(Context &c, const double *x, int64_t n, double *out);

@@ -24,6 +24,10 @@
 #include <cstdio>
 #include <mutex>
 
+#include <condition_variable>
+#include <deque>
+#include <map>
+
 #include "dcg_common.cuh"
 
 namespace dcg {
@@ -550,14 +554,13 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
         // cannot overwrite what a slower block still reads for column k.
         if (!wait_published(gb, (unsigned)(k + 1))) return;
         cplx *pb = pbuf + (size_t)(k & 1) * (n + 1);
-        double2 *pt = part + (size_t)(k & 1) * (nb + 1);
+        double2 *pt = part + (size_t)(k & 1) * (n + 1);   // per-column terms conj(p_j) v_j
         const cplx t = ldcg(tau + k);
         const bool active = (t.x != 0.0 || t.y != 0.0);
         for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sv[r] = ldcg(A + r + (int64_t)k * lda);
         __syncthreads();
         // first owned column index > k
         const int c0 = k + 1 > b ? (k + 1 - b + (int)nb - 1) / (int)nb : 0;
-        double pr = 0.0, pim = 0.0;
         if (active) {
             for (int c = c0 + wib; c < nown; c += nwb) {
                 const int j = b + c * (int)nb;
@@ -576,17 +579,16 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
                     const cplx xp = cmul(t, mk(ar, ai));
                     pb[j] = xp;
                     const cplx xv = cmul(cconj(xp), sv[j]);
-                    pr += xv.x;
-                    pim += xv.y;
+                    pt[j] = make_double2(xv.x, xv.y);
                 }
             }
         }
-        eig_block_sum2(pr, pim, red);
-        if (threadIdx.x == 0) pt[b] = make_double2(pr, pim);
         if (!grid_barrier(gb, nb)) return;
         if (active) {
+            // p^H v summed over the columns in a fixed order (thread stride, then the block
+            // sum): the same bits whatever the number of blocks reducing this matrix
             double sr = 0.0, si = 0.0;
-            for (unsigned q = threadIdx.x; q < nb; q += blockDim.x) {
+            for (int q = k + 1 + threadIdx.x; q < n; q += blockDim.x) {
                 const double2 v = __ldcg(pt + q);
                 sr += v.x;
                 si += v.y;
@@ -1323,19 +1325,28 @@ static double trd_cost(int n, int nb) {
     return 4.0 * (double)n * n * n / (nb * 4.0e9) + 1.4 * n * (3.0e-6 + 0.02e-6 * nb);   // one barrier + one signal
 }
 
-static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
-    std::lock_guard<std::mutex> coop(g_coop_mutex);
-    const int sms = std::max(1, c.num_sms);
+static size_t trd_bytes_for(int n, int nbk) { return (size_t)(((n + nbk - 1) / nbk) + 2) * n * sizeof(cplx); }
+
+// Shared-memory limit of one block of the batched kernel (its static shared memory aside).
+static size_t trd_smem_limit(const Context &c) {
     int optin = 0;
     DCG_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, c.device));
-    const size_t limit = (size_t)std::max(0, optin - 1024);   // static shared memory of the kernel
-    auto bytes_for = [](int n, int nbk) { return (size_t)(((n + nbk - 1) / nbk) + 2) * n * sizeof(cplx); };
-    int total = 0;
+    return (size_t)std::max(0, optin - 1024);
+}
+
+// Block groups of one batched launch: every job gets the fewest blocks whose shared memory holds
+// its columns, then the remaining SMs go one by one to the job that is currently the slowest
+// and that they help (trd_cost); b0 and the largest block's shared memory follow.  False when
+// the jobs do not fit one launch.
+static bool trd_plan(const Context &c, std::vector<TrdJob> &jobs, int &total, size_t &smem) {
+    const int sms = std::max(1, c.num_sms);
+    const size_t limit = trd_smem_limit(c);
+    total = 0;
     for (TrdJob &j : jobs) {
         if (j.n > kTridiagSmemMaxN) return false;
         int nb = 1;
-        while (nb < std::min(sms, j.n) && bytes_for(j.n, nb) > limit) nb++;
-        if (bytes_for(j.n, nb) > limit) return false;
+        while (nb < std::min(sms, j.n) && trd_bytes_for(j.n, nb) > limit) nb++;
+        if (trd_bytes_for(j.n, nb) > limit) return false;
         j.nb = nb;
         total += nb;
     }
@@ -1356,29 +1367,179 @@ static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
         jobs[best].nb++;
         total++;
     }
-    size_t smem = 0;
+    smem = 0;
     int b0 = 0;
     for (TrdJob &j : jobs) {
-        smem = std::max(smem, bytes_for(j.n, j.nb));
+        smem = std::max(smem, trd_bytes_for(j.n, j.nb));
         j.b0 = b0;
         b0 += j.nb;
     }
-    DCG_CUDA(cudaFuncSetAttribute(tridiag_smem_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    DCG_CUDA(cudaFuncSetAttribute(tridiag_smem_batched_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)limit));
     int per_sm = 0;
     DCG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, tridiag_smem_batched_kernel, TRD_THREADS, smem));
-    if (per_sm < 1 || total > per_sm * sms) return false;
-    for (size_t q = 0; q < jobs.size(); q++) gridbar_reset(c, jobs[q].gb);
-    TrdJob *dj = wsget<TrdJob>(c, "trd.jobs", jobs.size());
-    DCG_CUDA(cudaMemcpyAsync(dj, jobs.data(), jobs.size() * sizeof(TrdJob), cudaMemcpyHostToDevice, c.stream));
+    return per_sm >= 1 && total <= per_sm * sms;
+}
+
+// The cooperative launch of planned jobs on `stream` (their barriers already reset in stream
+// order), then their barrier error flags, read back after the launch completes.
+static std::vector<GridBar> trd_launch(Context &c, std::vector<TrdJob> &jobs, int total, size_t smem,
+                                       cudaStream_t stream, const char *table) {
+    TrdJob *dj = wsget<TrdJob>(c, table, jobs.size());
+    DCG_CUDA(cudaMemcpyAsync(dj, jobs.data(), jobs.size() * sizeof(TrdJob), cudaMemcpyHostToDevice, stream));
     int nj = (int)jobs.size();
     void *args[] = {&dj, &nj};
     DCG_CUDA(cudaLaunchCooperativeKernel((const void *)tridiag_smem_batched_kernel, dim3(total), dim3(TRD_THREADS),
-                                         args, smem, c.stream));
-    DCG_LAUNCHED(c);
+                                         args, smem, stream));
+    DCG_CUDA(cudaGetLastError());
     std::vector<GridBar> hb(jobs.size());
     for (size_t q = 0; q < jobs.size(); q++)
-        DCG_CUDA(cudaMemcpyAsync(&hb[q], jobs[q].gb, sizeof(GridBar), cudaMemcpyDeviceToHost, c.stream));
-    DCG_CUDA(cudaStreamSynchronize(c.stream));
+        DCG_CUDA(cudaMemcpyAsync(&hb[q], jobs[q].gb, sizeof(GridBar), cudaMemcpyDeviceToHost, stream));
+    DCG_CUDA(cudaStreamSynchronize(stream));
+    return hb;
+}
+
+// ---- merging the reductions of several contexts (the serving loop's slots)
+// A context with merge_reductions set hands its batched reduction to a per-device batcher
+// instead of launching it.  The first waiting thread that finds the batcher idle becomes the
+// leader: it takes, in arrival order, the submissions whose jobs fit one launch together, makes
+// a batcher stream wait for each submission's ready event, launches them as one cooperative
+// kernel (each job its own block group and barrier) and hands every submission its result.
+// Requests that run concurrently then overlap their barrier-bound column loops inside one kernel
+// instead of queueing on the cooperative-launch lock.  The block-group sizes change with the
+// company, the arithmetic of a job does not: its partial sums do not depend on the number of
+// blocks reducing it, so a matrix gets the same bits alone and merged.
+struct CoopSub {
+    Context *c = nullptr;
+    std::vector<TrdJob> jobs;
+    cudaEvent_t ready = nullptr;
+    int state = 0;   // 0 waiting, 1 reduced, 2 does not fit a launch, 3 a wait timed out, 4 CUDA error
+    std::string msg;
+};
+
+struct CoopBatcher {
+    std::mutex mu;
+    std::condition_variable cv;
+    std::deque<CoopSub *> pending;
+    bool busy = false;
+    cudaStream_t stream = nullptr;
+    int64_t launches = 0, joint = 0, carried = 0;
+};
+
+static std::mutex g_batchers_mu;
+static std::map<int, CoopBatcher *> g_batchers;   // per device, for the life of the process
+
+static CoopBatcher &coop_batcher(int device) {
+    std::lock_guard<std::mutex> lk(g_batchers_mu);
+    CoopBatcher *&b = g_batchers[device];
+    if (!b) {
+        b = new CoopBatcher;
+        DCG_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    }
+    return *b;
+}
+
+// One joint launch of the taken submissions (leader thread, leader context's workspace).
+static void coop_run(Context &leader, CoopBatcher &B, std::vector<CoopSub *> &take) {
+    std::vector<TrdJob> all;
+    for (CoopSub *s : take) all.insert(all.end(), s->jobs.begin(), s->jobs.end());
+    try {
+        std::lock_guard<std::mutex> coop(g_coop_mutex);
+        int total = 0;
+        size_t smem = 0;
+        if (!trd_plan(leader, all, total, smem)) throw Error{DCG_E_CUDA, "merged reduction does not fit"};
+        for (CoopSub *s : take) DCG_CUDA(cudaStreamWaitEvent(B.stream, s->ready, 0));
+        const std::vector<GridBar> hb = trd_launch(leader, all, total, smem, B.stream, "trd.jobs.joint");
+        size_t q = 0;
+        for (CoopSub *s : take) {
+            bool err = false;
+            for (size_t k = 0; k < s->jobs.size(); k++, q++) err = err || hb[q].err != 0;
+            s->state = err ? 3 : 1;
+            s->c->launches++;
+        }
+        B.launches++;
+        if (take.size() > 1) B.joint++;
+        B.carried += (int64_t)take.size();
+    } catch (const Error &e) {
+        for (CoopSub *s : take) {
+            s->state = 4;
+            s->msg = e.msg;
+        }
+    }
+}
+
+static bool tridiag_smem_merged(Context &c, std::vector<TrdJob> &jobs) {
+    {   // a submission that cannot run even alone goes the unbatched way
+        std::vector<TrdJob> alone = jobs;
+        int total = 0;
+        size_t smem = 0;
+        if (!trd_plan(c, alone, total, smem)) return false;
+    }
+    for (TrdJob &j : jobs) gridbar_reset(c, j.gb);
+    CoopSub me;
+    me.c = &c;
+    me.jobs = jobs;
+    DCG_CUDA(cudaEventCreateWithFlags(&me.ready, cudaEventDisableTiming));
+    const cudaError_t er = cudaEventRecord(me.ready, c.stream);
+    if (er != cudaSuccess) {
+        cudaEventDestroy(me.ready);
+        throw Error{DCG_E_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(er)};
+    }
+    CoopBatcher &B = coop_batcher(c.device);
+    {
+        std::unique_lock<std::mutex> lk(B.mu);
+        B.pending.push_back(&me);
+        while (me.state == 0) {
+            if (B.busy) {
+                B.cv.wait(lk);
+                continue;
+            }
+            B.busy = true;
+            std::vector<CoopSub *> take;
+            std::vector<TrdJob> trial;
+            while (!B.pending.empty()) {
+                CoopSub *s = B.pending.front();
+                std::vector<TrdJob> t2 = trial;
+                t2.insert(t2.end(), s->jobs.begin(), s->jobs.end());
+                int total = 0;
+                size_t smem = 0;
+                bool fits = false;
+                try {
+                    fits = trd_plan(c, t2, total, smem);
+                } catch (const Error &) {
+                    fits = false;
+                }
+                if (!fits && !take.empty()) break;   // the rest waits for the next launch
+                B.pending.pop_front();
+                if (!fits) {                            // cannot run merged at all
+                    s->state = 2;
+                    continue;
+                }
+                take.push_back(s);
+                trial.swap(t2);
+            }
+            lk.unlock();
+            if (!take.empty()) coop_run(c, B, take);
+            lk.lock();
+            B.busy = false;
+            B.cv.notify_all();
+        }
+    }
+    cudaEventDestroy(me.ready);
+    if (me.state == 2) return false;
+    if (me.state == 3) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
+    if (me.state == 4) throw Error{DCG_E_CUDA, "merged tridiagonalisation: " + me.msg};
+    return true;
+}
+
+static bool tridiag_smem_batched(Context &c, std::vector<TrdJob> &jobs) {
+    if (c.merge_reductions) return tridiag_smem_merged(c, jobs);
+    std::lock_guard<std::mutex> coop(g_coop_mutex);
+    int total = 0;
+    size_t smem = 0;
+    if (!trd_plan(c, jobs, total, smem)) return false;
+    for (size_t q = 0; q < jobs.size(); q++) gridbar_reset(c, jobs[q].gb);
+    const std::vector<GridBar> hb = trd_launch(c, jobs, total, smem, c.stream, "trd.jobs");
+    c.launches++;
     for (const GridBar &g : hb)
         if (g.err) throw Error{DCG_E_NUMERIC, "tridiagonalisation: a grid barrier wait timed out"};
     return true;
@@ -1443,7 +1604,7 @@ void heev_values_batched(Context &c, const std::vector<EigJob> &jobs) {
             t.e = hw[q].e;
             t.tau = hw[q].tau;
             t.pbuf = wsget<cplx>(c, slot_name("trd.p", j.slot), 2 * ((size_t)j.n + 1));   // two parities
-            t.part = wsget<double2>(c, slot_name("trd.part", j.slot), 2 * ((size_t)std::max(1, c.num_sms) + 1));
+            t.part = wsget<double2>(c, slot_name("trd.part", j.slot), 2 * ((size_t)j.n + 1));   // two parities
             t.gb = wsget<GridBar>(c, slot_name("trd.bar", j.slot), 1);
             t.n = j.n;
             t.b0 = t.nb = 0;
@@ -1773,4 +1934,19 @@ const double *stedc(Context &c, int n, const double *d, const double *e, double 
     return Q;
 }
 
+}  // namespace dcg
+
+namespace dcg {
+// Joint-launch counters of the merged reductions on a device: launches, launches that carried
+// more than one context's submission, and submissions carried.
+void coop_merge_stats(int device, int64_t out[3]) {
+    out[0] = out[1] = out[2] = 0;
+    std::lock_guard<std::mutex> lk(g_batchers_mu);
+    auto it = g_batchers.find(device);
+    if (it == g_batchers.end()) return;
+    std::lock_guard<std::mutex> lb(it->second->mu);
+    out[0] = it->second->launches;
+    out[1] = it->second->joint;
+    out[2] = it->second->carried;
+}
 }  // namespace dcg

@@ -208,6 +208,9 @@ int dcg_server_create(int device, int precision, int32_t slots, int64_t hbm_budg
         // a served stream meets most shapes once: its slots use tuned entries and heuristics
         // and run no tuning trials of their own (they would sit in the requests' latency)
         dcg_set_autotune_trials(c, 0);
+        // the slots' Householder reductions run merged: requests solving at the same time share
+        // one cooperative launch (dcg_set_merge_reductions)
+        dcg_set_merge_reductions(c, 1);
         sv->ctx.push_back(c);
         sv->held.push_back(dcg_device_bytes(c));
     }

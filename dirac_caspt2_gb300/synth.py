@@ -54,6 +54,10 @@ CONFIGS = {
     "cas_20_12_300": SynthConfig(20, 12, 300, 6, name="cas_20_12_300"),
     # large single solve: 40 inactive, 14 active (8 e), 800 secondary
     "cas_40_14_800": SynthConfig(40, 14, 800, 8, name="cas_40_14_800"),
+    # the same active space and inactive count with 160 secondary spinors: every active-space
+    # structure of the large solve (3003 determinants, 2744-dimensional A and C blocks, Gram
+    # factors of 2002 rows) at a size the CPU oracle finishes in minutes
+    "cas_40_14_160": SynthConfig(40, 14, 160, 8, name="cas_40_14_160"),
 }
 
 

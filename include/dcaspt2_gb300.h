@@ -345,6 +345,19 @@ int64_t dcg_server_device_bytes(dcg_server *srv);
 /* Drop queued requests, finish the running ones, join the workers and free the contexts. */
 int dcg_server_destroy(dcg_server *srv);
 
+/* Merged eigensolver reductions.  A context with on != 0 hands its batched Householder
+ * reductions (the cooperative kernel that reduces the S, metric and B' matrices of a solve, the
+ * role of the ZHETRD inside the ZHEEV calls of diag.F90:66-128) to a per-device batcher: the
+ * submissions of all such contexts that wait at the same time run as one cooperative launch,
+ * each matrix with its own block group and barrier, so concurrent requests overlap their
+ * barrier-bound column loops instead of queueing for the GPU one after the other.  A matrix's
+ * result is the same bits alone and merged.  The serving slots set it; other contexts do not
+ * by default. */
+int dcg_set_merge_reductions(dcg_ctx *ctx, int32_t on);
+/* Counters of the merged reductions on `device` since the process started: out[0] launches,
+ * out[1] launches that carried more than one context's reductions, out[2] submissions carried. */
+int dcg_merged_reduction_stats(int device, int64_t out[3]);
+
 /* The CASCI check of e0test (e0test.F90:4-272, called by r4dcasci.F90:89) for the selected
  * root of the last dcg_casci: out[0..1] energyHF(1), energyHF(2) of the lowest
  * ninact + nelec spinors; out[2..5] energy 1..4 (inactive one- and two-electron, active

@@ -1,6 +1,7 @@
 """The serving loop (dcg_server_*) on the GPU: each request's result in a mix of concurrently
 running requests of different sizes equals the result of the same request solved alone in a
-fresh context (bit-identical; stated tolerance 1e-12 Eh), the HBM budget bounds what runs at
+fresh context (bit-identical; stated tolerance 1e-12 Eh), also when the Householder reductions
+of concurrent requests ran merged in joint cooperative launches, the HBM budget bounds what runs at
 once, oversize requests are refused, and the footprint estimate bounds a solve's device
 memory.  The systems come from the device generator (records resident in HBM); one of them is
 also checked against the oracle."""
@@ -51,6 +52,7 @@ def test_mix_equals_alone(stream, alone):
     """All requests queued at once on 4 slots (several run concurrently, on separate streams)."""
     from dirac_caspt2_gb300 import api
     prec, ref = alone
+    m0 = api.merged_reduction_stats(0)
     with api.Caspt2Server(0, prec, slots=4) as srv:
         for rep in range(2):   # the second pass reuses the slots' resident workspaces
             for k, s in enumerate(stream):
@@ -69,6 +71,10 @@ def test_mix_equals_alone(stream, alone):
                 assert r.status == 0
                 assert r.ndet == ref[k].ndet
                 assert _same(r, ref[k]) <= TOL_MIX, (k, _same(r, ref[k]))
+    # the slots' Householder reductions ran merged: some launches carried several requests
+    m1 = api.merged_reduction_stats(0)
+    assert m1["launches"] > m0["launches"]
+    assert m1["joint_launches"] > m0["joint_launches"]
 
 
 def test_budget_serialises(stream, gpu_lib):

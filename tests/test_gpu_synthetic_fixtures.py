@@ -1,5 +1,7 @@
 """The benchmark systems at their full sizes against committed oracle energies: the seeded
-synthetic 8/6/40 (4 electrons) and 20/12/300 (6 electrons) systems, whose CPU-oracle results
+synthetic 8/6/40 (4 electrons) and 20/12/300 (6 electrons) systems, and 40/14/160 (8 electrons:
+the active space and inactive count of the 40/14/800 large solve, 3003 determinants, with the
+secondary space cut to what the CPU oracle finishes in minutes), whose CPU-oracle results
 tests/golden/make_synthetic_fixtures.py stored in tests/golden/synthetic_<name>.json.  Both GPU
 paths, FP64 and split precision, are held to the stated targets: CASCI and every subspace's
 e2X within 1e-9 Eh, the total within 1e-8 Eh (sumc2,X within 1e-9)."""
@@ -17,7 +19,7 @@ TOL_SUB = 1e-9
 TOL_TOTAL = 1e-8
 
 
-@pytest.fixture(scope="module", params=["cas_8_6_40", "cas_20_12_300"])
+@pytest.fixture(scope="module", params=["cas_8_6_40", "cas_20_12_300", "cas_40_14_160"])
 def case(request):
     from dirac_caspt2_gb300 import api, synth
     ref = json.load(open(os.path.join(GOLDEN_DIR, f"synthetic_{request.param}.json")))
