@@ -412,9 +412,76 @@ def run_ours(args, cfg_name):
     torch.cuda.empty_cache()
     if args.serve_requests > 0:
         line["serve"] = serve_leg(args, local, world)
+    if args.large_config and world == 1:
+        line["large_solve"] = large_leg(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def large_leg(args, local):
+    """The large single solve (40 inactive, 14 active with 8 electrons, 800 secondary spinors;
+    650 M records, largest class about 16 GB), generated on the device with its records resident:
+    one split-precision solve after a warm-up solve, timed with CUDA events, then one plain FP64
+    solve of the same system (after its own warm-up unless args.large_fp64_cold), with the
+    largest per-subspace |dE2| between the two paths and the live rates of the kernel families
+    the size stresses (tensor-core GEMMs, H streaming, Householder reduction)."""
+    import torch
+    from dirac_caspt2_gb300 import api, synth, synth_device as sd
+    cfg = synth.CONFIGS[args.large_config]
+    t0 = time.perf_counter()
+    dsys = sd.make_system_device(cfg, f"cuda:{local}")
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    bufs = dsys.buffers()
+    sin = dsys.system_input()
+    peaks, src = _peaks()
+    out = {"workload": args.large_config, "ninact": cfg.ninact, "nact": cfg.nact, "nsec": cfg.nsec,
+           "nelec": cfg.nelec, "records": dsys.nrec, "record_gb": round(dsys.record_bytes / 1e9, 2),
+           "generate_s": round(gen_s, 1)}
+    res = {}
+    for name, prec in (("split", api.DCG_PREC_SPLIT), ("fp64", api.DCG_PREC_FP64)):
+        with api.Caspt2Session(local, prec) as ses:
+            strm = torch.cuda.ExternalStream(ses.stream_ptr, device=local)
+            ses.solve(sin, bufs=bufs)                       # warm-up: workspaces, tuner
+            fams = {}
+            for fam in (("split_mma", "hstream", "eig_tri") if name == "split" else ("hstream",)):
+                ses.time_family(fam)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(strm)
+                r = ses.solve(sin, bufs=bufs)
+                b.record(strm)
+                torch.cuda.synchronize()
+                f_ms, f_n, f_w = ses.family_stats()
+                ses.time_family("none")
+                if f_n:
+                    if fam == "hstream":
+                        ach = f_w / (f_ms * 1e-3) / 1e9
+                        fams[fam] = {"ms": f_ms, "achieved": ach, "unit": "GB/s", "frac": ach / peaks["hbm_gbs"]}
+                    elif fam == "split_mma":
+                        ach = f_w / (f_ms * 1e-3) / 1e12
+                        fams[fam] = {"ms": f_ms, "achieved": ach, "unit": "TFLOP/s",
+                                     "frac": ach / peaks["bf16_tflops_sustained"]}
+                    else:
+                        ach = f_w / (f_ms * 1e-3) / 1e12
+                        fams[fam] = {"ms": f_ms, "achieved": ach, "unit": "TFLOP/s",
+                                     "frac": ach / (152 * 4 * 2.070e-3)}
+            ms = a.elapsed_time(b)
+            res[name] = r
+            out[name] = {"ms_per_solve": ms, "solves_per_s": 1e3 / ms,
+                         "stage_ms": {k: round(v, 2) for k, v in r.stage_ms.items()},
+                         "total_energy": r.total_energy, "families": fams,
+                         "device_gb": round(ses.device_bytes() / 1e9, 1)}
+            ses.trim()
+        torch.cuda.empty_cache()
+    sp, fp = res["split"], res["fp64"]
+    out["max_abs_dE2_subspace"] = max(abs(sp.e2[k] - fp.e2[k]) for k in sp.e2)
+    out["abs_dE_total"] = abs(sp.total_energy - fp.total_energy)
+    out["abs_dE_casci"] = abs(sp.casci_energies[0] - fp.casci_energies[0])
+    out["peak_source"] = src
+    del bufs, dsys
+    torch.cuda.empty_cache()
+    return out
 
 
 def serve_leg(args, local, world):
@@ -493,6 +560,8 @@ def main():
                     help="requests of the served-stream leg (0 skips it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="mean Poisson arrival rate of the stream (1/s)")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the serving loop")
+    ap.add_argument("--large-config", default="cas_40_14_800",
+                    help="the large single solve reported beside the line ('' to skip)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args, args.config)

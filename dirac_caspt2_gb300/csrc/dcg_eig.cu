@@ -24,6 +24,7 @@
 #include <cstdio>
 #include <mutex>
 
+#include <chrono>
 #include <condition_variable>
 #include <deque>
 #include <map>
@@ -1485,15 +1486,22 @@ static bool tridiag_smem_merged(Context &c, std::vector<TrdJob> &jobs) {
         throw Error{DCG_E_CUDA, std::string("cudaEventRecord: ") + cudaGetErrorString(er)};
     }
     CoopBatcher &B = coop_batcher(c.device);
+    // merge window: a leader that finds no other submission waits this long for one
+    // (DCG_MERGE_WINDOW_US, default 0: launch at once)
+    const char *wenv = getenv("DCG_MERGE_WINDOW_US");
+    const long window_us = wenv ? std::max(0L, std::min(5000000L, atol(wenv))) : 0L;
     {
         std::unique_lock<std::mutex> lk(B.mu);
         B.pending.push_back(&me);
+        B.cv.notify_all();
         while (me.state == 0) {
             if (B.busy) {
                 B.cv.wait(lk);
                 continue;
             }
             B.busy = true;
+            if (window_us > 0 && B.pending.size() < 2)
+                B.cv.wait_for(lk, std::chrono::microseconds(window_us), [&] { return B.pending.size() >= 2; });
             std::vector<CoopSub *> take;
             std::vector<TrdJob> trial;
             while (!B.pending.empty()) {

@@ -71,10 +71,10 @@ def test_mix_equals_alone(stream, alone):
                 assert r.status == 0
                 assert r.ndet == ref[k].ndet
                 assert _same(r, ref[k]) <= TOL_MIX, (k, _same(r, ref[k]))
-    # the slots' Householder reductions ran merged: some launches carried several requests
+    # the slots' Householder reductions went through the batcher (whether two requests met in
+    # one launch depends on timing; tests/test_gpu_merge.py makes them meet)
     m1 = api.merged_reduction_stats(0)
     assert m1["launches"] > m0["launches"]
-    assert m1["joint_launches"] > m0["joint_launches"]
 
 
 def test_budget_serialises(stream, gpu_lib):
