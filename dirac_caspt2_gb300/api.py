@@ -26,6 +26,7 @@ LIB_PATH = os.path.join(_HERE, "libdcaspt2_gb300.so")
 
 DCG_PREC_FP64 = 0
 DCG_PREC_SPLIT = 1
+DCG_PREC_SPLIT_ACC = 2   # dcg_zgemm: the seven-slice split product
 CASCI_SOLVERS = {"auto": 0, "dense": 1, "davidson": 2}
 METRIC_SOLVERS = {"auto": 0, "eigen": 1}
 SUBSPACES = "ABCDEFGH"

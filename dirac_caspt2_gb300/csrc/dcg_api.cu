@@ -917,15 +917,48 @@ static void bprime_product(Context &c, int Mp, int dm, const cplx *P, const cplx
     }
 }
 
+// The three Gram-route products whose errors Lambda^-1 amplifies: the metric K = G G^H, G v and
+// P^H (G v).  On the split path they run on the tensor cores through the seven-slice product
+// (~2^-45 of row max x column max per term; the five-slice product, ~2^-36, moved e2c by
+// 1.2e-9 Eh on 20/12/300 when it carried K), otherwise in FP64.  DCG_GRAM_SPLIT_ACC=0 keeps them
+// in FP64 on the split path too.
+static bool gram_acc_split(const Context &c) {
+    if (c.precision != DCG_PREC_SPLIT) return false;
+    const char *e = getenv("DCG_GRAM_SPLIT_ACC");
+    return !(e && e[0] == '0');
+}
+// K = G G^H (Mp x Mp; at least the upper triangle, the caller mirrors it)
+static void gram_metric(Context &c, int Mp, int dimn, const cplx *G, cplx *K) {
+    if (gram_acc_split(c)) zgemm_split_acc(c, Mp, Mp, dimn, 1, G, 1, Mp, 0, G, Mp, 3, K, 1, Mp, 0, false);
+    else zherk_upper(c, Mp, dimn, G, Mp, K, Mp);
+}
+// GV = G Vsel (Mp x nouter)
+static void gram_gv(Context &c, int Mp, int nouter, int dimn, const cplx *G, const cplx *Vsel, cplx *GV) {
+    if (gram_acc_split(c)) {
+        zgemm_split_acc(c, Mp, nouter, dimn, 1, G, 1, Mp, 0, Vsel, dimn, 0, GV, 1, Mp, 0, false);
+    } else {
+        const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+        zgemm(c, OP_N, OP_N, Mp, nouter, dimn, one, G, Mp, 0, Vsel, dimn, 0, zero, GV, Mp, 0, 1);
+    }
+}
+// VC0 = P^H GV (dm x nouter), on the split path as its transpose GV^T conj(P)
+static void gram_phgv(Context &c, int dm, int nouter, int Mp, const cplx *P, const cplx *GV, cplx *VC0) {
+    if (gram_acc_split(c)) {
+        zgemm_split_acc(c, nouter, dm, Mp, 1, GV, Mp, 1, 0, P, Mp, 1, VC0, dm, 1, 0, false);
+    } else {
+        const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+        zgemm(c, OP_C, OP_N, dm, nouter, Mp, one, P, Mp, 0, GV, Mp, 0, zero, VC0, dm, 0, 1);
+    }
+}
+
 static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, const double *Dd, const cplx *Vsel,
                                  int nouter, const double *alpha) {
     BlockOut r;
     const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
     // K is the overlap metric itself: its small eigenvalues (down to the 1e-8 cutoff) set X through
-    // Lambda^-1, and a 2^-36-relative error in K moves their eigenvectors by |dK| / gap.  On the
-    // 20/12/300 system the split product shifted e2c by 1.2e-9 Eh, so K stays in FP64.
+    // Lambda^-1, and an error in K moves their eigenvectors by |dK| / gap (see gram_metric).
     cplx *K = wsget<cplx>(c, "gram.K", (size_t)Mp * Mp);
-    zherk_upper(c, Mp, dimn, G, Mp, K, Mp);
+    gram_metric(c, Mp, dimn, G, K);
     herm_from_upper(c, Mp, K, Mp);
     cplx *Kc = nullptr;
     if (c.metric_solver == DCG_METRIC_AUTO && nouter > 0) {   // kept for the Cholesky route
@@ -962,9 +995,9 @@ static BlockOut solve_gram_block(Context &c, int Mp, int dimn, const cplx *G, co
     heev_vectors_only(c, Mp, K, Mp, wk, vlo, Mp, P, Mp);
     // VC0 = Lambda^-1 P^H (G v)
     cplx *GV = wsget<cplx>(c, "gram.GV", (size_t)Mp * nouter);
-    zgemm(c, OP_N, OP_N, Mp, nouter, dimn, one, G, Mp, 0, Vsel, dimn, 0, zero, GV, Mp, 0, 1);
+    gram_gv(c, Mp, nouter, dimn, G, Vsel, GV);
     cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
-    zgemm(c, OP_C, OP_N, dimm, nouter, Mp, one, P, Mp, 0, GV, Mp, 0, zero, VC0, dimm, 0, 1);
+    gram_phgv(c, dimm, nouter, Mp, P, GV, VC0);
     launch_scale_rows(c, dimm, nouter, VC0, dimm, wk, vlo, true);
     // B' = P^H D P
     cplx *PD = wsget<cplx>(c, "gram.PD", (size_t)Mp * dimm);
@@ -1012,7 +1045,7 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
         for (size_t j = 0; j < np; j++) {   // metrics, and (AUTO) their definiteness above the cutoff
             GramJob &g = all[p0 + j];
             K[j] = wsget<cplx>(c, nm("gj.K", j), (size_t)g.Mp * g.Mp);
-            zherk_upper(c, g.Mp, g.dimn, g.G, g.Mp, K[j], g.Mp);   // K = G G^H, FP64 (the metric)
+            gram_metric(c, g.Mp, g.dimn, g.G, K[j]);   // K = G G^H (the metric)
             herm_from_upper(c, g.Mp, K[j], g.Mp);
             if (c.metric_solver == DCG_METRIC_AUTO && g.nouter > 0) {   // kept for the Cholesky route
                 Kc[j] = wsget<cplx>(c, nm("gj.Kc", j), (size_t)g.Mp * g.Mp);
@@ -1081,9 +1114,9 @@ static void solve_gram_jobs(Context &c, std::vector<GramJob> &all, double e2_sub
             GramJob &g = all[p0 + j];
             const int dm = dimm[j], Mp = g.Mp;
             cplx *GV = wsget<cplx>(c, nm("gj.GV", j), (size_t)Mp * g.nouter);
-            zgemm(c, OP_N, OP_N, Mp, g.nouter, g.dimn, one, g.G, Mp, 0, g.Vsel, g.dimn, 0, zero, GV, Mp, 0, 1);
+            gram_gv(c, Mp, g.nouter, g.dimn, g.G, g.Vsel, GV);
             VC0[j] = wsget<cplx>(c, nm("gj.VC0", j), (size_t)dm * g.nouter);
-            zgemm(c, OP_C, OP_N, dm, g.nouter, Mp, one, P[j], Mp, 0, GV, Mp, 0, zero, VC0[j], dm, 0, 1);
+            gram_phgv(c, dm, g.nouter, Mp, P[j], GV, VC0[j]);
             launch_scale_rows(c, dm, g.nouter, VC0[j], dm, wk[j], vlo[j], true);   // Lambda^-1 P^H G v
             cplx *PD = wsget<cplx>(c, nm("gj.PD", j), (size_t)Mp * dm);
             DCG_CUDA(cudaMemcpyAsync(PD, P[j], sizeof(cplx) * (size_t)Mp * dm, cudaMemcpyDeviceToDevice, c.stream));
@@ -1206,7 +1239,7 @@ static void run_blocks(SubCtx &sc, char sub, const cplx *V, std::vector<BlockSpe
                 cplx *G = wsget<cplx>(c, "gram.G", (size_t)Mp * b.dimn);
                 launch_gram(c, c.na, Mp, d_dets_p, sc.M, sc.Y, ind, b.dimn, sub == 'A' ? 1 : 0, G);
                 cplx *K = wsget<cplx>(c, "gram.Kcount", (size_t)Mp * Mp);
-                zherk_upper(c, Mp, b.dimn, G, Mp, K, Mp);
+                gram_metric(c, Mp, b.dimn, G, K);
                 sym_record(c, sub - 'A', b.isym, 0.0, 0.0, kept_count(c, Mp, K, Mp));
                 continue;
             }
@@ -2100,16 +2133,21 @@ int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int3
               int64_t a_sk, int64_t a_sb, const void *B, int64_t ldb, int32_t conj_b, void *C, int64_t c_si,
               int64_t c_sj, int64_t c_sb, int32_t accumulate) {
     if (M < 0 || N < 0 || K < 0 || batch < 0 || (M * (int64_t)N * batch > 0 && (!A || !B || !C))) return DCG_E_ARG;
-    if (precision != DCG_PREC_FP64 && precision != DCG_PREC_SPLIT) return DCG_E_ARG;
+    if (precision != DCG_PREC_FP64 && precision != DCG_PREC_SPLIT && precision != DCG_PREC_SPLIT_ACC)
+        return DCG_E_ARG;
     DCG_API_BODY(ctx, {
         if ((int64_t)M * N * batch == 0) return DCG_OK;
         const dcg::cplx *a = static_cast<const dcg::cplx *>(A);
         const dcg::cplx *b = static_cast<const dcg::cplx *>(B);
         dcg::cplx *cc = static_cast<dcg::cplx *>(C);
-        if (precision == DCG_PREC_SPLIT) {
+        if (precision == DCG_PREC_SPLIT || precision == DCG_PREC_SPLIT_ACC) {
             dcg::split_reset(c_);
-            dcg::zgemm_split(c_, M, N, K, batch, a, a_si, a_sk, a_sb, b, ldb, conj_b ? 1 : 0, cc, c_si, c_sj, c_sb,
-                             accumulate != 0, c_.split_lbo, c_.split_sbo);
+            if (precision == DCG_PREC_SPLIT)
+                dcg::zgemm_split(c_, M, N, K, batch, a, a_si, a_sk, a_sb, b, ldb, conj_b ? 1 : 0, cc, c_si, c_sj, c_sb,
+                                 accumulate != 0, c_.split_lbo, c_.split_sbo);
+            else
+                dcg::zgemm_split_acc(c_, M, N, K, batch, a, a_si, a_sk, a_sb, b, ldb, conj_b ? 1 : 0, cc, c_si, c_sj,
+                                     c_sb, accumulate != 0);
             if (dcg::split_error(c_)) throw(Error{DCG_E_NUMERIC, "split GEMM: a pipeline wait timed out"});
         } else {
             if (a_si != 1 || c_si != 1) throw(Error{DCG_E_ARG, "FP64 dcg_zgemm needs column-major A and C"});

@@ -67,29 +67,30 @@ __device__ __forceinline__ int sp_exponent_bits(long long mb) {
 }
 __device__ __forceinline__ long long sp_absbits(double x) { return __double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFll; }
 
-// The SPLIT_S pre-scaled slices of x 2^-e (|x| <= 2^e): X = round(x 2^(35-e)) as a signed
-// integer, cut into balanced base-128 digits d_0..d_4 (|d_0| <= 128, others <= 64);
-// out[p] = d_p 2^(-7p), so that x 2^-e = 2^-7 sum_p out[p] up to 2^-36.
-__device__ __forceinline__ void sp_slices(double x, int e, __nv_bfloat16 out[SPLIT_S]) {
+// The S pre-scaled slices of x 2^-e (|x| <= 2^e): X = round(x 2^(7S-e)) as a signed integer,
+// cut into balanced base-128 digits d_0..d_{S-1} (|d_0| <= 128, others <= 64);
+// out[p] = d_p 2^(-7p), so that x 2^-e = 2^-7 sum_p out[p] up to 2^-(7S+1).  S = 5 for the
+// transformation products, S = 7 for the products that feed the metric's inverse.
+template <int S>
+__device__ __forceinline__ void sp_slices(double x, int e, __nv_bfloat16 out[S]) {
     const long long bits = __double_as_longlong(x);
     const int ex = (int)((bits >> 52) & 0x7FF);
     long long X = 0;
     if (ex != 0) {
         const long long mant = (bits & ((1ll << 52) - 1)) | (1ll << 52);   // |x| = mant 2^(ex-1075)
-        const int sh = ex - 1075 + 35 - e;
+        const int sh = ex - 1075 + SPLIT_BITS * S - e;
         if (sh >= 0) X = mant << sh;                                        // only when |x| ~ 2^e and tiny mantissa
         else if (sh > -54) X = (mant + (1ll << (-sh - 1))) >> (-sh);
         if (bits < 0) X = -X;
     }
 #pragma unroll
-    for (int p = 0; p < SPLIT_S - 1; p++) {
-        const int sft = SPLIT_BITS * (SPLIT_S - 1 - p);
+    for (int p = 0; p < S - 1; p++) {
+        const int sft = SPLIT_BITS * (S - 1 - p);
         const long long d = (X + (1ll << (sft - 1))) >> sft;
         X -= d << sft;
         out[p] = __float2bfloat16_rn(__int2float_rn((int)d) * __int_as_float((127 - SPLIT_BITS * p) << 23));
     }
-    out[SPLIT_S - 1] = __float2bfloat16_rn(__int2float_rn((int)X) *
-                                           __int_as_float((127 - SPLIT_BITS * (SPLIT_S - 1)) << 23));
+    out[S - 1] = __float2bfloat16_rn(__int2float_rn((int)X) * __int_as_float((127 - SPLIT_BITS * (S - 1)) << 23));
 }
 
 // Row exponents of the large operand: element (i, k) of batch z at A[z*sb + i*si + k*sk].
@@ -124,6 +125,7 @@ __global__ void sp_rowexp_kernel(int M, int K, const cplx *__restrict__ A, int64
 
 // A slices in tiles: tile (p, z, rb, ks) at ((p*nz + z)*nrb + rb)*nks + ks, 4 KB each.
 // One thread per (row, group of 4 complex k) writes one 16-byte core-matrix row per slice.
+template <int S>
 __global__ void sp_slice_a_kernel(int M, int K, const cplx *__restrict__ A, int64_t si, int64_t sk, int64_t sb,
                                   const int *__restrict__ eexp, int nz, int nrb, int nks, __nv_bfloat16 *As) {
     const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -132,7 +134,7 @@ __global__ void sp_slice_a_kernel(int M, int K, const cplx *__restrict__ A, int6
     const int64_t rows = (int64_t)nrb * SP_TM;
     if (idx >= rows * ng) return;
     const int i = (int)(idx % rows), g = (int)(idx / rows);
-    __align__(16) __nv_bfloat16 sl[SPLIT_S][8];
+    __align__(16) __nv_bfloat16 sl[S][8];
     if (i < M) {
         const int e = eexp[(int64_t)z * M + i];
         const cplx *a = A + (int64_t)z * sb + (int64_t)i * si;
@@ -141,24 +143,24 @@ __global__ void sp_slice_a_kernel(int M, int K, const cplx *__restrict__ A, int6
             const int k = g * 4 + c;
             cplx v = mk(0.0, 0.0);
             if (k < K) v = a[(int64_t)k * sk];
-            __nv_bfloat16 re[SPLIT_S], im[SPLIT_S];
-            sp_slices(v.x, e, re);
-            sp_slices(v.y, e, im);
+            __nv_bfloat16 re[S], im[S];
+            sp_slices<S>(v.x, e, re);
+            sp_slices<S>(v.y, e, im);
 #pragma unroll
-            for (int p = 0; p < SPLIT_S; p++) {
+            for (int p = 0; p < S; p++) {
                 sl[p][2 * c] = re[p];
                 sl[p][2 * c + 1] = im[p];
             }
         }
     } else {
 #pragma unroll
-        for (int p = 0; p < SPLIT_S; p++)
+        for (int p = 0; p < S; p++)
 #pragma unroll
             for (int q = 0; q < 8; q++) sl[p][q] = __float2bfloat16_rn(0.0f);
     }
     const int rb = i / SP_TM, r = i % SP_TM;
     const int ks = g / (SP_TK / 8), kk = (g % (SP_TK / 8)) * 8;
-    for (int p = 0; p < SPLIT_S; p++) {
+    for (int p = 0; p < S; p++) {
         const int64_t tile = (((int64_t)p * nz + z) * nrb + rb) * nks + ks;
         char *dst = reinterpret_cast<char *>(As) + tile * SP_TILE_BYTES + sp_tile_off(r, kk);
         *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(sl[p]);
@@ -168,6 +170,7 @@ __global__ void sp_slice_a_kernel(int M, int K, const cplx *__restrict__ A, int6
 // B' slices (N'-major tiles: tile (q, nb, ks) at (q*nnb + nb)*nks + ks) and column exponents.
 // op(B)(k, j) = B[k + j ldb], or B[j + k ldb] when opb & 2 (B stored transposed), conjugated
 // when opb & 1.  One block per complex column j.
+template <int S>
 __global__ void sp_slice_b_kernel(int K, int N, const cplx *__restrict__ B, int64_t ldb, int opb, int nnb, int nks,
                                   __nv_bfloat16 *Bs, int *fexp) {
     __shared__ long long red[32];
@@ -199,14 +202,14 @@ __global__ void sp_slice_b_kernel(int K, int N, const cplx *__restrict__ B, int6
         // column 2j: (Re, -Im) down the real rows; column 2j+1: (Im, Re)
         const double c0 = part == 0 ? v.x : -v.y;
         const double c1 = part == 0 ? v.y : v.x;
-        __nv_bfloat16 s0[SPLIT_S], s1[SPLIT_S];
-        sp_slices(c0, f, s0);
-        sp_slices(c1, f, s1);
+        __nv_bfloat16 s0[S], s1[S];
+        sp_slices<S>(c0, f, s0);
+        sp_slices<S>(c1, f, s1);
         const int ks = kr / SP_TK, kk = kr % SP_TK;
         for (int col = 0; col < 2; col++) {
             const int jr = 2 * j + col;
             const int nb = jr / SP_TN, r = jr % SP_TN;
-            for (int q = 0; q < SPLIT_S; q++) {
+            for (int q = 0; q < S; q++) {
                 const int64_t tile = ((int64_t)q * nnb + nb) * nks + ks;
                 __nv_bfloat16 *dst = reinterpret_cast<__nv_bfloat16 *>(reinterpret_cast<char *>(Bs) +
                                                                        tile * SP_TILE_BYTES + sp_tile_off(r, kk));
@@ -680,6 +683,160 @@ __global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_persist_kernel(SplitArg
     }
 }
 
+// ------------------------------------------------------------------------- accurate form
+// The same product with SPA_S = 7 slices per operand (49 bits), for the contractions whose
+// errors the metric's inverse amplifies (the Gram metric K = G G^H, G v and P^H (G v) of the A
+// and C blocks): the products with p + q <= 6 (28 of 49) go to five TMEM accumulators of 64
+// columns by weight p + q = 0, 1, 2, 3 and >= 4.  The first three are exact (integer partial
+// sums below 2^24 for K' <= 1024 real); the weight-3 group holds terms 2^-21 of the leading one
+// and the last 2^-28, so their FP32 rounding is ~2^-45 of the result, the same size as the
+// omitted products (weights >= 7, 2^-49 each).  The epilogue converts the five groups to FP64
+// and adds them smallest first.  Result: ~2^-45 of max|row of A| * max|column of B| per term.
+// One 128 x 64 output tile per CTA; producer, MMA issuer and epilogue warps as sp_gemm_kernel.
+constexpr int SPA_S = 7;
+constexpr int SPA_TN = 64;
+constexpr int SPA_GROUPS = 5;
+constexpr int SPA_STAGES = 4;
+constexpr int SPA_STAGE_BYTES = SPA_S * SP_TILE_BYTES + SPA_S * (SP_TILE_BYTES / 2);   // 42 KB
+constexpr int SPA_SMEM = SPA_STAGES * SPA_STAGE_BYTES + 1024;
+
+__global__ void __launch_bounds__(SP_THREADS, 1) sp_gemm_acc_kernel(SplitArgs a) {
+    extern __shared__ __align__(1024) unsigned char sp_raw[];
+    __shared__ __align__(8) uint64_t bar_full[SPA_STAGES], bar_empty[SPA_STAGES], bar_done;
+    __shared__ uint32_t s_tmem;
+    unsigned char *smem = reinterpret_cast<unsigned char *>((reinterpret_cast<uintptr_t>(sp_raw) + 1023) & ~(uintptr_t)1023);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int nnh = (2 * a.N + SPA_TN - 1) / SPA_TN;        // 64-column halves of the 128-column B tiles
+    const int rb = (int)(blockIdx.x / (unsigned)nnh);
+    const int nh = (int)(blockIdx.x % (unsigned)nnh);
+    const int nb = nh >> 1, half = nh & 1;
+    const int z = blockIdx.z;
+
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < SPA_STAGES; q++) {
+            mbar_init(&bar_full[q], 1);
+            mbar_init(&bar_empty[q], 1);
+        }
+        mbar_init(&bar_done, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {   // 5 groups x 64 columns used of a 512-column allocation (a power of two)
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s_tmem)),
+                     "r"(512));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;");
+    const uint32_t tmem = s_tmem;
+    const int nks = a.nks;
+    int issued = 0;
+
+    if (warp == 4) {
+        if (lane == 0) {   // producer: SPA_S A tiles (4 KB) and SPA_S B half-tiles (2 KB) per stage
+            for (int ks = 0; ks < nks; ks++) {
+                const int st_i = ks % SPA_STAGES;
+                if (ks >= SPA_STAGES &&
+                    !mbar_wait(&bar_empty[st_i], ((ks / SPA_STAGES) - 1) & 1, a.err, a.wait_ns))
+                    break;
+                issued = ks + 1;
+                unsigned char *st = smem + st_i * SPA_STAGE_BYTES;
+                mbar_expect_tx(&bar_full[st_i], SPA_STAGE_BYTES);
+                for (int p = 0; p < SPA_S; p++) {
+                    const int64_t ta = (((int64_t)p * a.nz + z) * a.nrb + rb) * nks + ks;
+                    bulk_g2s(st + p * SP_TILE_BYTES, reinterpret_cast<const char *>(a.As) + ta * SP_TILE_BYTES,
+                             SP_TILE_BYTES, &bar_full[st_i]);
+                    const int64_t tb = ((int64_t)p * a.nnb + nb) * nks + ks;
+                    bulk_g2s(st + SPA_S * SP_TILE_BYTES + p * (SP_TILE_BYTES / 2),
+                             reinterpret_cast<const char *>(a.Bs) + tb * SP_TILE_BYTES + half * (SP_TILE_BYTES / 2),
+                             SP_TILE_BYTES / 2, &bar_full[st_i]);
+                }
+            }
+        }
+    } else if (warp == 5) {
+        if (lane == 0) {   // MMA issuer: 28 products per K step, by weight p + q
+            for (int ks = 0; ks < nks; ks++) {
+                const int st_i = ks % SPA_STAGES;
+                if (!mbar_wait(&bar_full[st_i], (ks / SPA_STAGES) & 1, a.err, a.wait_ns)) break;
+                asm volatile("tcgen05.fence::after_thread_sync;");
+                const unsigned char *st = smem + st_i * SPA_STAGE_BYTES;
+                uint64_t da[SPA_S], db[SPA_S];
+#pragma unroll
+                for (int p = 0; p < SPA_S; p++) {
+                    da[p] = sp_desc(st + p * SP_TILE_BYTES, a.lbo, a.sbo);
+                    db[p] = sp_desc(st + SPA_S * SP_TILE_BYTES + p * (SP_TILE_BYTES / 2), a.lbo, a.sbo);
+                }
+#pragma unroll
+                for (int w = 0; w < SPA_S; w++) {
+                    const int g = w < SPA_GROUPS - 1 ? w : SPA_GROUPS - 1;
+#pragma unroll
+                    for (int p = 0; p <= w; p++) {
+                        // the first product into a group at the first K step overwrites it
+                        const bool first = ks == 0 && p == 0 && w < SPA_GROUPS;
+                        umma_f16_n64(tmem + (uint32_t)(g * SPA_TN), da[p], db[w - p], first ? 0u : 1u);
+                    }
+                }
+                umma_commit(&bar_empty[st_i]);
+            }
+            umma_commit(&bar_done);   // arrives once every MMA issued above has completed
+        }
+    } else {
+        // epilogue: warp w reads TMEM lanes 32w..32w+31 = tile rows
+        const bool ok = mbar_wait(&bar_done, 0, a.err, a.wait_ns);
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        if (ok) {
+            const int r = warp * 32 + lane;
+            const int64_t i = (int64_t)rb * SP_TM + r;
+            const bool row_ok = i < a.M;
+            const int e = row_ok ? a.eexp[(int64_t)z * a.M + i] : 0;
+            for (int c0 = 0; c0 < SPA_TN; c0 += 32) {
+                uint32_t g0[32], g1[32], g2[32], g3[32], g4[32];
+                const uint32_t base = tmem + ((uint32_t)(warp * 32) << 16) + c0;
+                SP_LD32(base + 0 * SPA_TN, g0);
+                SP_LD32(base + 1 * SPA_TN, g1);
+                SP_LD32(base + 2 * SPA_TN, g2);
+                SP_LD32(base + 3 * SPA_TN, g3);
+                SP_LD32(base + 4 * SPA_TN, g4);
+                asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+                if (!row_ok) continue;
+#pragma unroll
+                for (int q = 0; q < 32; q += 2) {
+                    const int jr = nh * SPA_TN + c0 + q;   // real column (even: Re)
+                    const int j = jr >> 1;
+                    if (j >= a.N) break;
+                    const int sc = e + a.fexp[j] - 2 * SPLIT_BITS;
+                    double v2[2];
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        double v = (double)__uint_as_float(g4[q + h]);
+                        v += (double)__uint_as_float(g3[q + h]);
+                        v += (double)__uint_as_float(g2[q + h]);
+                        v += (double)__uint_as_float(g1[q + h]);
+                        v += (double)__uint_as_float(g0[q + h]);
+                        v2[h] = scale_pow2(v, sc);
+                    }
+                    cplx val = mk(v2[0], v2[1]);
+                    cplx *dst = a.C + (int64_t)z * a.c_sb + i * a.c_si + (int64_t)j * a.c_sj;
+                    if (a.accumulate) val = cadd(val, *dst);
+                    *dst = val;
+                }
+            }
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;");
+    __syncthreads();
+    // after a wait gave up: copies in flight land and issued MMAs complete before TMEM is freed
+    if (warp == 4 && lane == 0)
+        for (int ks = issued - 1; ks >= 0 && ks >= issued - SPA_STAGES; ks--)
+            mbar_drain(&bar_full[ks % SPA_STAGES], (uint32_t)((ks / SPA_STAGES) & 1));
+    if (warp == 5 && lane == 0) mbar_drain(&bar_done, 0);
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+    }
+}
+
 // ------------------------------------------------------------------------- host driver
 // C = A * op(B) (+ C when accumulate), complex FP64 in and out, through the split path.
 // Large operand: element (i, k) of batch z at A[z*a_sb + i*a_si + k*a_sk], i < M, k < K.
@@ -731,10 +888,10 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     {
         const int64_t work = (int64_t)nrb * SP_TM * nks * (SP_TK / 8);
         dim3 g(grid1d(work, 256), batch);
-        sp_slice_a_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, eexp, batch, nrb, nks, As);
+        sp_slice_a_kernel<SPLIT_S><<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, eexp, batch, nrb, nks, As);
         DCG_LAUNCHED(c);
     }
-    sp_slice_b_kernel<<<N, 128, 0, c.stream>>>(K, N, B, ldb, opb, nnb, nks, Bs, fexp);
+    sp_slice_b_kernel<SPLIT_S><<<N, 128, 0, c.stream>>>(K, N, B, ldb, opb, nnb, nks, Bs, fexp);
     DCG_LAUNCHED(c);
     DCG_CUDA(cudaFuncSetAttribute(sp_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SP_SMEM));
     SplitArgs sa;
@@ -784,6 +941,91 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
         FamScope fs(c, DCG_FAM_SPLIT_MMA, tensor_work);
         launch(pick);
     }
+}
+
+// C = A * op(B) (+ C) as zgemm_split, through the accurate seven-slice kernel (~2^-45 of
+// max|row of A| * max|column of B| per term instead of ~2^-36).  No tuning: one kernel.
+void zgemm_split_acc(Context &c, int M, int N, int K, int batch, const cplx *A, int64_t a_si, int64_t a_sk,
+                     int64_t a_sb, const cplx *B, int64_t ldb, int opb, cplx *C, int64_t c_si, int64_t c_sj,
+                     int64_t c_sb, bool accumulate) {
+    if (M <= 0 || N <= 0 || batch <= 0) return;
+    if (batch > 65535) {
+        for (int z0 = 0; z0 < batch; z0 += 65535)
+            zgemm_split_acc(c, M, N, K, std::min(65535, batch - z0), A + z0 * a_sb, a_si, a_sk, a_sb, B, ldb, opb,
+                            C + z0 * c_sb, c_si, c_sj, c_sb, accumulate);
+        return;
+    }
+    const int kmax = SP_KMAX / 2;
+    if (K > kmax) {   // exact FP32 groups need K' <= SP_KMAX: chain K chunks through C
+        for (int k0 = 0; k0 < K; k0 += kmax) {
+            const int kc = std::min(kmax, K - k0);
+            zgemm_split_acc(c, M, N, kc, batch, A + k0 * a_sk, a_si, a_sk, a_sb, (opb & 2) ? B + k0 * ldb : B + k0,
+                            ldb, opb, C, c_si, c_sj, c_sb, accumulate || k0 > 0);
+        }
+        return;
+    }
+    if (K <= 0) {   // empty sum
+        if (!accumulate) {
+            const cplx zero = mk(0.0, 0.0);
+            zgemm(c, OP_N, OP_N, M, N, 0, zero, A, std::max<int64_t>(a_sk, 1), 0, B, std::max<int64_t>(ldb, 1), 0, zero,
+                  C, c_sj, c_sb, batch);
+        }
+        return;
+    }
+    GemmTrace trace(c, "split_acc", M, N, K, batch);
+    const int nks = (2 * K + SP_TK - 1) / SP_TK;
+    const int nrb = (M + SP_TM - 1) / SP_TM;
+    const int nnb = (2 * N + SP_TN - 1) / SP_TN;
+    const int nnh = (2 * N + SPA_TN - 1) / SPA_TN;
+    const size_t tiles_a = (size_t)SPA_S * batch * nrb * nks, tiles_b = (size_t)SPA_S * nnb * nks;
+    __nv_bfloat16 *As = wsget<__nv_bfloat16>(c, "splitacc.A", tiles_a * SP_TILE_BYTES / 2);
+    __nv_bfloat16 *Bs = wsget<__nv_bfloat16>(c, "splitacc.B", tiles_b * SP_TILE_BYTES / 2);
+    int *eexp = wsget<int>(c, "splitacc.e", (size_t)M * batch);
+    int *fexp = wsget<int>(c, "splitacc.f", (size_t)N);
+    int *err = wsget<int>(c, "split.err", 1);
+    DCG_CUDA(cudaMemsetAsync(Bs, 0, tiles_b * SP_TILE_BYTES, c.stream));
+    if (a_si == 1) {
+        dim3 g(grid1d(M, 256), batch);
+        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 1, eexp);
+    } else {
+        dim3 g(grid1d((int64_t)M * 32, 256), batch);
+        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 0, eexp);
+    }
+    DCG_LAUNCHED(c);
+    {
+        const int64_t work = (int64_t)nrb * SP_TM * nks * (SP_TK / 8);
+        dim3 g(grid1d(work, 256), batch);
+        sp_slice_a_kernel<SPA_S><<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, eexp, batch, nrb, nks, As);
+        DCG_LAUNCHED(c);
+    }
+    sp_slice_b_kernel<SPA_S><<<N, 128, 0, c.stream>>>(K, N, B, ldb, opb, nnb, nks, Bs, fexp);
+    DCG_LAUNCHED(c);
+    DCG_CUDA(cudaFuncSetAttribute(sp_gemm_acc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SPA_SMEM));
+    SplitArgs sa;
+    sa.As = As;
+    sa.Bs = Bs;
+    sa.eexp = eexp;
+    sa.fexp = fexp;
+    sa.C = C;
+    sa.c_si = c_si;
+    sa.c_sj = c_sj;
+    sa.c_sb = c_sb;
+    sa.M = M;
+    sa.N = N;
+    sa.nz = batch;
+    sa.nrb = nrb;
+    sa.nnb = nnb;
+    sa.nks = nks;
+    sa.lbo = c.split_lbo;
+    sa.sbo = c.split_sbo;
+    sa.accumulate = accumulate ? 1 : 0;
+    sa.order = 0;
+    sa.err = err;
+    sa.wait_ns = c.wait_limit_ns ? c.wait_limit_ns : SP_WAIT_NS;
+    const double tensor_work = 28.0 * 8.0 * (double)M * N * K * batch;   // 28 slice products
+    FamScope fs(c, DCG_FAM_SPLIT_MMA, tensor_work);
+    sp_gemm_acc_kernel<<<dim3((unsigned)((int64_t)nrb * nnh), 1, batch), SP_THREADS, SPA_SMEM, c.stream>>>(sa);
+    DCG_LAUNCHED(c);
 }
 
 void split_reset(Context &c) {

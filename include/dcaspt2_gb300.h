@@ -43,6 +43,9 @@ extern "C" {
 /* precision of the dense contractions (the transformation and S/B/V builds) */
 #define DCG_PREC_FP64 0       /* native FP64 everywhere                                  */
 #define DCG_PREC_SPLIT 1      /* split-precision tensor-core contractions, FP64 recombine */
+#define DCG_PREC_SPLIT_ACC 2  /* dcg_zgemm only: the seven-slice split product (~2^-45 relative per
+                                 term instead of ~2^-36), which the split path uses for the Gram
+                                 metric and the products Lambda^-1 amplifies                  */
 
 typedef struct dcg_ctx dcg_ctx;
 
@@ -234,7 +237,9 @@ int dcg_stedc(dcg_ctx *ctx, int32_t n, const double *d, const double *e, double 
  *   C[z*c_sb + i*c_si + j*c_sj] (+)= sum_{k<K} A[z*a_sb + i*a_si + k*a_sk] * op(B)(k, j)
  * with op(B)(k, j) = B[k + j*ldb], conjugated when conj_b; strides count complex elements
  * (double2).  DCG_PREC_SPLIT runs the BF16 tensor-core path with FP64 recombination (any
- * strides); DCG_PREC_FP64 needs a_si = c_si = 1.  accumulate != 0 adds to C. */
+ * strides; five slices per operand, ~2^-36 of max|row of A| max|column of op(B)| per term),
+ * DCG_PREC_SPLIT_ACC the same with seven slices (~2^-45); DCG_PREC_FP64 needs a_si = c_si = 1.
+ * accumulate != 0 adds to C. */
 int dcg_zgemm(dcg_ctx *ctx, int precision, int32_t M, int32_t N, int32_t K, int32_t batch, const void *A, int64_t a_si,
               int64_t a_sk, int64_t a_sb, const void *B, int64_t ldb, int32_t conj_b, void *C, int64_t c_si,
               int64_t c_sj, int64_t c_sb, int32_t accumulate);

@@ -131,3 +131,36 @@ def test_split_gemm_kernel_variants_agree(session, monkeypatch, M, N, K, batch):
         assert torch.equal(C, out[0])
     Cref = torch.matmul(A.cuda(), B.cuda())
     _check(out[2].transpose(1, 2), Cref, A.abs().amax(dim=(0, 2)).cuda(), B.abs().amax(dim=0).cuda(), K)
+
+
+@pytest.mark.parametrize("M,N,K,batch,conj", [(128, 64, 8, 1, False), (300, 40, 50, 1, False),
+                                              (130, 20, 33, 3, True), (792, 300, 1728, 1, False),
+                                              (64, 129, 129, 1, True)])
+def test_split_gemm_seven_slices(session, M, N, K, batch, conj):
+    """The seven-slice product (DCG_PREC_SPLIT_ACC): within 1e-13 * K * row max * column max
+    (2^-45 ~ 2.8e-14 per term), and far more accurate than the five-slice product on the same
+    operands (the Gram metric and the products Lambda^-1 amplifies take it)."""
+    from dirac_caspt2_gb300 import api
+    gen = torch.Generator().manual_seed(M + 5 * N + 11 * K + batch)
+    A = _rand((batch, K, M), gen).transpose(1, 2)
+    A = A * torch.logspace(-6, 6, M, dtype=torch.float64)[None, :, None]
+    B = _rand((N, K), gen).T
+    A_cm = torch.empty((batch, K, M), dtype=torch.complex128, device="cuda")
+    A_cm.copy_(A.transpose(1, 2))
+    B_cm = torch.empty((N, K), dtype=torch.complex128, device="cuda")
+    B_cm.copy_(B.T)
+    out = {}
+    for prec in (SPLIT, api.DCG_PREC_SPLIT_ACC):
+        C = torch.zeros((batch, N, M), dtype=torch.complex128, device="cuda")
+        session.zgemm(prec, M, N, K, batch, A_cm.data_ptr(), 1, M, M * K, B_cm.data_ptr(), K, conj,
+                      C.data_ptr(), 1, M, M * N)
+        torch.cuda.synchronize()
+        out[prec] = C.transpose(1, 2)
+    Bop = B.conj() if conj else B
+    Cref = torch.matmul(A.cuda(), Bop.cuda())
+    rmax, cmax = A.abs().amax(dim=(0, 2)).cuda(), B.abs().amax(dim=0).cuda()
+    scale = K * (rmax[:, None] * cmax[None, :])
+    acc = ((out[api.DCG_PREC_SPLIT_ACC] - Cref).abs() / scale).max().item()
+    five = ((out[SPLIT] - Cref).abs() / scale).max().item()
+    assert acc <= 1e-13, acc
+    assert acc * 50 <= five or five <= 1e-13, (acc, five)
