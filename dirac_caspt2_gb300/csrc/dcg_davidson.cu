@@ -112,8 +112,12 @@ __global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, cons
                 cs_q[k] = q;
                 double c = 1.0, sn = 0.0, pr = 1.0, pi = 0.0;
                 const cplx b = A[p + np * q];
-                const double ab = sqrt(b.x * b.x + b.y * b.y);
-                if (q < n && ab > 0.0) {
+                const double ab2 = b.x * b.x + b.y * b.y;
+                // a rotation whose off-diagonal element is below 1e-34 of the squared norm is
+                // skipped (all of them together stay under the 1e-30 stopping test): the late
+                // sweeps of the quadratic convergence then cost little FP64 work
+                if (q < n && ab2 > 1e-34 * fro) {
+                    const double ab = sqrt(ab2);
                     const double app = A[p + np * p].x, aqq = A[q + np * q].x;
                     const double zeta = (aqq - app) / (2.0 * ab);
                     const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
@@ -128,11 +132,12 @@ __global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, cons
                 cs_pi[k] = pi;
             }
             __syncthreads();
-            // columns: A <- A J, V <- V J
+            // columns: A <- A J, V <- V J (identity rotations skipped)
             for (int e = tid; e < np * npair; e += nt) {
                 const int i = e % np, k = e / np;
-                const int p = cs_p[k], q = cs_q[k];
                 const double c = cs_c[k], sn = cs_s[k];
+                if (sn == 0.0) continue;
+                const int p = cs_p[k], q = cs_q[k];
                 const cplx sp = mk(sn * cs_pr[k], sn * cs_pi[k]);    // s e^{i phi}
                 const cplx sm = mk(sn * cs_pr[k], -sn * cs_pi[k]);   // s e^{-i phi}
                 const cplx ap = A[i + np * p], aq = A[i + np * q];
@@ -146,8 +151,9 @@ __global__ void __launch_bounds__(kJacobiThreads) jacobi_heev_kernel(int n, cons
             // rows: A <- J^H A
             for (int e = tid; e < np * npair; e += nt) {
                 const int j = e % np, k = e / np;
-                const int p = cs_p[k], q = cs_q[k];
                 const double c = cs_c[k], sn = cs_s[k];
+                if (sn == 0.0) continue;
+                const int p = cs_p[k], q = cs_q[k];
                 const cplx sp = mk(sn * cs_pr[k], sn * cs_pi[k]);
                 const cplx sm = mk(sn * cs_pr[k], -sn * cs_pi[k]);
                 const cplx ap = A[p + np * j], aq = A[q + np * j];
