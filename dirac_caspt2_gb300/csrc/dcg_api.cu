@@ -917,24 +917,28 @@ static void bprime_product(Context &c, int Mp, int dm, const cplx *P, const cplx
     }
 }
 
-// The three Gram-route products whose errors Lambda^-1 amplifies: the metric K = G G^H, G v and
-// P^H (G v).  On the split path they run on the tensor cores through the seven-slice product
-// (~2^-45 of row max x column max per term; the five-slice product, ~2^-36, moved e2c by
-// 1.2e-9 Eh on 20/12/300 when it carried K), otherwise in FP64.  DCG_GRAM_SPLIT_ACC=0 keeps them
-// in FP64 on the split path too.
-static bool gram_acc_split(const Context &c) {
+// The Gram-route products whose errors Lambda^-1 amplifies: the metric K = G G^H, G v and
+// P^H (G v).  On the split path the first two run on the tensor cores through the seven-slice
+// product (~2^-45 of row max x column max per term; the five-slice product moved e2c by 1.2e-9 Eh
+// on 20/12/300 when it carried K).  Measured there against the oracle, K and G v on seven slices
+// change no e2 by more than 3e-12 Eh; P^H (G v) on seven slices moved e2c by 2.2e-10 Eh (its
+// outputs along the modes near the cutoff are ~1e-4 of its inputs and are divided by Lambda next),
+// so it stays in FP64.  which: 1 the metric, 2 G v, 4 P^H (G v); DCG_GRAM_SPLIT_ACC is a mask of
+// them (default 3; 0 keeps all three in FP64).
+static bool gram_acc_split(const Context &c, int which) {
     if (c.precision != DCG_PREC_SPLIT) return false;
     const char *e = getenv("DCG_GRAM_SPLIT_ACC");
-    return !(e && e[0] == '0');
+    const int mask = e ? atoi(e) : 3;
+    return (mask & which) != 0;
 }
 // K = G G^H (Mp x Mp; at least the upper triangle, the caller mirrors it)
 static void gram_metric(Context &c, int Mp, int dimn, const cplx *G, cplx *K) {
-    if (gram_acc_split(c)) zgemm_split_acc(c, Mp, Mp, dimn, 1, G, 1, Mp, 0, G, Mp, 3, K, 1, Mp, 0, false);
+    if (gram_acc_split(c, 1)) zgemm_split_acc(c, Mp, Mp, dimn, 1, G, 1, Mp, 0, G, Mp, 3, K, 1, Mp, 0, false);
     else zherk_upper(c, Mp, dimn, G, Mp, K, Mp);
 }
 // GV = G Vsel (Mp x nouter)
 static void gram_gv(Context &c, int Mp, int nouter, int dimn, const cplx *G, const cplx *Vsel, cplx *GV) {
-    if (gram_acc_split(c)) {
+    if (gram_acc_split(c, 2)) {
         zgemm_split_acc(c, Mp, nouter, dimn, 1, G, 1, Mp, 0, Vsel, dimn, 0, GV, 1, Mp, 0, false);
     } else {
         const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
@@ -943,7 +947,7 @@ static void gram_gv(Context &c, int Mp, int nouter, int dimn, const cplx *G, con
 }
 // VC0 = P^H GV (dm x nouter), on the split path as its transpose GV^T conj(P)
 static void gram_phgv(Context &c, int dm, int nouter, int Mp, const cplx *P, const cplx *GV, cplx *VC0) {
-    if (gram_acc_split(c)) {
+    if (gram_acc_split(c, 4)) {
         zgemm_split_acc(c, nouter, dm, Mp, 1, GV, Mp, 1, 0, P, Mp, 1, VC0, dm, 1, 0, false);
     } else {
         const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
