@@ -38,7 +38,33 @@ def main(argv=None) -> int:
     ap.add_argument("--heev", type=int, default=0,
                     help="instead of a solve: dcg_heev (all eigenpairs) of a seeded random Hermitian matrix "
                          "of this size, --warmup + --solves times")
+    ap.add_argument("--zgemm", type=int, nargs=3, default=None, metavar=("M", "N", "K"),
+                    help="instead of a solve: dcg_zgemm of seeded random column-major operands, "
+                         "--warmup + --solves times, at --gemm-precision")
+    ap.add_argument("--gemm-precision", default="split_acc", choices=["fp64", "split", "split_acc"])
     a = ap.parse_args(argv)
+    if a.zgemm:
+        import numpy as np
+        import torch
+        M, N, K = a.zgemm
+        g = torch.Generator().manual_seed(a.seed)
+        dev = lambda r, c: (torch.randn((c, r), dtype=torch.float64, generator=g) +
+                            1j * torch.randn((c, r), dtype=torch.float64, generator=g)).cuda()
+        A, B = dev(M, K), dev(K, N)           # (cols, rows) storage: column-major M x K and K x N
+        C = torch.zeros((N, M), dtype=torch.complex128, device="cuda")
+        prec = {"fp64": api.DCG_PREC_FP64, "split": api.DCG_PREC_SPLIT, "split_acc": api.DCG_PREC_SPLIT_ACC}
+        ses = api.Caspt2Session(0, api.DCG_PREC_SPLIT)
+        t0 = time.time()
+        for _ in range(a.warmup + a.solves):
+            ses.zgemm(prec[a.gemm_precision], M, N, K, 1, A.data_ptr(), 1, M, 0, B.data_ptr(), K, False,
+                      C.data_ptr(), 1, M, 0)
+        torch.cuda.synchronize()
+        ref = A.T @ B.T
+        err = ((C.T - ref).abs().max() / (A.abs().max() * B.abs().max())).item()
+        print(json.dumps({"zgemm": [M, N, K], "precision": a.gemm_precision, "calls": a.warmup + a.solves,
+                          "wall_s": round(time.time() - t0, 3), "max_rel_error": err}))
+        ses.close()
+        return 0
     if a.heev > 0:
         import numpy as np
         rng = np.random.default_rng(a.seed)
