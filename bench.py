@@ -478,6 +478,17 @@ def large_leg(args, local):
     out["max_abs_dE2_subspace"] = max(abs(sp.e2[k] - fp.e2[k]) for k in sp.e2)
     out["abs_dE_total"] = abs(sp.total_energy - fp.total_energy)
     out["abs_dE_casci"] = abs(sp.casci_energies[0] - fp.casci_energies[0])
+    # CPU-oracle energies of this system, when tests/golden holds them (made once on a host with
+    # the memory for it by tests/golden/make_synthetic_fixtures.py --device-generator)
+    fx_path = os.path.join(HERE, "tests", "golden", f"synthetic_{args.large_config}.json")
+    if os.path.exists(fx_path):
+        fx = json.load(open(fx_path))
+        if fx["fingerprint"]["nrec"] == out["records"]:
+            out["oracle"] = {name: {"max_abs_dE2_subspace": max(abs(r.e2[k] - fx["e2"][k]) for k in "ABCDEFGH"),
+                                    "abs_dE_total": abs(r.total_energy - fx["total"]),
+                                    "abs_dE_casci": abs(r.casci_energies[0] - fx["casci"])}
+                             for name, r in res.items()}
+            out["oracle"]["fixture"] = os.path.basename(fx_path)
     out["peak_source"] = src
     del bufs, dsys
     torch.cuda.empty_cache()

@@ -660,16 +660,24 @@ class Result:
 
 
 def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool = False,
-        active_pair_rotation: Optional[np.random.Generator] = None) -> Result:
+        active_pair_rotation: Optional[np.random.Generator] = None, lean: bool = False) -> Result:
     """r4dcasci (r4dcasci.F90:1-134) followed by r4dcaspt2_tra (r4dcaspt2_tra.F90:4-482).
 
     ``active_pair_rotation``: when given, the eigenvectors of every exactly degenerate pair of
     active Fock eigenvalues are rotated by a random unitary 2x2 matrix.  Such a rotation is
     an equally valid ZHEEV result; every subspace except E is invariant under it (see
-    ``e_subspace_envelope``)."""
+    ``e_subspace_envelope``).
+
+    ``lean``: release memory as soon as it is no longer read (for the largest systems): the
+    record arrays of ``s`` after the integral expansion (``s.rec_idx``/``s.rec_val`` become
+    empty), the Fock-only blocks after the Fock build, and each original-basis class block once
+    it has been transformed.  The numbers are the same."""
     ni, na, ns = s.ninact, s.nact, s.nsec
     nmoc = ni + na
     ints = Integrals(s)
+    if lean:
+        s.rec_idx = np.zeros((0, 4), np.int32)
+        s.rec_val = np.zeros(0, np.complex128)
     g_occ = ints.occ_block()
     dets = enumerate_dets(s)
     ndet = len(dets)
@@ -685,6 +693,9 @@ def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool 
     # ---- Fock matrix of the CASCI state and its diagonalisation
     rd_c = RDM(fs, c0, order=1)
     f = fock_casci(s, ints, g_occ, rd_c.D1)
+    if lean:   # blocks only the Fock build reads
+        for pat in ((3, 3, 1, 1), (3, 3, 2, 2), (3, 1, 1, 3), (3, 2, 2, 3)):
+            ints._cache.pop(pat, None)
     U, eps = fock_diag(s, f)
     if active_pair_rotation is not None:
         for p in range(ni, nmoc - 1):
@@ -706,6 +717,8 @@ def run(s: System, mode: str = "rdm", subspaces: str = SUBSPACES, verbose: bool 
                 "H": (3, 1, 3, 1)}
     for name, pat in patterns.items():
         cls[name] = transform_block(ints.block(pat), U, [ints.rng(p) for p in pat])
+        if lean:
+            ints._cache.pop(pat, None)
     hU = np.conj(U).T @ s.h @ U                                       # tramo1 (tramo.F90:4-68)
 
     res_e2, res_sc2, res_sym = {}, {}, {}
