@@ -588,28 +588,15 @@ __device__ void tridiag_smem_body(int n, cplx *A, int64_t lda, double *d, double
         if (active) {
             // p^H v summed over the columns in a fixed order (thread stride, then the block
             // sum): the same bits whatever the number of blocks reducing this matrix
-            // p is read in the same pass (registers), so its L2 round trip overlaps the sum's
-            static_assert(kTridiagSmemMaxN <= 3 * TRD_THREADS, "three rows per thread");
             double sr = 0.0, si = 0.0;
-            cplx pr3[3];
-#pragma unroll
-            for (int u = 0; u < 3; u++) {
-                const int q = k + 1 + threadIdx.x + u * TRD_THREADS;
-                pr3[u] = mk(0.0, 0.0);
-                if (q < n) {
-                    const double2 v = __ldcg(pt + q);
-                    pr3[u] = ldcg(pb + q);
-                    sr += v.x;
-                    si += v.y;
-                }
+            for (int q = k + 1 + threadIdx.x; q < n; q += blockDim.x) {
+                const double2 v = __ldcg(pt + q);
+                sr += v.x;
+                si += v.y;
             }
             eig_block_sum2(sr, si, red);
             const cplx al = cmul(mk(-0.5, 0.0), cmul(t, mk(sr, si)));
-#pragma unroll
-            for (int u = 0; u < 3; u++) {
-                const int r = k + 1 + threadIdx.x + u * TRD_THREADS;
-                if (r < n) sw[r] = cadd(pr3[u], cmul(al, sv[r]));
-            }
+            for (int r = k + 1 + threadIdx.x; r < n; r += blockDim.x) sw[r] = cadd(ldcg(pb + r), cmul(al, sv[r]));
             __syncthreads();
         }
         // update owned columns > k; the warp that owns column k+1 then publishes its reflector

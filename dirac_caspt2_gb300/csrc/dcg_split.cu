@@ -123,6 +123,47 @@ __global__ void sp_rowexp_kernel(int M, int K, const cplx *__restrict__ A, int64
     }
 }
 
+// The same for few contiguous rows (si == 1, M small, K long: the Gram factor of the A/C blocks):
+// a block takes 32 rows and 32 strands of k, so each warp reads 32 adjacent rows at one k and a
+// thread scans K/32 entries instead of K; the strands' maxima meet in shared memory.
+__global__ void __launch_bounds__(1024) sp_rowexp_tile_kernel(int M, int K, const cplx *__restrict__ A, int64_t sk,
+                                                              int64_t sb, int *eexp) {
+    __shared__ long long red[32][33];
+    const int z = blockIdx.y;
+    const int r = threadIdx.x & 31, g = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + r;
+    long long mb = 0;
+    if (i < M) {
+        const cplx *a = A + (int64_t)z * sb + i;
+        for (int k = g; k < K; k += 32) {
+            const cplx v = a[(int64_t)k * sk];
+            mb = max(mb, max(sp_absbits(v.x), sp_absbits(v.y)));
+        }
+    }
+    red[g][r] = mb;
+    __syncthreads();
+    if (g == 0 && i < M) {
+        long long m = 0;
+        for (int q = 0; q < 32; q++) m = max(m, red[q][r]);
+        eexp[(int64_t)z * M + i] = sp_exponent_bits(m);
+    }
+}
+
+// Row exponents through whichever kernel suits the shape.
+static void launch_rowexp(Context &c, int M, int K, int batch, const cplx *A, int64_t a_si, int64_t a_sk, int64_t a_sb,
+                          int *eexp) {
+    if (a_si == 1 && M < 32768 && K >= 64) {
+        sp_rowexp_tile_kernel<<<dim3((unsigned)((M + 31) / 32), batch), 1024, 0, c.stream>>>(M, K, A, a_sk, a_sb, eexp);
+    } else if (a_si == 1) {
+        dim3 g(grid1d(M, 256), batch);
+        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 1, eexp);
+    } else {
+        dim3 g(grid1d((int64_t)M * 32, 256), batch);
+        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 0, eexp);
+    }
+    DCG_LAUNCHED(c);
+}
+
 // A slices in tiles: tile (p, z, rb, ks) at ((p*nz + z)*nrb + rb)*nks + ks, 4 KB each.
 // One thread per (row, group of 4 complex k) writes one 16-byte core-matrix row per slice.
 template <int S>
@@ -876,15 +917,7 @@ void zgemm_split(Context &c, int M, int N, int K, int batch, const cplx *A, int6
     // B' tiles may have padding columns beyond 2N: zero them all first.  The error flag is
     // reset by split_reset() at the start of a solve and read by split_error() at its end.
     DCG_CUDA(cudaMemsetAsync(Bs, 0, tiles_b * SP_TILE_BYTES, c.stream));
-    const bool rows_contig = (a_si == 1);
-    if (rows_contig) {
-        dim3 g(grid1d(M, 256), batch);
-        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 1, eexp);
-    } else {
-        dim3 g(grid1d((int64_t)M * 32, 256), batch);
-        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 0, eexp);
-    }
-    DCG_LAUNCHED(c);
+    launch_rowexp(c, M, K, batch, A, a_si, a_sk, a_sb, eexp);
     {
         const int64_t work = (int64_t)nrb * SP_TM * nks * (SP_TK / 8);
         dim3 g(grid1d(work, 256), batch);
@@ -984,14 +1017,7 @@ void zgemm_split_acc(Context &c, int M, int N, int K, int batch, const cplx *A, 
     int *fexp = wsget<int>(c, "splitacc.f", (size_t)N);
     int *err = wsget<int>(c, "split.err", 1);
     DCG_CUDA(cudaMemsetAsync(Bs, 0, tiles_b * SP_TILE_BYTES, c.stream));
-    if (a_si == 1) {
-        dim3 g(grid1d(M, 256), batch);
-        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 1, eexp);
-    } else {
-        dim3 g(grid1d((int64_t)M * 32, 256), batch);
-        sp_rowexp_kernel<<<g, 256, 0, c.stream>>>(M, K, A, a_si, a_sk, a_sb, 0, eexp);
-    }
-    DCG_LAUNCHED(c);
+    launch_rowexp(c, M, K, batch, A, a_si, a_sk, a_sb, eexp);
     {
         const int64_t work = (int64_t)nrb * SP_TM * nks * (SP_TK / 8);
         dim3 g(grid1d(work, 256), batch);
