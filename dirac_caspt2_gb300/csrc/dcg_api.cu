@@ -458,6 +458,41 @@ static void e2_from_bprime(Context &c, int dimm, cplx *Bp, const cplx *VC, int n
     launch_e2(c, VC1, dimm, nouter, alpha, wb, e2o, sco);
 }
 
+// The S-route products of B, D, E, F and G on the split path through the seven-slice kernel,
+// by DCG_SROUTE_SPLIT_ACC (bit mask: 1 the B' build X^H (B X), 2 X^H Vsel, 4 the combined
+// basis X W and (X W)^H Vsel; default 7, all three); FP64 otherwise.  On 20 inactive, 12
+// active, 300 secondary spinors all three move no subspace E2 by more than 4e-13 Eh against
+// the FP64 products and take the B-G stage from 20.9 to 14.7 ms.
+static bool sroute_acc_split(const Context &c, int which) {
+    if (c.precision != DCG_PREC_SPLIT) return false;
+    static const int mask = [] {
+        const char *e = getenv("DCG_SROUTE_SPLIT_ACC");
+        return e ? atoi(e) : 7;
+    }();
+    return (mask & which) != 0;
+}
+// C (M x N, ld ldc) = A (M x K, ld lda) B (K x N, ld ldb)
+static void prod_nn(Context &c, bool split, int M, int N, int K, const cplx *A, int64_t lda, const cplx *B,
+                    int64_t ldb, cplx *C, int64_t ldc) {
+    if (split) {
+        zgemm_split_acc(c, M, N, K, 1, A, 1, lda, 0, B, ldb, 0, C, 1, ldc, 0, false);
+    } else {
+        const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+        zgemm(c, OP_N, OP_N, M, N, K, one, A, lda, 0, B, ldb, 0, zero, C, ldc, 0, 1);
+    }
+}
+// C (M x N, ld ldc) = A^H B with A (K x M, ld lda), B (K x N, ld ldb); on the split path as
+// its transpose B^T conj(A)
+static void prod_cn(Context &c, bool split, int M, int N, int K, const cplx *A, int64_t lda, const cplx *B,
+                    int64_t ldb, cplx *C, int64_t ldc) {
+    if (split) {
+        zgemm_split_acc(c, N, M, K, 1, B, ldb, 1, 0, A, lda, 1, C, ldc, 1, 0, false);
+    } else {
+        const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+        zgemm(c, OP_C, OP_N, M, N, K, one, A, lda, 0, B, ldb, 0, zero, C, ldc, 0, 1);
+    }
+}
+
 // S,B (dimn x dimn) already assembled; Vsel (dimn x nouter); alphas on device.
 static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *Vsel, int nouter, const double *alpha) {
     BlockOut r;
@@ -483,14 +518,14 @@ static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *
     // B' = X^H B X
     cplx *BX = wsget<cplx>(c, "blk.BX", (size_t)dimn * dimm);
     cplx *Bp = wsget<cplx>(c, "blk.Bp", (size_t)dimm * dimm);
-    zgemm(c, OP_N, OP_N, dimn, dimm, dimn, one, B, dimn, 0, X, dimn, 0, zero, BX, dimn, 0, 1);
-    zgemm(c, OP_C, OP_N, dimm, dimm, dimn, one, X, dimn, 0, BX, dimn, 0, zero, Bp, dimm, 0, 1);
+    prod_nn(c, sroute_acc_split(c, 1), dimn, dimm, dimn, B, dimn, X, dimn, BX, dimn);
+    prod_cn(c, sroute_acc_split(c, 1), dimm, dimm, dimn, X, dimn, BX, dimn, Bp, dimm);
     herm_from_upper(c, dimm, Bp, dimm);
     double *e2o = wsget<double>(c, "blk.e2o", nouter);
     double *sco = wsget<double>(c, "blk.sco", nouter);
     cplx *VC0 = wsget<cplx>(c, "blk.VC0", (size_t)dimm * nouter);
     if (tridiag_e2_pays(dimm, nouter)) {
-        zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, X, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
+        prod_cn(c, sroute_acc_split(c, 2), dimm, nouter, dimn, X, dimn, Vsel, dimn, VC0, dimm);
         e2_from_bprime(c, dimm, Bp, VC0, nouter, alpha, e2o, sco);
     } else {
         // B' = W w W^H, then the outer-index vectors in the combined basis (X W)^H Vsel: one
@@ -499,8 +534,8 @@ static BlockOut solve_block(Context &c, int dimn, cplx *S, cplx *B, const cplx *
         cplx *W = wsget<cplx>(c, "blk.W", (size_t)dimm * dimm);
         heev(c, dimm, Bp, dimm, wb, 0, dimm, W, dimm);
         cplx *XW = wsget<cplx>(c, "blk.XW", (size_t)dimn * dimm);
-        zgemm(c, OP_N, OP_N, dimn, dimm, dimm, one, X, dimn, 0, W, dimm, 0, zero, XW, dimn, 0, 1);
-        zgemm(c, OP_C, OP_N, dimm, nouter, dimn, one, XW, dimn, 0, Vsel, dimn, 0, zero, VC0, dimm, 0, 1);
+        prod_nn(c, sroute_acc_split(c, 4), dimn, dimm, dimm, X, dimn, W, dimm, XW, dimn);
+        prod_cn(c, sroute_acc_split(c, 4), dimm, nouter, dimn, XW, dimn, Vsel, dimn, VC0, dimm);
         launch_e2(c, VC0, dimm, nouter, alpha, wb, e2o, sco);
     }
     double *red = wsget<double>(c, "blk.red", 2);
@@ -587,9 +622,8 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
             launch_scale_cols(c, X[j], b.dimn, b.dimn, dimm[j], ws[j], vlo[j]);   // X = U lambda^-1/2
             cplx *BX = wsget<cplx>(c, "bj.BX", (size_t)b.dimn * dimm[j]);
             Bp[j] = wsget<cplx>(c, nm("bj.Bp", j), (size_t)dimm[j] * dimm[j]);
-            zgemm(c, OP_N, OP_N, b.dimn, dimm[j], b.dimn, one, b.B, b.dimn, 0, X[j], b.dimn, 0, zero, BX, b.dimn, 0, 1);
-            zgemm(c, OP_C, OP_N, dimm[j], dimm[j], b.dimn, one, X[j], b.dimn, 0, BX, b.dimn, 0, zero, Bp[j], dimm[j], 0,
-                  1);
+            prod_nn(c, sroute_acc_split(c, 1), b.dimn, dimm[j], b.dimn, b.B, b.dimn, X[j], b.dimn, BX, b.dimn);
+            prod_cn(c, sroute_acc_split(c, 1), dimm[j], dimm[j], b.dimn, X[j], b.dimn, BX, b.dimn, Bp[j], dimm[j]);
             herm_from_upper(c, dimm[j], Bp[j], dimm[j]);
             wb[j] = wsget<double>(c, nm("bj.wb", j), dimm[j]);
             if (tridiag_e2_pays(dimm[j], b.nouter) && band_e2_pays(dimm[j], b.nouter)) {
@@ -620,11 +654,11 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
             sco[j] = wsget<double>(c, nm("bj.sco", j), b.nouter);
             if (band[j]) {
                 cplx *VC = wsget<cplx>(c, nm("bj.VC", j), (size_t)m * b.nouter);
-                zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, X[j], b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
+                prod_cn(c, sroute_acc_split(c, 2), m, b.nouter, b.dimn, X[j], b.dimn, b.Vsel, b.dimn, VC, m);
                 band_e2(c, (int)j, m, Bp[j], m, VC, m, b.nouter, b.alpha, e2o[j], sco[j]);
             } else if (tridiag_e2_pays(m, b.nouter)) {
                 cplx *VC = wsget<cplx>(c, nm("bj.VC", j), (size_t)m * b.nouter);
-                zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, X[j], b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
+                prod_cn(c, sroute_acc_split(c, 2), m, b.nouter, b.dimn, X[j], b.dimn, b.Vsel, b.dimn, VC, m);
                 TE2Job t;
                 t.slot = (int)j;
                 t.n = m;
@@ -656,8 +690,8 @@ static void solve_block_jobs(Context &c, std::vector<BlockJob> &all, double e2_s
             if (W[j]) {
                 cplx *VC = wsget<cplx>(c, "bj.VCw", (size_t)m * b.nouter);
                 cplx *XW = wsget<cplx>(c, "bj.XW", (size_t)b.dimn * m);
-                zgemm(c, OP_N, OP_N, b.dimn, m, m, one, X[j], b.dimn, 0, W[j], m, 0, zero, XW, b.dimn, 0, 1);
-                zgemm(c, OP_C, OP_N, m, b.nouter, b.dimn, one, XW, b.dimn, 0, b.Vsel, b.dimn, 0, zero, VC, m, 0, 1);
+                prod_nn(c, sroute_acc_split(c, 4), b.dimn, m, m, X[j], b.dimn, W[j], m, XW, b.dimn);
+                prod_cn(c, sroute_acc_split(c, 4), m, b.nouter, b.dimn, XW, b.dimn, b.Vsel, b.dimn, VC, m);
                 launch_e2(c, VC, m, b.nouter, b.alpha, wb[j], e2o[j], sco[j]);
             }
             red[j] = wsget<double>(c, nm("bj.red", j), 2);

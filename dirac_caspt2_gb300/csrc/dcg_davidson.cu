@@ -514,7 +514,7 @@ void davidson_lowest_csr(Context &c, const CsrMatrix &H, int nwant, double *w, c
     const int hx_blocks = (int)(((int64_t)n * 32 + 255) / 256);
     auto enqueue_step = [&]() {
         rr_kernel<<<dim3(mmax, mmax), 256, 0, c.stream>>>(n, V, W, ld, G, mmax, st);
-        jacobi_heev_kernel<<<1, 64, jsmem, c.stream>>>(mmax, &st->m, G, mmax, th, Y, mmax, &st->jac);
+        jacobi_heev_kernel<<<1, kJacobiThreads, jsmem, c.stream>>>(mmax, &st->m, G, mmax, th, Y, mmax, &st->jac);
         ritz_kernel<<<dim3(grid1d(n, 128), nb, 2), 128, 0, c.stream>>>(n, V, W, ld, Y, mmax, X, HX, st);
         residual_kernel<<<nb, 256, 0, c.stream>>>(n, HX, X, ld, th, H.diag, T, h2);
         step_begin_kernel<<<1, 32, 0, c.stream>>>(nwant, h2, st);

@@ -673,9 +673,36 @@ __global__ void dc_leaf_kernel(int n, const double *__restrict__ d, const double
     Q[i + (int64_t)i * n] = 1.0;
 }
 
-// One block per node: rank-one vector, merge order, deflation (thread 0 scans the merged
-// order), rotations applied to the node's eigenvector columns.  Dynamic shared memory:
-// 20 bytes per node column.
+// Exclusive block prefix sum of one int per thread (blockDim.x <= 1024); total gets the sum.
+// Every thread of the block must call it.
+__device__ int dc_block_excl_scan(int v, int *wsum, int &total) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    int x = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[wid] = x;
+    __syncthreads();
+    if (wid == 0) {
+        int t = lane < nw ? wsum[lane] : 0;
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, t, o);
+            if (lane >= o) t += y;
+        }
+        __syncwarp();
+        wsum[lane] = t;
+    }
+    __syncthreads();
+    total = wsum[nw - 1];
+    const int base = (wid > 0 ? wsum[wid - 1] : 0) + x - v;
+    __syncthreads();
+    return base;
+}
+
+// One block per node: rank-one vector, merge order, deflation (in parallel, or thread 0
+// scanning the merged order when a pair rotation is due), rotations applied to the node's
+// eigenvector columns.  Dynamic shared memory: 20 bytes per node column.
 __global__ void dc_prep_kernel(int n, int half, int full, const double *__restrict__ e, DcBufs b) {
     extern __shared__ double smem[];
     __shared__ double red[32];
@@ -730,7 +757,48 @@ __global__ void dc_prep_kernel(int n, int half, int full, const double *__restri
         }
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    // Deflation, first in parallel: the z test of every entry, the compaction of the kept and
+    // deflated lists (a block scan over contiguous chunks of the merged order) and the
+    // rotation test of every neighbouring kept pair on the unrotated values.  When no pair
+    // qualifies for a rotation (the usual case) these lists are exactly the serial scan's; when
+    // one does, thread 0 runs the serial scan below, since a rotation changes later tests.  One
+    // thread scanning N entries costs N dependent FP64 chains on a unit that retires two
+    // operations per clock per SM.
+    __shared__ int s_wsum[32], s_rot;
+    {
+        const int per = (N + (int)blockDim.x - 1) / (int)blockDim.x;
+        const int t0 = min(N, (int)threadIdx.x * per), t1 = min(N, t0 + per);
+        int cnt = 0;
+        for (int t = t0; t < t1; t++) cnt += !(rho * fabs(sz[sp[t]]) <= tol);
+        int total;
+        int kb = dc_block_excl_scan(cnt, s_wsum, total);
+        for (int t = t0; t < t1; t++) {
+            const int nj = sp[t];
+            if (!(rho * fabs(sz[nj]) <= tol)) b.Kl[s + kb++] = nj;
+            else b.defl[s + (t - kb)] = nj;
+        }
+        if (threadIdx.x == 0) s_rot = 0;
+        __syncthreads();
+        int rot = 0;
+        for (int m = 1 + (int)threadIdx.x; m < total; m += blockDim.x) {
+            const int pj = b.Kl[s + m - 1], nj = b.Kl[s + m];
+            double S = sz[pj], C = sz[nj];
+            const double tt = hypot(C, S);
+            const double T = sd[nj] - sd[pj];
+            C /= tt;
+            S = -S / tt;
+            rot |= fabs(T * C * S) <= tol;
+        }
+        if (rot) atomicOr(&s_rot, 1);
+        __syncthreads();
+        if (threadIdx.x == 0 && !s_rot) {
+            b.kcnt[node] = total;
+            b.ndef[node] = N - total;
+            b.nrot[node] = 0;
+            b.rho[node] = rho;
+        }
+    }
+    if (threadIdx.x == 0 && s_rot) {
         int kc = 0, nd = 0, nr = 0, pj = -1;
         for (int t = 0; t < N; t++) {
             const int nj = sp[t];
@@ -843,14 +911,16 @@ __global__ void dc_secular_kernel(int n, int full, DcBufs b) {
     for (int it = 0; it < kSecularMaxIter; it++) {
         double ps = 0.0, ph = 0.0, dps = 0.0, dph = 0.0;
         for (int i = lane; i < k; i += 32) {
-            const double den = (dk[i] - d_o) - tau;
-            const double t = zk[i] * zk[i] / den;
+            // one division per pole (a GB300 FP64 division is a chain of FP64 operations on a
+            // unit that retires two per clock per SM): t = z^2 / den and t / den from 1 / den
+            const double r = 1.0 / ((dk[i] - d_o) - tau);
+            const double t = zk[i] * zk[i] * r;
             if (i <= L) {
                 ps += t;
-                dps += t / den;
+                dps += t * r;
             } else {
                 ph += t;
-                dph += t / den;
+                dph += t * r;
             }
         }
         ps = eig_warp_sum(ps);

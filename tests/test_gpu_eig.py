@@ -37,6 +37,9 @@ def _cases():
     out["kramers_498"] = _kramers(rng, 249)
     out["gram_rank120_400"] = _gram(rng, 120, 400)
     out["gram_rank496_1000"] = _gram(rng, 496, 1000)
+    # the A/C metric order at 12 active spinors and the largest shared-memory order
+    out["gram_rank700_792"] = _gram(rng, 700, 792)
+    out["random_1400"] = (lambda x: x + x.conj().T)(rng.normal(size=(1400, 1400)) + 1j * rng.normal(size=(1400, 1400)))
     out["gram_real_rank50_333"] = _gram(rng, 50, 333, cplx=False)
     q, _ = np.linalg.qr(rng.normal(size=(150, 150)) + 1j * rng.normal(size=(150, 150)))
     w = np.repeat([-1.0, 0.0, 2.0, 5.0, 5.0 + 1e-13], 30)
