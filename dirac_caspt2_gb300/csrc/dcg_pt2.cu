@@ -206,29 +206,42 @@ void launch_v_B(Context &c, const RDMView &rv, const cplx *Bc, int ni, cplx *V) 
 
 // D: V[(a + ns i) + ns ni (t + na u)] = sum_kl (ai|kl) D2(u,t,k,l) - sum_jk (aj|ki) D2(u,t,k,j)
 //    + effh(a,i) D1(u,t)   (solve_D_subspace.F90 vDmat 426-609)
-__global__ void v_D_kernel(RD r, const cplx *__restrict__ D1c, const cplx *__restrict__ D2c,
-                           const cplx *__restrict__ effh, int ni, int ns, cplx *V) {
-    const int na = r.na;
+// as one FP64 product: with X[(a,i),(k,l)] = (ai|kl) - (al|ki) (the second sum renamed j -> l)
+// and D2 viewed as the na^2 x na^2 matrix G2[(t,u),(k,l)], V = X G2^T + effh (x) D1.  Forming X
+// first halves the FP64 operations of the contraction (one complex product per (k,l) instead
+// of two), and the product runs on the tuned GEMM.
+__global__ void v_D_x_kernel(const cplx *__restrict__ D1c, const cplx *__restrict__ D2c, int ni, int ns, int na,
+                             cplx *X) {
     const int64_t nsi = (int64_t)ns * ni;
     const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= nsi * na * na) return;
     const int a = (int)(q % ns), i = (int)((q / ns) % ni);
+    const int k = (int)((q / nsi) % na), l = (int)(q / (nsi * na));
+    const int64_t S = ns, A = na;
+    X[q] = csub(D1c[q], D2c[a + S * (l + A * (k + A * (int64_t)i))]);
+}
+
+__global__ void v_D_effh_kernel(RD r, const cplx *__restrict__ effh, int ni, int ns, cplx *V) {
+    const int na = r.na;
+    const int64_t nsi = (int64_t)ns * ni;
+    const int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= nsi * na * na) return;
+    const int64_t ai = q % nsi;
     const int t = (int)((q / nsi) % na), u = (int)(q / (nsi * na));
-    const int64_t S = ns, I = ni, A = na;
-    cplx v = cmul(effh[a + S * i], r.D1(u, t));
-    for (int l = 0; l < na; l++)
-        for (int k = 0; k < na; k++) {
-            v = cadd(v, cmul(D1c[a + S * (i + I * (k + A * (int64_t)l))], r.D2(u, t, k, l)));
-            v = csub(v, cmul(D2c[a + S * (l + A * (k + A * (int64_t)i))], r.D2(u, t, k, l)));
-        }
-    V[q] = v;
+    V[q] = cadd(V[q], cmul(effh[ai], r.D1(u, t)));
 }
 
 void launch_v_D(Context &c, const RDMView &rv, const cplx *D1c, const cplx *D2c, const cplx *effh, int ni, int ns,
                 cplx *V) {
-    const int64_t n = (int64_t)ns * ni * rv.na * rv.na;
+    const int na = rv.na;
+    const int64_t nsi = (int64_t)ns * ni, n = nsi * na * na;
     if (n == 0) return;
-    v_D_kernel<<<grid1d(n, 128), 128, 0, c.stream>>>(rd_of(rv), D1c, D2c, effh, ni, ns, V);
+    cplx *X = wsget<cplx>(c, "v.Dx", (size_t)n);
+    v_D_x_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(D1c, D2c, ni, ns, na, X);
+    DCG_LAUNCHED(c);
+    const cplx one = mk(1.0, 0.0), zero = mk(0.0, 0.0);
+    zgemm(c, OP_N, OP_T, (int)nsi, na * na, na * na, one, X, nsi, 0, rv.g2, (int64_t)na * na, 0, zero, V, nsi, 0, 1);
+    v_D_effh_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(rd_of(rv), effh, ni, ns, V);
     DCG_LAUNCHED(c);
 }
 
