@@ -264,6 +264,7 @@ def run_ours(args, cfg_name):
     for _ in range(args.warmup):          # allocations, module load
         one(ses, hb_dev)
     per_v, launches_v, clocks_v, res_v, fam = timed(ses, hb_dev, args.steps, family)
+    one(ses, hb_host)                      # untimed: the host-buffer path's record buffers
     per_e, _, clocks_e, res_e, _ = timed(ses, hb_host, args.steps)
     stage = ses.stage_ms()
     tot_v = sum(per_v) / 1e3
@@ -298,9 +299,9 @@ def run_ours(args, cfg_name):
         finally:
             srv.close()
 
-    # enough requests that the four slots stay busy past the first and last one
-    e2e_steps = max(args.steps, 16)
-    tot_s, res_s = e2e_served(e2e_steps)
+    # enough requests that the slots stay busy well past the first and the last one
+    e2e_steps = max(args.steps, args.e2e_requests)
+    tot_s, res_s = e2e_served(e2e_steps, args.e2e_slots)
 
     # every kernel family timed live on two more steps each, against the roofline that bounds it:
     # the BF16 tensor pipe (measured sustained peak), HBM (measured copy bandwidth) or the FP64
@@ -399,9 +400,10 @@ def run_ours(args, cfg_name):
             "p50_ms": float(np.percentile(per_v, 50)), "p99_ms": float(np.percentile(per_v, 99)),
             "e2e": {"value": e2e_s, "unit": "solves/s", "h2d_bytes_per_step": hb_host.h2d_bytes,
                     "d2h_bytes_per_step": 8 * (1 + 8 + 8 + 2),
-                    "path": "dcg_server with 4 slots (public serving API): each step one request from "
+                    "path": f"dcg_server with {args.e2e_slots} slots (public serving API): each step one request from "
                             "pinned host buffers, host wall clock from the first submit to the last result; "
-                            "up to 4 requests in flight overlap their copies and latency-bound phases. "
+                            f"up to {args.e2e_slots} requests in flight overlap their copies and latency-bound "
+                            "phases. "
                             "single_context below is the same requests one after another on one context "
                             "(dcg_set_system / dcg_casci / dcg_caspt2 from pinned host buffers)",
                     "requests": e2e_steps,
@@ -411,6 +413,7 @@ def run_ours(args, cfg_name):
                     "single_context": {"value": e2e, "unit": "solves/s",
                                        "p50_ms": float(np.percentile(per_e, 50)),
                                        "p99_ms": float(np.percentile(per_e, 99)),
+                                       "per_step_ms": [round(x, 2) for x in per_e],
                                        "timing": "CUDA events on the context's stream"}},
             "gpu_launches": int(launches_v),
             "clocks": clocks_v, "roofline": roof,
@@ -606,6 +609,9 @@ def main():
                     help="requests of the served-stream leg (0 skips it)")
     ap.add_argument("--serve-rate", type=float, default=20.0, help="mean Poisson arrival rate of the stream (1/s)")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the serving loop")
+    ap.add_argument("--e2e-slots", type=int, default=4, help="server slots of the end-to-end leg")
+    ap.add_argument("--e2e-requests", type=int, default=32,
+                    help="requests of the end-to-end leg (at least --steps)")
     ap.add_argument("--large-config", default="cas_40_14_800",
                     help="the large single solve reported beside the line ('' to skip)")
     args = ap.parse_args()

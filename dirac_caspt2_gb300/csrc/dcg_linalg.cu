@@ -485,8 +485,31 @@ __global__ void dsum_kernel(const double *x, int64_t n, double *out) {
     if (threadIdx.x == 0) *out = s;
 }
 
+// Partial sums of contiguous chunks of x (chunk elements each), one block per chunk.
+__global__ void dsum_part_kernel(const double *x, int64_t n, int64_t chunk, double *part) {
+    __shared__ double sh[32];
+    const int64_t lo = (int64_t)blockIdx.x * chunk, hi = min(n, lo + chunk);
+    double s = 0.0;
+    for (int64_t i = lo + threadIdx.x; i < hi; i += blockDim.x) s += x[i];
+    s = block_sum(s, sh);
+    if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// Sum of x[0..n) into *out.  Long vectors (the per-outer-index E2 terms of F, G and H run to
+// millions) are summed in fixed chunks by many blocks, then the chunk sums in order: the order
+// depends on n only, so the result is deterministic.
 void dsum(Context &c, const double *x, int64_t n, double *out) {
-    dsum_kernel<<<1, 1024, 0, c.stream>>>(x, n, out);
+    constexpr int64_t kChunk = 8192;
+    if (n <= 4 * kChunk) {
+        dsum_kernel<<<1, 1024, 0, c.stream>>>(x, n, out);
+        DCG_LAUNCHED(c);
+        return;
+    }
+    const int64_t nb = (n + kChunk - 1) / kChunk;
+    double *part = wsget<double>(c, "dsum.part", (size_t)nb);
+    dsum_part_kernel<<<(unsigned)nb, 256, 0, c.stream>>>(x, n, kChunk, part);
+    DCG_LAUNCHED(c);
+    dsum_kernel<<<1, 1024, 0, c.stream>>>(part, nb, out);
     DCG_LAUNCHED(c);
 }
 
