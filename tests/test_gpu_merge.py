@@ -16,7 +16,7 @@ def _herm(n, seed):
     return X + X.conj().T
 
 
-@pytest.mark.parametrize("n0,n1", [(300, 300), (792, 180)])
+@pytest.mark.parametrize("n0,n1", [(300, 300), (792, 180), (520, 520)])
 def test_two_contexts_share_one_launch(gpu_lib, monkeypatch, n0, n1):
     from dirac_caspt2_gb300 import api
     mats = [_herm(n0, 1), _herm(n1, 2)]
