@@ -1924,9 +1924,9 @@ static bool tridiag_cluster_group(Context &c, std::vector<TrdJob> &jobs, int nct
 }
 
 // Whether the cluster form takes the matrices it fits (DCG_TRD_CLUSTER=1).  Off by default:
-// on GB300 it measured slower than the cooperative form (the 300 x 300 Fock block 6.4 against
-// 4.35 ms, the B-G batch 1.84 against 1.73 ms), both bound by the FP64 chains of the warp that
-// updates a column and forms the next reflector rather than by the exchange.
+// on GB300 it measured slower than the cooperative form (the 300 x 300 Fock block 6.4 ms on
+// 16 SMs against 4.35 ms on 63, the B-G batch 1.84 against 1.73 ms): a 16-block cluster
+// carries four times the per-block FP64 work of a column, more than its faster exchange saves.
 static bool trd_cluster_enabled() {
     static const bool on = [] {
         const char *e = getenv("DCG_TRD_CLUSTER");
