@@ -638,7 +638,7 @@ def main():
     ap.add_argument("--serve-rate", type=float, default=20.0, help="mean Poisson arrival rate of the stream (1/s)")
     ap.add_argument("--serve-slots", type=int, default=4, help="concurrent solves of the serving loop")
     ap.add_argument("--e2e-slots", type=int, default=4, help="server slots of the end-to-end leg")
-    ap.add_argument("--e2e-requests", type=int, default=32,
+    ap.add_argument("--e2e-requests", type=int, default=64,
                     help="requests of the end-to-end leg (at least --steps)")
     ap.add_argument("--large-config", default="cas_40_14_800",
                     help="the large single solve reported beside the line ('' to skip)")

@@ -1402,9 +1402,11 @@ static const double *tridiag_dc(Context &c, int n, const double *d, const double
         const int nmax = std::min(full, n);
         dc_prep_kernel<<<nodes, 256, 20 * (size_t)nmax, c.stream>>>(n, half, full, e, b);
         DCG_LAUNCHED(c);
-        dc_secular_kernel<<<grid1d((int64_t)n * 32, 256), 256, 0, c.stream>>>(n, full, b);
+        // one warp per root in blocks of two warps: a 792-root merge spreads over 396 blocks,
+        // every SM (eight warps a block left 53 of 152 SMs idle on an FP64-bound kernel)
+        dc_secular_kernel<<<grid1d((int64_t)n * 32, 64), 64, 0, c.stream>>>(n, full, b);
         DCG_LAUNCHED(c);
-        dc_zhat_kernel<<<grid1d((int64_t)n * 32, 256), 256, 0, c.stream>>>(n, full, b);
+        dc_zhat_kernel<<<grid1d((int64_t)n * 32, 64), 64, 0, c.stream>>>(n, full, b);
         DCG_LAUNCHED(c);
         dc_rank_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, full, b);
         DCG_LAUNCHED(c);
