@@ -1244,10 +1244,13 @@ __global__ void dc_zhat_kernel(int n, int full, DcBufs b) {
     if (lane == 0) b.zh[s + i] = copysign(sqrt(p), b.zK[s + i]);
 }
 
-// One thread per node entry: the rank of its eigenvalue in the merged ascending order
+// One warp per node entry: the rank of its eigenvalue in the merged ascending order
 // (ties by entry index) gives its column in the next level.
 __global__ void dc_rank_kernel(int n, int full, DcBufs b) {
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    // one warp per entry (the N comparisons are FP64 operations: one thread per entry left a
+    // 792-entry merge on four SMs); every exit below is uniform over the warp
+    const int g = (int)(((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
     if (g >= n) return;
     const int node = g / full, s = node * full, i = g - s;
     const int k = b.kcnt[node];
@@ -1256,12 +1259,15 @@ __global__ void dc_rank_kernel(int n, int full, DcBufs b) {
     if (i >= N) return;
     const double v = i < k ? b.lamK[s + i] : b.dv[s + i - k];
     int r = 0;
-    for (int m = 0; m < N; m++) {
+    for (int m = lane; m < N; m += 32) {
         const double u = m < k ? b.lamK[s + m] : b.dv[s + m - k];
         r += (u < v) || (u == v && m < i);
     }
-    b.lamB[s + r] = v;
-    b.outc[s + i] = s + r;
+    r = __reduce_add_sync(0xffffffffu, r);
+    if (lane == 0) {
+        b.lamB[s + r] = v;
+        b.outc[s + i] = s + r;
+    }
 }
 
 // One block per node entry: column of the merge eigenvector matrix (undeflated entries),
@@ -1408,7 +1414,7 @@ static const double *tridiag_dc(Context &c, int n, const double *d, const double
         DCG_LAUNCHED(c);
         dc_zhat_kernel<<<grid1d((int64_t)n * 32, 64), 64, 0, c.stream>>>(n, full, b);
         DCG_LAUNCHED(c);
-        dc_rank_kernel<<<grid1d(n, 256), 256, 0, c.stream>>>(n, full, b);
+        dc_rank_kernel<<<grid1d((int64_t)n * 32, 64), 64, 0, c.stream>>>(n, full, b);
         DCG_LAUNCHED(c);
         dc_vec_kernel<<<n, 128, 0, c.stream>>>(n, full, b);
         DCG_LAUNCHED(c);
@@ -2223,7 +2229,9 @@ void tridiag_e2(Context &c, int slot, int n, const cplx *A, int64_t lda, const c
     double *U = wsget<double>(c, slot_name("te2.U", slot), sz);
     double *U2 = wsget<double>(c, slot_name("te2.U2", slot), sz);
     cplx *B = wsget<cplx>(c, slot_name("te2.B", slot), sz);
-    tridiag_solve_e2_kernel<<<grid1d(nouter, 64), 64, 0, c.stream>>>(n, h.d, h.e, Y, n, nouter, alpha, D, U, U2, B,
+    // one thread per outer index, its tridiagonal solve a serial FP64 chain: blocks of one warp
+    // spread the indices over as many SMs as there are warps
+    tridiag_solve_e2_kernel<<<grid1d(nouter, 32), 32, 0, c.stream>>>(n, h.d, h.e, Y, n, nouter, alpha, D, U, U2, B,
                                                                       e2o, sco);
     DCG_LAUNCHED(c);
 }
